@@ -1,0 +1,614 @@
+// The DNS-aided LES case: one DNS with attached LES grids, advanced with
+// classical RK4 and the exact closure evaluated at every stage.
+//
+// Mirrors the loop of `dnsaid_project` (src/N.jl:1239-1332): each stage s
+// computes the projected DNS right-hand side k_s = P_h RHS_h(u_s) (pressure
+// from `project!`, src/N.jl:1305-1309); each LES grid gets the filtered
+// target ubar_s = P_H filter(u_s) (`apply_DHpi`, src/N.jl:1228-1237; the face
+// filter needs no projection), the exact commutator
+//   m_s = P_H filter(k_s) - P_H RHS_H(ubar_s)
+// (equal to the projected closure of `step_DHpi_classic_flux_div!`,
+// src/N.jl:1189-1206, because the box filter along a derivative axis
+// telescopes the fine difference), and two LES states advance with it: the
+// exact-closure LES (k = P_H RHS_H(v_s) + m_s) and the no-model LES
+// (`step_forwardeuler!` on the LES grid, src/N.jl:1315).  The whole step is
+// captured once into a CUDA graph (dt lives on the device, so nothing waits
+// on the host) and replayed.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+#include "fields.cuh"
+#include "filter.cuh"
+
+namespace exc {
+
+template <typename T>
+struct LesState {
+  int c = 0, kind = 0, m = 0;
+  long long M = 0;
+  exc_poisson ps;
+  T* buf = nullptr;  // one allocation, sliced below (3M words each)
+  T *ub, *fk, *mcl, *mlast, *rtmp;
+  T *ve[2], *ves, *ke;  // exact LES: state (ping-pong), stage, k
+  T *vn[2], *vns, *kn;  // no-model LES
+};
+
+}  // namespace exc
+
+struct exc_case {
+  exc_case_desc desc{};
+  int precision = EXC_F64;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  void* impl = nullptr;
+  int (*step_fn)(exc_case*, int, double) = nullptr;
+  void (*destroy_fn)(exc_case*) = nullptr;
+};
+
+namespace exc {
+
+template <typename T>
+struct CaseImpl {
+  int n = 0;
+  long long N = 0;
+  double h = 0;
+  exc_poisson ps;
+  T* u[2] = {nullptr, nullptr};  // state ping-pong: u[cur] is the current velocity
+  T* us = nullptr;               // stage state
+  T* rhs = nullptr;              // RHS, then k in place
+  int cur = 0;
+  double* dscal = nullptr;       // [0] dt, [1] clock, [2] umax, [3..] scratch
+  int* dflag = nullptr;
+  double* part = nullptr;        // reduction partials
+  int nles = 0;
+  LesState<T> les[EXC_MAX_LES];
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  double graph_dt_fixed[2] = {NAN, NAN};
+  int kernels_per_step = 0;  // kernel nodes in the captured step graph
+};
+
+template <typename T>
+static int project_vec(exc_poisson* ps, T* u, cudaStream_t st) {
+  cudaError_t e = poisson_solve_inplace<T>(ps, u, true, st);
+  if (e == cudaSuccess) e = launch_gradient<T>(ps->n, (T)ps->h, u, reinterpret_cast<const T*>(ps->work), 2 * ps->P, st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+// ubar = target(src): filter, then project for the volume filter.
+template <typename T>
+static int les_target(CaseImpl<T>* ci, LesState<T>& L, const T* src, T* out, cudaStream_t st) {
+  int rc = filter_vector<T>(ci->n, L.c, L.kind, nullptr, 0, src, out, st);
+  if (rc) return rc;
+  if (L.kind == EXC_FILTER_VOLUME) rc = project_vec<T>(&L.ps, out, st);
+  return rc;
+}
+
+// Enqueue one RK4 step (no host synchronisation).
+template <typename T>
+static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed) {
+  cudaStream_t st = cs->stream;
+  const int n = ci->n;
+  const T h = (T)ci->h, visc = (T)cs->desc.visc;
+  T* u0 = ci->u[cur];
+  T* ufin = ci->u[cur ^ 1];
+  double* dt = ci->dscal;
+  cudaError_t e;
+  // dt from the current DNS velocity (propose_timestep, src/N.jl:348-356)
+  e = launch_max_abs<T>((size_t)(3 * ci->N), u0, ci->dscal + 2, ci->part, RED_PARTS, st);
+  if (e == cudaSuccess)
+    e = launch_set_dt(ci->dscal + 2, ci->h, cs->desc.visc, cs->desc.cfl, dt_fixed, dt, ci->dscal + 1, ci->dflag, st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  for (int s = 0; s < 4; ++s) {
+    const T* src = s == 0 ? u0 : ci->us;
+    e = launch_rhs<T>(n, h, visc, src, ci->rhs, false, st);
+    if (e == cudaSuccess) e = poisson_solve_inplace<T>(&ci->ps, ci->rhs, true, st);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    // LES targets use the stage state before it is overwritten
+    for (int li = 0; li < ci->nles; ++li) {
+      LesState<T>& L = ci->les[li];
+      int rc = les_target<T>(ci, L, src, L.ub, st);
+      if (rc) return rc;
+    }
+    e = launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0, ci->us, ufin, s,
+                           dt, st);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    for (int li = 0; li < ci->nles; ++li) {
+      LesState<T>& L = ci->les[li];
+      const int m = L.m;
+      const T H = (T)(cs->desc.l / m);
+      // m_s = P_H(filter(k_s) - RHS_H(ubar_s))
+      int rc = filter_vector<T>(n, L.c, L.kind, nullptr, 0, ci->rhs, L.mcl, st);
+      if (rc) return rc;
+      e = launch_rhs<T>(m, H, visc, L.ub, L.rtmp, false, st);
+      if (e == cudaSuccess) e = launch_axpy<T>(3 * L.M, L.mcl, L.rtmp, (T)-1, st);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      rc = project_vec<T>(&L.ps, L.mcl, st);
+      if (rc) return rc;
+      if (s == 0) {
+        e = cudaMemcpyAsync(L.mlast, L.mcl, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      }
+      // exact-closure LES
+      T* ve0 = L.ve[cur];
+      T* vefin = L.ve[cur ^ 1];
+      e = launch_rhs<T>(m, H, visc, s == 0 ? ve0 : L.ves, L.ke, false, st);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      rc = project_vec<T>(&L.ps, L.ke, st);
+      if (rc) return rc;
+      e = launch_axpy<T>(3 * L.M, L.ke, L.mcl, (T)1, st);
+      if (e == cudaSuccess) e = launch_rk_stage<T>(m, H, L.ke, nullptr, 0, ve0, L.ves, vefin, s, dt, st);
+      // no-model LES
+      T* vn0 = L.vn[cur];
+      T* vnfin = L.vn[cur ^ 1];
+      if (e == cudaSuccess) e = launch_rhs<T>(m, H, visc, s == 0 ? vn0 : L.vns, L.kn, false, st);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      rc = project_vec<T>(&L.ps, L.kn, st);
+      if (rc) return rc;
+      e = launch_rk_stage<T>(m, H, L.kn, nullptr, 0, vn0, L.vns, vnfin, s, dt, st);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    }
+  }
+  return EXC_OK;
+}
+
+static int count_kernel_nodes(cudaGraph_t g) {
+  size_t num = 0;
+  if (cudaGraphGetNodes(g, nullptr, &num) != cudaSuccess || num == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(num);
+  if (cudaGraphGetNodes(g, nodes.data(), &num) != cudaSuccess) return 0;
+  int k = 0;
+  for (size_t i = 0; i < num; ++i) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
+template <typename T>
+static int case_step(exc_case* cs, int nsteps, double dt_fixed) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaStream_t st = cs->stream;
+  for (int it = 0; it < nsteps; ++it) {
+    int cur = ci->cur;
+    double key = dt_fixed > 0 ? dt_fixed : -1.0;
+    if (!ci->graph[cur] || !(ci->graph_dt_fixed[cur] == key)) {
+      if (ci->graph[cur]) { cudaGraphExecDestroy(ci->graph[cur]); ci->graph[cur] = nullptr; }
+      cudaGraph_t g;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      int rc = enqueue_step<T>(cs, ci, cur, key);
+      e = cudaStreamEndCapture(st, &g);
+      if (rc) { if (e == cudaSuccess) cudaGraphDestroy(g); return rc; }
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      ci->kernels_per_step = count_kernel_nodes(g);
+      e = cudaGraphInstantiate(&ci->graph[cur], g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      ci->graph_dt_fixed[cur] = key;
+    }
+    cudaError_t e = cudaGraphLaunch(ci->graph[cur], st);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    ci->cur ^= 1;
+  }
+  return EXC_OK;
+}
+
+template <typename T>
+static void case_destroy(exc_case* cs) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  if (!ci) return;
+  for (int k = 0; k < 2; ++k) if (ci->graph[k]) cudaGraphExecDestroy(ci->graph[k]);
+  poisson_free(&ci->ps);
+  if (ci->u[0]) cudaFree(ci->u[0]);
+  if (ci->dscal) cudaFree(ci->dscal);
+  if (ci->dflag) cudaFree(ci->dflag);
+  if (ci->part) cudaFree(ci->part);
+  for (int li = 0; li < ci->nles; ++li) {
+    poisson_free(&ci->les[li].ps);
+    if (ci->les[li].buf) cudaFree(ci->les[li].buf);
+  }
+  delete ci;
+  cs->impl = nullptr;
+}
+
+template <typename T>
+static int case_create(exc_case* cs) {
+  const exc_case_desc& d = cs->desc;
+  CaseImpl<T>* ci = new CaseImpl<T>();
+  cs->impl = ci;
+  cs->step_fn = case_step<T>;
+  cs->destroy_fn = case_destroy<T>;
+  ci->n = d.n;
+  ci->N = (long long)d.n * d.n * d.n;
+  ci->h = d.l / d.n;
+  int rc = poisson_init(&ci->ps, cs->precision, d.n, d.l, nullptr);
+  if (rc) return rc;
+  size_t vb = 3 * ci->N * sizeof(T);
+  void* big = nullptr;
+  if (cudaMalloc(&big, 4 * vb) != cudaSuccess) { set_last_error("out of device memory (DNS fields)"); return EXC_ERR_OOM; }
+  ci->u[0] = reinterpret_cast<T*>(big);
+  ci->u[1] = ci->u[0] + 3 * ci->N;
+  ci->us = ci->u[1] + 3 * ci->N;
+  ci->rhs = ci->us + 3 * ci->N;
+  cudaMemset(big, 0, 4 * vb);
+  if (cudaMalloc(&ci->dscal, 16 * sizeof(double)) != cudaSuccess || cudaMalloc(&ci->dflag, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ci->part, (size_t)(SHELL_BLOCKS * 1024 + 2 * 1024) * sizeof(double)) != cudaSuccess) {
+    set_last_error("out of device memory (scalars)");
+    return EXC_ERR_OOM;
+  }
+  cudaMemset(ci->dscal, 0, 16 * sizeof(double));
+  cudaMemset(ci->dflag, 0, sizeof(int));
+  ci->nles = d.nles;
+  for (int li = 0; li < d.nles; ++li) {
+    LesState<T>& L = ci->les[li];
+    L.c = d.les[li].ratio;
+    L.kind = d.les[li].kind;
+    L.m = d.n / L.c;
+    L.M = (long long)L.m * L.m * L.m;
+    rc = poisson_init(&L.ps, cs->precision, L.m, d.l, nullptr);
+    if (rc) return rc;
+    size_t nb = 14 * 3 * L.M * sizeof(T);
+    if (cudaMalloc(&L.buf, nb) != cudaSuccess) { set_last_error("out of device memory (LES fields)"); return EXC_ERR_OOM; }
+    cudaMemset(L.buf, 0, nb);
+    T* p = L.buf;
+    auto take = [&]() { T* q = p; p += 3 * L.M; return q; };
+    L.ub = take(); L.fk = take(); L.mcl = take(); L.mlast = take(); L.rtmp = take();
+    L.ve[0] = take(); L.ve[1] = take(); L.ves = take(); L.ke = take();
+    L.vn[0] = take(); L.vn[1] = take(); L.vns = take(); L.kn = take();
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host-facing helpers (templated)
+// ---------------------------------------------------------------------------
+template <typename T>
+static int reset_les(exc_case* cs) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaStream_t st = cs->stream;
+  for (int li = 0; li < ci->nles; ++li) {
+    LesState<T>& L = ci->les[li];
+    int rc = les_target<T>(ci, L, ci->u[ci->cur], L.ub, st);
+    if (rc) return rc;
+    size_t b = 3 * L.M * sizeof(T);
+    cudaMemcpyAsync(L.ve[ci->cur], L.ub, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(L.vn[ci->cur], L.ub, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(L.mlast, 0, b, st);
+  }
+  cudaMemsetAsync(ci->dscal, 0, 16 * sizeof(double), st);
+  cudaMemsetAsync(ci->dflag, 0, sizeof(int), st);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+template <typename T>
+static int set_velocity(exc_case* cs, const double* host) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaStream_t st = cs->stream;
+  size_t cnt = 3 * ci->N;
+  if (sizeof(T) == sizeof(double)) {
+    cudaError_t e = cudaMemcpyAsync(ci->u[ci->cur], host, cnt * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  } else {
+    // stage through the (double-sized) rhs+us region
+    double* tmp = reinterpret_cast<double*>(ci->us);
+    cudaError_t e = cudaMemcpyAsync(tmp, host, cnt * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_convert<double, T>((long long)cnt, tmp, ci->u[ci->cur], st);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  }
+  return reset_les<T>(cs);
+}
+
+template <typename T>
+static int download(exc_case* cs, const T* dev, long long cnt, double* host) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaStream_t st = cs->stream;
+  cudaError_t e;
+  if (sizeof(T) == sizeof(double)) {
+    e = cudaMemcpyAsync(host, dev, cnt * sizeof(double), cudaMemcpyDeviceToHost, st);
+  } else {
+    // us and rhs are adjacent: 6 n^3 floats = 3 n^3 doubles of scratch
+    double* tmp = reinterpret_cast<double*>(ci->us);
+    e = launch_convert<T, double>(cnt, dev, tmp, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, tmp, cnt * sizeof(double), cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+// Random solenoidal field with the peak spectrum (src/N.jl:394-476).
+template <typename T>
+static int init_random(exc_case* cs, double kpeak, double energy, uint64_t seed) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaStream_t st = cs->stream;
+  const int n = ci->n, P = ci->ps.P;
+  T* u = ci->u[ci->cur];
+  cudaError_t e = launch_normals<T>(3 * ci->N, (unsigned long long)seed, u, st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  int rc = project_vec<T>(&ci->ps, u, st);
+  if (rc) return rc;
+  // three spectra
+  using C = cplx<T>;
+  const long long cstride = (long long)n * n * P;
+  C* spec = nullptr;
+  if (cudaMalloc(&spec, 3 * cstride * sizeof(C)) != cudaSuccess) { set_last_error("out of device memory (init spectra)"); return EXC_ERR_OOM; }
+  cudaMemsetAsync(spec, 0, 3 * cstride * sizeof(C), st);
+  exc_poisson tmp = ci->ps;
+  for (int c = 0; c < 3; ++c) {
+    tmp.work = spec + c * cstride;
+    e = fft3d_forward<T>(&tmp, u + c * ci->N, st);
+    if (e != cudaSuccess) break;
+  }
+  const int kmax = n / 2;
+  const int kdiag = (int)std::floor(std::sqrt(3.0) * kmax);
+  const int nshell = kdiag + 1;
+  double* eshell = ci->part + SHELL_BLOCKS * 1024;  // nshell <= 1024
+  double* factor = eshell + 1024;
+  double* partials = ci->part;
+  const double N = (double)ci->N;
+  if (e == cudaSuccess)
+    e = launch_shell_energy<T>(n, P, 3, spec, cstride, 1.0 / (N * N), nshell, partials, SHELL_BLOCKS, eshell, st);
+  if (e == cudaSuccess) e = launch_shell_factor(nshell, kpeak, energy, eshell, factor, st);
+  if (e == cudaSuccess) e = launch_shell_scale<T>(n, P, 3, spec, cstride, nshell, factor, st);
+  for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+    tmp.work = spec + c * cstride;
+    e = fft3d_inverse<T>(&tmp, st);
+    if (e == cudaSuccess)
+      e = launch_unpitch<T>(n, reinterpret_cast<const T*>(tmp.work), 2 * P, u + c * ci->N, (T)(1.0 / N), st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(spec);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  rc = project_vec<T>(&ci->ps, u, st);
+  if (rc) return rc;
+  return reset_les<T>(cs);
+}
+
+template <typename T>
+static int les_field(exc_case* cs, int li, int which, double* host) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  LesState<T>& L = ci->les[li];
+  const T* src = nullptr;
+  if (which == 0) {
+    int rc = les_target<T>(ci, L, ci->u[ci->cur], L.ub, cs->stream);
+    if (rc) return rc;
+    src = L.ub;
+  } else if (which == 1) src = L.ve[ci->cur];
+  else if (which == 2) src = L.vn[ci->cur];
+  else src = L.mlast;
+  return download<T>(cs, src, 3 * L.M, host);
+}
+
+template <typename T>
+static int les_errors(exc_case* cs, int li, double* err2) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  LesState<T>& L = ci->les[li];
+  cudaStream_t st = cs->stream;
+  int rc = les_target<T>(ci, L, ci->u[ci->cur], L.ub, st);
+  if (rc) return rc;
+  double* out = ci->dscal + 4;  // 4..9: per-component pairs
+  double host[2][6];
+  for (int which = 0; which < 2; ++which) {
+    const T* v = which == 0 ? L.ve[ci->cur] : L.vn[ci->cur];
+    for (int c = 0; c < 3; ++c) {
+      cudaError_t e = launch_sqdiff<T>(L.M, v + c * L.M, L.ub + c * L.M, ci->part, out + 2 * c, st);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    }
+    cudaError_t e = cudaMemcpyAsync(host[which], out, 6 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  }
+  // compute_errors (src/N.jl:1334-1349): sqrt(mean_i sum|a_i-b_i|^2 / sum|b_i|^2)
+  for (int which = 0; which < 2; ++which) {
+    double s = 0;
+    for (int c = 0; c < 3; ++c) s += host[which][2 * c] / host[which][2 * c + 1];
+    err2[which] = std::sqrt(s / 3.0);
+  }
+  return EXC_OK;
+}
+
+template <typename T>
+static int energy(exc_case* cs, double* out) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaStream_t st = cs->stream;
+  double* dv = ci->dscal + 10;
+  cudaError_t e = launch_sqdiff<T>(3 * ci->N, ci->u[ci->cur], nullptr, ci->part, dv, st);
+  double host[2];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, dv, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  *out = host[0] / 2.0 / (double)ci->N;
+  return EXC_OK;
+}
+
+template <typename T>
+static int spectrum(exc_case* cs, double* host_e, int nshell) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaStream_t st = cs->stream;
+  const int n = ci->n, P = ci->ps.P;
+  using C = cplx<T>;
+  const long long cstride = (long long)n * n * P;
+  C* spec = nullptr;
+  if (cudaMalloc(&spec, 3 * cstride * sizeof(C)) != cudaSuccess) { set_last_error("out of device memory (spectrum)"); return EXC_ERR_OOM; }
+  exc_poisson tmp = ci->ps;
+  cudaError_t e = cudaSuccess;
+  for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+    tmp.work = spec + c * cstride;
+    e = fft3d_forward<T>(&tmp, ci->u[ci->cur] + c * ci->N, st);
+  }
+  const int nfull = (int)std::floor(std::sqrt(3.0) * (n / 2)) + 1;
+  double* eshell = ci->part + SHELL_BLOCKS * 1024;
+  const double N = (double)ci->N;
+  if (e == cudaSuccess)
+    e = launch_shell_energy<T>(n, P, 3, spec, cstride, 1.0 / (N * N), nfull, ci->part, SHELL_BLOCKS, eshell, st);
+  std::vector<double> all(nfull);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(all.data(), eshell, nfull * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(spec);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  for (int k = 1; k <= nshell && k < nfull; ++k) host_e[k - 1] = all[k];
+  return EXC_OK;
+}
+
+template <typename T>
+static int launches(exc_case* cs) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  return ci->kernels_per_step;
+}
+
+template <typename T>
+static void* device_ptr(exc_case* cs) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  return ci->u[ci->cur];
+}
+
+template <typename T>
+static int read_scalars(exc_case* cs, double* host3, int* flag) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaError_t e = cudaMemcpyAsync(host3, ci->dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost, cs->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(flag, ci->dflag, sizeof(int), cudaMemcpyDeviceToHost, cs->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs->stream);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+}  // namespace exc
+
+using namespace exc;
+
+#define DISPATCH(cs, fn, ...) ((cs)->precision == EXC_F64 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
+
+extern "C" {
+
+int exc_case_create(const exc_case_desc* desc, void* stream, exc_case** out) {
+  if (!desc || !out) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  *out = nullptr;
+  if (!fft_size_ok(desc->n)) { set_last_error("DNS grid size must be 2^a 3^b, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (desc->precision != EXC_F64 && desc->precision != EXC_F32) { set_last_error("bad precision"); return EXC_ERR_ARG; }
+  if (!(desc->l > 0) || !(desc->visc > 0) || !(desc->cfl > 0)) { set_last_error("l, visc and cfl must be positive"); return EXC_ERR_ARG; }
+  if (desc->nles < 0 || desc->nles > EXC_MAX_LES) { set_last_error("nles out of range"); return EXC_ERR_ARG; }
+  for (int i = 0; i < desc->nles; ++i) {
+    int c = desc->les[i].ratio;
+    if (c < 1 || desc->n % c != 0) { set_last_error("LES ratio must divide n"); return EXC_ERR_RATIO; }
+    if (!fft_size_ok(desc->n / c)) { set_last_error("LES grid size n/ratio must be 2^a 3^b, a >= 1, >= 4"); return EXC_ERR_RATIO; }
+    if (desc->les[i].kind != EXC_FILTER_VOLUME && desc->les[i].kind != EXC_FILTER_FACE) { set_last_error("bad filter kind"); return EXC_ERR_ARG; }
+  }
+  exc_case* cs = new exc_case();
+  cs->desc = *desc;
+  cs->precision = desc->precision;
+  cs->stream = reinterpret_cast<cudaStream_t>(stream);
+  if (!cs->stream) {
+    // graph capture needs a real stream
+    if (cudaStreamCreateWithFlags(&cs->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete cs;
+      set_last_error("cannot create a CUDA stream");
+      return EXC_ERR_CUDA;
+    }
+    cs->own_stream = true;
+  }
+  int rc = configure_device();
+  if (rc == EXC_OK) rc = DISPATCH(cs, case_create, cs);
+  if (rc) {
+    if (cs->destroy_fn) cs->destroy_fn(cs);
+    if (cs->own_stream) cudaStreamDestroy(cs->stream);
+    delete cs;
+    return rc;
+  }
+  *out = cs;
+  return EXC_OK;
+}
+
+int exc_case_destroy(exc_case* cs) {
+  if (!cs) return EXC_OK;
+  cudaStreamSynchronize(cs->stream);
+  if (cs->destroy_fn) cs->destroy_fn(cs);
+  if (cs->own_stream) cudaStreamDestroy(cs->stream);
+  delete cs;
+  return EXC_OK;
+}
+
+int exc_case_init_random(exc_case* cs, double kpeak, double energy_, uint64_t seed) {
+  if (!cs || !(kpeak > 0) || !(energy_ > 0)) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, init_random, cs, kpeak, energy_, seed);
+}
+
+int exc_case_set_velocity(exc_case* cs, const double* host_u) {
+  if (!cs || !host_u) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, set_velocity, cs, host_u);
+}
+
+int exc_case_get_velocity(exc_case* cs, double* host_u) {
+  if (!cs || !host_u) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  long long cnt = 3LL * cs->desc.n * cs->desc.n * cs->desc.n;
+  if (cs->precision == EXC_F64)
+    return download<double>(cs, reinterpret_cast<const double*>(device_ptr<double>(cs)), cnt, host_u);
+  return download<float>(cs, reinterpret_cast<const float*>(device_ptr<float>(cs)), cnt, host_u);
+}
+
+int exc_case_get_les(exc_case* cs, int li, int which, double* host) {
+  if (!cs || !host || li < 0 || li >= cs->desc.nles || which < 0 || which > 3) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, les_field, cs, li, which, host);
+}
+
+int exc_case_step(exc_case* cs, int nsteps, double dt_fixed) {
+  if (!cs || nsteps < 0) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return cs->step_fn(cs, nsteps, dt_fixed);
+}
+
+int exc_case_errors(exc_case* cs, int li, double* err2) {
+  if (!cs || !err2 || li < 0 || li >= cs->desc.nles) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, les_errors, cs, li, err2);
+}
+
+int exc_case_time(exc_case* cs, double* t, double* last_dt) {
+  if (!cs) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  double h3[3];
+  int flag = 0;
+  int rc = DISPATCH(cs, read_scalars, cs, h3, &flag);
+  if (rc) return rc;
+  if (t) *t = h3[1];
+  if (last_dt) *last_dt = h3[0];
+  return EXC_OK;
+}
+
+int exc_case_energy(exc_case* cs, double* e) {
+  if (!cs || !e) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, energy, cs, e);
+}
+
+int exc_case_spectrum(exc_case* cs, double* host_e, int nshell) {
+  if (!cs || !host_e || nshell < 1) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, spectrum, cs, host_e, nshell);
+}
+
+int exc_case_device_ptr(exc_case* cs, int which, void** ptr) {
+  if (!cs || !ptr || which != 0) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  *ptr = DISPATCH(cs, device_ptr, cs);
+  return EXC_OK;
+}
+
+int exc_case_launches_per_step(exc_case* cs, int* count) {
+  if (!cs || !count) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  *count = DISPATCH(cs, launches, cs);
+  if (*count == 0) { set_last_error("no step has been captured yet"); return EXC_ERR_STATE; }
+  return EXC_OK;
+}
+
+int exc_case_sync(exc_case* cs) {
+  if (!cs) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  double h3[3];
+  int flag = 0;
+  int rc = DISPATCH(cs, read_scalars, cs, h3, &flag);
+  if (rc) return rc;
+  if (flag) { set_last_error("non-finite DNS velocity detected"); return EXC_ERR_NONFINITE; }
+  return EXC_OK;
+}
+
+}  // extern "C"

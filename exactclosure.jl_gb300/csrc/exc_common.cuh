@@ -1,0 +1,76 @@
+// Common types and helpers of libexc (GB300 / sm_103a).
+//
+// Field layout (the reference's column-major Field, src/N.jl:29 and :45): a
+// scalar field is n^3 contiguous words, x fastest; a vector field is three
+// such arrays, component slowest.  The spectral work array is
+// [n][n][P] complex with P = pad8(n/2 + 1) (the rfft half axis is x, like
+// FFTW's first-dimension halving in src/N.jl:207-217); its real view holds
+// the pressure as [n][n][2P] words after the inverse transform.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+#include "../../include/exc.h"
+
+namespace exc {
+
+template <typename T> struct cplx_t;
+template <> struct cplx_t<double> { using type = double2; };
+template <> struct cplx_t<float> { using type = float2; };
+template <typename T> using cplx = typename cplx_t<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T a, T b) { cplx<T> r; r.x = a; r.y = b; return r; }
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+// a * b
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+  C r;
+  r.x = fma(a.x, b.x, -a.y * b.y);
+  r.y = fma(a.x, b.y, a.y * b.x);
+  return r;
+}
+// a * conj(b)
+template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b) {
+  C r;
+  r.x = fma(a.x, b.x, a.y * b.y);
+  r.y = fma(a.y, b.x, -a.x * b.y);
+  return r;
+}
+template <typename C> __host__ __device__ __forceinline__ C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV, typename C> __host__ __device__ __forceinline__ C mul_mi(C a) {
+  C r;
+  if (INV) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; }
+  return r;
+}
+
+__host__ __device__ __forceinline__ int pad8(int m) { return (m + 7) & ~7; }
+__host__ __device__ __forceinline__ int spec_pitch(int n) { return pad8(n / 2 + 1); }
+
+// Periodic neighbour index along one axis.
+__device__ __forceinline__ int wrap_up(int i, int n) { return (i + 1 == n) ? 0 : i + 1; }
+__device__ __forceinline__ int wrap_dn(int i, int n) { return (i == 0) ? n - 1 : i - 1; }
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Grid sizes the FFT supports: n = 2^a 3^b with a >= 1, 4 <= n <= 1024.
+inline bool fft_size_ok(int n) {
+  if (n < 4 || n > 1024 || (n & 1)) return false;
+  int m = n;
+  while (m % 2 == 0) m /= 2;
+  while (m % 3 == 0) m /= 3;
+  return m == 1;
+}
+
+}  // namespace exc
+
+#define EXC_CHECK_CUDA(call)                               \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) { exc::set_last_error(cudaGetErrorString(e_)); return EXC_ERR_CUDA; } \
+  } while (0)
+
+namespace exc {
+void set_last_error(const char* msg);
+}

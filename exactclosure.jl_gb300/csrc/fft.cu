@@ -1,0 +1,389 @@
+// FFT Poisson solver: R2C along x, complex passes along y and z with the
+// spectral divide of `project!` (src/N.jl:272-298) fused between the forward
+// and inverse z transforms, then C2R along x back into the work array.
+#include <cmath>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace exc {
+
+// ---------------------------------------------------------------------------
+// x pass, real -> half complex.  A CTA transforms `rows` x-lines of n reals as
+// complex lines of length n/2 (z_m = x_2m + i x_2m+1) and untangles them:
+//   X_k = (Z_k + conj Z_{n/2-k})/2 - (i/2) W_n^k (Z_k - conj Z_{n/2-k}).
+// With DIV the input line is d = div(u) (src/N.jl:222-238) computed on the fly.
+// ---------------------------------------------------------------------------
+template <typename T, bool DIV>
+__global__ void __launch_bounds__(FFT_THREADS)
+r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ out, int P,
+             const cplx<T>* __restrict__ tw, FftPlan plan, int rows_per_cta) {
+  using C = cplx<T>;
+  extern __shared__ unsigned char smem_raw[];
+  C* s = reinterpret_cast<C*>(smem_raw);
+  const int N2 = n / 2;
+  const int ls = N2 + 1;
+  const long long nn = (long long)n * n;
+  const long long N = nn * n;
+  const long long row0 = (long long)blockIdx.x * rows_per_cta;
+  const int rows = (int)min((long long)rows_per_cta, nn - row0);
+  // load
+  for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
+    int r = t / N2, m = t - r * N2;
+    long long row = row0 + r;
+    long long base = row * n;
+    T a, b;
+    if (!DIV) {
+      a = src[base + 2 * m];
+      b = src[base + 2 * m + 1];
+    } else {
+      int y = (int)(row % n), z = (int)(row / n);
+      long long rowy = (long long)z * n + (y == 0 ? n - 1 : y - 1);
+      long long rowz = (long long)(z == 0 ? n - 1 : z - 1) * n + y;
+      const T* ux = src;
+      const T* uy = src + N;
+      const T* uz = src + 2 * N;
+      int x0 = 2 * m, x1 = 2 * m + 1;
+      int xm = (x0 == 0) ? n - 1 : x0 - 1;
+      a = ((ux[base + x0] - ux[base + xm]) + (uy[base + x0] - uy[rowy * n + x0]) +
+           (uz[base + x0] - uz[rowz * n + x0])) * inv_h;
+      b = ((ux[base + x1] - ux[base + x0]) + (uy[base + x1] - uy[rowy * n + x1]) +
+           (uz[base + x1] - uz[rowz * n + x1])) * inv_h;
+    }
+    s[r * ls + m] = mk<T>(a, b);
+  }
+  __syncthreads();
+  fft_lines<false>(s, ls, rows, plan, tw, n);
+  // untangle and store k = 0..N2
+  for (int t = threadIdx.x; t < rows * (N2 + 1); t += blockDim.x) {
+    int r = t / (N2 + 1), k = t - r * (N2 + 1);
+    C zk = s[r * ls + (k == N2 ? 0 : k)];
+    C zc = cconj(s[r * ls + (k == 0 ? 0 : N2 - k)]);
+    C e = cadd(zk, zc);
+    C o = csub(zk, zc);
+    C w = tw[k];                  // W_n^k, k <= n/2 < n
+    C wo = cmul(o, w);            // W^k (Z_k - conj Z_{N2-k})
+    // X = e/2 - i/2 * wo
+    C X;
+    X.x = (T)0.5 * (e.x + wo.y);
+    X.y = (T)0.5 * (e.y - wo.x);
+    out[(row0 + r) * P + k] = X;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Column passes along y (elem_stride = P, outer = z) or z (elem_stride = n P,
+// outer = y): a CTA loads `W` consecutive kx columns of one outer index.
+// ---------------------------------------------------------------------------
+template <typename T, bool INV>
+__global__ void __launch_bounds__(FFT_THREADS)
+cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_stride,
+            long long outer_stride, const cplx<T>* __restrict__ tw, FftPlan plan) {
+  using C = cplx<T>;
+  extern __shared__ unsigned char smem_raw[];
+  C* s = reinterpret_cast<C*>(smem_raw);
+  const int ls = n + 1;
+  const int kx0 = blockIdx.x * W;
+  const int lines = min(W, nkx - kx0);
+  C* base = g + (long long)blockIdx.y * outer_stride + kx0;
+  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+    int e = t / lines, l = t - e * lines;
+    s[l * ls + e] = base[e * elem_stride + l];
+  }
+  __syncthreads();
+  fft_lines<INV>(s, ls, lines, plan, tw, n);
+  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+    int e = t / lines, l = t - e * lines;
+    base[e * elem_stride + l] = s[l * ls + e];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z pass with the spectral divide: forward FFT along z, multiply by
+// 1/(lambda N) with lambda = -4/h^2 sum_d sin^2(pi k_d/n) (src/N.jl:281-291)
+// and the mean mode set to zero (src/N.jl:298), inverse FFT along z.  The
+// divide is computed in float64 for every precision.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(FFT_THREADS)
+zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<T>* __restrict__ tw,
+              FftPlan plan, const double* __restrict__ sin2, double coef) {
+  using C = cplx<T>;
+  extern __shared__ unsigned char smem_raw[];
+  C* s = reinterpret_cast<C*>(smem_raw);
+  const int ls = n + 1;
+  const int kx0 = blockIdx.x * W;
+  const int ky = blockIdx.y;
+  const int lines = min(W, nkx - kx0);
+  const long long es = (long long)n * P;
+  C* base = g + (long long)ky * P + kx0;
+  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+    int e = t / lines, l = t - e * lines;
+    s[l * ls + e] = base[e * es + l];
+  }
+  __syncthreads();
+  fft_lines<false>(s, ls, lines, plan, tw, n);
+  const double sy = sin2[ky];
+  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+    int l = t / n, kz = t - l * n;
+    int kx = kx0 + l;
+    double den = sin2[kx] + sy + sin2[kz];
+    double f = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef / den;
+    C v = s[l * ls + kz];
+    v.x = (T)((double)v.x * f);
+    v.y = (T)((double)v.y * f);
+    s[l * ls + kz] = v;
+  }
+  __syncthreads();
+  fft_lines<true>(s, ls, lines, plan, tw, n);
+  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+    int e = t / lines, l = t - e * lines;
+    base[e * es + l] = s[l * ls + e];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x pass, half complex -> real, in place (row pitch P complex = 2P reals):
+//   Z_k = (X_k + conj X_{N2-k}) + i W_n^-k (X_k - conj X_{N2-k}),
+//   z = IDFT_{N2}(Z) (unnormalised), x_2m = Re z_m, x_2m+1 = Im z_m.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(FFT_THREADS)
+c2r_x_kernel(cplx<T>* __restrict__ g, int n, int P, const cplx<T>* __restrict__ tw, FftPlan plan,
+             int rows_per_cta) {
+  using C = cplx<T>;
+  extern __shared__ unsigned char smem_raw[];
+  C* s = reinterpret_cast<C*>(smem_raw);
+  const int N2 = n / 2;
+  const int ls = N2 + 1;
+  const long long nn = (long long)n * n;
+  const long long row0 = (long long)blockIdx.x * rows_per_cta;
+  const int rows = (int)min((long long)rows_per_cta, nn - row0);
+  for (int t = threadIdx.x; t < rows * (N2 + 1); t += blockDim.x) {
+    int r = t / (N2 + 1), k = t - r * (N2 + 1);
+    s[r * ls + k] = g[(row0 + r) * P + k];
+  }
+  __syncthreads();
+  // pairs (k, N2-k) handled by one thread, so the tangle is in place
+  const int half = N2 / 2 + 1;
+  for (int t = threadIdx.x; t < rows * half; t += blockDim.x) {
+    int r = t / half, k = t - r * half;
+    int k2 = N2 - k;
+    C xa = s[r * ls + k], xb = s[r * ls + k2];
+    C wa = tw[k], wb = tw[k2];
+    // Z_k
+    C e = cadd(xa, cconj(xb));
+    C o = cmulc(csub(xa, cconj(xb)), wa);  // W^-k (X_k - conj X_k2)
+    C za; za.x = e.x - o.y; za.y = e.y + o.x;
+    // Z_k2
+    C e2 = cadd(xb, cconj(xa));
+    C o2 = cmulc(csub(xb, cconj(xa)), wb);
+    C zb; zb.x = e2.x - o2.y; zb.y = e2.y + o2.x;
+    if (k < N2) s[r * ls + k] = za;
+    if (k2 < N2 && k2 != k) s[r * ls + k2] = zb;
+  }
+  __syncthreads();
+  fft_lines<true>(s, ls, rows, plan, tw, n);
+  T* gr = reinterpret_cast<T*>(g);
+  for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
+    int r = t / N2, m = t - r * N2;
+    C z = s[r * ls + m];
+    T* row = gr + (row0 + r) * (2LL * P);
+    row[2 * m] = z.x;
+    row[2 * m + 1] = z.y;
+  }
+}
+
+template <typename T>
+__global__ void copy_pitched_kernel(const T* __restrict__ src, int pitch, T* __restrict__ dst, int n) {
+  long long N = (long long)n * n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long row = i / n;
+    int x = (int)(i - row * n);
+    dst[i] = src[row * pitch + x];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static int col_width(int n) {
+  int w = 1;
+  while (w * 2 * n <= FFT_TILE && w < 64) w *= 2;
+  return w;
+}
+
+template <typename T>
+cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st) {
+  using C = cplx<T>;
+  const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
+  C* g = reinterpret_cast<C*>(ps->work);
+  const C* tw = reinterpret_cast<const C*>(ps->tw);
+  const long long nn = (long long)n * n;
+  // x forward
+  int rows = FFT_TILE / (N2 + 1);
+  if (rows > nn) rows = (int)nn;
+  size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
+  int gx = (int)((nn + rows - 1) / rows);
+  if (src_is_vector)
+    r2c_x_kernel<T, true><<<gx, FFT_THREADS, shx, st>>>(src, n, (T)(1.0 / ps->h), g, P, tw, ps->plan_h, rows);
+  else
+    r2c_x_kernel<T, false><<<gx, FFT_THREADS, shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows);
+  // y forward
+  int W = col_width(n);
+  dim3 gc((nkx + W - 1) / W, n);
+  size_t shc = (size_t)W * (n + 1) * sizeof(C);
+  cols_kernel<T, false><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  // z forward + divide + inverse; coef = 1/(lambda N) numerator: -h^2/(4 N)
+  double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
+  zsolve_kernel<T><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef);
+  // y inverse
+  cols_kernel<T, true><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  // x inverse (in place)
+  c2r_x_kernel<T><<<gx, FFT_THREADS, shx, st>>>(g, n, P, tw, ps->plan_h, rows);
+  return cudaGetLastError();
+}
+
+// Plain 3-D real transforms on the work array (no divide): forward leaves the
+// half spectrum [n][n][P]; inverse (unnormalised) leaves reals at pitch 2P.
+template <typename T>
+cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st) {
+  using C = cplx<T>;
+  const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
+  C* g = reinterpret_cast<C*>(ps->work);
+  const C* tw = reinterpret_cast<const C*>(ps->tw);
+  const long long nn = (long long)n * n;
+  int rows = FFT_TILE / (N2 + 1);
+  if (rows > nn) rows = (int)nn;
+  size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
+  int gx = (int)((nn + rows - 1) / rows);
+  r2c_x_kernel<T, false><<<gx, FFT_THREADS, shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows);
+  int W = col_width(n);
+  dim3 gc((nkx + W - 1) / W, n);
+  size_t shc = (size_t)W * (n + 1) * sizeof(C);
+  cols_kernel<T, false><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  cols_kernel<T, false><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t fft3d_inverse(exc_poisson* ps, cudaStream_t st) {
+  using C = cplx<T>;
+  const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
+  C* g = reinterpret_cast<C*>(ps->work);
+  const C* tw = reinterpret_cast<const C*>(ps->tw);
+  const long long nn = (long long)n * n;
+  int W = col_width(n);
+  dim3 gc((nkx + W - 1) / W, n);
+  size_t shc = (size_t)W * (n + 1) * sizeof(C);
+  cols_kernel<T, true><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n);
+  cols_kernel<T, true><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  int rows = FFT_TILE / (N2 + 1);
+  if (rows > nn) rows = (int)nn;
+  size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
+  int gx = (int)((nn + rows - 1) / rows);
+  c2r_x_kernel<T><<<gx, FFT_THREADS, shx, st>>>(g, n, P, tw, ps->plan_h, rows);
+  return cudaGetLastError();
+}
+
+template cudaError_t fft3d_forward<double>(exc_poisson*, const double*, cudaStream_t);
+template cudaError_t fft3d_forward<float>(exc_poisson*, const float*, cudaStream_t);
+template cudaError_t fft3d_inverse<double>(exc_poisson*, cudaStream_t);
+template cudaError_t fft3d_inverse<float>(exc_poisson*, cudaStream_t);
+
+template <typename T>
+cudaError_t copy_pressure(const exc_poisson* ps, T* p, cudaStream_t st) {
+  long long N = (long long)ps->n * ps->n * ps->n;
+  int blocks = (int)std::min<long long>((N + 255) / 256, 152LL * 16);
+  copy_pitched_kernel<T><<<blocks, 256, 0, st>>>(reinterpret_cast<const T*>(ps->work), 2 * ps->P, p, ps->n);
+  return cudaGetLastError();
+}
+
+template cudaError_t poisson_solve_inplace<double>(exc_poisson*, const double*, bool, cudaStream_t);
+template cudaError_t poisson_solve_inplace<float>(exc_poisson*, const float*, bool, cudaStream_t);
+template cudaError_t copy_pressure<double>(const exc_poisson*, double*, cudaStream_t);
+template cudaError_t copy_pressure<float>(const exc_poisson*, float*, cudaStream_t);
+
+template <typename T>
+static cudaError_t configure_fft_t() {
+  using C = cplx<T>;
+  int maxsh = (int)(FFT_TILE + 64 * 2) * (int)sizeof(C);
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(cols_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(cols_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(zsolve_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(c2r_x_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+cudaError_t configure_fft() {
+  cudaError_t e = configure_fft_t<double>();
+  if (e == cudaSuccess) e = configure_fft_t<float>();
+  return e;
+}
+
+int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
+  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!(l > 0)) { set_last_error("domain size must be positive"); return EXC_ERR_ARG; }
+  if (precision != EXC_F64 && precision != EXC_F32) { set_last_error("bad precision"); return EXC_ERR_ARG; }
+  ps->precision = precision;
+  ps->n = n;
+  ps->l = l;
+  ps->h = l / n;
+  ps->P = spec_pitch(n);
+  ps->plan_n = make_plan(n);
+  ps->plan_h = make_plan(n / 2);
+  size_t csz = precision == EXC_F64 ? sizeof(double2) : sizeof(float2);
+  int crc = configure_device();
+  if (crc) return crc;
+  // twiddles W_n^m and sin^2 table, from long double on the host
+  std::vector<double2> twd(n);
+  std::vector<float2> twf(n);
+  std::vector<double> s2(n);
+  const long double pi_l = 3.141592653589793238462643383279502884L;
+  for (int m = 0; m < n; ++m) {
+    long double a = -2.0L * pi_l * (long double)m / (long double)n;
+    double c = (double)cosl(a), s = (double)sinl(a);
+    twd[m] = make_double2(c, s);
+    twf[m] = make_float2((float)cosl(a), (float)sinl(a));
+    long double sn = sinl(pi_l * (long double)m / (long double)n);
+    s2[m] = (double)(sn * sn);
+  }
+  if (cudaMalloc(&ps->tw, n * csz) != cudaSuccess || cudaMalloc(&ps->sin2, n * sizeof(double)) != cudaSuccess) {
+    set_last_error("out of device memory (poisson tables)");
+    poisson_free(ps);
+    return EXC_ERR_OOM;
+  }
+  cudaMemcpy(ps->tw, precision == EXC_F64 ? (const void*)twd.data() : (const void*)twf.data(), n * csz,
+             cudaMemcpyHostToDevice);
+  cudaMemcpy(ps->sin2, s2.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+  size_t wbytes = (size_t)n * n * ps->P * csz;
+  if (work) {
+    ps->work = work;
+    ps->external_work = true;
+  } else {
+    if (cudaMalloc(&ps->work, wbytes) != cudaSuccess) {
+      set_last_error("out of device memory (poisson work array)");
+      poisson_free(ps);
+      return EXC_ERR_OOM;
+    }
+    cudaMemset(ps->work, 0, wbytes);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); poisson_free(ps); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+void poisson_free(exc_poisson* ps) {
+  if (ps->tw) cudaFree(ps->tw);
+  if (ps->sin2) cudaFree(ps->sin2);
+  if (ps->work && !ps->external_work) cudaFree(ps->work);
+  ps->tw = nullptr;
+  ps->sin2 = nullptr;
+  ps->work = nullptr;
+}
+
+}  // namespace exc

@@ -1,0 +1,371 @@
+// Pointwise field kernels: RK4 stage combination, the projected-RHS update
+// k = rhs - grad p, the counter-based normal generator, FP64 reductions and
+// the deterministic shell histogram used by `randomfield` and `spectrum`.
+#include "internal.cuh"
+#include "fields.cuh"
+
+namespace exc {
+
+static inline int grid_for(long long N, int threads = 256) {
+  long long b = (N + threads - 1) / threads;
+  return (int)(b < 152LL * 32 ? b : 152LL * 32);
+}
+
+// ---------------------------------------------------------------------------
+// k = rhs - grad p in place (rhs <- k), p read at pitch 2P from the Poisson
+// work array (`pressuregradient!`, src/N.jl:240-254), then the RK4 stage
+// combination of the tableau of `rk4_timestep!` (src/Burgers.jl:120-142):
+//   s = 0: xfin = x0 + dt/6 k;  xs = x0 + dt/2 k
+//   s = 1: xfin += dt/3 k;      xs = x0 + dt/2 k
+//   s = 2: xfin += dt/3 k;      xs = x0 + dt k
+//   s = 3: xfin += dt/6 k
+// ---------------------------------------------------------------------------
+template <typename T, bool GRAD>
+__global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __restrict__ p, int ppitch,
+                                const T* __restrict__ x0, T* __restrict__ xs, T* __restrict__ xfin, int stage,
+                                const double* __restrict__ dtp) {
+  const long long N = (long long)n * n * n;
+  const double dt = *dtp;
+  const T cf = (T)((stage == 0 || stage == 3) ? dt / 6.0 : dt / 3.0);
+  const T cs = (T)(stage == 2 ? dt : 0.5 * dt);
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
+    T k0 = k[g], k1 = k[N + g], k2 = k[2 * N + g];
+    if (GRAD) {
+      long long r = g / n;
+      int x = (int)(g - r * n);
+      int z = (int)(r / n);
+      int y = (int)(r - (long long)z * n);
+      T pc = p[r * ppitch + x];
+      T px = p[r * ppitch + wrap_up(x, n)];
+      T py = p[((long long)z * n + wrap_up(y, n)) * ppitch + x];
+      T pz = p[((long long)wrap_up(z, n) * n + y) * ppitch + x];
+      k0 -= (px - pc) * inv_h;
+      k1 -= (py - pc) * inv_h;
+      k2 -= (pz - pc) * inv_h;
+      k[g] = k0;
+      k[N + g] = k1;
+      k[2 * N + g] = k2;
+    }
+    T a0 = x0[g], a1 = x0[N + g], a2 = x0[2 * N + g];
+    if (stage == 0) {
+      xfin[g] = a0 + cf * k0;
+      xfin[N + g] = a1 + cf * k1;
+      xfin[2 * N + g] = a2 + cf * k2;
+    } else {
+      xfin[g] += cf * k0;
+      xfin[N + g] += cf * k1;
+      xfin[2 * N + g] += cf * k2;
+    }
+    if (stage < 3) {
+      xs[g] = a0 + cs * k0;
+      xs[N + g] = a1 + cs * k1;
+      xs[2 * N + g] = a2 + cs * k2;
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
+                            const double* dtp, cudaStream_t st) {
+  long long N = (long long)n * n * n;
+  if (p)
+    rk_stage_kernel<T, true><<<grid_for(N), 256, 0, st>>>(n, (T)(1.0 / (double)h), k, p, ppitch, x0, xs, xfin, stage, dtp);
+  else
+    rk_stage_kernel<T, false><<<grid_for(N), 256, 0, st>>>(n, (T)0, k, nullptr, 0, x0, xs, xfin, stage, dtp);
+  return cudaGetLastError();
+}
+
+// a = a + b * scale (elementwise, count words)
+template <typename T>
+__global__ void axpy_kernel(long long count, T* __restrict__ a, const T* __restrict__ b, T scale) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    a[i] += scale * b[i];
+}
+template <typename T>
+cudaError_t launch_axpy(long long count, T* a, const T* b, T scale, cudaStream_t st) {
+  axpy_kernel<T><<<grid_for(count), 256, 0, st>>>(count, a, b, scale);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// dt = min(cfl*h/umax, cfl*h^2/visc/6) (`propose_timestep`, src/N.jl:348-356),
+// or the fixed dt; flags a non-finite umax; advances the clock.
+// ---------------------------------------------------------------------------
+__global__ void set_dt_kernel(const double* __restrict__ umax, double h, double visc, double cfl, double fixed,
+                              double* __restrict__ dt, double* __restrict__ clock, int* __restrict__ flag) {
+  double m = *umax;
+  double d;
+  if (fixed > 0) d = fixed;
+  else {
+    double dt_adv = cfl * h / m;
+    double dt_visc = cfl * h * h / visc / 6.0;
+    d = dt_adv < dt_visc ? dt_adv : dt_visc;
+  }
+  if (!(m < 1e300)) { *flag = 1; d = 0.0; }
+  *dt = d;
+  *clock += d;
+}
+cudaError_t launch_set_dt(const double* umax, double h, double visc, double cfl, double fixed, double* dt,
+                          double* clock, int* flag, cudaStream_t st) {
+  set_dt_kernel<<<1, 1, 0, st>>>(umax, h, visc, cfl, fixed, dt, clock, flag);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Counter-based normals: splitmix64 of seed*phi + 2m (+1) -> two uniforms in
+// (0,1) -> Box-Muller.  The oracle evaluates the same formula.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long x) {
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+template <typename T>
+__global__ void normal_kernel(long long count, unsigned long long seed, T* __restrict__ out) {
+  const unsigned long long base = seed * 0x9E3779B97F4A7C15ull;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    unsigned long long m = (unsigned long long)i;
+    unsigned long long z1 = splitmix(base + 2ull * m);
+    unsigned long long z2 = splitmix(base + 2ull * m + 1ull);
+    double u1 = ((double)(z1 >> 11) + 0.5) * 0x1.0p-53;
+    double u2 = ((double)(z2 >> 11) + 0.5) * 0x1.0p-53;
+    out[i] = (T)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+  }
+}
+template <typename T>
+cudaError_t launch_normals(long long count, unsigned long long seed, T* out, cudaStream_t st) {
+  normal_kernel<T><<<grid_for(count), 256, 0, st>>>(count, seed, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic FP64 reductions.  Fixed grid; per-block partials; one block
+// folds them in index order.
+// ---------------------------------------------------------------------------
+constexpr int RED_BLOCKS = 304;
+
+// sums[0] = sum (a-b)^2, sums[1] = sum b^2 over count words (b may be null: sum a^2)
+template <typename T>
+__global__ void sqdiff_partial_kernel(long long count, const T* __restrict__ a, const T* __restrict__ b,
+                                      double* __restrict__ part) {
+  __shared__ double r0[256], r1[256];
+  double s0 = 0, s1 = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    double av = (double)a[i];
+    double bv = b ? (double)b[i] : 0.0;
+    double d = av - bv;
+    s0 += d * d;
+    s1 += bv * bv;
+  }
+  r0[threadIdx.x] = s0;
+  r1[threadIdx.x] = s1;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) { r0[threadIdx.x] += r0[threadIdx.x + o]; r1[threadIdx.x] += r1[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = r0[0]; part[2 * blockIdx.x + 1] = r1[0]; }
+}
+__global__ void fold_pairs_kernel(int nb, const double* __restrict__ part, double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    double s0 = 0, s1 = 0;
+    for (int b = 0; b < nb; ++b) { s0 += part[2 * b]; s1 += part[2 * b + 1]; }
+    out[0] = s0;
+    out[1] = s1;
+  }
+}
+template <typename T>
+cudaError_t launch_sqdiff(long long count, const T* a, const T* b, double* part, double* out, cudaStream_t st) {
+  sqdiff_partial_kernel<T><<<RED_BLOCKS, 256, 0, st>>>(count, a, b, part);
+  fold_pairs_kernel<<<1, 32, 0, st>>>(RED_BLOCKS, part, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Shell histogram on the rfft half grid: e = scale * sum_c |F_c|^2 / 2 with
+// the conjugate weight 2 for kx = 1..n/2-1 (src/N.jl:443, 534-543), binned by
+// shell k = isqrt(kx^2+ky^2+kz^2) (src/N.jl:375-392).  Lanes of a warp add in
+// lane order into the warp's shared row, warps fold in order, blocks fold in
+// order: bit-reproducible.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int isqrt_ll(long long v) {
+  long long r = (long long)sqrt((double)v);
+  while (r * r > v) --r;
+  while ((r + 1) * (r + 1) <= v) ++r;
+  return (int)r;
+}
+__device__ __forceinline__ int wavenum(int i, int n) { return i <= (n - 1) / 2 ? i : i - n; }
+
+template <typename T>
+__global__ void shell_partial_kernel(int n, int P, int ncomp, const cplx<T>* __restrict__ spec, long long cstride,
+                                     double scale, int nshell, double* __restrict__ part) {
+  extern __shared__ double acc[];  // [8][nshell]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < 8 * nshell; i += blockDim.x) acc[i] = 0.0;
+  __syncthreads();
+  const int nkx = n / 2 + 1;
+  const long long total = (long long)n * n * nkx;
+  double* my = acc + warp * nshell;
+  for (long long base = (long long)blockIdx.x * blockDim.x + warp * 32; base < total;
+       base += (long long)gridDim.x * blockDim.x) {
+    long long g = base + lane;
+    int sh = -1;
+    double e = 0.0;
+    if (g < total) {
+      long long r = g / nkx;
+      int kx = (int)(g - r * nkx);
+      int kz = (int)(r / n);
+      int ky = (int)(r - (long long)kz * n);
+      long long off = r * P + kx;
+      for (int c = 0; c < ncomp; ++c) {
+        cplx<T> v = spec[c * cstride + off];
+        e += ((double)v.x * v.x + (double)v.y * v.y);
+      }
+      double w = (kx >= 1 && kx <= n / 2 - 1) ? 2.0 : 1.0;
+      e *= 0.5 * scale * w;
+      int a = wavenum(ky, n), b = wavenum(kz, n);
+      long long kk = (long long)kx * kx + (long long)a * a + (long long)b * b;
+      sh = isqrt_ll(kk);
+      if (sh >= nshell) sh = -1;
+    }
+    for (int l = 0; l < 32; ++l) {
+      if (lane == l && sh >= 0) my[sh] += e;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int s = threadIdx.x; s < nshell; s += blockDim.x) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += acc[w * nshell + s];
+    part[(long long)blockIdx.x * nshell + s] = t;
+  }
+}
+__global__ void shell_fold_kernel(int nb, int nshell, const double* __restrict__ part, double* __restrict__ out) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nshell; s += gridDim.x * blockDim.x) {
+    double t = 0.0;
+    for (int b = 0; b < nb; ++b) t += part[(long long)b * nshell + s];
+    out[s] = t;
+  }
+}
+template <typename T>
+cudaError_t launch_shell_energy(int n, int P, int ncomp, const cplx<T>* spec, long long cstride, double scale,
+                                int nshell, double* part, int nblocks, double* out, cudaStream_t st) {
+  size_t sh = (size_t)8 * nshell * sizeof(double);
+  shell_partial_kernel<T><<<nblocks, 256, sh, st>>>(n, P, ncomp, spec, cstride, scale, nshell, part);
+  shell_fold_kernel<<<(nshell + 255) / 256, 256, 0, st>>>(nblocks, nshell, part, out);
+  return cudaGetLastError();
+}
+
+cudaError_t configure_fields() {
+  cudaError_t e = cudaFuncSetAttribute(shell_partial_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 80 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(shell_partial_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 80 * 1024);
+  return e;
+}
+
+// Multiply every mode of shell k (k <= kdiag) by factor[k] (src/N.jl:441-449).
+template <typename T>
+__global__ void shell_scale_kernel(int n, int P, int ncomp, cplx<T>* __restrict__ spec, long long cstride,
+                                   int nshell, const double* __restrict__ factor) {
+  const int nkx = n / 2 + 1;
+  const long long total = (long long)n * n * nkx;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+    long long r = g / nkx;
+    int kx = (int)(g - r * nkx);
+    int kz = (int)(r / n);
+    int ky = (int)(r - (long long)kz * n);
+    int a = wavenum(ky, n), b = wavenum(kz, n);
+    long long kk = (long long)kx * kx + (long long)a * a + (long long)b * b;
+    int sh = isqrt_ll(kk);
+    if (sh >= nshell) continue;
+    double f = factor[sh];
+    long long off = r * P + kx;
+    for (int c = 0; c < ncomp; ++c) {
+      cplx<T> v = spec[c * cstride + off];
+      v.x = (T)((double)v.x * f);
+      v.y = (T)((double)v.y * f);
+      spec[c * cstride + off] = v;
+    }
+  }
+}
+template <typename T>
+cudaError_t launch_shell_scale(int n, int P, int ncomp, cplx<T>* spec, long long cstride, int nshell,
+                               const double* factor, cudaStream_t st) {
+  long long total = (long long)n * n * (n / 2 + 1);
+  shell_scale_kernel<T><<<grid_for(total), 256, 0, st>>>(n, P, ncomp, spec, cstride, nshell, factor);
+  return cudaGetLastError();
+}
+
+// Host-side shell factors sqrt(E0/Eshell) with E0 = energy * profile(k) / sum
+// of profiles (src/N.jl:436-451); computed on the device to avoid a sync.
+__global__ void shell_factor_kernel(int nshell, double kpeak, double energy, const double* __restrict__ eshell,
+                                    double* __restrict__ factor) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double tot = 0.0;
+    for (int k = 0; k < nshell; ++k) {
+      double q = k / kpeak;
+      tot += (double)k * k * (double)k * k * exp(-2.0 * q * q);
+    }
+    for (int k = 0; k < nshell; ++k) {
+      double q = k / kpeak;
+      double prof = (double)k * k * (double)k * k * exp(-2.0 * q * q);
+      double e0 = energy * prof / tot;
+      double es = eshell[k];
+      factor[k] = es > 0 ? sqrt(e0 / es) : 1.0;
+    }
+  }
+}
+cudaError_t launch_shell_factor(int nshell, double kpeak, double energy, const double* eshell, double* factor,
+                                cudaStream_t st) {
+  shell_factor_kernel<<<1, 32, 0, st>>>(nshell, kpeak, energy, eshell, factor);
+  return cudaGetLastError();
+}
+
+// dense (n^3) <- pitched real view (row pitch `pitch` words), scaled
+template <typename T>
+__global__ void unpitch_kernel(int n, const T* __restrict__ src, int pitch, T* __restrict__ dst, T scale) {
+  long long N = (long long)n * n * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    long long row = i / n;
+    int x = (int)(i - row * n);
+    dst[i] = src[row * pitch + x] * scale;
+  }
+}
+template <typename T>
+cudaError_t launch_unpitch(int n, const T* src, int pitch, T* dst, T scale, cudaStream_t st) {
+  long long N = (long long)n * n * n;
+  unpitch_kernel<T><<<grid_for(N), 256, 0, st>>>(n, src, pitch, dst, scale);
+  return cudaGetLastError();
+}
+
+// precision conversion
+template <typename A, typename B>
+__global__ void convert_kernel(long long count, const A* __restrict__ a, B* __restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (B)a[i];
+}
+template <typename A, typename B>
+cudaError_t launch_convert(long long count, const A* a, B* b, cudaStream_t st) {
+  convert_kernel<A, B><<<grid_for(count), 256, 0, st>>>(count, a, b);
+  return cudaGetLastError();
+}
+
+#define INST(T)                                                                                                 \
+  template cudaError_t launch_rk_stage<T>(int, T, T*, const T*, int, const T*, T*, T*, int, const double*,      \
+                                          cudaStream_t);                                                        \
+  template cudaError_t launch_axpy<T>(long long, T*, const T*, T, cudaStream_t);                                \
+  template cudaError_t launch_normals<T>(long long, unsigned long long, T*, cudaStream_t);                      \
+  template cudaError_t launch_sqdiff<T>(long long, const T*, const T*, double*, double*, cudaStream_t);         \
+  template cudaError_t launch_shell_energy<T>(int, int, int, const cplx<T>*, long long, double, int, double*,   \
+                                              int, double*, cudaStream_t);                                      \
+  template cudaError_t launch_shell_scale<T>(int, int, int, cplx<T>*, long long, int, const double*,            \
+                                             cudaStream_t);                                                     \
+  template cudaError_t launch_unpitch<T>(int, const T*, int, T*, T, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+template cudaError_t launch_convert<double, float>(long long, const double*, float*, cudaStream_t);
+template cudaError_t launch_convert<float, double>(long long, const float*, double*, cudaStream_t);
+template cudaError_t launch_convert<double, double>(long long, const double*, double*, cudaStream_t);
+
+}  // namespace exc

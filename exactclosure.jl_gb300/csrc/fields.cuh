@@ -1,0 +1,35 @@
+// Pointwise field kernels and deterministic reductions (see fields.cu).
+#pragma once
+#include "exc_common.cuh"
+
+namespace exc {
+
+constexpr int SHELL_BLOCKS = 152;
+
+template <typename T>
+cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
+                            const double* dtp, cudaStream_t st);
+template <typename T>
+cudaError_t launch_axpy(long long count, T* a, const T* b, T scale, cudaStream_t st);
+cudaError_t launch_set_dt(const double* umax, double h, double visc, double cfl, double fixed, double* dt,
+                          double* clock, int* flag, cudaStream_t st);
+template <typename T>
+cudaError_t launch_normals(long long count, unsigned long long seed, T* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_sqdiff(long long count, const T* a, const T* b, double* part, double* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_shell_energy(int n, int P, int ncomp, const cplx<T>* spec, long long cstride, double scale,
+                                int nshell, double* part, int nblocks, double* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_shell_scale(int n, int P, int ncomp, cplx<T>* spec, long long cstride, int nshell,
+                               const double* factor, cudaStream_t st);
+cudaError_t launch_shell_factor(int nshell, double kpeak, double energy, const double* eshell, double* factor,
+                                cudaStream_t st);
+template <typename T>
+cudaError_t launch_unpitch(int n, const T* src, int pitch, T* dst, T scale, cudaStream_t st);
+template <typename A, typename B>
+cudaError_t launch_convert(long long count, const A* a, B* b, cudaStream_t st);
+
+constexpr int RED_PARTS = 304;
+
+}  // namespace exc

@@ -1,0 +1,30 @@
+// Separable filter stencils (see filter.cu).
+#pragma once
+#include "exc_common.cuh"
+
+namespace exc {
+
+constexpr int MAX_TAPS = 40;
+
+struct Taps1D {
+  int cnt;
+  int off[MAX_TAPS];
+  double w[MAX_TAPS];
+};
+struct Taps3 {
+  Taps1D a[3];  // x, y, z
+};
+
+Taps1D build_taps(int c, bool stag, bool point, const double* fdelta, int nfd);
+int make_taps3(int c, const bool stag[3], const bool point[3], const double* fdelta, int nfd, Taps3* out);
+
+template <typename T>
+int filter_vector(int n, int c, int kind, const double* fdelta, int nfd, const T* u, T* ub, cudaStream_t st);
+template <typename T>
+int closure_flux(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, const T* p,
+                 T* r9, cudaStream_t st);
+template <typename T>
+int filtered_stress(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, T* s6,
+                    cudaStream_t st);
+
+}  // namespace exc

@@ -1,0 +1,67 @@
+// Internal interfaces shared by the translation units of libexc.
+#pragma once
+#include "exc_common.cuh"
+#include "fft.cuh"
+
+// The FFT Poisson solver (`poissonsolver`, src/N.jl:202-220): spectral work
+// array, twiddles and plans for one grid.
+struct exc_poisson {
+  int precision = EXC_F64;
+  int n = 0;
+  double l = 1.0, h = 1.0;
+  int P = 0;               // padded half-axis pitch, complex words
+  void* work = nullptr;    // complex [n][n][P]; real view [n][n][2P]
+  void* tw = nullptr;      // W_n^m, m < n (precision's complex type)
+  double* sin2 = nullptr;  // sin^2(pi k / n), k < n
+  exc::FftPlan plan_n{}, plan_h{};
+  bool external_work = false;
+};
+
+namespace exc {
+
+// Allocate/free the device tables of a solver; `work` may be supplied by the
+// caller (external_work) and is otherwise allocated here.
+int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work);
+void poisson_free(exc_poisson* ps);
+
+// Pressure solve into the real view of ps->work (pitch 2P):
+//   src_is_vector: d = div(src) computed on the fly (scaled by 1/h),
+//   otherwise src is the scalar right-hand side d.
+template <typename T>
+cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st);
+
+// Plain forward (half spectrum into ps->work) and unnormalised inverse (reals
+// at pitch 2P in ps->work) 3-D transforms.
+template <typename T>
+cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st);
+template <typename T>
+cudaError_t fft3d_inverse(exc_poisson* ps, cudaStream_t st);
+
+// Shared-memory opt-ins of every kernel that needs them, once per device;
+// called before any launch (and so before any stream capture).
+int configure_device();
+cudaError_t configure_fft();
+cudaError_t configure_stencil();
+cudaError_t configure_fields();
+
+// Copy the pressure from the work array (pitch 2P) to a dense n^3 field.
+template <typename T>
+cudaError_t copy_pressure(const exc_poisson* ps, T* p, cudaStream_t st);
+
+// ---- stencil kernels (stencil.cu) ----
+template <typename T>
+cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st);
+template <typename T>
+cudaError_t launch_stress(int n, T h, T visc, const T* u, T* s6, cudaStream_t st);
+template <typename T>
+cudaError_t launch_tensordiv(int n, T h, int nsym, const T* s, T* du, bool doadd, cudaStream_t st);
+template <typename T>
+cudaError_t launch_divergence(int n, T h, const T* u, T* d, cudaStream_t st);
+// u_i -= (p[I+e_i] - p[I]) / h with p read at row pitch `ppitch` words.
+template <typename T>
+cudaError_t launch_gradient(int n, T h, T* u, const T* p, int ppitch, cudaStream_t st);
+template <typename T>
+cudaError_t launch_max_abs(size_t count, const T* x, double* out_dev, double* partial, int npartial,
+                           cudaStream_t st);
+
+}  // namespace exc

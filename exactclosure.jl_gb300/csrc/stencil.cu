@@ -1,0 +1,332 @@
+// Staggered-grid stencils: the convection-diffusion RHS, divergence,
+// pressure gradient and explicit tensor divergences (src/N.jl:94-254).
+#include "internal.cuh"
+
+namespace exc {
+
+// ---------------------------------------------------------------------------
+// RHS sweep: du = doadd*du - div sigma(u) (`stresstensor` + `tensordivergence!`,
+// src/N.jl:94-160).  A CTA stages its TX x TY x TZ tile of u plus a one-cell
+// halo in shared memory, evaluates each stress component once on the index
+// set the divergence needs (diagonal: tile + 1 along i; edge ij: tile - 1
+// along i and j), then forms the divergence.  Stresses are kept divided by h.
+// ---------------------------------------------------------------------------
+constexpr int RTX = 16, RTY = 8, RTZ = 4;
+constexpr int RBX = RTX + 2, RBY = RTY + 2, RBZ = RTZ + 2;  // u and stress box, origin tile-1
+constexpr int RHS_THREADS = 256;
+
+template <typename T>
+struct RhsSmem {
+  T u[3][RBZ][RBY][RBX];
+  T s[6][RBZ][RBY][RBX];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(RHS_THREADS)
+rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, int doadd) {
+  extern __shared__ unsigned char smem_raw[];
+  RhsSmem<T>& sm = *reinterpret_cast<RhsSmem<T>*>(smem_raw);
+  const long long N = (long long)n * n * n;
+  const int x0 = blockIdx.x * RTX, y0 = blockIdx.y * RTY, z0 = blockIdx.z * RTZ;
+  const int tid = threadIdx.x;
+  // stage u (periodic wrap); box coordinate b <-> global tile0 - 1 + b
+  for (int t = tid; t < 3 * RBZ * RBY * RBX; t += RHS_THREADS) {
+    int c = t / (RBZ * RBY * RBX);
+    int r = t - c * (RBZ * RBY * RBX);
+    int bz = r / (RBY * RBX);
+    r -= bz * (RBY * RBX);
+    int by = r / RBX, bx = r - by * RBX;
+    int gx = x0 - 1 + bx, gy = y0 - 1 + by, gz = z0 - 1 + bz;
+    // gx >= -1; the modulo also covers grids smaller than the tile
+    gx = (gx + n) % n;
+    gy = (gy + n) % n;
+    gz = (gz + n) % n;
+    sm.u[c][bz][by][bx] = u[c * N + ((long long)gz * n + gy) * n + gx];
+  }
+  __syncthreads();
+  const T kd = (T)0.25 * inv_h;             // (a+b)^2/4/h
+  const T kv = visc * inv_h * inv_h;        // visc/h^2
+  // stress box index sb <-> u box index sb (same origin), tile cells at 1..T
+  // diagonal sigma_ii at stress-box cells: b_i in [1, T_i + 1], others [1, T]
+  // edge sigma_ij: b_i, b_j in [0, T], other [1, T]
+  for (int comp = 0; comp < 6; ++comp) {
+    int i, j;
+    if (comp < 3) { i = j = comp; } else { i = comp - 3; j = (i + 1) % 3; }  // 12, 23, 31
+    int lo[3] = {1, 1, 1}, hi[3] = {RTX, RTY, RTZ};  // inclusive, box coords
+    if (i == j) { hi[i] += 1; }
+    else { lo[i] = 0; lo[j] = 0; }
+    int ex = hi[0] - lo[0] + 1, ey = hi[1] - lo[1] + 1, ez = hi[2] - lo[2] + 1;
+    int tot = ex * ey * ez;
+    for (int t = tid; t < tot; t += RHS_THREADS) {
+      int bz = t / (ex * ey);
+      int r = t - bz * ex * ey;
+      int by = r / ex, bx = r - by * ex;
+      bx += lo[0]; by += lo[1]; bz += lo[2];
+      T val;
+      if (i == j) {
+        // sigma_ii[I] uses u_i[I - e_i], u_i[I] (src/N.jl:106-118 with i == j)
+        int dx = (i == 0), dy = (i == 1), dz = (i == 2);
+        T a = sm.u[i][bz][by][bx], b = sm.u[i][bz - dz][by - dy][bx - dx];
+        T s = a + b, d = a - b;
+        val = s * s * kd - (T)2 * kv * d;
+      } else {
+        // sigma_ij[I] at edge I+e_i/2+e_j/2: u_i[I], u_i[I+e_j], u_j[I], u_j[I+e_i]
+        int jx = (j == 0), jy = (j == 1), jz = (j == 2);
+        int ix = (i == 0), iy = (i == 1), iz = (i == 2);
+        T a = sm.u[i][bz][by][bx], b = sm.u[i][bz + jz][by + jy][bx + jx];
+        T c = sm.u[j][bz][by][bx], d = sm.u[j][bz + iz][by + iy][bx + ix];
+        val = (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
+      }
+      sm.s[comp][bz][by][bx] = val;
+    }
+  }
+  __syncthreads();
+  // divergence at tile cells
+  for (int t = tid; t < RTX * RTY * RTZ; t += RHS_THREADS) {
+    int tz = t / (RTX * RTY);
+    int r = t - tz * RTX * RTY;
+    int ty = r / RTX, tx = r - ty * RTX;
+    int bx = tx + 1, by = ty + 1, bz = tz + 1;
+    int gx = x0 + tx, gy = y0 + ty, gz = z0 + tz;
+    if (gx >= n || gy >= n || gz >= n) continue;
+    const auto& S = sm.s;
+    // s12 = S[3], s23 = S[4], s31 = S[5]
+    T d1 = (S[0][bz][by][bx + 1] - S[0][bz][by][bx]) + (S[3][bz][by][bx] - S[3][bz][by - 1][bx]) +
+           (S[5][bz][by][bx] - S[5][bz - 1][by][bx]);
+    T d2 = (S[3][bz][by][bx] - S[3][bz][by][bx - 1]) + (S[1][bz][by + 1][bx] - S[1][bz][by][bx]) +
+           (S[4][bz][by][bx] - S[4][bz - 1][by][bx]);
+    T d3 = (S[5][bz][by][bx] - S[5][bz][by][bx - 1]) + (S[4][bz][by][bx] - S[4][bz][by - 1][bx]) +
+           (S[2][bz + 1][by][bx] - S[2][bz][by][bx]);
+    long long g = ((long long)gz * n + gy) * n + gx;
+    if (doadd) {
+      du[g] -= d1;
+      du[N + g] -= d2;
+      du[2 * N + g] -= d3;
+    } else {
+      du[g] = -d1;
+      du[N + g] = -d2;
+      du[2 * N + g] = -d3;
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st) {
+  dim3 grid((n + RTX - 1) / RTX, (n + RTY - 1) / RTY, (n + RTZ - 1) / RTZ);
+  rhs_kernel<T><<<grid, RHS_THREADS, sizeof(RhsSmem<T>), st>>>(n, (T)(1.0 / (double)h), visc, u, du, doadd ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t configure_stencil() {
+  cudaError_t e = cudaFuncSetAttribute(rhs_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sizeof(RhsSmem<double>));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(rhs_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RhsSmem<float>));
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+// Simple per-cell kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cell_of(long long g, int n, int& x, int& y, int& z) {
+  long long r = g / n;
+  x = (int)(g - r * n);
+  z = (int)(r / n);
+  y = (int)(r - (long long)z * n);
+}
+
+// The 6 stress components materialised (src/N.jl:94-118).
+template <typename T>
+__global__ void stress_kernel(int n, T h, T visc, const T* __restrict__ u, T* __restrict__ s6) {
+  const long long N = (long long)n * n * n;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    cell_of(g, n, x, y, z);
+    int c[3] = {x, y, z};
+    const int comps[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {2, 0}};
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      int i = comps[m][0], j = comps[m][1];
+      auto idx = [&](int d, int s) {
+        int cc[3] = {c[0], c[1], c[2]};
+        cc[d] = (cc[d] + s + n) % n;
+        return ((long long)cc[2] * n + cc[1]) * n + cc[0];
+      };
+      int off = (i != j);
+      T uir = u[i * N + idx(j, off)], uil = u[i * N + idx(j, off - 1)];
+      T ujr = u[j * N + idx(i, off)], ujl = u[j * N + idx(i, off - 1)];
+      T etaj_ui = (uir + uil) / 2, etai_uj = (ujr + ujl) / 2;
+      T dj_ui = (uir - uil) / h, di_uj = (ujr - ujl) / h;
+      s6[m * N + g] = etaj_ui * etai_uj - visc * (dj_ui + di_uj);
+    }
+  }
+}
+
+// du_i = doadd*du_i - sum_j delta_j s_ij with an explicit tensor (src/N.jl:120-200).
+template <typename T>
+__global__ void tensordiv_kernel(int n, T h, int nsym, const T* __restrict__ s, T* __restrict__ du, int doadd) {
+  const long long N = (long long)n * n * n;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    cell_of(g, n, x, y, z);
+    int c[3] = {x, y, z};
+    auto nb = [&](int d, int sgn) {
+      int cc[3] = {c[0], c[1], c[2]};
+      cc[d] = (cc[d] + sgn + n) % n;
+      return ((long long)cc[2] * n + cc[1]) * n + cc[0];
+    };
+    for (int i = 0; i < 3; ++i) {
+      T acc = doadd ? du[i * N + g] : (T)0;
+      for (int j = 0; j < 3; ++j) {
+        int m;
+        if (nsym == 9) m = 3 * j + i;  // s11,s21,s31,s12,... (src/N.jl:181)
+        else {
+          if (i == j) m = i;
+          else {
+            int a = i < j ? i : j, b = i < j ? j : i;
+            m = (a == 0 && b == 1) ? 3 : (a == 1 && b == 2) ? 4 : 5;
+          }
+        }
+        const T* sc = s + (long long)m * N;
+        if (i == j) acc -= (sc[nb(j, 1)] - sc[g]) / h;
+        else acc -= (sc[g] - sc[nb(j, -1)]) / h;
+      }
+      du[i * N + g] = acc;
+    }
+  }
+}
+
+template <typename T>
+__global__ void divergence_kernel(int n, T h, const T* __restrict__ u, T* __restrict__ d) {
+  const long long N = (long long)n * n * n;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    cell_of(g, n, x, y, z);
+    long long gx = g - x + wrap_dn(x, n);
+    long long gy = ((long long)z * n + wrap_dn(y, n)) * n + x;
+    long long gz = ((long long)wrap_dn(z, n) * n + y) * n + x;
+    d[g] = (u[g] - u[gx]) / h + (u[N + g] - u[N + gy]) / h + (u[2 * N + g] - u[2 * N + gz]) / h;
+  }
+}
+
+// u_i -= (p[I+e_i] - p[I]) / h, p at row pitch ppitch (src/N.jl:240-254).
+template <typename T>
+__global__ void gradient_kernel(int n, T inv_h, T* __restrict__ u, const T* __restrict__ p, int ppitch) {
+  const long long N = (long long)n * n * n;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
+    int x, y, z;
+    cell_of(g, n, x, y, z);
+    long long row = (long long)z * n + y;
+    T pc = p[row * ppitch + x];
+    T px = p[row * ppitch + wrap_up(x, n)];
+    T py = p[((long long)z * n + wrap_up(y, n)) * ppitch + x];
+    T pz = p[((long long)wrap_up(z, n) * n + y) * ppitch + x];
+    u[g] -= (px - pc) * inv_h;
+    u[N + g] -= (py - pc) * inv_h;
+    u[2 * N + g] -= (pz - pc) * inv_h;
+  }
+}
+
+static inline int grid_for(long long N, int threads) {
+  long long b = (N + threads - 1) / threads;
+  return (int)(b < 152LL * 32 ? b : 152LL * 32);
+}
+
+template <typename T>
+cudaError_t launch_stress(int n, T h, T visc, const T* u, T* s6, cudaStream_t st) {
+  long long N = (long long)n * n * n;
+  stress_kernel<T><<<grid_for(N, 256), 256, 0, st>>>(n, h, visc, u, s6);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_tensordiv(int n, T h, int nsym, const T* s, T* du, bool doadd, cudaStream_t st) {
+  long long N = (long long)n * n * n;
+  tensordiv_kernel<T><<<grid_for(N, 256), 256, 0, st>>>(n, h, nsym, s, du, doadd ? 1 : 0);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_divergence(int n, T h, const T* u, T* d, cudaStream_t st) {
+  long long N = (long long)n * n * n;
+  divergence_kernel<T><<<grid_for(N, 256), 256, 0, st>>>(n, h, u, d);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_gradient(int n, T h, T* u, const T* p, int ppitch, cudaStream_t st) {
+  long long N = (long long)n * n * n;
+  gradient_kernel<T><<<grid_for(N, 256), 256, 0, st>>>(n, (T)(1.0 / (double)h), u, p, ppitch);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// max |x|: per-block maxima into `partial`, then one block folds them
+// (deterministic; no atomics).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void maxabs_partial_kernel(size_t count, const T* __restrict__ x, double* __restrict__ partial) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    double v = fabs((double)x[i]);
+    m = (v > m || v != v) ? v : m;  // NaN propagates
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (w > m || w != w) ? w : m;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      double w = __shfl_xor_sync(0xffffffffu, m, o);
+      m = (w > m || w != w) ? w : m;
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+  }
+}
+
+__global__ void maxabs_final_kernel(int np, const double* __restrict__ partial, double* __restrict__ out) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    double v = partial[i];
+    m = (v > m || v != v) ? v : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (w > m || w != w) ? w : m;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      double w = __shfl_xor_sync(0xffffffffu, m, o);
+      m = (w > m || w != w) ? w : m;
+    }
+    if (threadIdx.x == 0) *out = m;
+  }
+}
+
+template <typename T>
+cudaError_t launch_max_abs(size_t count, const T* x, double* out_dev, double* partial, int npartial,
+                           cudaStream_t st) {
+  int blocks = (int)std::min<size_t>((count + 255) / 256, (size_t)npartial);
+  if (blocks < 1) blocks = 1;
+  maxabs_partial_kernel<T><<<blocks, 256, 0, st>>>(count, x, partial);
+  maxabs_final_kernel<<<1, 1024, 0, st>>>(blocks, partial, out_dev);
+  return cudaGetLastError();
+}
+
+#define INST(T)                                                                                   \
+  template cudaError_t launch_rhs<T>(int, T, T, const T*, T*, bool, cudaStream_t);                \
+  template cudaError_t launch_stress<T>(int, T, T, const T*, T*, cudaStream_t);                   \
+  template cudaError_t launch_tensordiv<T>(int, T, int, const T*, T*, bool, cudaStream_t);        \
+  template cudaError_t launch_divergence<T>(int, T, const T*, T*, cudaStream_t);                  \
+  template cudaError_t launch_gradient<T>(int, T, T*, const T*, int, cudaStream_t);               \
+  template cudaError_t launch_max_abs<T>(size_t, const T*, double*, double*, int, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace exc

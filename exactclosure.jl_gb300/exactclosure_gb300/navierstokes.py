@@ -1,0 +1,276 @@
+"""Host-side mirror of the reference's ``NavierStokes`` module (``src/N.jl``)
+over the libexc C ABI.
+
+Operator functions keep the reference's names and argument meaning; fields
+are CUDA tensors (torch is used only to own device memory and streams) shaped
+``(3, n, n, n)`` / ``(n, n, n)`` in the reference's byte layout (x fastest,
+component slowest).  Every call goes through ``libexc.so``; nothing here
+computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import (EXC_F32, EXC_F64, EXC_FILTER_FACE, EXC_FILTER_VOLUME, CaseDesc, call, lib)
+
+KINDS = {"volume": EXC_FILTER_VOLUME, "face": EXC_FILTER_FACE}
+
+
+def _torch():
+    import torch  # device memory and streams only
+
+    return torch
+
+
+def _prec(t) -> int:
+    torch = _torch()
+    if t.dtype == torch.float64:
+        return EXC_F64
+    if t.dtype == torch.float32:
+        return EXC_F32
+    raise TypeError(f"fields must be float64 or float32, got {t.dtype}")
+
+
+def _ptr(t) -> C.c_void_p:
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("fields must be contiguous CUDA tensors")
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return C.c_void_p(_torch().cuda.current_stream().cuda_stream)
+
+
+def _taps(fdelta):
+    if fdelta is None or len(fdelta) <= 1:
+        return None, 0
+    a = np.ascontiguousarray(fdelta, dtype=np.float64)
+    return a.ctypes.data_as(C.POINTER(C.c_double)), len(a)
+
+
+@dataclass(frozen=True)
+class Grid:
+    """``Grid{3}(l, n)`` (``src/N.jl:22-25``)."""
+
+    l: float
+    n: int
+
+    @property
+    def h(self) -> float:
+        return self.l / self.n
+
+
+def tensordivergence(du, u, visc: float, grid: Grid, doadd: bool = False):
+    """``tensordivergence!(du, stresstensor(u, visc), doadd)`` (``src/N.jl:94-160``)."""
+    call("exc_tensordivergence", _prec(u), grid.n, grid.l, visc, _ptr(u), _ptr(du), int(doadd), _stream())
+    return du
+
+
+def tensordivergence_tensor(du, s, grid: Grid, doadd: bool = False):
+    """``tensordivergence!`` (6 components) or ``tensordivergence_nonsym!`` (9)
+    with an explicit tensor ``s`` shaped ``(6|9, n, n, n)`` (``src/N.jl:120-200``)."""
+    call("exc_tensordivergence_tensor", _prec(s), grid.n, grid.l, s.shape[0], _ptr(s), _ptr(du), int(doadd),
+         _stream())
+    return du
+
+
+def stresstensor(s6, u, visc: float, grid: Grid):
+    """Materialised ``stresstensor(u, visc)`` (``src/N.jl:94-118``) into ``s6``."""
+    call("exc_stresstensor", _prec(u), grid.n, grid.l, visc, _ptr(u), _ptr(s6), _stream())
+    return s6
+
+
+def divergence(d, u, grid: Grid):
+    """``divergence!(d, u)`` (``src/N.jl:222-238``)."""
+    call("exc_divergence", _prec(u), grid.n, grid.l, _ptr(u), _ptr(d), _stream())
+    return d
+
+
+def pressuregradient(u, p, grid: Grid):
+    """``pressuregradient!(u, p)`` (``src/N.jl:240-254``)."""
+    call("exc_pressuregradient", _prec(u), grid.n, grid.l, _ptr(u), _ptr(p), _stream())
+    return u
+
+
+class PoissonSolver:
+    """``poissonsolver(grid, backend)`` (``src/N.jl:202-220``): owns the
+    spectral work array and FFT tables of one grid on the device."""
+
+    def __init__(self, grid: Grid, precision: int = EXC_F64):
+        self.grid = grid
+        self.precision = precision
+        h = C.c_void_p()
+        call("exc_poisson_create", precision, grid.n, grid.l, C.byref(h))
+        self._h = h
+
+    def solve(self, p, d):
+        """``p`` with ``L_h p = d`` and zero mean (``src/N.jl:262-301``)."""
+        call("exc_poisson_solve", self._h, _ptr(d), _ptr(p), _stream())
+        return p
+
+    def project(self, u, p=None):
+        """``project!(u, poisson)`` (``src/N.jl:256-307``), in place; the
+        pressure goes to ``p`` when given."""
+        call("exc_project", self._h, _ptr(u), _ptr(p) if p is not None else None, _stream())
+        return u
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().exc_poisson_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def poissonsolver(grid: Grid, precision: int = EXC_F64) -> PoissonSolver:
+    return PoissonSolver(grid, precision)
+
+
+def project(u, poisson: PoissonSolver, p=None):
+    return poisson.project(u, p)
+
+
+def propose_timestep(u, visc: float, cfl: float, grid: Grid) -> float:
+    """``propose_timestep`` (``src/N.jl:348-356``)."""
+    dt = C.c_double()
+    call("exc_propose_timestep", _prec(u), grid.n, grid.l, visc, cfl, _ptr(u), C.byref(dt), _stream())
+    return dt.value
+
+
+def apply_filter(ubar, u, ratio: int, kind: str = "volume", fdelta=None):
+    """``lazycoarsegrain(faces[i], lazyfilter(u_i, GDH))`` for each component
+    (volume) or the face average (face), materialised into ``ubar``
+    (``src/N.jl:655-698``, ``src/N.jl:1228-1237`` without the projection)."""
+    t, nt = _taps(fdelta)
+    call("exc_filter", _prec(u), u.shape[1], ratio, KINDS[kind], t, nt, _ptr(u), _ptr(ubar), _stream())
+    return ubar
+
+
+def apply_DHpi(ubar, u, poisson_les: PoissonSolver, ratio: int, fdelta=None):
+    """``apply_DHpi(ubar, u, poisson, GDH)`` (``src/N.jl:1228-1237``)."""
+    apply_filter(ubar, u, ratio, "volume", fdelta)
+    return poisson_les.project(ubar)
+
+
+def get_rDHi(r9, u, p, visc: float, grid: Grid, ratio: int, fdelta=None):
+    """``get_rDHi(get_r(stresstensor(u), p), GDHi, g_dns, g_les)``
+    (``src/N.jl:1022-1073``), materialised into ``r9`` (9 LES arrays)."""
+    t, nt = _taps(fdelta)
+    call("exc_closure_flux", _prec(u), grid.n, ratio, grid.l, visc, t, nt, _ptr(u), _ptr(p), _ptr(r9), _stream())
+    return r9
+
+
+def get_sigmaDH(s6, u, visc: float, grid: Grid, ratio: int, fdelta=None):
+    """``get_sigmaDH(stresstensor(u), g_dns, g_les, GDH)`` (``src/N.jl:1088-1115``)."""
+    t, nt = _taps(fdelta)
+    call("exc_filtered_stress", _prec(u), grid.n, ratio, grid.l, visc, t, nt, _ptr(u), _ptr(s6), _stream())
+    return s6
+
+
+class Case:
+    """A DNS with attached LES grids advanced by RK4 with the exact closure at
+    every stage (the ``dnsaid_project`` loop, ``src/N.jl:1239-1332``), fully
+    device resident.  Host arrays are float64 ``(3, n, n, n)``."""
+
+    def __init__(self, n: int, l: float = 1.0, visc: float = 1 / 2000, cfl: float = 0.3,
+                 precision: int = EXC_F64, les=(), stream: int | None = None):
+        d = CaseDesc()
+        d.n, d.l, d.visc, d.cfl, d.precision = n, l, visc, cfl, precision
+        d.nles = len(les)
+        for i, (ratio, kind) in enumerate(les):
+            d.les[i].ratio = ratio
+            d.les[i].kind = KINDS[kind] if isinstance(kind, str) else kind
+        self.desc = d
+        self.n, self.l, self.visc = n, l, visc
+        self.les_list = [(r, k) for r, k in les]
+        h = C.c_void_p()
+        call("exc_case_create", C.byref(d), C.c_void_p(stream) if stream else None, C.byref(h))
+        self._h = h
+
+    def _buf(self, shape):
+        a = np.empty(shape, dtype=np.float64)
+        return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+    def init_random(self, kpeak: float, energy: float = 1.0, seed: int = 0):
+        """``randomfield(peak_profile, ...)`` (``src/N.jl:394-476``)."""
+        call("exc_case_init_random", self._h, kpeak, energy, seed)
+
+    def set_velocity(self, u: np.ndarray):
+        a = np.ascontiguousarray(u, dtype=np.float64)
+        assert a.shape == (3, self.n, self.n, self.n)
+        call("exc_case_set_velocity", self._h, a.ctypes.data_as(C.POINTER(C.c_double)))
+
+    def velocity(self) -> np.ndarray:
+        a, p = self._buf((3, self.n, self.n, self.n))
+        call("exc_case_get_velocity", self._h, p)
+        return a
+
+    def les(self, index: int, which: str = "exact") -> np.ndarray:
+        """LES field: 'target' (filtered DNS), 'exact', 'nomodel' or 'closure'."""
+        w = {"target": 0, "exact": 1, "nomodel": 2, "closure": 3}[which]
+        m = self.n // self.les_list[index][0]
+        a, p = self._buf((3, m, m, m))
+        call("exc_case_get_les", self._h, index, w, p)
+        return a
+
+    def get_velocity_into(self, out: np.ndarray):
+        """Download the DNS velocity into a caller-owned (e.g. pinned) array."""
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == 3 * self.n ** 3
+        call("exc_case_get_velocity", self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def device_ptr(self) -> int:
+        """Device address of the current DNS velocity (zero-copy callers)."""
+        p = C.c_void_p()
+        call("exc_case_device_ptr", self._h, 0, C.byref(p))
+        return p.value
+
+    def launches_per_step(self) -> int:
+        k = C.c_int()
+        call("exc_case_launches_per_step", self._h, C.byref(k))
+        return k.value
+
+    def step(self, nsteps: int = 1, dt: float = 0.0):
+        call("exc_case_step", self._h, nsteps, dt)
+
+    def errors(self, index: int) -> tuple[float, float]:
+        e = (C.c_double * 2)()
+        call("exc_case_errors", self._h, index, e)
+        return e[0], e[1]
+
+    def time(self) -> tuple[float, float]:
+        t, dt = C.c_double(), C.c_double()
+        call("exc_case_time", self._h, C.byref(t), C.byref(dt))
+        return t.value, dt.value
+
+    def energy(self) -> float:
+        e = C.c_double()
+        call("exc_case_energy", self._h, C.byref(e))
+        return e.value
+
+    def spectrum(self) -> np.ndarray:
+        ns = (2 * (self.n // 2)) // 3
+        a, p = self._buf((ns,))
+        call("exc_case_spectrum", self._h, p, ns)
+        return a
+
+    def sync(self):
+        call("exc_case_sync", self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().exc_case_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,204 @@
+/*
+ * exc.h -- C ABI of libexc, the GB300 (sm_103a) implementation of the
+ * DNS-aided LES hot path of agdestein/ExactClosure.jl.
+ *
+ * The reference is a Julia module (src/N.jl, `module NavierStokes`) whose
+ * operators take tuples of CuArrays; this ABI is what a `ccall` from that
+ * module binds.  Every entry point returns an int status (EXC_OK == 0);
+ * nothing throws across the boundary; exc_last_error() gives the message of
+ * the last failure on the calling thread.
+ *
+ * Conventions
+ *   - `precision` is EXC_F64 or EXC_F32 and fixes the word type of every
+ *     field argument (double or float).
+ *   - Scalar fields are n^3 words, x fastest (the reference's column-major
+ *     Field, src/N.jl:34-42); vector fields are three such arrays, component
+ *     slowest (the tuple of src/N.jl:45).  Operator-level pointers are DEVICE
+ *     pointers owned by the caller; `stream` is a cudaStream_t (NULL = the
+ *     legacy default stream).
+ *   - Tensor arguments hold 6 symmetric components in the reference's order
+ *     (s11, s22, s33, s12, s23, s31; src/N.jl:94-104) or 9 non-symmetric
+ *     ones in the order (s11, s21, s31, s12, s22, s32, s13, s23, s33)
+ *     (src/N.jl:181), each an n^3 (or n_les^3) array.
+ *   - Grid sizes: n = 2^a 3^b, a >= 1, 4 <= n <= 1024; an LES ratio c must
+ *     divide n and n/c must itself be a supported size for LES projection.
+ *   - Case-level host pointers are borrowed for the duration of the call.
+ *   - A handle is not re-entrant; distinct handles may be used from
+ *     distinct threads.
+ */
+#ifndef EXC_H
+#define EXC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum exc_status {
+  EXC_OK = 0,
+  EXC_ERR_ARG = 1,       /* null pointer, bad enum or out-of-range scalar */
+  EXC_ERR_SHAPE = 2,     /* unsupported grid size */
+  EXC_ERR_RATIO = 3,     /* filter ratio does not divide the grid */
+  EXC_ERR_OOM = 4,       /* device or pinned allocation failed */
+  EXC_ERR_CUDA = 5,      /* CUDA runtime error */
+  EXC_ERR_NONFINITE = 6, /* a non-finite velocity was detected */
+  EXC_ERR_TIMEOUT = 7,   /* a bounded device-side wait ran out */
+  EXC_ERR_STATE = 8      /* call made in the wrong state */
+};
+
+enum exc_precision { EXC_F64 = 0, EXC_F32 = 1 };
+enum exc_filter_kind { EXC_FILTER_VOLUME = 0, EXC_FILTER_FACE = 1 };
+
+/* Message of the last failed call on this thread (never NULL). */
+const char* exc_last_error(void);
+/* ABI version (major*100 + minor). */
+int exc_version(void);
+
+/* ======================================================================
+ * Operator level (device pointers owned by the caller)
+ * ====================================================================== */
+
+/* du = doadd*du - div sigma(u): `stresstensor` + `tensordivergence!`
+ * (src/N.jl:94-160).  u, du: vector fields on the n^3 grid of side l. */
+int exc_tensordivergence(int precision, int n, double l, double visc,
+                         const void* u, void* du, int doadd, void* stream);
+
+/* du = doadd*du - sum_j delta_j s_ij for an explicit tensor s:
+ * `tensordivergence!` with 6 symmetric components (nsym == 6) or
+ * `tensordivergence_nonsym!` with 9 components (nsym == 9)
+ * (src/N.jl:120-200).  s: nsym n^3 arrays, contiguous. */
+int exc_tensordivergence_tensor(int precision, int n, double l, int nsym,
+                                const void* s, void* du, int doadd, void* stream);
+
+/* The 6 components of the staggered stress (src/N.jl:94-118), materialised. */
+int exc_stresstensor(int precision, int n, double l, double visc,
+                     const void* u, void* s6, void* stream);
+
+/* d = div u at cell centres (`divergence!`, src/N.jl:222-238). */
+int exc_divergence(int precision, int n, double l, const void* u, void* d, void* stream);
+
+/* u -= grad p (`pressuregradient!`, src/N.jl:240-254). */
+int exc_pressuregradient(int precision, int n, double l, void* u, const void* p, void* stream);
+
+/* FFT Poisson solver bound to one grid (`poissonsolver`, src/N.jl:202-220).
+ * Owns its spectral work array and twiddle tables. */
+typedef struct exc_poisson exc_poisson;
+int exc_poisson_create(int precision, int n, double l, exc_poisson** out);
+int exc_poisson_destroy(exc_poisson* ps);
+/* p with L_h p = d, mean(p) = 0 (src/N.jl:262-301).  d and p may alias. */
+int exc_poisson_solve(exc_poisson* ps, const void* d, void* p, void* stream);
+/* In-place projection u <- u - grad L^-1 div u (`project!`, src/N.jl:256-307).
+ * p_out (n^3, may be NULL) receives the pressure. */
+int exc_project(exc_poisson* ps, void* u, void* p_out, void* stream);
+
+/* max_i |x_i| over `count` words, written as a double to *out_dev (device). */
+int exc_max_abs(int precision, size_t count, const void* x, double* out_dev, void* stream);
+
+/* dt = min(cfl*h/max|u|, cfl*h^2/visc/6) (`propose_timestep`,
+ * src/N.jl:348-356); synchronises `stream` and returns dt on the host. */
+int exc_propose_timestep(int precision, int n, double l, double visc, double cfl,
+                         const void* u, double* dt_host, void* stream);
+
+/* Discrete filter + coarse-grain of a vector field from n^3 to (n/ratio)^3:
+ * kind VOLUME is `lazycoarsegrain(faces[i], lazyfilter(u_i, GDH))`
+ * (src/N.jl:1228-1237 without the projection), kind FACE the face average.
+ * fdelta (host, odd length nfdelta, may be NULL) is the optional Gaussian
+ * FDelta of `get_kernels` (src/N.jl:1008-1020), convolved into the box. */
+int exc_filter(int precision, int n, int ratio, int kind, const double* fdelta, int nfdelta,
+               const void* u, void* ubar, void* stream);
+
+/* Face-filtered total flux rDHi (src/N.jl:1038-1073): the 9 components of
+ * r = sigma(u) + p*I (`get_r`, src/N.jl:1022-1036) filtered with GDHi[j]
+ * and coarse-grained at LES centres/edges; output r9: 9 (n/ratio)^3 arrays. */
+int exc_closure_flux(int precision, int n, int ratio, double l, double visc,
+                     const double* fdelta, int nfdelta,
+                     const void* u, const void* p, void* r9, void* stream);
+
+/* Volume-filtered DNS stress sigmaDH at LES centres/edges (`get_sigmaDH`,
+ * src/N.jl:1088-1115); output s6: 6 (n/ratio)^3 arrays. */
+int exc_filtered_stress(int precision, int n, int ratio, double l, double visc,
+                        const double* fdelta, int nfdelta,
+                        const void* u, void* s6, void* stream);
+
+/* ======================================================================
+ * Case level: a DNS with attached LES grids, RK4 with the exact closure
+ * evaluated at every stage (the `dnsaid_project` loop, src/N.jl:1239-1332,
+ * with RK4 stages in place of forward Euler).  Device memory is owned by the
+ * case.  Host arrays are float64 in the field layout above.
+ * ====================================================================== */
+
+#define EXC_MAX_LES 4
+
+typedef struct {
+  int ratio; /* n / n_les */
+  int kind;  /* exc_filter_kind */
+} exc_les_desc;
+
+typedef struct {
+  int n;          /* DNS cells per side */
+  double l;       /* domain side */
+  double visc;    /* kinematic viscosity */
+  double cfl;     /* CFL factor of propose_timestep */
+  int precision;  /* exc_precision of stencil, filter and RK stages */
+  int nles;       /* number of attached LES grids (0..EXC_MAX_LES) */
+  exc_les_desc les[EXC_MAX_LES];
+} exc_case_desc;
+
+typedef struct exc_case exc_case;
+
+/* `stream` (cudaStream_t, may be NULL) is bound to the case for life. */
+int exc_case_create(const exc_case_desc* desc, void* stream, exc_case** out);
+int exc_case_destroy(exc_case* cs);
+
+/* Solenoidal random field with E(k) ~ k^4 exp(-2 (k/kpeak)^2) normalised to
+ * `energy` (`randomfield` + `peak_profile`, src/N.jl:366-476) from the
+ * project's counter-based normal generator with `seed`; resets the LES
+ * states to the filtered DNS and the clock to 0. */
+int exc_case_init_random(exc_case* cs, double kpeak, double energy, uint64_t seed);
+
+/* Copy the DNS velocity in (3 n^3 doubles) and reset LES states and clock. */
+int exc_case_set_velocity(exc_case* cs, const double* host_u);
+int exc_case_get_velocity(exc_case* cs, double* host_u);
+
+/* LES field `which`: 0 = filtered DNS target, 1 = exact-closure LES,
+ * 2 = no-model LES, 3 = last exact closure m (stage 1 of the last step);
+ * 3 (n/ratio)^3 doubles. */
+int exc_case_get_les(exc_case* cs, int les_index, int which, double* host_v);
+
+/* Advance `nsteps` RK4 steps.  dt_fixed > 0 uses that step, otherwise
+ * propose_timestep on the device every step (no host synchronisation). */
+int exc_case_step(exc_case* cs, int nsteps, double dt_fixed);
+
+/* Relative L2 errors of the exact and no-model LES against the filtered DNS
+ * (`compute_errors`, src/N.jl:1334-1349): err[0] exact, err[1] no-model. */
+int exc_case_errors(exc_case* cs, int les_index, double* err2);
+
+/* Simulated time and the last dt (host; synchronises the case stream). */
+int exc_case_time(exc_case* cs, double* t, double* last_dt);
+
+/* Mean kinetic energy of the DNS (FP64 reduction). */
+int exc_case_energy(exc_case* cs, double* energy);
+
+/* Shell spectrum E(k), k = 1..nshell (`spectrum`, src/N.jl:576-590),
+ * nshell = div(2*div(n,2), 3); FP64. */
+int exc_case_spectrum(exc_case* cs, double* host_e, int nshell);
+
+/* Device pointer of an internal field (0 = DNS velocity) for zero-copy
+ * callers; valid until the case is destroyed. */
+int exc_case_device_ptr(exc_case* cs, int which, void** ptr);
+
+/* Number of kernel launches in one captured RK4 step (valid after the first
+ * exc_case_step). */
+int exc_case_launches_per_step(exc_case* cs, int* count);
+
+/* Synchronise the case stream; returns EXC_ERR_NONFINITE if a non-finite
+ * velocity was flagged during the last steps. */
+int exc_case_sync(exc_case* cs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EXC_H */

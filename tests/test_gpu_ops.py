@@ -1,0 +1,209 @@
+"""GPU parity of the operator-level C ABI against the oracle (float64: 1e-12
+relative; float32 form: 1e-5 relative), on seeded fields and the golden
+vectors of the literal restatement."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import ns
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).with_name("golden")
+TOL64 = 1e-12
+TOL32 = 2e-5
+
+
+@pytest.fixture(scope="module")
+def NS(built_lib):
+    from exactclosure_gb300 import navierstokes
+
+    return navierstokes
+
+
+def dev(a, dtype="float64"):
+    import torch
+
+    return torch.tensor(np.ascontiguousarray(a), dtype=getattr(torch, dtype), device="cuda")
+
+
+def host(t):
+    import torch
+
+    torch.cuda.synchronize()
+    return t.double().cpu().numpy()
+
+
+def rel(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def seeded_field(n, l, seed=0):
+    rng = np.random.default_rng(seed)
+    u = rng.standard_normal((3, n, n, n))
+    return ns.project(u, l / n)
+
+
+SIZES = [4, 6, 8, 12, 16, 24, 32, 48, 64, 96]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_rhs_f64(NS, n):
+    import torch
+
+    l, visc = 1.0, 1 / 700
+    u = seeded_field(n, l, n)
+    g = NS.Grid(l, n)
+    du = torch.empty((3, n, n, n), dtype=torch.float64, device="cuda")
+    NS.tensordivergence(du, dev(u), visc, g)
+    ref = ns.rhs(u, visc, l / n)
+    assert rel(host(du), ref) < TOL64
+    # doadd accumulates
+    base = np.ones_like(ref)
+    du2 = dev(base)
+    NS.tensordivergence(du2, dev(u), visc, g, doadd=True)
+    assert rel(host(du2), base + ref) < TOL64
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_project_f64(NS, n):
+    import torch
+
+    l = 2.0
+    rng = np.random.default_rng(n)
+    u = rng.standard_normal((3, n, n, n))
+    ps = NS.poissonsolver(NS.Grid(l, n))
+    ut = dev(u)
+    p = torch.empty((n, n, n), dtype=torch.float64, device="cuda")
+    ps.project(ut, p)
+    ref, pref = ns.project(u, l / n, return_p=True)
+    assert rel(host(ut), ref) < TOL64
+    assert rel(host(p), pref) < TOL64
+
+
+@pytest.mark.parametrize("n", [8, 12, 32, 96])
+def test_poisson_solve_and_divergence(NS, n):
+    import torch
+
+    l = 1.0
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((3, n, n, n))
+    g = NS.Grid(l, n)
+    d = torch.empty((n, n, n), dtype=torch.float64, device="cuda")
+    NS.divergence(d, dev(u), g)
+    dref = ns.divergence(u, l / n)
+    assert rel(host(d), dref) < TOL64
+    ps = NS.poissonsolver(g)
+    p = torch.empty_like(d)
+    ps.solve(p, d)
+    assert rel(host(p), ns.poisson_solve(dref, l / n)) < TOL64
+    ut = dev(u)
+    NS.pressuregradient(ut, p, g)
+    assert rel(host(ut), ns.pressuregradient(u, ns.poisson_solve(dref, l / n), l / n)) < TOL64
+
+
+@pytest.mark.parametrize("n", [16, 64])
+def test_f32_form_operators(NS, n):
+    import torch
+
+    l, visc = 1.0, 1 / 2000
+    u = seeded_field(n, l, 7)
+    g = NS.Grid(l, n)
+    du = torch.empty((3, n, n, n), dtype=torch.float32, device="cuda")
+    NS.tensordivergence(du, dev(u, "float32"), visc, g)
+    assert rel(host(du), ns.rhs(u, visc, l / n)) < TOL32
+    ps = NS.poissonsolver(g, precision=1)
+    ut = dev(u * 0 + np.random.default_rng(1).standard_normal(u.shape), "float32")
+    ref = ns.project(host(ut), l / n)
+    ps.project(ut)
+    assert rel(host(ut), ref) < TOL32
+
+
+@pytest.mark.parametrize("c,kind,n", [(3, "volume", 12), (4, "volume", 32), (2, "volume", 16), (8, "volume", 64),
+                                      (4, "face", 32), (3, "face", 24)])
+def test_filters(NS, c, kind, n):
+    import torch
+
+    l = 1.0
+    u = seeded_field(n, l, c)
+    m = n // c
+    ub = torch.empty((3, m, m, m), dtype=torch.float64, device="cuda")
+    NS.apply_filter(ub, dev(u), c, kind)
+    assert rel(host(ub), ns.apply_filter(u, c, kind)) < TOL64
+
+
+def test_filter_with_gaussian(NS):
+    import torch
+
+    n, c, l = 24, 3, 1.0
+    u = seeded_field(n, l, 9)
+    fd = ns.gaussian(l / n, 2 * l / (n // c), 2)
+    m = n // c
+    ub = torch.empty((3, m, m, m), dtype=torch.float64, device="cuda")
+    NS.apply_filter(ub, dev(u), c, "volume", fdelta=fd)
+    assert rel(host(ub), ns.volume_filter(u, c, fd)) < TOL64
+
+
+@pytest.mark.parametrize("n,c", [(12, 3), (32, 4), (48, 6)])
+def test_closure_flux_and_filtered_stress(NS, n, c):
+    import torch
+
+    l, visc = 1.0, 1 / 1000
+    h = l / n
+    u = seeded_field(n, l, 11)
+    k, p = ns.projected_rhs(u, visc, h)
+    m = n // c
+    r9 = torch.empty((9, m, m, m), dtype=torch.float64, device="cuda")
+    NS.get_rDHi(r9, dev(u), dev(p), visc, NS.Grid(l, n), c)
+    rd = ns.get_rDHi(ns.get_r(ns.stresstensor(u, visc, h), p), c)
+    assert rel(host(r9), np.stack([rd[key] for key in ns.NONSYM9])) < TOL64
+    s6 = torch.empty((6, m, m, m), dtype=torch.float64, device="cuda")
+    NS.get_sigmaDH(s6, dev(u), visc, NS.Grid(l, n), c)
+    sd = ns.get_sigmaDH(ns.stresstensor(u, visc, h), c)
+    assert rel(host(s6), np.stack([sd[key] for key in ns.SYM6])) < TOL64
+    # the nonsym divergence of rDHi reproduces filter(k) up to projection
+    du = torch.zeros((3, m, m, m), dtype=torch.float64, device="cuda")
+    NS.tensordivergence_tensor(du, r9, NS.Grid(l, m))
+    H = l / m
+    got = ns.project(host(du), H)
+    ref = ns.project(ns.volume_filter(k, c), H)
+    assert rel(got, ref) < 1e-11
+
+
+@pytest.mark.parametrize("n", [12])
+def test_golden_vectors(NS, n):
+    import torch
+
+    gd = dict(np.load(GOLDEN / f"literal_n{n}.npz"))
+    c, l, visc = int(gd["c"]), float(gd["l"]), float(gd["visc"])
+    g = NS.Grid(l, n)
+    u = dev(gd["u"])
+    du = torch.empty_like(u)
+    NS.tensordivergence(du, u, visc, g)
+    assert rel(host(du), gd["rhs"]) < TOL64
+    ps = NS.poissonsolver(g)
+    p = torch.empty((n, n, n), dtype=torch.float64, device="cuda")
+    ps.project(du, p)
+    assert rel(host(du), gd["k"]) < TOL64
+    assert rel(host(p), gd["p_rhs"]) < TOL64
+    m = n // c
+    ub = torch.empty((3, m, m, m), dtype=torch.float64, device="cuda")
+    NS.apply_DHpi(ub, u, NS.poissonsolver(NS.Grid(l, m)), c)
+    assert rel(host(ub), gd["ubar"]) < TOL64
+    r9 = torch.empty((9, m, m, m), dtype=torch.float64, device="cuda")
+    NS.get_rDHi(r9, u, p, visc, g, c)
+    assert rel(host(r9), gd["rdhi"]) < TOL64
+
+
+def test_propose_timestep(NS):
+    n, l, visc = 16, 1.0, 1 / 2000
+    u = seeded_field(n, l, 2)
+    dt = NS.propose_timestep(dev(u), visc, 0.3, NS.Grid(l, n))
+    assert abs(dt - ns.propose_timestep(u, visc, 0.3, l / n)) <= 1e-15 * dt
+
+
+def test_errors_are_reported(NS):
+    from exactclosure_gb300 import ExcError
+
+    with pytest.raises(ExcError):
+        NS.poissonsolver(NS.Grid(1.0, 100))

@@ -1,0 +1,150 @@
+"""CPU checks of the oracle: the vectorised restatement against the literal
+loop restatement and its golden vectors, and the reference's recorded
+invariants (exact closure to round-off, divergence-free random field)."""
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import literal as L
+from oracle import ns
+
+GOLDEN = Path(__file__).with_name("golden")
+
+
+@pytest.fixture(scope="module", params=[6, 12])
+def gold(request):
+    return dict(np.load(GOLDEN / f"literal_n{request.param}.npz"))
+
+
+def test_golden_rhs_divergence_projection(gold):
+    n, l, visc = int(gold["n"]), float(gold["l"]), float(gold["visc"])
+    h = l / n
+    u = gold["u"]
+    np.testing.assert_allclose(ns.rhs(u, visc, h), gold["rhs"], rtol=0, atol=1e-12 * np.abs(gold["rhs"]).max())
+    np.testing.assert_allclose(ns.divergence(u, h), gold["div"], rtol=0, atol=1e-12 * np.abs(gold["div"]).max())
+    pu, p = ns.project(u, h, return_p=True)
+    np.testing.assert_allclose(pu, gold["proj"], rtol=0, atol=1e-12 * np.abs(u).max())
+    np.testing.assert_allclose(p, gold["p"], rtol=0, atol=1e-12 * np.abs(gold["p"]).max())
+    k, prhs = ns.projected_rhs(u, visc, h)
+    np.testing.assert_allclose(k, gold["k"], rtol=0, atol=1e-12 * np.abs(gold["k"]).max())
+    np.testing.assert_allclose(prhs, gold["p_rhs"], rtol=0, atol=1e-12 * np.abs(gold["p_rhs"]).max())
+
+
+def test_golden_filters_and_closure(gold):
+    n, c, l, visc, dt = int(gold["n"]), int(gold["c"]), float(gold["l"]), float(gold["visc"]), float(gold["dt"])
+    h = l / n
+    u = gold["u"]
+    ub = ns.apply_DHpi(u, c, l)
+    np.testing.assert_allclose(ub, gold["ubar"], rtol=0, atol=1e-12 * np.abs(ub).max())
+    _, prhs = ns.projected_rhs(u, visc, h)
+    rd = ns.get_rDHi(ns.get_r(ns.stresstensor(u, visc, h), prhs), c)
+    got = np.stack([rd[k] for k in ns.NONSYM9])
+    np.testing.assert_allclose(got, gold["rdhi"], rtol=0, atol=1e-12 * np.abs(got).max())
+    sd = ns.get_sigmaDH(ns.stresstensor(u, visc, h), c)
+    got = np.stack([sd[k] for k in ns.SYM6])
+    np.testing.assert_allclose(got, gold["sigmadh"], rtol=0, atol=1e-12 * np.abs(got).max())
+    st = ns.step_classic_flux_div(ub, ub, u, prhs, visc, l, c, dt)
+    np.testing.assert_allclose(st, gold["cfd"], rtol=0, atol=1e-12 * np.abs(st).max())
+
+
+def test_literal_gaussian_kernels_match():
+    """Filters with the Gaussian FDelta of ``get_kernels`` (src/N.jl:1008-1020)."""
+    n, c, l, visc = 6, 3, 1.0, 0.02
+    h, H = l / n, l / (n // c)
+    rng = np.random.default_rng(1)
+    u = ns.project(rng.standard_normal((3, n, n, n)), h)
+    fd = ns.gaussian(h, 2 * H, 2)
+    assert len(fd) > 1
+    uL = [L.Field(L.from_ns(u[i])) for i in range(3)]
+    GDH, GDHi = L.get_kernels(c, fd)
+    ubL = L.apply_DHpi(uL, n // c, GDH, H)
+    ub = ns.apply_DHpi(u, c, l, fd)
+    assert max(np.abs(ub[i] - L.to_ns(ubL[i].data)).max() for i in range(3)) < 1e-13
+
+
+def test_randomfield_divergence_free_and_energy():
+    """``navierstokes-test.jl:10-29``: the random field is divergence free."""
+    n, l = 16, 1.0
+    u = ns.randomfield(n, l, kpeak=4, seed=3)
+    h = l / n
+    assert np.abs(ns.divergence(u, h)).max() < 1e-12 * np.abs(u).max() / h
+    assert abs(ns.kinetic_energy(u) - 1.0) < 1e-3
+    k, s = ns.spectrum(u, l)
+    assert len(s) == (2 * (n // 2)) // 3 and np.all(s >= 0)
+
+
+def test_projection_is_idempotent_and_kills_divergence():
+    n, l = 12, 2.0
+    h = l / n
+    rng = np.random.default_rng(2)
+    u = rng.standard_normal((3, n, n, n))
+    pu = ns.project(u, h)
+    assert np.abs(ns.divergence(pu, h)).max() < 1e-12 * np.abs(u).max() / h
+    np.testing.assert_allclose(ns.project(pu, h), pu, atol=1e-13 * np.abs(u).max())
+
+
+@pytest.mark.parametrize("c,kind", [(3, "volume"), (2, "volume"), (4, "volume"), (4, "face"), (3, "face")])
+def test_exact_closure_invariant(c, kind):
+    """An LES carrying the exact commutator at every RK4 stage stays equal to
+    the filtered DNS (the reference's recorded 5.69e-15, navierstokes.jl:33)."""
+    n, l, visc = 24, 1.0, 1 / 2000
+    u = ns.randomfield(n, l, kpeak=4, seed=0)
+    les = [ns.Les(c=c, kind=kind)]
+    u1, dts, _ = ns.dnsaid_rk4(u, visc, l, 0.3, 4, les)
+    tgt = ns.filtered_target(u1, les[0], l)
+    assert ns.rel_l2(les[0].v_exact, tgt) < 1e-13
+    assert ns.rel_l2(les[0].v_nomodel, tgt) > 1e-3
+    assert all(d > 0 for d in dts)
+
+
+@pytest.mark.parametrize("c", [2, 3, 4])
+def test_flux_form_equals_commutator(c):
+    """P_H(delta_H sigma_H(ubar) - delta_H^ns rDHi) == P_H filter(k) - P_H RHS_H(ubar)
+    (src/N.jl:1189-1206), including the even-ratio extension."""
+    n, l, visc = 24, 1.0, 1 / 1000
+    h = l / n
+    u = ns.randomfield(n, l, kpeak=3, seed=5)
+    k, p = ns.projected_rhs(u, visc, h)
+    ub = ns.apply_DHpi(u, c, l)
+    m1 = ns.closure(k, ub, visc, l, c, "volume")
+    m2 = ns.project(ns.closure_flux_div(u, p, visc, l, c, ub), l / (n // c))
+    assert ns.rel_l2(m2, m1) < 1e-13
+
+
+def test_even_taps_reduce_to_box_and_trapezoid():
+    o, w = ns.axis_taps(4, ns.FACE, ns.VOLUME)
+    assert list(o) == [1, 2, 3, 4, 5] and np.allclose(w, [1 / 8, 1 / 4, 1 / 4, 1 / 4, 1 / 8])
+    o, w = ns.axis_taps(4, ns.CENTRE, ns.VOLUME)
+    assert list(o) == [0, 1, 2, 3] and np.allclose(w, 0.25)
+    o, w = ns.axis_taps(4, ns.CENTRE, ns.POINT)
+    assert list(o) == [1, 2] and np.allclose(w, 0.5)
+    o, w = ns.axis_taps(5, ns.CENTRE, ns.POINT)
+    assert list(o) == [2]
+    o, w = ns.axis_taps(5, ns.FACE, ns.VOLUME)
+    assert list(o) == [2, 3, 4, 5, 6] and np.allclose(w, 0.2)
+
+
+def test_rk4_fourth_order_in_time():
+    n, l, visc = 8, 1.0, 1 / 200
+    h = l / n
+    u = ns.randomfield(n, l, kpeak=2, seed=1)
+    T = 0.02
+    ref = u
+    for _ in range(64):
+        ref = ns.step_rk4(ref, visc, h, T / 64)
+    errs = []
+    for m in (4, 8):
+        v = u
+        for _ in range(m):
+            v = ns.step_rk4(v, visc, h, T / m)
+        errs.append(np.linalg.norm(v - ref))
+    order = math.log2(errs[0] / errs[1])
+    assert order > 3.5
+
+
+def test_counter_normal_statistics():
+    x = ns.counter_normal(0, 200000)
+    assert abs(x.mean()) < 0.01 and abs(x.std() - 1) < 0.01
+    assert np.array_equal(ns.counter_normal(5, 10, offset=3), ns.counter_normal(5, 13)[3:])

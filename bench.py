@@ -205,7 +205,7 @@ def main():
     stream = torch.cuda.Stream()
     cs = NS.Case(n, 1.0, args.visc, 0.3, precision=prec, les=les, stream=stream.cuda_stream)
     cs.init_random(args.kpeak, 1.0, seed=rank)
-    cs.step(max(args.warmup, 3) if args.warmup >= 3 else args.warmup)
+    cs.step(args.warmup)
     cs.sync()
     launches = cs.launches_per_step()
 

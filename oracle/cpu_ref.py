@@ -1,0 +1,117 @@
+"""ctypes driver of the oracle's C/OpenMP restatement (``oracle/cpu_ref.c``).
+
+TEST INFRASTRUCTURE ONLY: used by the tests as a second oracle and by
+``bench.py`` as the timed CPU baseline; never by the product path."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import time
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libexc_cpu_ref.so"
+_lib = None
+
+
+def available() -> bool:
+    return LIB.exists()
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(str(LIB))
+        L.cref_threads.restype = C.c_int
+        L.cref_create.restype = C.c_void_p
+        L.cref_create.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                                  C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.cref_destroy.argtypes = [C.c_void_p]
+        L.cref_init_random.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_uint64]
+        L.cref_set_velocity.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.cref_get_velocity.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.cref_get_les.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.cref_step.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        L.cref_stage.argtypes = [C.c_void_p, C.c_int]
+        L.cref_time.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        for f in ("cref_init_random", "cref_set_velocity", "cref_get_velocity", "cref_get_les", "cref_step",
+                  "cref_stage", "cref_time"):
+            getattr(L, f).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+class CpuCase:
+    """The C restatement of the RK4 DNS-aided LES step (same layout as libexc)."""
+
+    def __init__(self, n, l, visc, cfl, les):
+        r = (C.c_int * 4)(*[c for c, _ in les] + [0] * (4 - len(les)))
+        k = (C.c_int * 4)(*[0 if kd == "volume" else 1 for _, kd in les] + [0] * (4 - len(les)))
+        self.n = n
+        self.les = list(les)
+        self._h = lib().cref_create(n, l, visc, cfl, len(les), r, k)
+        if not self._h:
+            raise MemoryError("cref_create failed")
+
+    def init_random(self, kpeak, energy, seed):
+        assert lib().cref_init_random(self._h, kpeak, energy, seed) == 0
+
+    def set_velocity(self, u):
+        import numpy as np
+
+        a = np.ascontiguousarray(u, dtype=np.float64)
+        assert lib().cref_set_velocity(self._h, a.ctypes.data_as(C.POINTER(C.c_double))) == 0
+
+    def velocity(self):
+        import numpy as np
+
+        a = np.empty((3, self.n, self.n, self.n))
+        assert lib().cref_get_velocity(self._h, a.ctypes.data_as(C.POINTER(C.c_double))) == 0
+        return a
+
+    def les_field(self, i, which):
+        import numpy as np
+
+        m = self.n // self.les[i][0]
+        a = np.empty((3, m, m, m))
+        w = {"target": 0, "exact": 1, "nomodel": 2}[which]
+        assert lib().cref_get_les(self._h, i, w, a.ctypes.data_as(C.POINTER(C.c_double))) == 0
+        return a
+
+    def step(self, nsteps=1, dt=0.0):
+        assert lib().cref_step(self._h, nsteps, dt) == 0
+
+    def stage(self, s):
+        assert lib().cref_stage(self._h, s) == 0
+
+    def close(self):
+        if self._h:
+            lib().cref_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def time_stages(n, les, kpeak, visc, budget_s=20.0):
+    """Time whole RK4 stages of the full-size workload on all host threads."""
+    cs = CpuCase(n, 1.0, visc, 0.3, les)
+    cs.init_random(kpeak, 1.0, 0)
+    cs.stage(0)  # warm-up (page faults, dt)
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        cs.stage(1 + (k % 3))
+        k += 1
+        if time.perf_counter() - t0 > budget_s * 0.5 or k >= 8:
+            break
+    el = time.perf_counter() - t0
+    cs.close()
+    steps = k / 4.0
+    threads = lib().cref_threads()
+    return {"cell_updates_per_s": n ** 3 * steps / el, "threads": threads,
+            "sample": f"C/OpenMP restatement, {k} RK4 stage(s) of the {n}^3 DNS with LES ratios "
+                      f"{[c for c, _ in les]} at full size ({k}/4 RK4 steps), {threads} threads"}

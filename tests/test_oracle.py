@@ -144,6 +144,35 @@ def test_rk4_fourth_order_in_time():
     assert order > 3.5
 
 
+def test_c_restatement_matches_numpy_oracle():
+    """The C/OpenMP restatement (the timed CPU baseline) agrees with the NumPy
+    oracle on the full DNS-aided RK4 step, odd/even ratios, both filters."""
+    import importlib.util
+    from pathlib import Path
+
+    spec = importlib.util.spec_from_file_location("bc", Path(__file__).parents[1] / "oracle" / "build_cpu.py")
+    bc = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bc)
+    if bc.build() is None:
+        pytest.skip("no C compiler")
+    from oracle import cpu_ref
+
+    n, l, visc = 24, 1.0, 1 / 2000
+    les = [(3, "volume"), (2, "face"), (4, "volume")]
+    cs = cpu_ref.CpuCase(n, l, visc, 0.3, les)
+    cs.init_random(4, 1.0, 0)
+    ref = ns.randomfield(n, l, 4, 0)
+    assert ns.rel_l2(cs.velocity(), ref) < 1e-13
+    ol = [ns.Les(c=c, kind=k) for c, k in les]
+    r1, _, _ = ns.dnsaid_rk4(ref, visc, l, 0.3, 2, ol)
+    cs.step(2)
+    assert ns.rel_l2(cs.velocity(), r1) < 1e-13
+    for i in range(3):
+        assert ns.rel_l2(cs.les_field(i, "exact"), ol[i].v_exact) < 1e-13
+        assert ns.rel_l2(cs.les_field(i, "nomodel"), ol[i].v_nomodel) < 1e-13
+    cs.close()
+
+
 def test_counter_normal_statistics():
     x = ns.counter_normal(0, 200000)
     assert abs(x.mean()) < 0.01 and abs(x.std() - 1) < 0.01

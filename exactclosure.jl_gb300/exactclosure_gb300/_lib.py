@@ -52,6 +52,7 @@ SIGNATURES = {
     "exc_poisson_destroy": [vp],
     "exc_poisson_solve": [vp, vp, vp, vp],
     "exc_project": [vp, vp, vp, vp],
+    "exc_project_noalloc": [i32, i32, f64, vp, vp, vp],
     "exc_max_abs": [i32, szt, vp, vp, vp],
     "exc_propose_timestep": [i32, i32, f64, f64, f64, vp, dp, vp],
     "exc_filter": [i32, i32, i32, i32, dp, i32, vp, vp, vp],

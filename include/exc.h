@@ -93,6 +93,18 @@ int exc_poisson_solve(exc_poisson* ps, const void* d, void* p, void* stream);
  * p_out (n^3, may be NULL) receives the pressure. */
 int exc_project(exc_poisson* ps, void* u, void* p_out, void* stream);
 
+/* exc_project without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc (a host whose
+ * device memory belongs to its own pool, a loop under a fixed memory budget,
+ * code that cannot afford the synchronisation cudaFree implies).  Its work
+ * array lives in one static 4 MiB device array that every GPU loading the
+ * library holds until exit, so grids are limited to n <= 72 (EXC_F64) and
+ * n <= 96 (EXC_F32); larger n returns EXC_ERR_SHAPE.  The first call on a
+ * device looks the array up (cudaGetSymbolAddress) and should come before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race. */
+int exc_project_noalloc(int precision, int n, double l, void* u, void* p_out, void* stream);
+
 /* max_i |x_i| over `count` words, written as a double to *out_dev (device). */
 int exc_max_abs(int precision, size_t count, const void* x, double* out_dev, void* stream);
 

@@ -30,6 +30,7 @@ struct LesState {
   long long M = 0;
   exc_poisson ps;
   T* buf = nullptr;  // one allocation, sliced below (3M words each)
+  T* tb = nullptr;   // filter scratch: 3 n (n/c)^2 words (transverse box sums)
   T *ub, *fk, *mcl, *mlast, *rtmp;
   T *ve[2], *ves, *ke;  // exact LES: state (ping-pong), stage, k
   T *vn[2], *vns, *kn;  // no-model LES
@@ -80,8 +81,9 @@ static int project_vec(exc_poisson* ps, T* u, cudaStream_t st) {
 // ubar = target(src): filter, then project for the volume filter.
 template <typename T>
 static int les_target(CaseImpl<T>* ci, LesState<T>& L, const T* src, T* out, cudaStream_t st) {
-  int rc = filter_vector<T>(ci->n, L.c, L.kind, nullptr, 0, src, out, st);
-  if (rc) return rc;
+  cudaError_t e = filter_vector_box<T>(ci->n, L.c, L.kind, src, out, L.tb, st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  int rc = EXC_OK;
   if (L.kind == EXC_FILTER_VOLUME) rc = project_vec<T>(&L.ps, out, st);
   return rc;
 }
@@ -120,8 +122,9 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
       const int m = L.m;
       const T H = (T)(cs->desc.l / m);
       // m_s = P_H(filter(k_s) - RHS_H(ubar_s))
-      int rc = filter_vector<T>(n, L.c, L.kind, nullptr, 0, ci->rhs, L.mcl, st);
-      if (rc) return rc;
+      e = filter_vector_box<T>(n, L.c, L.kind, ci->rhs, L.mcl, L.tb, st);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      int rc;
       e = launch_rhs<T>(m, H, visc, L.ub, L.rtmp, false, st);
       if (e == cudaSuccess) e = launch_axpy<T>(3 * L.M, L.mcl, L.rtmp, (T)-1, st);
       if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
@@ -209,6 +212,7 @@ static void case_destroy(exc_case* cs) {
   for (int li = 0; li < ci->nles; ++li) {
     poisson_free(&ci->les[li].ps);
     if (ci->les[li].buf) cudaFree(ci->les[li].buf);
+    if (ci->les[li].tb) cudaFree(ci->les[li].tb);
   }
   delete ci;
   cs->impl = nullptr;
@@ -253,6 +257,8 @@ static int case_create(exc_case* cs) {
     size_t nb = 14 * 3 * L.M * sizeof(T);
     if (cudaMalloc(&L.buf, nb) != cudaSuccess) { set_last_error("out of device memory (LES fields)"); return EXC_ERR_OOM; }
     cudaMemset(L.buf, 0, nb);
+    size_t tbb = 3 * (size_t)d.n * L.m * L.m * sizeof(T);
+    if (cudaMalloc(&L.tb, tbb) != cudaSuccess) { set_last_error("out of device memory (LES filter scratch)"); return EXC_ERR_OOM; }
     T* p = L.buf;
     auto take = [&]() { T* q = p; p += 3 * L.M; return q; };
     L.ub = take(); L.fk = take(); L.mcl = take(); L.mlast = take(); L.rtmp = take();
@@ -428,6 +434,21 @@ static int energy(exc_case* cs, double* out) {
   return EXC_OK;
 }
 
+// visc * mean_ij (delta_j u_i)^2 summed over i, j (FP64).
+template <typename T>
+static int dissipation(exc_case* cs, double* out) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  cudaStream_t st = cs->stream;
+  double* dv = ci->dscal + 12;
+  cudaError_t e = launch_gradsq<T>(ci->n, ci->u[ci->cur], ci->part, dv, st);
+  double host[2];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, dv, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  *out = cs->desc.visc * host[0] / (ci->h * ci->h) / (double)ci->N;
+  return EXC_OK;
+}
+
 template <typename T>
 static int spectrum(exc_case* cs, double* host_e, int nshell) {
   CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
@@ -581,6 +602,11 @@ int exc_case_time(exc_case* cs, double* t, double* last_dt) {
 int exc_case_energy(exc_case* cs, double* e) {
   if (!cs || !e) { set_last_error("null argument"); return EXC_ERR_ARG; }
   return DISPATCH(cs, energy, cs, e);
+}
+
+int exc_case_dissipation(exc_case* cs, double* eps) {
+  if (!cs || !eps) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, dissipation, cs, eps);
 }
 
 int exc_case_spectrum(exc_case* cs, double* host_e, int nshell) {

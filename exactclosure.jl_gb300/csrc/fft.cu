@@ -15,7 +15,7 @@ namespace exc {
 // With DIV the input line is d = div(u) (src/N.jl:222-238) computed on the fly.
 // ---------------------------------------------------------------------------
 template <typename T, bool DIV>
-__global__ void __launch_bounds__(FFT_THREADS)
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ out, int P,
              const cplx<T>* __restrict__ tw, FftPlan plan, int rows_per_cta) {
   using C = cplx<T>;
@@ -76,7 +76,7 @@ r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ ou
 // outer = y): a CTA loads `W` consecutive kx columns of one outer index.
 // ---------------------------------------------------------------------------
 template <typename T, bool INV>
-__global__ void __launch_bounds__(FFT_THREADS)
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_stride,
             long long outer_stride, const cplx<T>* __restrict__ tw, FftPlan plan) {
   using C = cplx<T>;
@@ -98,6 +98,17 @@ cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_strid
   }
 }
 
+// 1/d in float64 for d in (0, 3] (a sum of three sin^2): a single-precision
+// estimate refined by two Newton-Raphson steps r <- r + r(1 - d r), each of
+// which squares the relative error (6e-8 -> 4e-15 -> below the float64 ulp).
+__device__ __forceinline__ double recip_f64(double d) {
+  double r = (double)__frcp_rn((float)d);
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
 // ---------------------------------------------------------------------------
 // z pass with the spectral divide: forward FFT along z, multiply by
 // 1/(lambda N) with lambda = -4/h^2 sum_d sin^2(pi k_d/n) (src/N.jl:281-291)
@@ -105,7 +116,7 @@ cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_strid
 // divide is computed in float64 for every precision.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(FFT_THREADS)
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<T>* __restrict__ tw,
               FftPlan plan, const double* __restrict__ sin2, double coef) {
   using C = cplx<T>;
@@ -128,7 +139,7 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
     int l = t / n, kz = t - l * n;
     int kx = kx0 + l;
     double den = sin2[kx] + sy + sin2[kz];
-    double f = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef / den;
+    double f = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef * recip_f64(den);
     C v = s[l * ls + kz];
     v.x = (T)((double)v.x * f);
     v.y = (T)((double)v.y * f);
@@ -148,7 +159,7 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
 //   z = IDFT_{N2}(Z) (unnormalised), x_2m = Re z_m, x_2m+1 = Im z_m.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(FFT_THREADS)
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 c2r_x_kernel(cplx<T>* __restrict__ g, int n, int P, const cplx<T>* __restrict__ tw, FftPlan plan,
              int rows_per_cta) {
   using C = cplx<T>;
@@ -208,9 +219,9 @@ __global__ void copy_pitched_kernel(const T* __restrict__ src, int pitch, T* __r
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-static int col_width(int n) {
+static int col_width(int n, int tile) {
   int w = 1;
-  while (w * 2 * n <= FFT_TILE && w < 64) w *= 2;
+  while (w * 2 * n <= tile && w < 64) w *= 2;
   return w;
 }
 
@@ -222,26 +233,26 @@ cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vec
   const C* tw = reinterpret_cast<const C*>(ps->tw);
   const long long nn = (long long)n * n;
   // x forward
-  int rows = FFT_TILE / (N2 + 1);
+  int rows = fft_tile<C>() / (N2 + 1);
   if (rows > nn) rows = (int)nn;
   size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
   int gx = (int)((nn + rows - 1) / rows);
   if (src_is_vector)
-    r2c_x_kernel<T, true><<<gx, FFT_THREADS, shx, st>>>(src, n, (T)(1.0 / ps->h), g, P, tw, ps->plan_h, rows);
+    r2c_x_kernel<T, true><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)(1.0 / ps->h), g, P, tw, ps->plan_h, rows);
   else
-    r2c_x_kernel<T, false><<<gx, FFT_THREADS, shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows);
+    r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows);
   // y forward
-  int W = col_width(n);
+  int W = col_width(n, fft_tile<C>());
   dim3 gc((nkx + W - 1) / W, n);
   size_t shc = (size_t)W * (n + 1) * sizeof(C);
-  cols_kernel<T, false><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
   // z forward + divide + inverse; coef = 1/(lambda N) numerator: -h^2/(4 N)
   double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
-  zsolve_kernel<T><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef);
+  zsolve_kernel<T><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef);
   // y inverse
-  cols_kernel<T, true><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
   // x inverse (in place)
-  c2r_x_kernel<T><<<gx, FFT_THREADS, shx, st>>>(g, n, P, tw, ps->plan_h, rows);
+  c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows);
   return cudaGetLastError();
 }
 
@@ -254,16 +265,16 @@ cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st) {
   C* g = reinterpret_cast<C*>(ps->work);
   const C* tw = reinterpret_cast<const C*>(ps->tw);
   const long long nn = (long long)n * n;
-  int rows = FFT_TILE / (N2 + 1);
+  int rows = fft_tile<C>() / (N2 + 1);
   if (rows > nn) rows = (int)nn;
   size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
   int gx = (int)((nn + rows - 1) / rows);
-  r2c_x_kernel<T, false><<<gx, FFT_THREADS, shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows);
-  int W = col_width(n);
+  r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows);
+  int W = col_width(n, fft_tile<C>());
   dim3 gc((nkx + W - 1) / W, n);
   size_t shc = (size_t)W * (n + 1) * sizeof(C);
-  cols_kernel<T, false><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
-  cols_kernel<T, false><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n);
+  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n);
   return cudaGetLastError();
 }
 
@@ -274,16 +285,16 @@ cudaError_t fft3d_inverse(exc_poisson* ps, cudaStream_t st) {
   C* g = reinterpret_cast<C*>(ps->work);
   const C* tw = reinterpret_cast<const C*>(ps->tw);
   const long long nn = (long long)n * n;
-  int W = col_width(n);
+  int W = col_width(n, fft_tile<C>());
   dim3 gc((nkx + W - 1) / W, n);
   size_t shc = (size_t)W * (n + 1) * sizeof(C);
-  cols_kernel<T, true><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n);
-  cols_kernel<T, true><<<gc, FFT_THREADS, shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
-  int rows = FFT_TILE / (N2 + 1);
+  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n);
+  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  int rows = fft_tile<C>() / (N2 + 1);
   if (rows > nn) rows = (int)nn;
   size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
   int gx = (int)((nn + rows - 1) / rows);
-  c2r_x_kernel<T><<<gx, FFT_THREADS, shx, st>>>(g, n, P, tw, ps->plan_h, rows);
+  c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows);
   return cudaGetLastError();
 }
 
@@ -308,7 +319,7 @@ template cudaError_t copy_pressure<float>(const exc_poisson*, float*, cudaStream
 template <typename T>
 static cudaError_t configure_fft_t() {
   using C = cplx<T>;
-  int maxsh = (int)(FFT_TILE + 64 * 2) * (int)sizeof(C);
+  int maxsh = (int)(fft_tile<C>() + 64 * 2) * (int)sizeof(C);
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;

@@ -12,14 +12,15 @@
 
 namespace exc {
 
-constexpr int FFT_THREADS = 256;
-constexpr int FFT_TILE = 4096;  // max complex values per CTA (nlines * L)
-constexpr int FFT_MAXPASS = 12;
-
+// Threads per CTA: one radix-8 butterfly per thread per pass over a full tile.
+template <typename C> constexpr int fft_threads() { return sizeof(C) == 16 ? 256 : 512; }
+// Max complex values per CTA (nlines * L): 32 KB of shared memory.
+template <typename C> constexpr int fft_tile() { return 32768 / (int)sizeof(C); }
+// Pass sequence of a length-L transform: n8 radix-8 passes, then at most one
+// radix-4 or radix-2 pass, then n3 radix-3 passes (L = 8^n8 4^n4 2^n2 3^n3).
 struct FftPlan {
-  int L;             // transform length
-  int npass;
-  int radix[FFT_MAXPASS];
+  int L;
+  int n8, n4, n2, n3;
 };
 
 inline FftPlan make_plan(int L) {
@@ -28,12 +29,10 @@ inline FftPlan make_plan(int L) {
   int m = L, a = 0, b = 0;
   while (m % 2 == 0) { m /= 2; ++a; }
   while (m % 3 == 0) { m /= 3; ++b; }
-  int np = 0;
-  while (a >= 3) { p.radix[np++] = 8; a -= 3; }
-  if (a == 2) p.radix[np++] = 4;
-  if (a == 1) p.radix[np++] = 2;
-  while (b-- > 0) p.radix[np++] = 3;
-  p.npass = np;
+  p.n8 = a / 3;
+  p.n4 = (a % 3) == 2;
+  p.n2 = (a % 3) == 1;
+  p.n3 = b;
   return p;
 }
 
@@ -91,7 +90,8 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft_small
 template <int R, bool INV, typename C>
 __device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns,
                                          const C* __restrict__ tw, int n) {
-  constexpr int NB = (FFT_TILE / R + FFT_THREADS - 1) / FFT_THREADS;
+  constexpr int NT = fft_threads<C>();
+  constexpr int NB = (fft_tile<C>() / R + NT - 1) / NT;
   const int nb = L / R;
   const int total = nlines * nb;
   const int twmul = n / (Ns * R);
@@ -99,7 +99,7 @@ __device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns
   int obase[NB];
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
-    int t = threadIdx.x + b * FFT_THREADS;
+    int t = threadIdx.x + b * NT;
     obase[b] = -1;
     if (t < total) {
       int line = t / nb, j = t - line * nb;
@@ -129,21 +129,17 @@ __device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns
   __syncthreads();
 }
 
-// Full transform of every line in the tile (natural-order in and out).
+// Full transform of every line in the tile (natural-order in and out).  One
+// loop per radix keeps each pass body's registers separate.
 template <bool INV, typename C>
 __device__ void fft_lines(C* s, int ls, int nlines, const FftPlan& plan,
                           const C* __restrict__ tw, int n) {
   int Ns = 1;
-  for (int p = 0; p < plan.npass; ++p) {
-    int R = plan.radix[p];
-    switch (R) {
-      case 8: fft_pass<8, INV>(s, ls, nlines, plan.L, Ns, tw, n); break;
-      case 4: fft_pass<4, INV>(s, ls, nlines, plan.L, Ns, tw, n); break;
-      case 3: fft_pass<3, INV>(s, ls, nlines, plan.L, Ns, tw, n); break;
-      default: fft_pass<2, INV>(s, ls, nlines, plan.L, Ns, tw, n); break;
-    }
-    Ns *= R;
-  }
+  const int L = plan.L;
+  for (int q = 0; q < plan.n8; ++q) { fft_pass<8, INV>(s, ls, nlines, L, Ns, tw, n); Ns *= 8; }
+  if (plan.n4) { fft_pass<4, INV>(s, ls, nlines, L, Ns, tw, n); Ns *= 4; }
+  if (plan.n2) { fft_pass<2, INV>(s, ls, nlines, L, Ns, tw, n); Ns *= 2; }
+  for (int q = 0; q < plan.n3; ++q) { fft_pass<3, INV>(s, ls, nlines, L, Ns, tw, n); Ns *= 3; }
 }
 
 }  // namespace exc

@@ -174,6 +174,46 @@ __global__ void fold_pairs_kernel(int nb, const double* __restrict__ part, doubl
     out[1] = s1;
   }
 }
+// sum_ij (delta_j u_i)^2 over all cells (forward differences, FP64): the
+// discrete dissipation of the viscous term -visc delta_j(delta_j u_i +
+// delta_i u_j) of `stress` (src/N.jl:106-118) for a divergence-free u.
+template <typename T>
+__global__ void gradsq_partial_kernel(int n, const T* __restrict__ u, double* __restrict__ part) {
+  __shared__ double r0[256];
+  const long long N = (long long)n * n * n;
+  double s = 0;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
+    long long r = g / n;
+    int x = (int)(g - r * n);
+    int z = (int)(r / n);
+    int y = (int)(r - (long long)z * n);
+    long long nb[3] = {g - x + wrap_up(x, n), ((long long)z * n + wrap_up(y, n)) * n + x,
+                       ((long long)wrap_up(z, n) * n + y) * n + x};
+    for (int i = 0; i < 3; ++i) {
+      double c = (double)u[i * N + g];
+      for (int j = 0; j < 3; ++j) {
+        double d = (double)u[i * N + nb[j]] - c;
+        s += d * d;
+      }
+    }
+  }
+  r0[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) r0[threadIdx.x] += r0[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = r0[0]; part[2 * blockIdx.x + 1] = 0.0; }
+}
+template <typename T>
+cudaError_t launch_gradsq(int n, const T* u, double* part, double* out, cudaStream_t st) {
+  gradsq_partial_kernel<T><<<RED_BLOCKS, 256, 0, st>>>(n, u, part);
+  fold_pairs_kernel<<<1, 32, 0, st>>>(RED_BLOCKS, part, out);
+  return cudaGetLastError();
+}
+template cudaError_t launch_gradsq<double>(int, const double*, double*, double*, cudaStream_t);
+template cudaError_t launch_gradsq<float>(int, const float*, double*, double*, cudaStream_t);
+
 template <typename T>
 cudaError_t launch_sqdiff(long long count, const T* a, const T* b, double* part, double* out, cudaStream_t st) {
   sqdiff_partial_kernel<T><<<RED_BLOCKS, 256, 0, st>>>(count, a, b, part);

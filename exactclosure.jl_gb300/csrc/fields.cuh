@@ -16,6 +16,8 @@ cudaError_t launch_set_dt(const double* umax, double h, double visc, double cfl,
 template <typename T>
 cudaError_t launch_normals(long long count, unsigned long long seed, T* out, cudaStream_t st);
 template <typename T>
+cudaError_t launch_gradsq(int n, const T* u, double* part, double* out, cudaStream_t st);
+template <typename T>
 cudaError_t launch_sqdiff(long long count, const T* a, const T* b, double* part, double* out, cudaStream_t st);
 template <typename T>
 cudaError_t launch_shell_energy(int n, int P, int ncomp, const cplx<T>* spec, long long cstride, double scale,
@@ -30,6 +32,6 @@ cudaError_t launch_unpitch(int n, const T* src, int pitch, T* dst, T scale, cuda
 template <typename A, typename B>
 cudaError_t launch_convert(long long count, const A* a, B* b, cudaStream_t st);
 
-constexpr int RED_PARTS = 304;
+constexpr int RED_PARTS = 1216;
 
 }  // namespace exc

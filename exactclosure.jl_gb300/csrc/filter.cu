@@ -210,7 +210,94 @@ int filtered_stress(int n, int c, double l, double visc, const double* fdelta, i
   return EXC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Two-stage box filter of a vector field (volume or face average without a
+// Gaussian), the form the case stepper uses every stage.  Stage 1 reads each
+// fine value once, coalesced: for component i it sums the c x c fine cells of
+// each coarse transverse cell at every fine position along axis i,
+//   tb_0[(Jz m + Jy) n + x], tb_1[(Jz n + y) m + Jx], tb_2[(z m + Jy) m + Jx].
+// Stage 2 applies the own-axis taps of build_taps (trapezoid/box or face
+// point sample) and the transverse weight 1/c^2.  Both stages sum in a fixed
+// order, so the result is bit-reproducible.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void tb_kernel(const T* __restrict__ f3, int n, int c, T* __restrict__ tb3) {
+  const int comp = blockIdx.y;
+  const int m = n / c;
+  const long long N = (long long)n * n * n;
+  const long long Mt = (long long)n * m * m;
+  const T* __restrict__ f = f3 + comp * N;
+  T* __restrict__ tb = tb3 + comp * Mt;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < Mt; g += (long long)gridDim.x * blockDim.x) {
+    T acc = (T)0;
+    if (comp == 0) {
+      const int x = (int)(g % n);
+      const long long r = g / n;
+      const int Jy = (int)(r % m), Jz = (int)(r / m);
+      const T* p = f + ((long long)(c * Jz) * n + c * Jy) * n + x;
+      for (int dz = 0; dz < c; ++dz)
+        for (int dy = 0; dy < c; ++dy) acc += p[((long long)dz * n + dy) * n];
+    } else if (comp == 1) {
+      const int Jx = (int)(g % m);
+      const long long r = g / m;
+      const int y = (int)(r % n), Jz = (int)(r / n);
+      const T* p = f + ((long long)(c * Jz) * n + y) * n + c * Jx;
+      for (int dz = 0; dz < c; ++dz)
+        for (int dx = 0; dx < c; ++dx) acc += p[(long long)dz * n * n + dx];
+    } else {
+      const int Jx = (int)(g % m);
+      const long long r = g / m;
+      const int Jy = (int)(r % m), z = (int)(r / m);
+      const T* p = f + ((long long)z * n + c * Jy) * n + c * Jx;
+      for (int dy = 0; dy < c; ++dy)
+        for (int dx = 0; dx < c; ++dx) acc += p[(long long)dy * n + dx];
+    }
+    tb[g] = acc;
+  }
+}
+
+template <typename T>
+__global__ void oa_kernel(const T* __restrict__ tb3, int n, int c, Taps1D taps, double scale, T* __restrict__ out3) {
+  const int comp = blockIdx.y;
+  const int m = n / c;
+  const long long M = (long long)m * m * m;
+  const long long Mt = (long long)n * m * m;
+  const T* __restrict__ tb = tb3 + comp * Mt;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < M; g += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(g % m);
+    const long long r = g / m;
+    const int iy = (int)(r % m), iz = (int)(r / m);
+    const int own = comp == 0 ? ix : (comp == 1 ? iy : iz);
+    double acc = 0.0;
+    for (int t = 0; t < taps.cnt; ++t) {
+      int fi = c * own + taps.off[t];
+      fi = fi >= n ? fi - n : (fi < 0 ? fi + n : fi);
+      long long idx;
+      if (comp == 0) idx = ((long long)iz * m + iy) * n + fi;
+      else if (comp == 1) idx = ((long long)iz * n + fi) * m + ix;
+      else idx = ((long long)fi * m + iy) * m + ix;
+      acc += taps.w[t] * (double)tb[idx];
+    }
+    out3[comp * M + g] = (T)(acc * scale);
+  }
+}
+
+template <typename T>
+cudaError_t filter_vector_box(int n, int c, int kind, const T* u, T* ub, T* tb, cudaStream_t st) {
+  const int m = n / c;
+  const long long Mt = (long long)n * m * m;
+  const long long M = (long long)m * m * m;
+  Taps1D taps = build_taps(c, true, kind == EXC_FILTER_FACE, nullptr, 0);
+  // the transverse box weight 1/c is applied once per axis here; the own-axis
+  // taps already carry their 1/c
+  const double scale = 1.0 / ((double)c * c);
+  tb_kernel<T><<<dim3(grid_for(Mt), 3), 256, 0, st>>>(u, n, c, tb);
+  oa_kernel<T><<<dim3(grid_for(M), 3), 256, 0, st>>>(tb, n, c, taps, scale, ub);
+  return cudaGetLastError();
+}
+
 #define INST(T)                                                                                          \
+  template cudaError_t filter_vector_box<T>(int, int, int, const T*, T*, T*, cudaStream_t);              \
   template int filter_vector<T>(int, int, int, const double*, int, const T*, T*, cudaStream_t);          \
   template int closure_flux<T>(int, int, double, double, const double*, int, const T*, const T*, T*,     \
                                cudaStream_t);                                                            \

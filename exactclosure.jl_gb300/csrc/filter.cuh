@@ -20,6 +20,10 @@ int make_taps3(int c, const bool stag[3], const bool point[3], const double* fde
 
 template <typename T>
 int filter_vector(int n, int c, int kind, const double* fdelta, int nfd, const T* u, T* ub, cudaStream_t st);
+// Box-only volume/face filter in two coalesced passes; tb: 3 n (n/c)^2 words
+// of scratch.
+template <typename T>
+cudaError_t filter_vector_box(int n, int c, int kind, const T* u, T* ub, T* tb, cudaStream_t st);
 template <typename T>
 int closure_flux(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, const T* p,
                  T* r9, cudaStream_t st);

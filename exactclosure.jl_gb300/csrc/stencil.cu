@@ -5,127 +5,6 @@
 namespace exc {
 
 // ---------------------------------------------------------------------------
-// RHS sweep: du = doadd*du - div sigma(u) (`stresstensor` + `tensordivergence!`,
-// src/N.jl:94-160).  A CTA stages its TX x TY x TZ tile of u plus a one-cell
-// halo in shared memory, evaluates each stress component once on the index
-// set the divergence needs (diagonal: tile + 1 along i; edge ij: tile - 1
-// along i and j), then forms the divergence.  Stresses are kept divided by h.
-// ---------------------------------------------------------------------------
-constexpr int RTX = 16, RTY = 8, RTZ = 4;
-constexpr int RBX = RTX + 2, RBY = RTY + 2, RBZ = RTZ + 2;  // u and stress box, origin tile-1
-constexpr int RHS_THREADS = 256;
-
-template <typename T>
-struct RhsSmem {
-  T u[3][RBZ][RBY][RBX];
-  T s[6][RBZ][RBY][RBX];
-};
-
-template <typename T>
-__global__ void __launch_bounds__(RHS_THREADS)
-rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, int doadd) {
-  extern __shared__ unsigned char smem_raw[];
-  RhsSmem<T>& sm = *reinterpret_cast<RhsSmem<T>*>(smem_raw);
-  const long long N = (long long)n * n * n;
-  const int x0 = blockIdx.x * RTX, y0 = blockIdx.y * RTY, z0 = blockIdx.z * RTZ;
-  const int tid = threadIdx.x;
-  // stage u (periodic wrap); box coordinate b <-> global tile0 - 1 + b
-  for (int t = tid; t < 3 * RBZ * RBY * RBX; t += RHS_THREADS) {
-    int c = t / (RBZ * RBY * RBX);
-    int r = t - c * (RBZ * RBY * RBX);
-    int bz = r / (RBY * RBX);
-    r -= bz * (RBY * RBX);
-    int by = r / RBX, bx = r - by * RBX;
-    int gx = x0 - 1 + bx, gy = y0 - 1 + by, gz = z0 - 1 + bz;
-    // gx >= -1; the modulo also covers grids smaller than the tile
-    gx = (gx + n) % n;
-    gy = (gy + n) % n;
-    gz = (gz + n) % n;
-    sm.u[c][bz][by][bx] = u[c * N + ((long long)gz * n + gy) * n + gx];
-  }
-  __syncthreads();
-  const T kd = (T)0.25 * inv_h;             // (a+b)^2/4/h
-  const T kv = visc * inv_h * inv_h;        // visc/h^2
-  // stress box index sb <-> u box index sb (same origin), tile cells at 1..T
-  // diagonal sigma_ii at stress-box cells: b_i in [1, T_i + 1], others [1, T]
-  // edge sigma_ij: b_i, b_j in [0, T], other [1, T]
-  for (int comp = 0; comp < 6; ++comp) {
-    int i, j;
-    if (comp < 3) { i = j = comp; } else { i = comp - 3; j = (i + 1) % 3; }  // 12, 23, 31
-    int lo[3] = {1, 1, 1}, hi[3] = {RTX, RTY, RTZ};  // inclusive, box coords
-    if (i == j) { hi[i] += 1; }
-    else { lo[i] = 0; lo[j] = 0; }
-    int ex = hi[0] - lo[0] + 1, ey = hi[1] - lo[1] + 1, ez = hi[2] - lo[2] + 1;
-    int tot = ex * ey * ez;
-    for (int t = tid; t < tot; t += RHS_THREADS) {
-      int bz = t / (ex * ey);
-      int r = t - bz * ex * ey;
-      int by = r / ex, bx = r - by * ex;
-      bx += lo[0]; by += lo[1]; bz += lo[2];
-      T val;
-      if (i == j) {
-        // sigma_ii[I] uses u_i[I - e_i], u_i[I] (src/N.jl:106-118 with i == j)
-        int dx = (i == 0), dy = (i == 1), dz = (i == 2);
-        T a = sm.u[i][bz][by][bx], b = sm.u[i][bz - dz][by - dy][bx - dx];
-        T s = a + b, d = a - b;
-        val = s * s * kd - (T)2 * kv * d;
-      } else {
-        // sigma_ij[I] at edge I+e_i/2+e_j/2: u_i[I], u_i[I+e_j], u_j[I], u_j[I+e_i]
-        int jx = (j == 0), jy = (j == 1), jz = (j == 2);
-        int ix = (i == 0), iy = (i == 1), iz = (i == 2);
-        T a = sm.u[i][bz][by][bx], b = sm.u[i][bz + jz][by + jy][bx + jx];
-        T c = sm.u[j][bz][by][bx], d = sm.u[j][bz + iz][by + iy][bx + ix];
-        val = (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
-      }
-      sm.s[comp][bz][by][bx] = val;
-    }
-  }
-  __syncthreads();
-  // divergence at tile cells
-  for (int t = tid; t < RTX * RTY * RTZ; t += RHS_THREADS) {
-    int tz = t / (RTX * RTY);
-    int r = t - tz * RTX * RTY;
-    int ty = r / RTX, tx = r - ty * RTX;
-    int bx = tx + 1, by = ty + 1, bz = tz + 1;
-    int gx = x0 + tx, gy = y0 + ty, gz = z0 + tz;
-    if (gx >= n || gy >= n || gz >= n) continue;
-    const auto& S = sm.s;
-    // s12 = S[3], s23 = S[4], s31 = S[5]
-    T d1 = (S[0][bz][by][bx + 1] - S[0][bz][by][bx]) + (S[3][bz][by][bx] - S[3][bz][by - 1][bx]) +
-           (S[5][bz][by][bx] - S[5][bz - 1][by][bx]);
-    T d2 = (S[3][bz][by][bx] - S[3][bz][by][bx - 1]) + (S[1][bz][by + 1][bx] - S[1][bz][by][bx]) +
-           (S[4][bz][by][bx] - S[4][bz - 1][by][bx]);
-    T d3 = (S[5][bz][by][bx] - S[5][bz][by][bx - 1]) + (S[4][bz][by][bx] - S[4][bz][by - 1][bx]) +
-           (S[2][bz + 1][by][bx] - S[2][bz][by][bx]);
-    long long g = ((long long)gz * n + gy) * n + gx;
-    if (doadd) {
-      du[g] -= d1;
-      du[N + g] -= d2;
-      du[2 * N + g] -= d3;
-    } else {
-      du[g] = -d1;
-      du[N + g] = -d2;
-      du[2 * N + g] = -d3;
-    }
-  }
-}
-
-template <typename T>
-cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st) {
-  dim3 grid((n + RTX - 1) / RTX, (n + RTY - 1) / RTY, (n + RTZ - 1) / RTZ);
-  rhs_kernel<T><<<grid, RHS_THREADS, sizeof(RhsSmem<T>), st>>>(n, (T)(1.0 / (double)h), visc, u, du, doadd ? 1 : 0);
-  return cudaGetLastError();
-}
-
-cudaError_t configure_stencil() {
-  cudaError_t e = cudaFuncSetAttribute(rhs_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sizeof(RhsSmem<double>));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rhs_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RhsSmem<float>));
-  return e;
-}
-
-// ---------------------------------------------------------------------------
 // Simple per-cell kernels
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void cell_of(long long g, int n, int& x, int& y, int& z) {
@@ -319,7 +198,6 @@ cudaError_t launch_max_abs(size_t count, const T* x, double* out_dev, double* pa
 }
 
 #define INST(T)                                                                                   \
-  template cudaError_t launch_rhs<T>(int, T, T, const T*, T*, bool, cudaStream_t);                \
   template cudaError_t launch_stress<T>(int, T, T, const T*, T*, cudaStream_t);                   \
   template cudaError_t launch_tensordiv<T>(int, T, int, const T*, T*, bool, cudaStream_t);        \
   template cudaError_t launch_divergence<T>(int, T, const T*, T*, cudaStream_t);                  \

@@ -68,6 +68,7 @@ SIGNATURES = {
     "exc_case_errors": [vp, i32, dp],
     "exc_case_time": [vp, dp, dp],
     "exc_case_energy": [vp, dp],
+    "exc_case_dissipation": [vp, dp],
     "exc_case_spectrum": [vp, dp, i32],
     "exc_case_device_ptr": [vp, i32, C.POINTER(vp)],
     "exc_case_launches_per_step": [vp, C.POINTER(i32)],

@@ -255,6 +255,12 @@ class Case:
         call("exc_case_energy", self._h, C.byref(e))
         return e.value
 
+    def dissipation(self) -> float:
+        """Viscous dissipation ``visc <|grad u|^2>`` of the DNS (FP64)."""
+        e = C.c_double()
+        call("exc_case_dissipation", self._h, C.byref(e))
+        return e.value
+
     def spectrum(self) -> np.ndarray:
         ns = (2 * (self.n // 2)) // 3
         a, p = self._buf((ns,))

@@ -193,6 +193,12 @@ int exc_case_time(exc_case* cs, double* t, double* last_dt);
 /* Mean kinetic energy of the DNS (FP64 reduction). */
 int exc_case_energy(exc_case* cs, double* energy);
 
+/* Viscous dissipation visc/N sum_ij (delta_j u_i)^2 of the DNS (FP64): the
+ * energy drained by the viscous part of `stress` (src/N.jl:106-118) for a
+ * divergence-free field (the reference computes it with Turbulox,
+ * dns_aid.jl:92-94). */
+int exc_case_dissipation(exc_case* cs, double* eps);
+
 /* Shell spectrum E(k), k = 1..nshell (`spectrum`, src/N.jl:576-590),
  * nshell = div(2*div(n,2), 3); FP64. */
 int exc_case_spectrum(exc_case* cs, double* host_e, int nshell);

@@ -312,6 +312,18 @@ def spectrum(u: np.ndarray, l: float):
     return 2 * np.pi / l * np.arange(1, kcut + 1), s
 
 
+def dissipation(u: np.ndarray, visc: float, h: float) -> float:
+    """``visc * mean sum_ij (delta_j u_i)^2`` with forward differences: the
+    energy drained by the viscous part of ``stress`` (``src/N.jl:106-118``) for
+    a divergence-free field; the reference takes it from Turbulox
+    (``dns_aid.jl:92-94``)."""
+    s = 0.0
+    for i in range(3):
+        for j in range(3):
+            s += float(np.sum(((at(u[i], j, 1) - u[i]) / h) ** 2))
+    return visc * s / u[0].size
+
+
 def kinetic_energy(u: np.ndarray) -> float:
     """Mean kinetic energy ``sum(u^2)/2/N`` (``src/NavierStokes.jl:74``)."""
     return float(np.sum(u * u) / 2 / u[0].size)

@@ -30,6 +30,8 @@ def test_init_random_matches_oracle(NS, n, kpeak, seed):
     assert abs(cs.energy() - ns.kinetic_energy(ref)) < 1e-12
     k, s = ns.spectrum(ref, 1.0)
     assert rel(cs.spectrum(), s) < 1e-12
+    eps = ns.dissipation(ref, 1 / 2000, 1.0 / n)
+    assert abs(cs.dissipation() - eps) < 1e-12 * eps
 
 
 @pytest.mark.parametrize("n,les", [(32, [(4, "volume")]), (24, [(3, "volume"), (2, "face")]),

@@ -126,6 +126,19 @@ def test_even_taps_reduce_to_box_and_trapezoid():
     assert list(o) == [2, 3, 4, 5, 6] and np.allclose(w, 0.2)
 
 
+def test_dissipation_matches_energy_decay():
+    """dE/dt of the inviscid-free part vanishes, so the kinetic energy decays
+    at the discrete viscous dissipation rate (energy budget of the scheme)."""
+    n, l, visc = 16, 1.0, 1 / 100
+    h = l / n
+    u = ns.randomfield(n, l, 3, 2)
+    dt = 1e-5
+    e0 = ns.kinetic_energy(u)
+    e1 = ns.kinetic_energy(ns.step_rk4(u, visc, h, dt))
+    eps = ns.dissipation(u, visc, h)
+    assert abs((e0 - e1) / dt - eps) < 2e-3 * eps
+
+
 def test_rk4_fourth_order_in_time():
     n, l, visc = 8, 1.0, 1 / 200
     h = l / n

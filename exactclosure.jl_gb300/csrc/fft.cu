@@ -118,7 +118,7 @@ __device__ __forceinline__ double recip_f64(double d) {
 template <typename T>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<T>* __restrict__ tw,
-              FftPlan plan, const double* __restrict__ sin2, double coef) {
+              FftPlan plan, const double* __restrict__ sin2, double coef, const double* __restrict__ invlap) {
   using C = cplx<T>;
   extern __shared__ unsigned char smem_raw[];
   C* s = reinterpret_cast<C*>(smem_raw);
@@ -136,10 +136,16 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
   fft_lines<false>(s, ls, lines, plan, tw, n);
   const double sy = sin2[ky];
   for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-    int l = t / n, kz = t - l * n;
+    int kz = t / lines, l = t - kz * lines;
     int kx = kx0 + l;
-    double den = sin2[kx] + sy + sin2[kz];
-    double f = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef * recip_f64(den);
+    double f;
+    if (invlap) {
+      // precomputed 1/(lambda N), one float64 per mode ([kz][ky][kx])
+      f = invlap[((long long)kz * n + ky) * nkx + kx];
+    } else {
+      double den = sin2[kx] + sy + sin2[kz];
+      f = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef * recip_f64(den);
+    }
     C v = s[l * ls + kz];
     v.x = (T)((double)v.x * f);
     v.y = (T)((double)v.y * f);
@@ -216,6 +222,18 @@ __global__ void copy_pitched_kernel(const T* __restrict__ src, int pitch, T* __r
   }
 }
 
+// 1/(lambda N) on the half spectrum [kz][ky][kx], 0 for the mean mode.
+__global__ void invlap_kernel(int n, const double* __restrict__ sin2, double coef, double* __restrict__ out) {
+  const int nkx = n / 2 + 1;
+  const long long tot = (long long)n * n * nkx;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(g % nkx);
+    const long long r = g / nkx;
+    const int ky = (int)(r % n), kz = (int)(r / n);
+    out[g] = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef / (sin2[kx] + sin2[ky] + sin2[kz]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
@@ -248,7 +266,7 @@ cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vec
   cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
   // z forward + divide + inverse; coef = 1/(lambda N) numerator: -h^2/(4 N)
   double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
-  zsolve_kernel<T><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef);
+  zsolve_kernel<T><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef, ps->invlap);
   // y inverse
   cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
   // x inverse (in place)
@@ -371,6 +389,18 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
   cudaMemcpy(ps->tw, precision == EXC_F64 ? (const void*)twd.data() : (const void*)twf.data(), n * csz,
              cudaMemcpyHostToDevice);
   cudaMemcpy(ps->sin2, s2.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+  {
+    // 1/(lambda N) per half-spectrum mode, from an exact float64 division
+    const size_t tb = (size_t)n * n * (n / 2 + 1) * sizeof(double);
+    if (cudaMalloc(&ps->invlap, tb) != cudaSuccess) {
+      set_last_error("out of device memory (poisson inverse symbol)");
+      poisson_free(ps);
+      return EXC_ERR_OOM;
+    }
+    const double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
+    const long long tot = (long long)n * n * (n / 2 + 1);
+    invlap_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152LL * 32), 256>>>(n, ps->sin2, coef, ps->invlap);
+  }
   size_t wbytes = (size_t)n * n * ps->P * csz;
   if (work) {
     ps->work = work;
@@ -391,6 +421,8 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
 void poisson_free(exc_poisson* ps) {
   if (ps->tw) cudaFree(ps->tw);
   if (ps->sin2) cudaFree(ps->sin2);
+  if (ps->invlap) cudaFree(ps->invlap);
+  ps->invlap = nullptr;
   if (ps->work && !ps->external_work) cudaFree(ps->work);
   ps->tw = nullptr;
   ps->sin2 = nullptr;

@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--visc", type=float, default=1 / 2000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-forms", action="store_true")
+    ap.add_argument("--serve-only", action="store_true")
     return ap.parse_args()
 
 
@@ -146,6 +149,97 @@ def cpu_sample(n_full: int, les, kpeak: float, visc: float, budget_s: float = 20
                       f"{[c for c, _ in les]} (same physics, grid reduced to bound CPU time), single thread"}
 
 
+SERVE_SIZES = (64, 96, 128, 192, 256)
+SERVE_VISC = (1 / 1000, 1 / 2000, 1 / 4000)
+
+
+def serve_requests(nreq=96, rate=20.0, seed=0, nsteps=200):
+    """The serving stream: seeded Poisson arrivals (mean `rate` per second),
+    grid sizes uniform over SERVE_SIZES, viscosities uniform over SERVE_VISC."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    n = rng.choice(SERVE_SIZES, nreq)
+    v = rng.choice(SERVE_VISC, nreq)
+    return [dict(t=float(t[i]), n=int(n[i]), visc=float(v[i]), seed=1000 + i, nsteps=nsteps) for i in range(nreq)]
+
+
+def serve_stream(precision=1, nreq=96, rate=20.0, nsteps=200):
+    """Replay the stream in real time through the serving form; returns
+    aggregate cell-updates/s and solve-latency percentiles."""
+    import numpy as np
+
+    from exactclosure_gb300 import serving
+
+    reqs = serve_requests(nreq, rate, nsteps=nsteps)
+    sv = serving.Server(precision=precision, mem_fraction=0.6)
+    # warm the per-size batches (allocation, autotuning, graph capture) untimed
+    for n in SERVE_SIZES:
+        sv.submit(n, 1 / 1000, 1, seed=1)
+    sv.drain()
+    sv.poll()
+    done = {}
+    i = 0
+    t0 = time.perf_counter()
+    clock0 = sv.stats()["clock"]
+    while len(done) < nreq:
+        now = time.perf_counter() - t0
+        while i < nreq and reqs[i]["t"] <= now:
+            q = reqs[i]
+            rid = sv.submit(q["n"], q["visc"], q["nsteps"], seed=q["seed"], kpeak=4.0)
+            done.setdefault("_ids", {})[rid] = i
+            i += 1
+        active, queued = sv.tick()
+        for r in sv.poll():
+            if r["id"] in done.get("_ids", {}):
+                done[r["id"]] = r
+        if active == 0 and queued == 0 and i < nreq:
+            time.sleep(max(0.0, min(0.01, reqs[i]["t"] - (time.perf_counter() - t0))))
+        done_count = len(done) - ("_ids" in done)
+        if done_count >= nreq:
+            break
+    res = [r for k, r in done.items() if k != "_ids"]
+    lat = np.array([r["t_finish"] - r["t_submit"] for r in res])
+    t_first = min(r["t_submit"] for r in res)
+    t_last = max(r["t_finish"] for r in res)
+    cells = sum(r["n"] ** 3 * r["nsteps"] for r in res)
+    st = sv.stats()
+    sv.close()
+    return {"value": cells / (t_last - t_first), "unit": "cell-updates/s", "solves": len(res),
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "makespan_s": t_last - t_first, "ticks": st["ticks"], "chunks": st["chunks"],
+            "dtype": "f32 (FP64 spectral divide and diagnostics)" if precision == 1 else "f64",
+            "stream": f"{nreq} solves, Poisson arrivals {rate}/s (seed 0), n in {list(SERVE_SIZES)}, "
+                      f"visc in {{1/1000, 1/2000, 1/4000}}, {nsteps} RK4 steps each"}
+
+
+def plain_fp64_stream_sample(nsolves=10, nsteps=8):
+    """The plain FP64 path on the first requests of the same stream, one solve
+    at a time through the case API (no batching)."""
+    import torch
+
+    from exactclosure_gb300 import navierstokes as NS
+
+    reqs = serve_requests()[:nsolves]
+    cells = 0
+    el = 0.0
+    for q in reqs:
+        cs = NS.Case(q["n"], 1.0, q["visc"], 0.3, precision=0)
+        cs.init_random(4.0, 1.0, q["seed"])
+        cs.step(1)
+        cs.sync()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cs.step(nsteps)
+        cs.sync()
+        el += time.perf_counter() - t0
+        cells += q["n"] ** 3 * nsteps
+        cs.close()
+    return {"value": cells / el, "unit": "cell-updates/s",
+            "sample": f"first {nsolves} solves of the stream, {nsteps} RK4 steps each, one at a time (FP64)"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -153,14 +247,29 @@ def run_reference(args):
     les = les_list(args.les)
     from oracle import cpu_ref
 
-    vals = []
-    info = None
-    for i in range(args.warmup + args.steps):
-        r = cpu_sample(args.n, les, args.kpeak, args.visc, budget_s=8.0)
-        if i >= args.warmup:
-            vals.append(r["value"])
-        info = r
-    v = sum(vals) / len(vals)
+    if cpu_ref.available():
+        # one "step" of the reference arm = one RK4 stage of the full workload
+        # (a quarter of an RK4 step) on all host threads
+        cs = cpu_ref.timing_case(args.n, les, args.visc)
+        for s in range(args.warmup):
+            cs.stage(1 + s % 3)
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            cs.stage(1 + s % 3)
+        el = time.perf_counter() - t0
+        cs.close()
+        v = args.n ** 3 * (args.steps / 4.0) / el
+        info = {"cores": cpu_ref.lib().cref_threads(), "kind": "port",
+                "sample": f"C/OpenMP restatement of the path, {args.steps} RK4 stages of the {args.n}^3 DNS with "
+                          f"LES {args.les} (one stage per step), all host threads"}
+    else:
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = cpu_sample(args.n, les, args.kpeak, args.visc, budget_s=8.0)
+            if i >= args.warmup:
+                vals.append(r["value"])
+            info = r
+        v = sum(vals) / len(vals)
     line = {
         "impl": "reference", "metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -198,6 +307,10 @@ def main():
     from exactclosure_gb300 import _lib
     from exactclosure_gb300 import navierstokes as NS
 
+    if args.serve_only:
+        served = serve_stream(precision=0 if args.precision == "f64" else 1, nsteps=args.steps)
+        print(json.dumps({"serving": served}))
+        return
     prec = 0 if args.precision == "f64" else 1
     les = les_list(args.les)
     n = args.n
@@ -268,6 +381,41 @@ def main():
     if rank == 0:
         roof = roofline(cs, NS, n, prec, args, stream)
 
+    # ---- the other precision on the same workload, and the serving stream ----
+    forms = None
+    serving_line = None
+    if rank == 0 and world == 1:
+        cs.close()
+        torch.cuda.empty_cache()
+        if not args.no_forms:
+            other = 1 - prec
+            c2 = NS.Case(n, 1.0, args.visc, 0.3, precision=other, les=les, stream=stream.cuda_stream)
+            c2.init_random(args.kpeak, 1.0, seed=rank)
+            c2.step(max(1, args.warmup))
+            c2.sync()
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            f0.record(stream)
+            c2.step(args.steps)
+            f1.record(stream)
+            torch.cuda.synchronize()
+            fms = f0.elapsed_time(f1)
+            c2.sync()
+            forms = {("f32" if other == 1 else "f64"): {
+                "value": N * args.steps / (fms / 1e3), "unit": "cell-updates/s", "ms_per_step": fms / args.steps,
+                "note": "same workload; f32 = stencil/filter/RK in FP32 with FP64 spectral divide and diagnostics"}}
+            c2.close()
+            torch.cuda.empty_cache()
+        if not args.no_serve:
+            try:
+                served = serve_stream(precision=1)
+                plain = plain_fp64_stream_sample()
+                served["plain_fp64_same_stream"] = plain
+                served["served_over_plain_fp64"] = served["value"] / plain["value"]
+                serving_line = served
+            except Exception as ex:
+                serving_line = {"error": str(ex)}
+
     # ---- CPU baseline ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -292,6 +440,8 @@ def main():
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "forms": forms,
+            "serving": serving_line,
         }
         print(json.dumps(line))
     if world > 1:

@@ -335,45 +335,15 @@ static int init_random(exc_case* cs, double kpeak, double energy, uint64_t seed)
   CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
   cudaStream_t st = cs->stream;
   const int n = ci->n, P = ci->ps.P;
-  T* u = ci->u[ci->cur];
-  cudaError_t e = launch_normals<T>(3 * ci->N, (unsigned long long)seed, u, st);
-  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-  int rc = project_vec<T>(&ci->ps, u, st);
-  if (rc) return rc;
-  // three spectra
   using C = cplx<T>;
   const long long cstride = (long long)n * n * P;
   C* spec = nullptr;
   if (cudaMalloc(&spec, 3 * cstride * sizeof(C)) != cudaSuccess) { set_last_error("out of device memory (init spectra)"); return EXC_ERR_OOM; }
-  cudaMemsetAsync(spec, 0, 3 * cstride * sizeof(C), st);
-  exc_poisson tmp = ci->ps;
-  for (int c = 0; c < 3; ++c) {
-    tmp.work = spec + c * cstride;
-    e = fft3d_forward<T>(&tmp, u + c * ci->N, st);
-    if (e != cudaSuccess) break;
-  }
-  const int kmax = n / 2;
-  const int kdiag = (int)std::floor(std::sqrt(3.0) * kmax);
-  const int nshell = kdiag + 1;
-  double* eshell = ci->part + SHELL_BLOCKS * 1024;  // nshell <= 1024
-  double* factor = eshell + 1024;
-  double* partials = ci->part;
-  const double N = (double)ci->N;
-  if (e == cudaSuccess)
-    e = launch_shell_energy<T>(n, P, 3, spec, cstride, 1.0 / (N * N), nshell, partials, SHELL_BLOCKS, eshell, st);
-  if (e == cudaSuccess) e = launch_shell_factor(nshell, kpeak, energy, eshell, factor, st);
-  if (e == cudaSuccess) e = launch_shell_scale<T>(n, P, 3, spec, cstride, nshell, factor, st);
-  for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
-    tmp.work = spec + c * cstride;
-    e = fft3d_inverse<T>(&tmp, st);
-    if (e == cudaSuccess)
-      e = launch_unpitch<T>(n, reinterpret_cast<const T*>(tmp.work), 2 * P, u + c * ci->N, (T)(1.0 / N), st);
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  int rc = init_random_field<T>(&ci->ps, ci->u[ci->cur], spec, ci->part, kpeak, energy, seed, st);
+  cudaError_t e = cudaStreamSynchronize(st);
   cudaFree(spec);
-  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-  rc = project_vec<T>(&ci->ps, u, st);
   if (rc) return rc;
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   return reset_les<T>(cs);
 }
 

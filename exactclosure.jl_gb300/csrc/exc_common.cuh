@@ -52,6 +52,15 @@ __host__ __device__ __forceinline__ int spec_pitch(int n) { return pad8(n / 2 + 
 __device__ __forceinline__ int wrap_up(int i, int n) { return (i + 1 == n) ? 0 : i + 1; }
 __device__ __forceinline__ int wrap_dn(int i, int n) { return (i == 0) ? n - 1 : i - 1; }
 
+// A batch of same-size solves laid out slot after slot (serving form).  The
+// slot index comes from a grid dimension; inactive slots return at once.
+struct SlotBatch {
+  long long ustride = 0;          // words between slots of a vector field (3 n^3)
+  long long wstride = 0;          // complex words between slots of the spectral work array
+  const int* active = nullptr;    // per-slot flag, null = all active
+  const void* visc = nullptr;     // per-slot viscosity (field word type), null = scalar argument
+};
+
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 // Grid sizes the FFT supports: n = 2^a 3^b with a >= 1, 4 <= n <= 1024.

@@ -17,10 +17,14 @@ namespace exc {
 template <typename T, bool DIV>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ out, int P,
-             const cplx<T>* __restrict__ tw, FftPlan plan, int rows_per_cta) {
+             const cplx<T>* __restrict__ tw, FftPlan plan, int rows_per_cta, SlotBatch sb) {
   using C = cplx<T>;
   extern __shared__ unsigned char smem_raw[];
   C* s = reinterpret_cast<C*>(smem_raw);
+  const int slot = blockIdx.y;
+  if (sb.active && !sb.active[slot]) return;
+  src += slot * sb.ustride;
+  out += slot * sb.wstride;
   const int N2 = n / 2;
   const int ls = N2 + 1;
   const long long nn = (long long)n * n;
@@ -78,10 +82,12 @@ r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ ou
 template <typename T, bool INV>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_stride,
-            long long outer_stride, const cplx<T>* __restrict__ tw, FftPlan plan) {
+            long long outer_stride, const cplx<T>* __restrict__ tw, FftPlan plan, SlotBatch sb) {
   using C = cplx<T>;
   extern __shared__ unsigned char smem_raw[];
   C* s = reinterpret_cast<C*>(smem_raw);
+  if (sb.active && !sb.active[blockIdx.z]) return;
+  g += blockIdx.z * sb.wstride;
   const int ls = n + 1;
   const int kx0 = blockIdx.x * W;
   const int lines = min(W, nkx - kx0);
@@ -118,10 +124,13 @@ __device__ __forceinline__ double recip_f64(double d) {
 template <typename T>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<T>* __restrict__ tw,
-              FftPlan plan, const double* __restrict__ sin2, double coef, const double* __restrict__ invlap) {
+              FftPlan plan, const double* __restrict__ sin2, double coef, const double* __restrict__ invlap,
+              SlotBatch sb) {
   using C = cplx<T>;
   extern __shared__ unsigned char smem_raw[];
   C* s = reinterpret_cast<C*>(smem_raw);
+  if (sb.active && !sb.active[blockIdx.z]) return;
+  g += blockIdx.z * sb.wstride;
   const int ls = n + 1;
   const int kx0 = blockIdx.x * W;
   const int ky = blockIdx.y;
@@ -167,10 +176,12 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
 template <typename T>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
 c2r_x_kernel(cplx<T>* __restrict__ g, int n, int P, const cplx<T>* __restrict__ tw, FftPlan plan,
-             int rows_per_cta) {
+             int rows_per_cta, SlotBatch sb) {
   using C = cplx<T>;
   extern __shared__ unsigned char smem_raw[];
   C* s = reinterpret_cast<C*>(smem_raw);
+  if (sb.active && !sb.active[blockIdx.y]) return;
+  g += blockIdx.y * sb.wstride;
   const int N2 = n / 2;
   const int ls = N2 + 1;
   const long long nn = (long long)n * n;
@@ -243,34 +254,48 @@ static int col_width(int n, int tile) {
   return w;
 }
 
+// Launch geometry of the passes: columns per CTA of the y/z passes and rows
+// per CTA of the x passes, from the solver's tuned values (autotuner) when
+// set and legal for the tile, else the largest that fills the 32 KB tile.
+template <typename C>
+static void geometry(const exc_poisson* ps, int& W, int& rows) {
+  const int n = ps->n, N2 = n / 2;
+  const long long nn = (long long)n * n;
+  const int wmax = col_width(n, fft_tile<C>());
+  W = (ps->col_w > 0 && ps->col_w <= wmax) ? ps->col_w : wmax;
+  const int rmax = fft_tile<C>() / (N2 + 1);
+  rows = (ps->x_rows > 0 && ps->x_rows <= rmax) ? ps->x_rows : rmax;
+  if (rows > nn) rows = (int)nn;
+}
+
 template <typename T>
-cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st) {
+cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st,
+                                  const SlotBatch& sb, int nslots) {
   using C = cplx<T>;
   const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
   C* g = reinterpret_cast<C*>(ps->work);
   const C* tw = reinterpret_cast<const C*>(ps->tw);
   const long long nn = (long long)n * n;
+  int W, rows;
+  geometry<C>(ps, W, rows);
   // x forward
-  int rows = fft_tile<C>() / (N2 + 1);
-  if (rows > nn) rows = (int)nn;
   size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
-  int gx = (int)((nn + rows - 1) / rows);
+  dim3 gx((unsigned)((nn + rows - 1) / rows), nslots);
   if (src_is_vector)
-    r2c_x_kernel<T, true><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)(1.0 / ps->h), g, P, tw, ps->plan_h, rows);
+    r2c_x_kernel<T, true><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)(1.0 / ps->h), g, P, tw, ps->plan_h, rows, sb);
   else
-    r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows);
+    r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows, sb);
   // y forward
-  int W = col_width(n, fft_tile<C>());
-  dim3 gc((nkx + W - 1) / W, n);
+  dim3 gc((nkx + W - 1) / W, n, nslots);
   size_t shc = (size_t)W * (n + 1) * sizeof(C);
-  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, sb);
   // z forward + divide + inverse; coef = 1/(lambda N) numerator: -h^2/(4 N)
   double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
-  zsolve_kernel<T><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef, ps->invlap);
+  zsolve_kernel<T><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef, ps->invlap, sb);
   // y inverse
-  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
+  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, sb);
   // x inverse (in place)
-  c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows);
+  c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows, sb);
   return cudaGetLastError();
 }
 
@@ -283,16 +308,16 @@ cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st) {
   C* g = reinterpret_cast<C*>(ps->work);
   const C* tw = reinterpret_cast<const C*>(ps->tw);
   const long long nn = (long long)n * n;
-  int rows = fft_tile<C>() / (N2 + 1);
-  if (rows > nn) rows = (int)nn;
+  int W, rows;
+  geometry<C>(ps, W, rows);
+  const SlotBatch one;
   size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
   int gx = (int)((nn + rows - 1) / rows);
-  r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows);
-  int W = col_width(n, fft_tile<C>());
+  r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows, one);
   dim3 gc((nkx + W - 1) / W, n);
   size_t shc = (size_t)W * (n + 1) * sizeof(C);
-  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
-  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n);
+  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, one);
+  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n, one);
   return cudaGetLastError();
 }
 
@@ -303,16 +328,16 @@ cudaError_t fft3d_inverse(exc_poisson* ps, cudaStream_t st) {
   C* g = reinterpret_cast<C*>(ps->work);
   const C* tw = reinterpret_cast<const C*>(ps->tw);
   const long long nn = (long long)n * n;
-  int W = col_width(n, fft_tile<C>());
+  int W, rows;
+  geometry<C>(ps, W, rows);
+  const SlotBatch one;
   dim3 gc((nkx + W - 1) / W, n);
   size_t shc = (size_t)W * (n + 1) * sizeof(C);
-  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n);
-  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n);
-  int rows = fft_tile<C>() / (N2 + 1);
-  if (rows > nn) rows = (int)nn;
+  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n, one);
+  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, one);
   size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
   int gx = (int)((nn + rows - 1) / rows);
-  c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows);
+  c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows, one);
   return cudaGetLastError();
 }
 
@@ -329,8 +354,10 @@ cudaError_t copy_pressure(const exc_poisson* ps, T* p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template cudaError_t poisson_solve_inplace<double>(exc_poisson*, const double*, bool, cudaStream_t);
-template cudaError_t poisson_solve_inplace<float>(exc_poisson*, const float*, bool, cudaStream_t);
+template cudaError_t poisson_solve_inplace<double>(exc_poisson*, const double*, bool, cudaStream_t, const SlotBatch&,
+                                                   int);
+template cudaError_t poisson_solve_inplace<float>(exc_poisson*, const float*, bool, cudaStream_t, const SlotBatch&,
+                                                  int);
 template cudaError_t copy_pressure<double>(const exc_poisson*, double*, cudaStream_t);
 template cudaError_t copy_pressure<float>(const exc_poisson*, float*, cudaStream_t);
 

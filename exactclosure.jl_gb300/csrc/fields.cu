@@ -23,9 +23,16 @@ static inline int grid_for(long long N, int threads = 256) {
 template <typename T, bool GRAD>
 __global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __restrict__ p, int ppitch,
                                 const T* __restrict__ x0, T* __restrict__ xs, T* __restrict__ xfin, int stage,
-                                const double* __restrict__ dtp) {
+                                const double* __restrict__ dtp, SlotBatch sb) {
   const long long N = (long long)n * n * n;
-  const double dt = *dtp;
+  const int slot = blockIdx.y;  // batch of same-size solves (serving form)
+  if (sb.active && !sb.active[slot]) return;
+  k += slot * sb.ustride;
+  x0 += slot * sb.ustride;
+  xs += slot * sb.ustride;
+  xfin += slot * sb.ustride;
+  if (GRAD) p += slot * 2 * sb.wstride;
+  const double dt = dtp[slot];
   const T cf = (T)((stage == 0 || stage == 3) ? dt / 6.0 : dt / 3.0);
   const T cs = (T)(stage == 2 ? dt : 0.5 * dt);
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
@@ -66,12 +73,13 @@ __global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __re
 
 template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
-                            const double* dtp, cudaStream_t st) {
+                            const double* dtp, cudaStream_t st, const SlotBatch& sb, int nslots) {
   long long N = (long long)n * n * n;
+  dim3 grid(nslots > 1 ? std::min(grid_for(N), 152 * 8) : grid_for(N), nslots);
   if (p)
-    rk_stage_kernel<T, true><<<grid_for(N), 256, 0, st>>>(n, (T)(1.0 / (double)h), k, p, ppitch, x0, xs, xfin, stage, dtp);
+    rk_stage_kernel<T, true><<<grid, 256, 0, st>>>(n, (T)(1.0 / (double)h), k, p, ppitch, x0, xs, xfin, stage, dtp, sb);
   else
-    rk_stage_kernel<T, false><<<grid_for(N), 256, 0, st>>>(n, (T)0, k, nullptr, 0, x0, xs, xfin, stage, dtp);
+    rk_stage_kernel<T, false><<<grid, 256, 0, st>>>(n, (T)0, k, nullptr, 0, x0, xs, xfin, stage, dtp, sb);
   return cudaGetLastError();
 }
 
@@ -392,7 +400,7 @@ cudaError_t launch_convert(long long count, const A* a, B* b, cudaStream_t st) {
 
 #define INST(T)                                                                                                 \
   template cudaError_t launch_rk_stage<T>(int, T, T*, const T*, int, const T*, T*, T*, int, const double*,      \
-                                          cudaStream_t);                                                        \
+                                          cudaStream_t, const SlotBatch&, int);                                                        \
   template cudaError_t launch_axpy<T>(long long, T*, const T*, T, cudaStream_t);                                \
   template cudaError_t launch_normals<T>(long long, unsigned long long, T*, cudaStream_t);                      \
   template cudaError_t launch_sqdiff<T>(long long, const T*, const T*, double*, double*, cudaStream_t);         \

@@ -16,6 +16,7 @@ struct exc_poisson {
   double* invlap = nullptr;  // 1/(lambda N) per half-spectrum mode, or null (computed on the fly)
   exc::FftPlan plan_n{}, plan_h{};
   bool external_work = false;
+  int col_w = 0, x_rows = 0;  // tuned launch geometry (0 = default)
 };
 
 namespace exc {
@@ -29,7 +30,8 @@ void poisson_free(exc_poisson* ps);
 //   src_is_vector: d = div(src) computed on the fly (scaled by 1/h),
 //   otherwise src is the scalar right-hand side d.
 template <typename T>
-cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st);
+cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st,
+                                  const SlotBatch& sb = SlotBatch(), int nslots = 1);
 
 // Plain forward (half spectrum into ps->work) and unnormalised inverse (reals
 // at pitch 2P in ps->work) 3-D transforms.
@@ -37,6 +39,12 @@ template <typename T>
 cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st);
 template <typename T>
 cudaError_t fft3d_inverse(exc_poisson* ps, cudaStream_t st);
+
+// Random solenoidal field with the peak spectrum into u (init.cu); spec3: 3
+// spectral arrays of scratch, part: SHELL_BLOCKS*1024 + 2048 doubles.
+template <typename T>
+int init_random_field(exc_poisson* ps, T* u, cplx<T>* spec3, double* part, double kpeak, double energy,
+                      uint64_t seed, cudaStream_t st);
 
 // Shared-memory opt-ins of every kernel that needs them, once per device;
 // called before any launch (and so before any stream capture).
@@ -51,7 +59,8 @@ cudaError_t copy_pressure(const exc_poisson* ps, T* p, cudaStream_t st);
 
 // ---- stencil kernels (stencil.cu) ----
 template <typename T>
-cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st);
+cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st,
+                       const SlotBatch& sb = SlotBatch(), int nslots = 1);
 template <typename T>
 cudaError_t launch_stress(int n, T h, T visc, const T* u, T* s6, cudaStream_t st);
 template <typename T>

@@ -59,12 +59,20 @@ __device__ __forceinline__ T s33(T up, T lo, T kd, T kv2) {
 
 template <typename T>
 __global__ void __launch_bounds__(PTX * PTY)
-rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, int doadd) {
+rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, int doadd, SlotBatch sb,
+           int zblocks) {
   __shared__ PlaneSmem<T> sm;
   const long long N = (long long)n * n * n;
+  // slot of a batch of same-size solves (serving form): blockIdx.z = slot * zblocks + zb
+  const int slot = blockIdx.z / zblocks;
+  const int zb = blockIdx.z - slot * zblocks;
+  if (sb.active && !sb.active[slot]) return;
+  u += slot * sb.ustride;
+  du += slot * sb.ustride;
+  if (sb.visc) visc = reinterpret_cast<const T*>(sb.visc)[slot];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int lane = tx, warp = ty;
-  const int x0 = blockIdx.x * PTX, y0 = blockIdx.y * PTY, z0 = blockIdx.z * PTZ;
+  const int x0 = blockIdx.x * PTX, y0 = blockIdx.y * PTY, z0 = zb * PTZ;
   const T kd = (T)0.25 * inv_h;
   const T kv = visc * inv_h * inv_h;
   const T kv2 = (T)2 * kv;
@@ -171,15 +179,19 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
 }
 
 template <typename T>
-cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st) {
-  dim3 grid((n + PTX - 1) / PTX, (n + PTY - 1) / PTY, (n + PTZ - 1) / PTZ);
-  rhs_kernel<T><<<grid, dim3(PTX, PTY), 0, st>>>(n, (T)(1.0 / (double)h), visc, u, du, doadd ? 1 : 0);
+cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st, const SlotBatch& sb,
+                       int nslots) {
+  const int zblocks = (n + PTZ - 1) / PTZ;
+  dim3 grid((n + PTX - 1) / PTX, (n + PTY - 1) / PTY, zblocks * nslots);
+  rhs_kernel<T><<<grid, dim3(PTX, PTY), 0, st>>>(n, (T)(1.0 / (double)h), visc, u, du, doadd ? 1 : 0, sb, zblocks);
   return cudaGetLastError();
 }
 
 cudaError_t configure_stencil() { return cudaSuccess; }
 
-template cudaError_t launch_rhs<double>(int, double, double, const double*, double*, bool, cudaStream_t);
-template cudaError_t launch_rhs<float>(int, float, float, const float*, float*, bool, cudaStream_t);
+template cudaError_t launch_rhs<double>(int, double, double, const double*, double*, bool, cudaStream_t,
+                                        const SlotBatch&, int);
+template cudaError_t launch_rhs<float>(int, float, float, const float*, float*, bool, cudaStream_t, const SlotBatch&,
+                                       int);
 
 }  // namespace exc

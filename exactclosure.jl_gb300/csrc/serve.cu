@@ -1,0 +1,663 @@
+// Serving form: continuous batching of independent periodic NS solves of
+// mixed grid sizes on one GPU (no counterpart in the reference, whose driver
+// runs one solve at a time, src/N.jl:1239-1332).
+//
+// Requests queue on the host.  Every tick admits what fits -- a free slot of
+// a chunk for the request's grid size, or a new chunk if the memory budget
+// (a share of the free HBM taken at creation) allows -- then advances every
+// active solve by one RK4 step and retires the solves that reached their step
+// count.  A chunk holds S same-size solves slot after slot in device memory
+// (velocity ping-pong, stage state, RHS, spectral work array; nothing moves
+// between steps) and replays one captured CUDA graph per step whose kernels
+// cover all S slots at once (the slot is a grid dimension; inactive slots
+// return at once, so admission never re-captures).  Each solve keeps its own
+// viscosity, CFL time step and clock.  Chunks of different sizes run on their
+// own streams and overlap on the device; the host runs at most two ticks ahead
+// of each chunk.  The FFT tile shapes of each grid size are chosen by timing
+// candidates on the chunk's own batched work (autotuner) before capture.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "internal.cuh"
+#include "fields.cuh"
+
+namespace exc {
+
+// ---------------------------------------------------------------------------
+// Batched kernels of the serving step
+// ---------------------------------------------------------------------------
+constexpr int SRV_RED = 64;  // partial blocks per slot for max |u|
+
+template <typename T>
+__global__ void slot_maxabs_partial(long long count, const T* __restrict__ u, long long stride,
+                                    const int* __restrict__ active, double* __restrict__ part) {
+  const int slot = blockIdx.y;
+  if (!active[slot]) return;
+  const T* x = u + slot * stride;
+  double m = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    double v = fabs((double)x[i]);
+    m = (v > m || v != v) ? v : m;
+  }
+  __shared__ double red[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (w > m || w != w) ? w : m;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = (red[w] > r || red[w] != red[w]) ? red[w] : r;
+    part[slot * SRV_RED + blockIdx.x] = r;
+  }
+}
+
+// per-slot dt = min(cfl h/umax, cfl h^2/visc/6) (propose_timestep,
+// src/N.jl:348-356); a non-finite umax flags the slot and freezes it (dt = 0)
+__global__ void slot_set_dt(int S, const int* __restrict__ active, const double* __restrict__ part, double h,
+                            double cfl, const double* __restrict__ viscd, double* __restrict__ dt,
+                            double* __restrict__ clock, int* __restrict__ flag) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S || !active[s]) return;
+  double m = 0.0;
+  for (int b = 0; b < SRV_RED; ++b) {
+    double v = part[s * SRV_RED + b];
+    m = (v > m || v != v) ? v : m;
+  }
+  double a = cfl * h / m, v = cfl * h * h / viscd[s] / 6.0;
+  double d = a < v ? a : v;
+  if (!(m < 1e300)) { flag[s] = 1; d = 0.0; }
+  dt[s] = d;
+  clock[s] += d;
+}
+
+__global__ void set_active_kernel(int S, unsigned long long mask, int* __restrict__ active) {
+  const int s = threadIdx.x;
+  if (s < S) active[s] = (int)((mask >> s) & 1ull);
+}
+
+template <typename T>
+__global__ void set_slot_kernel(int s, double visc, T* __restrict__ vdev, double* __restrict__ vd,
+                                double* __restrict__ clock, int* __restrict__ flag) {
+  vdev[s] = (T)visc;
+  vd[s] = visc;
+  clock[s] = 0.0;
+  flag[s] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct PendingReq {
+  int64_t id;
+  exc_solve_req req;
+  double t_submit;
+};
+
+struct FinishRec {
+  exc_solve_result res;
+  cudaEvent_t ev = nullptr;
+  double* pinned = nullptr;  // [0] sum u^2, [1] unused, [2] clock
+};
+
+class ChunkBase {
+ public:
+  virtual ~ChunkBase() = default;
+  int n = 0, S = 0;
+  double l = 1.0, cfl = 0.3;
+  size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<int64_t> slot_id;
+  std::vector<int> steps_left, nsteps;
+  std::vector<double> t_submit, t_admit;
+  std::vector<double*> result_host;
+  cudaEvent_t tick_ev[2] = {nullptr, nullptr};
+  int tick_parity = 0;
+  long long ticks = 0;
+  int free_slot() const {
+    for (int s = 0; s < S; ++s)
+      if (slot_id[s] < 0) return s;
+    return -1;
+  }
+  int active_count() const {
+    int c = 0;
+    for (int s = 0; s < S; ++s) c += slot_id[s] >= 0;
+    return c;
+  }
+};
+
+template <typename T>
+class Chunk : public ChunkBase {
+ public:
+  long long N = 0;
+  exc_poisson ps;
+  T* big = nullptr;  // u[0], u[1], us, rhs: S * 3N each
+  T* u[2] = {nullptr, nullptr};
+  T* us = nullptr;
+  T* rhs = nullptr;
+  void* work = nullptr;
+  T* visc = nullptr;
+  double *dt = nullptr, *clock = nullptr, *part = nullptr, *red = nullptr, *viscd = nullptr;
+  int *active = nullptr, *flag = nullptr;
+  int cur = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int kernels_per_step = 0;
+
+  ~Chunk() override {
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto& g : graph)
+      if (g) cudaGraphExecDestroy(g);
+    poisson_free(&ps);
+    if (work) cudaFree(work);
+    if (big) cudaFree(big);
+    if (visc) cudaFree(visc);
+    if (dt) cudaFree(dt);
+    if (active) cudaFree(active);
+    for (auto& e : tick_ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  SlotBatch batch() const {
+    SlotBatch sb;
+    sb.ustride = 3 * N;
+    sb.wstride = (long long)n * n * ps.P;
+    sb.active = active;
+    sb.visc = visc;
+    return sb;
+  }
+
+  // one batched RK4 step (same tableau and projection as the case stepper)
+  cudaError_t enqueue_step(int c) {
+    const SlotBatch sb = batch();
+    const T h = (T)(l / n);
+    T* u0 = u[c];
+    T* ufin = u[c ^ 1];
+    slot_maxabs_partial<T><<<dim3(SRV_RED, S), 256, 0, stream>>>(3 * N, u0, 3 * N, active, part);
+    slot_set_dt<<<(S + 63) / 64, 64, 0, stream>>>(S, active, part, l / n, cfl, viscd, dt, clock, flag);
+    cudaError_t e = cudaGetLastError();
+    for (int s = 0; s < 4 && e == cudaSuccess; ++s) {
+      const T* src = s == 0 ? u0 : us;
+      e = launch_rhs<T>(n, h, (T)0, src, rhs, false, stream, sb, S);
+      if (e == cudaSuccess) e = poisson_solve_inplace<T>(&ps, rhs, true, stream, sb, S);
+      if (e == cudaSuccess)
+        e = launch_rk_stage<T>(n, h, rhs, reinterpret_cast<const T*>(ps.work), 2 * ps.P, u0, us, ufin, s, dt, stream,
+                               sb, S);
+    }
+    return e;
+  }
+};
+
+// autotuned (col_w, x_rows) per (n, precision, S)
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tuned;
+
+}  // namespace exc
+
+struct exc_server {
+  exc_server_desc desc{};
+  size_t budget = 0, used = 0;
+  std::chrono::steady_clock::time_point t0;
+  cudaStream_t admit_stream = nullptr;
+  cudaEvent_t ev0 = nullptr;
+  std::deque<exc::PendingReq> pending;
+  std::vector<std::unique_ptr<exc::ChunkBase>> chunks;
+  std::vector<exc::FinishRec> finishing;
+  int64_t next_id = 1;
+  // init scratch (largest grid seen so far)
+  void* spec3 = nullptr;
+  size_t spec3_bytes = 0;
+  double* init_part = nullptr;
+  long long ticks = 0;
+  double now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+namespace exc {
+
+template <typename T>
+static int tune_chunk(exc_server* sv, Chunk<T>* ck) {
+  using C = cplx<T>;
+  const int prec = sizeof(T) == 8 ? EXC_F64 : EXC_F32;
+  auto key = std::make_tuple(ck->n, prec, ck->S);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      ck->ps.col_w = it->second.first;
+      ck->ps.x_rows = it->second.second;
+      return EXC_OK;
+    }
+  }
+  const int n = ck->n;
+  const int wmax = [&] { int w = 1; while (w * 2 * n <= fft_tile<C>() && w < 64) w *= 2; return w; }();
+  const int rmax = fft_tile<C>() / (n / 2 + 1);
+  std::vector<int> ws, rs;
+  for (int w = wmax; w >= 1 && (int)ws.size() < 4; w /= 2) ws.push_back(w);
+  for (int r = rmax; r >= 1 && (int)rs.size() < 3; r /= 2) rs.push_back(r);
+  set_active_kernel<<<1, 64, 0, ck->stream>>>(ck->S, ~0ull, ck->active);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  int bw = wmax, br = rmax;
+  for (int w : ws)
+    for (int r : rs) {
+      ck->ps.col_w = w;
+      ck->ps.x_rows = r;
+      poisson_solve_inplace<T>(&ck->ps, ck->rhs, true, ck->stream, ck->batch(), ck->S);  // warm
+      cudaEventRecord(a, ck->stream);
+      for (int rep = 0; rep < 3; ++rep) poisson_solve_inplace<T>(&ck->ps, ck->rhs, true, ck->stream, ck->batch(), ck->S);
+      cudaEventRecord(b, ck->stream);
+      cudaEventSynchronize(b);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms < best) { best = ms; bw = w; br = r; }
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  set_active_kernel<<<1, 64, 0, ck->stream>>>(ck->S, 0ull, ck->active);
+  ck->ps.col_w = bw;
+  ck->ps.x_rows = br;
+  cudaError_t e = cudaStreamSynchronize(ck->stream);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[key] = {bw, br};
+  return EXC_OK;
+}
+
+static size_t chunk_bytes(int n, int S, size_t w) {
+  const size_t N = (size_t)n * n * n;
+  const size_t P = (size_t)spec_pitch(n);
+  return S * (12 * N * w + (size_t)n * n * P * 2 * w) + (size_t)n * n * (n / 2 + 1) * 8 + S * 128 + S * SRV_RED * 8;
+}
+
+static int slots_for(const exc_server* sv, int n) {
+  if (sv->desc.slots_per_chunk > 0) return std::min(sv->desc.slots_per_chunk, 64);
+  if (n <= 64) return 16;
+  if (n <= 128) return 8;
+  if (n <= 192) return 4;
+  return 2;
+}
+
+template <typename T>
+static int make_chunk(exc_server* sv, int n, double l, double cfl, ChunkBase** out) {
+  const int S = slots_for(sv, n);
+  const size_t need = chunk_bytes(n, S, sizeof(T));
+  if (sv->used + need > sv->budget) return EXC_ERR_OOM;  // not an error: wait for memory
+  auto ck = std::make_unique<Chunk<T>>();
+  ck->n = n;
+  ck->S = S;
+  ck->l = l;
+  ck->cfl = cfl;
+  ck->N = (long long)n * n * n;
+  ck->slot_id.assign(S, -1);
+  ck->steps_left.assign(S, 0);
+  ck->nsteps.assign(S, 0);
+  ck->t_submit.assign(S, 0);
+  ck->t_admit.assign(S, 0);
+  ck->result_host.assign(S, nullptr);
+  if (cudaStreamCreateWithFlags(&ck->stream, cudaStreamNonBlocking) != cudaSuccess) { set_last_error("stream"); return EXC_ERR_CUDA; }
+  for (auto& e : ck->tick_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  using C = cplx<T>;
+  const long long wst = (long long)n * n * spec_pitch(n);
+  if (cudaMalloc(&ck->work, S * wst * sizeof(C)) != cudaSuccess) { set_last_error("out of device memory (chunk work)"); return EXC_ERR_OOM; }
+  int rc = poisson_init(&ck->ps, sizeof(T) == 8 ? EXC_F64 : EXC_F32, n, l, ck->work);
+  if (rc) return rc;
+  if (cudaMalloc(&ck->big, 4 * S * 3 * ck->N * sizeof(T)) != cudaSuccess) { set_last_error("out of device memory (chunk fields)"); return EXC_ERR_OOM; }
+  cudaMemsetAsync(ck->big, 0, 4 * S * 3 * ck->N * sizeof(T), ck->stream);
+  ck->u[0] = ck->big;
+  ck->u[1] = ck->u[0] + S * 3 * ck->N;
+  ck->us = ck->u[1] + S * 3 * ck->N;
+  ck->rhs = ck->us + S * 3 * ck->N;
+  if (cudaMalloc(&ck->visc, S * sizeof(T)) != cudaSuccess ||
+      cudaMalloc(&ck->dt, (4 * S + S * SRV_RED + 64 + 1024) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&ck->active, 2 * S * sizeof(int)) != cudaSuccess) {
+    set_last_error("out of device memory (chunk scalars)");
+    return EXC_ERR_OOM;
+  }
+  ck->clock = ck->dt + S;
+  ck->viscd = ck->clock + S;
+  ck->red = ck->viscd + S;  // energy reduction output (2 doubles) + spare
+  ck->part = ck->red + S + 64;
+  ck->flag = ck->active + S;
+  cudaMemsetAsync(ck->dt, 0, (4 * S + S * SRV_RED + 64 + 1024) * sizeof(double), ck->stream);
+  cudaMemsetAsync(ck->active, 0, 2 * S * sizeof(int), ck->stream);
+  std::vector<T> ones(S, (T)1e-3);
+  cudaMemcpyAsync(ck->visc, ones.data(), S * sizeof(T), cudaMemcpyHostToDevice, ck->stream);
+  cudaStreamSynchronize(ck->stream);
+  if (sv->desc.autotune) {
+    rc = tune_chunk<T>(sv, ck.get());
+    if (rc) return rc;
+  }
+  // capture the step graphs (one per velocity parity)
+  for (int c = 0; c < 2; ++c) {
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(ck->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaError_t e2 = ck->enqueue_step(c);
+      e = cudaStreamEndCapture(ck->stream, &g);
+      if (e2 != cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) {
+      size_t num = 0;
+      cudaGraphGetNodes(g, nullptr, &num);
+      ck->kernels_per_step = (int)num;
+      e = cudaGraphInstantiate(&ck->graph[c], g, 0);
+      cudaGraphDestroy(g);
+    }
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  }
+  ck->bytes = need;
+  sv->used += need;
+  *out = ck.get();
+  sv->chunks.push_back(std::move(ck));
+  return EXC_OK;
+}
+
+template <typename T>
+static int ensure_init_scratch(exc_server* sv, int n) {
+  using C = cplx<T>;
+  const size_t need = 3 * (size_t)n * n * spec_pitch(n) * sizeof(C);
+  if (need <= sv->spec3_bytes) return EXC_OK;
+  if (sv->spec3) { cudaStreamSynchronize(sv->admit_stream); cudaFree(sv->spec3); sv->spec3 = nullptr; }
+  if (cudaMalloc(&sv->spec3, need) != cudaSuccess) { sv->spec3_bytes = 0; set_last_error("out of device memory (init scratch)"); return EXC_ERR_OOM; }
+  sv->spec3_bytes = need;
+  return EXC_OK;
+}
+
+// Put request `pr` into a free slot (new chunk if needed and affordable).
+template <typename T>
+static int admit(exc_server* sv, const PendingReq& pr, bool* admitted) {
+  *admitted = false;
+  const exc_solve_req& q = pr.req;
+  Chunk<T>* ck = nullptr;
+  int slot = -1;
+  for (auto& cb : sv->chunks) {
+    if (cb->n != q.n || cb->l != q.l || cb->cfl != q.cfl) continue;
+    int s = cb->free_slot();
+    if (s >= 0) { ck = static_cast<Chunk<T>*>(cb.get()); slot = s; break; }
+  }
+  if (!ck) {
+    ChunkBase* nb = nullptr;
+    int rc = make_chunk<T>(sv, q.n, q.l, q.cfl, &nb);
+    if (rc == EXC_ERR_OOM && !sv->chunks.empty()) return EXC_OK;  // wait for memory to free up
+    if (rc) return rc;
+    ck = static_cast<Chunk<T>*>(nb);
+    slot = 0;
+  }
+  int rc = ensure_init_scratch<T>(sv, q.n);
+  if (rc) return rc;
+  // the slot's previous owner may still be finishing on the chunk stream
+  cudaEvent_t ready;
+  cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+  cudaEventRecord(ready, ck->stream);
+  cudaStreamWaitEvent(sv->admit_stream, ready, 0);
+  exc_poisson view = ck->ps;
+  view.work = reinterpret_cast<cplx<T>*>(ck->work) + slot * (long long)q.n * q.n * ck->ps.P;
+  T* u = ck->u[ck->cur] + slot * 3 * ck->N;
+  set_slot_kernel<T><<<1, 1, 0, sv->admit_stream>>>(slot, q.visc, ck->visc, ck->viscd, ck->clock, ck->flag);
+  rc = init_random_field<T>(&view, u, reinterpret_cast<cplx<T>*>(sv->spec3), sv->init_part, q.kpeak, q.energy, q.seed,
+                            sv->admit_stream);
+  cudaEventRecord(ready, sv->admit_stream);
+  cudaStreamWaitEvent(ck->stream, ready, 0);
+  cudaEventDestroy(ready);
+  if (rc) return rc;
+  ck->slot_id[slot] = pr.id;
+  ck->steps_left[slot] = q.nsteps;
+  ck->nsteps[slot] = q.nsteps;
+  ck->t_submit[slot] = pr.t_submit;
+  ck->t_admit[slot] = sv->now();
+  ck->result_host[slot] = q.result_host;
+  *admitted = true;
+  return EXC_OK;
+}
+
+template <typename T>
+static int tick_chunk(exc_server* sv, Chunk<T>* ck) {
+  unsigned long long mask = 0;
+  for (int s = 0; s < ck->S; ++s)
+    if (ck->slot_id[s] >= 0 && ck->steps_left[s] > 0) mask |= 1ull << s;
+  if (!mask) return EXC_OK;
+  // at most two ticks in flight per chunk
+  cudaEventSynchronize(ck->tick_ev[ck->tick_parity]);
+  set_active_kernel<<<1, 64, 0, ck->stream>>>(ck->S, mask, ck->active);
+  cudaError_t e = cudaGraphLaunch(ck->graph[ck->cur], ck->stream);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  ck->cur ^= 1;
+  ck->ticks++;
+  for (int s = 0; s < ck->S; ++s) {
+    if (!((mask >> s) & 1ull)) continue;
+    if (--ck->steps_left[s] > 0) continue;
+    // finished: FP64 energy and clock into pinned host memory, optional field copy
+    FinishRec rec;
+    cudaHostAlloc(&rec.pinned, 4 * sizeof(double), cudaHostAllocDefault);
+    T* uf = ck->u[ck->cur] + s * 3 * ck->N;
+    e = launch_sqdiff<T>(3 * ck->N, uf, nullptr, ck->part, ck->red, ck->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rec.pinned, ck->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, ck->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(rec.pinned + 2, ck->clock + s, sizeof(double), cudaMemcpyDeviceToHost, ck->stream);
+    if (e == cudaSuccess && ck->result_host[s]) {
+      // float64 copy of the final velocity through the slot's RHS buffer
+      double* stage = reinterpret_cast<double*>(ck->rhs + s * 3 * ck->N);
+      if (sizeof(T) == sizeof(double)) {
+        e = cudaMemcpyAsync(ck->result_host[s], uf, 3 * ck->N * sizeof(double), cudaMemcpyDeviceToHost, ck->stream);
+      } else {
+        // rhs slot (3N floats) holds half: convert and copy component by component
+        for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+          e = launch_convert<T, double>(ck->N, uf + c * ck->N, stage, ck->stream);
+          if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ck->result_host[s] + c * ck->N, stage, ck->N * sizeof(double), cudaMemcpyDeviceToHost,
+                                ck->stream);
+        }
+      }
+    }
+    if (e != cudaSuccess) { cudaFreeHost(rec.pinned); set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    cudaEventCreate(&rec.ev);
+    cudaEventRecord(rec.ev, ck->stream);
+    rec.res.id = ck->slot_id[s];
+    rec.res.n = ck->n;
+    rec.res.nsteps = ck->nsteps[s];
+    rec.res.t_submit = ck->t_submit[s];
+    rec.res.t_admit = ck->t_admit[s];
+    rec.res.t_finish = -1;
+    rec.res.energy = 0;
+    rec.res.sim_time = 0;
+    sv->finishing.push_back(rec);
+    ck->slot_id[s] = -1;
+    ck->result_host[s] = nullptr;
+  }
+  cudaEventRecord(ck->tick_ev[ck->tick_parity], ck->stream);
+  ck->tick_parity ^= 1;
+  return EXC_OK;
+}
+
+template <typename T>
+static int server_tick(exc_server* sv, int* active, int* queued) {
+  // admission (continuous batching): any queued request that fits; when a
+  // request waits for memory, idle chunks (no active slot) are released once
+  for (int pass = 0; pass < 2; ++pass) {
+    bool blocked = false;
+    for (size_t i = 0; i < sv->pending.size();) {
+      bool ok = false;
+      int rc = admit<T>(sv, sv->pending[i], &ok);
+      if (rc) return rc;
+      if (ok) sv->pending.erase(sv->pending.begin() + i);
+      else { blocked = true; ++i; }
+    }
+    if (!blocked || pass == 1) break;
+    bool freed = false;
+    for (size_t c = 0; c < sv->chunks.size();) {
+      if (sv->chunks[c]->active_count() == 0) {
+        sv->used -= sv->chunks[c]->bytes;
+        sv->chunks.erase(sv->chunks.begin() + c);  // synchronises its stream
+        freed = true;
+      } else {
+        ++c;
+      }
+    }
+    if (!freed) break;
+  }
+  int act = 0;
+  for (auto& cb : sv->chunks) {
+    int rc = tick_chunk<T>(sv, static_cast<Chunk<T>*>(cb.get()));
+    if (rc) return rc;
+    act += cb->active_count();
+  }
+  sv->ticks++;
+  if (active) *active = act;
+  if (queued) *queued = (int)sv->pending.size();
+  return EXC_OK;
+}
+
+}  // namespace exc
+
+using namespace exc;
+
+extern "C" {
+
+int exc_server_create(const exc_server_desc* desc, exc_server** out) {
+  if (!desc || !out) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  *out = nullptr;
+  if (desc->precision != EXC_F64 && desc->precision != EXC_F32) { set_last_error("bad precision"); return EXC_ERR_ARG; }
+  if (!(desc->mem_fraction > 0) || desc->mem_fraction > 0.95) { set_last_error("mem_fraction must be in (0, 0.95]"); return EXC_ERR_ARG; }
+  int rc = configure_device();
+  if (rc) return rc;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { set_last_error("cudaMemGetInfo failed"); return EXC_ERR_CUDA; }
+  auto sv = new exc_server();
+  sv->desc = *desc;
+  sv->budget = (size_t)(desc->mem_fraction * (double)fr);
+  if (desc->max_bytes > 0 && desc->max_bytes < (double)sv->budget) sv->budget = (size_t)desc->max_bytes;
+  sv->t0 = std::chrono::steady_clock::now();
+  if (cudaStreamCreateWithFlags(&sv->admit_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&sv->ev0) != cudaSuccess ||
+      cudaMalloc(&sv->init_part, (SHELL_BLOCKS * 1024 + 2048) * sizeof(double)) != cudaSuccess) {
+    delete sv;
+    set_last_error("cannot create server resources");
+    return EXC_ERR_CUDA;
+  }
+  cudaEventRecord(sv->ev0, sv->admit_stream);
+  cudaEventSynchronize(sv->ev0);
+  sv->t0 = std::chrono::steady_clock::now();
+  *out = sv;
+  return EXC_OK;
+}
+
+int exc_server_destroy(exc_server* sv) {
+  if (!sv) return EXC_OK;
+  cudaDeviceSynchronize();
+  sv->chunks.clear();
+  for (auto& r : sv->finishing) {
+    if (r.ev) cudaEventDestroy(r.ev);
+    if (r.pinned) cudaFreeHost(r.pinned);
+  }
+  if (sv->spec3) cudaFree(sv->spec3);
+  if (sv->init_part) cudaFree(sv->init_part);
+  if (sv->ev0) cudaEventDestroy(sv->ev0);
+  if (sv->admit_stream) cudaStreamDestroy(sv->admit_stream);
+  delete sv;
+  return EXC_OK;
+}
+
+int exc_server_submit(exc_server* sv, const exc_solve_req* req, int64_t* id) {
+  if (!sv || !req) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  if (!fft_size_ok(req->n)) { set_last_error("grid size must be 2^a 3^b, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!(req->l > 0) || !(req->visc > 0) || !(req->cfl > 0) || !(req->kpeak > 0) || !(req->energy > 0) ||
+      req->nsteps < 1) {
+    set_last_error("bad request parameters");
+    return EXC_ERR_ARG;
+  }
+  PendingReq pr;
+  pr.id = sv->next_id++;
+  pr.req = *req;
+  pr.t_submit = sv->now();
+  sv->pending.push_back(pr);
+  if (id) *id = pr.id;
+  return EXC_OK;
+}
+
+int exc_server_tick(exc_server* sv, int* active, int* queued) {
+  if (!sv) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  return sv->desc.precision == EXC_F64 ? server_tick<double>(sv, active, queued) : server_tick<float>(sv, active, queued);
+}
+
+int exc_server_poll(exc_server* sv, exc_solve_result* out, int max, int* count) {
+  if (!sv || !count || (max > 0 && !out)) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  int c = 0;
+  for (size_t i = 0; i < sv->finishing.size() && c < max;) {
+    FinishRec& r = sv->finishing[i];
+    cudaError_t q = cudaEventQuery(r.ev);
+    if (q == cudaErrorNotReady) { ++i; continue; }
+    if (q != cudaSuccess) { set_last_error(cudaGetErrorString(q)); return EXC_ERR_CUDA; }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, sv->ev0, r.ev);
+    r.res.t_finish = ms * 1e-3;
+    const int n = r.res.n;
+    r.res.energy = r.pinned[0] / 2.0 / ((double)n * n * n);
+    r.res.sim_time = r.pinned[2];
+    out[c++] = r.res;
+    cudaEventDestroy(r.ev);
+    cudaFreeHost(r.pinned);
+    sv->finishing.erase(sv->finishing.begin() + i);
+  }
+  *count = c;
+  return EXC_OK;
+}
+
+int exc_server_drain(exc_server* sv) {
+  if (!sv) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  int idle_ticks = 0;
+  for (;;) {
+    int act = 0, q = 0;
+    int rc = exc_server_tick(sv, &act, &q);
+    if (rc) return rc;
+    if (act == 0 && q == 0) break;
+    // solves retired in this tick free their slots for the next one; only a
+    // second tick without any active solve means the queue cannot be served
+    idle_ticks = act == 0 ? idle_ticks + 1 : 0;
+    if (idle_ticks >= 2) { set_last_error("queued requests cannot be admitted (memory budget)"); return EXC_ERR_OOM; }
+  }
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+int exc_server_stats(exc_server* sv, exc_server_info* st) {
+  if (!sv || !st) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  st->chunks = (int)sv->chunks.size();
+  st->slots = 0;
+  st->active = 0;
+  st->kernels_per_tick = 0;
+  for (auto& cb : sv->chunks) {
+    st->slots += cb->S;
+    st->active += cb->active_count();
+  }
+  st->queued = (int)sv->pending.size();
+  st->bytes_used = (double)sv->used;
+  st->bytes_budget = (double)sv->budget;
+  st->ticks = (double)sv->ticks;
+  st->clock = sv->now();
+  return EXC_OK;
+}
+
+int exc_server_tuning(int precision, int n, int slots, int* col_w, int* x_rows) {
+  if (!col_w || !x_rows) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(std::make_tuple(n, precision, slots));
+  if (it == g_tuned.end()) { set_last_error("no tuning recorded for this size"); return EXC_ERR_STATE; }
+  *col_w = it->second.first;
+  *x_rows = it->second.second;
+  return EXC_OK;
+}
+
+}  // extern "C"

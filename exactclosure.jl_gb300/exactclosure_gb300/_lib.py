@@ -35,6 +35,29 @@ class CaseDesc(C.Structure):
                 ("precision", C.c_int), ("nles", C.c_int), ("les", LesDesc * EXC_MAX_LES)]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [("precision", C.c_int), ("mem_fraction", C.c_double), ("max_bytes", C.c_double),
+                ("slots_per_chunk", C.c_int), ("autotune", C.c_int)]
+
+
+class SolveReq(C.Structure):
+    _fields_ = [("n", C.c_int), ("l", C.c_double), ("visc", C.c_double), ("cfl", C.c_double),
+                ("kpeak", C.c_double), ("energy", C.c_double), ("seed", C.c_uint64), ("nsteps", C.c_int),
+                ("result_host", C.POINTER(C.c_double))]
+
+
+class SolveResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("n", C.c_int), ("nsteps", C.c_int), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_finish", C.c_double), ("energy", C.c_double),
+                ("sim_time", C.c_double)]
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [("chunks", C.c_int), ("slots", C.c_int), ("active", C.c_int), ("queued", C.c_int),
+                ("kernels_per_tick", C.c_int), ("bytes_used", C.c_double), ("bytes_budget", C.c_double),
+                ("ticks", C.c_double), ("clock", C.c_double)]
+
+
 vp = C.c_void_p
 dp = C.POINTER(C.c_double)
 i32, f64, u64, szt = C.c_int, C.c_double, C.c_uint64, C.c_size_t
@@ -73,6 +96,14 @@ SIGNATURES = {
     "exc_case_device_ptr": [vp, i32, C.POINTER(vp)],
     "exc_case_launches_per_step": [vp, C.POINTER(i32)],
     "exc_case_sync": [vp],
+    "exc_server_create": [C.POINTER(ServerDesc), C.POINTER(vp)],
+    "exc_server_destroy": [vp],
+    "exc_server_submit": [vp, C.POINTER(SolveReq), C.POINTER(C.c_int64)],
+    "exc_server_tick": [vp, C.POINTER(i32), C.POINTER(i32)],
+    "exc_server_poll": [vp, C.POINTER(SolveResult), i32, C.POINTER(i32)],
+    "exc_server_drain": [vp],
+    "exc_server_stats": [vp, C.POINTER(ServerInfo)],
+    "exc_server_tuning": [i32, i32, i32, C.POINTER(i32), C.POINTER(i32)],
 }
 _RESTYPE = {"exc_last_error": C.c_char_p}
 

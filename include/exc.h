@@ -215,6 +215,65 @@ int exc_case_launches_per_step(exc_case* cs, int* count);
  * velocity was flagged during the last steps. */
 int exc_case_sync(exc_case* cs);
 
+/* ======================================================================
+ * Serving form (no counterpart in the reference, whose driver runs one
+ * solve at a time): continuous batching of independent periodic NS solves of
+ * mixed grid sizes.  Requests queue on the host; each tick admits every
+ * queued request for which a slot of its grid size is free or a new batch of
+ * slots fits the memory budget (a share of the free device memory at
+ * creation), advances every active solve by one RK4 step, and retires the
+ * solves that reached their step count.  Same-size solves are batched slot
+ * after slot and stepped by one captured CUDA graph per size whose kernels
+ * cover every slot; all state stays in device memory between steps.
+ * ====================================================================== */
+
+typedef struct exc_server exc_server;
+
+typedef struct {
+  int precision;       /* EXC_F32 (the served form) or EXC_F64 */
+  double mem_fraction; /* share of the free device memory the server may hold, (0, 0.95] */
+  double max_bytes;    /* absolute cap on that budget in bytes (0: none) */
+  int slots_per_chunk; /* same-size solves per batch (0: by grid size) */
+  int autotune;        /* nonzero: time FFT tile shapes per grid size before capture */
+} exc_server_desc;
+
+typedef struct {
+  int n;               /* grid cells per side */
+  double l, visc, cfl; /* domain side, viscosity, CFL factor */
+  double kpeak, energy; /* initial spectrum peak and kinetic energy (randomfield) */
+  uint64_t seed;       /* initial-field seed */
+  int nsteps;          /* RK4 steps to run */
+  double* result_host; /* optional: receives the final velocity, 3 n^3 doubles */
+} exc_solve_req;
+
+typedef struct {
+  int64_t id;
+  int n, nsteps;
+  double t_submit, t_admit, t_finish; /* seconds since creation; t_finish from the device clock */
+  double energy;       /* final mean kinetic energy (FP64 reduction) */
+  double sim_time;     /* simulated time reached */
+} exc_solve_result;
+
+typedef struct {
+  int chunks, slots, active, queued, kernels_per_tick;
+  double bytes_used, bytes_budget, ticks, clock;
+} exc_server_info;
+
+int exc_server_create(const exc_server_desc* desc, exc_server** out);
+int exc_server_destroy(exc_server* sv);
+/* Queue a solve; *id identifies its result. */
+int exc_server_submit(exc_server* sv, const exc_solve_req* req, int64_t* id);
+/* Admit, advance every active solve one RK4 step, retire finished solves
+ * (asynchronous: at most two ticks in flight per batch). */
+int exc_server_tick(exc_server* sv, int* active, int* queued);
+/* Up to `max` results of finished solves whose device work has completed. */
+int exc_server_poll(exc_server* sv, exc_solve_result* out, int max, int* count);
+/* Tick until every submitted solve has finished; synchronises the device. */
+int exc_server_drain(exc_server* sv);
+int exc_server_stats(exc_server* sv, exc_server_info* st);
+/* FFT tile shape the autotuner chose for (precision, n, slots per batch). */
+int exc_server_tuning(int precision, int n, int slots, int* col_w, int* x_rows);
+
 #ifdef __cplusplus
 }
 #endif

@@ -530,6 +530,25 @@ int cref_init_random(cref* cs, double kpeak, double energy, uint64_t seed) {
   return 0;
 }
 
+/* Smooth divergence-free field (u = sin 2pi y, v = sin 2pi z, w = sin 2pi x)
+ * for timing samples, where the values do not matter but must stay normal
+ * numbers. */
+int cref_init_analytic(cref* cs) {
+  const int n = cs->n;
+  const long N = cs->N;
+#pragma omp parallel for schedule(static)
+  for (int z = 0; z < n; ++z)
+    for (int y = 0; y < n; ++y)
+      for (int x = 0; x < n; ++x) {
+        long g = idx3(n, x, y, z);
+        cs->u0[g] = sin(2 * M_PI * (y + 0.5) / n);
+        cs->u0[N + g] = sin(2 * M_PI * (z + 0.5) / n);
+        cs->u0[2 * N + g] = sin(2 * M_PI * (x + 0.5) / n);
+      }
+  reset_les(cs);
+  return 0;
+}
+
 static void rk_combine(long cnt, double* k, const double* x0, double* xs, double* xfin, int s, double dt) {
   const double cf = (s == 0 || s == 3) ? dt / 6.0 : dt / 3.0, cst = s == 2 ? dt : 0.5 * dt;
 #pragma omp parallel for schedule(static)

@@ -33,6 +33,8 @@ def lib():
         L.cref_get_les.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.cref_step.argtypes = [C.c_void_p, C.c_int, C.c_double]
         L.cref_stage.argtypes = [C.c_void_p, C.c_int]
+        L.cref_init_analytic.argtypes = [C.c_void_p]
+        L.cref_init_analytic.restype = C.c_int
         L.cref_time.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         for f in ("cref_init_random", "cref_set_velocity", "cref_get_velocity", "cref_get_les", "cref_step",
                   "cref_stage", "cref_time"):
@@ -96,20 +98,30 @@ class CpuCase:
             pass
 
 
-def time_stages(n, les, kpeak, visc, budget_s=20.0):
-    """Time whole RK4 stages of the full-size workload on all host threads."""
+def timing_case(n, les, visc):
+    """A full-size CPU case with a smooth analytic field (values do not change
+    the work of a stage) for timing samples."""
     cs = CpuCase(n, 1.0, visc, 0.3, les)
-    cs.init_random(kpeak, 1.0, 0)
+    assert lib().cref_init_analytic(cs._h) == 0
     cs.stage(0)  # warm-up (page faults, dt)
+    return cs
+
+
+def time_stages(n, les, kpeak, visc, budget_s=20.0, cs=None, max_stages=8):
+    """Time whole RK4 stages of the full-size workload on all host threads."""
+    own = cs is None
+    if own:
+        cs = timing_case(n, les, visc)
     t0 = time.perf_counter()
     k = 0
     while True:
         cs.stage(1 + (k % 3))
         k += 1
-        if time.perf_counter() - t0 > budget_s * 0.5 or k >= 8:
+        if time.perf_counter() - t0 > budget_s * 0.5 or k >= max_stages:
             break
     el = time.perf_counter() - t0
-    cs.close()
+    if own:
+        cs.close()
     steps = k / 4.0
     threads = lib().cref_threads()
     return {"cell_updates_per_s": n ** 3 * steps / el, "threads": threads,

@@ -1,0 +1,105 @@
+"""GPU tests of the serving form (continuous batching of mixed-size solves):
+each result is identical alone and in the mix, equals the single-solve case
+path, matches the FP64 oracle, and the queue admits work as memory frees up."""
+import numpy as np
+import pytest
+
+from oracle import ns
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def SV(built_lib):
+    from exactclosure_gb300 import serving
+
+    return serving
+
+
+def run_alone(SV, prec, n, visc, seed, nsteps):
+    sv = SV.Server(precision=prec)
+    rid = sv.submit(n, visc, nsteps, seed=seed, keep_field=True)
+    sv.drain()
+    res = {r["id"]: r for r in sv.poll()}
+    sv.close()
+    return res[rid]
+
+
+@pytest.mark.parametrize("prec", [1, 0])
+def test_same_result_alone_and_in_the_mix(SV, prec):
+    target = dict(n=32, visc=1 / 1000, seed=7, nsteps=12)
+    alone = run_alone(SV, prec, **target)
+    sv = SV.Server(precision=prec)
+    ids = [sv.submit(16, 1 / 2000, 20, seed=1), sv.submit(32, 1 / 2000, 9, seed=2),
+           sv.submit(24, 1 / 4000, 15, seed=3)]
+    for _ in range(4):  # the target arrives while the others are on the GPU
+        sv.tick()
+    tid = sv.submit(target["n"], target["visc"], target["nsteps"], seed=target["seed"], keep_field=True)
+    ids += [sv.submit(48, 1 / 1000, 6, seed=4), sv.submit(32, 1 / 4000, 30, seed=5)]
+    for _ in range(3):
+        sv.tick()
+    ids.append(sv.submit(16, 1 / 1000, 5, seed=6))
+    sv.drain()
+    res = {r["id"]: r for r in sv.poll()}
+    assert set(res) == set(ids + [tid])
+    mixed = res[tid]
+    # bit-identical: every slot is computed independently with fixed-order reductions
+    assert np.array_equal(mixed["field"], alone["field"])
+    assert mixed["energy"] == alone["energy"] and mixed["sim_time"] == alone["sim_time"]
+    for r in res.values():
+        assert 0 <= r["t_submit"] <= r["t_admit"] <= r["t_finish"]
+        assert r["energy"] > 0
+    sv.close()
+
+
+@pytest.mark.parametrize("prec", [1, 0])
+def test_served_solve_equals_case_path(SV, prec, built_lib):
+    from exactclosure_gb300 import navierstokes as NS
+
+    n, visc, seed, nsteps = 24, 1 / 2000, 3, 8
+    r = run_alone(SV, prec, n, visc, seed, nsteps)
+    cs = NS.Case(n, 1.0, visc, 0.3, precision=prec)
+    cs.init_random(4.0, 1.0, seed)
+    cs.step(nsteps)
+    u = cs.velocity()
+    assert np.array_equal(r["field"], u)
+    t, _ = cs.time()
+    assert r["sim_time"] == t
+
+
+def test_served_fp64_matches_oracle(SV):
+    n, visc, seed, nsteps = 16, 1 / 1000, 9, 3
+    r = run_alone(SV, 0, n, visc, seed, nsteps)
+    u = ns.randomfield(n, 1.0, 4.0, seed)
+    for _ in range(nsteps):
+        u = ns.step_rk4(u, visc, 1.0 / n, ns.propose_timestep(u, visc, 0.3, 1.0 / n))
+    assert ns.rel_l2(r["field"], u) < 1e-12
+    assert abs(r["energy"] - ns.kinetic_energy(u)) < 1e-12
+
+
+def test_admission_waits_for_memory(SV):
+    """With a budget that holds one batch, a second grid size is admitted only
+    after the first batch drains and its memory is released."""
+    # one 32^3 batch of 4 slots needs ~7 MB, one 48^3 batch ~24 MB
+    sv = SV.Server(precision=1, max_bytes=28e6, slots_per_chunk=4)
+    a = sv.submit(32, 1 / 1000, 6, seed=1)
+    b = sv.submit(48, 1 / 1000, 4, seed=2)
+    c = sv.submit(32, 1 / 2000, 6, seed=3)
+    active, queued = sv.tick()
+    assert queued == 1  # the 48^3 request waits
+    sv.drain()
+    res = {r["id"]: r for r in sv.poll()}
+    assert set(res) == {a, b, c}
+    assert res[b]["t_admit"] >= max(res[a]["t_finish"], res[c]["t_finish"]) - 1e-3
+    st = sv.stats()
+    assert st["bytes_used"] <= st["bytes_budget"]
+    sv.close()
+
+
+def test_autotuner_records_a_choice(SV):
+    sv = SV.Server(precision=1, autotune=True, slots_per_chunk=2)
+    sv.submit(32, 1 / 1000, 2, seed=1)
+    sv.drain()
+    w, r = SV.Server.tuning(1, 32, 2)
+    assert w >= 1 and r >= 1
+    sv.close()

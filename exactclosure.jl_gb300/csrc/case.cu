@@ -34,6 +34,9 @@ struct LesState {
   T *ub, *fk, *mcl, *mlast, *rtmp;
   T *ve[2], *ves, *ke;  // exact LES: state (ping-pong), stage, k
   T *vn[2], *vns, *kn;  // no-model LES
+  T* ublast;            // target at stage 0 of the last step (pairs with mlast)
+  T *vl[2], *vls, *kl, *nn;  // LES driven by the learned closure (when a net is attached)
+  exc_net* net = nullptr;
 };
 
 }  // namespace exc
@@ -67,6 +70,7 @@ struct CaseImpl {
   LesState<T> les[EXC_MAX_LES];
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   double graph_dt_fixed[2] = {NAN, NAN};
+  long long net_gen = 0;  // workspace generations of attached nets at capture
   int kernels_per_step = 0;  // kernel nodes in the captured step graph
 };
 
@@ -132,6 +136,8 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
       if (rc) return rc;
       if (s == 0) {
         e = cudaMemcpyAsync(L.mlast, L.mcl, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(L.ublast, L.ub, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
       }
       // exact-closure LES
@@ -152,6 +158,22 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
       if (rc) return rc;
       e = launch_rk_stage<T>(m, H, L.kn, nullptr, 0, vn0, L.vns, vnfin, s, dt, st);
       if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      if (L.net) {
+        // learned-closure LES: k = P_H(RHS_H(v_s) + net(v_s))
+        T* vl0 = L.vl[cur];
+        T* vlfin = L.vl[cur ^ 1];
+        const T* vsrc = s == 0 ? vl0 : L.vls;
+        e = launch_rhs<T>(m, H, visc, vsrc, L.kl, false, st);
+        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+        rc = exc_net_forward(L.net, cs->precision, 1, m, vsrc, L.nn, st);
+        if (rc) return rc;
+        e = launch_axpy<T>(3 * L.M, L.kl, L.nn, (T)1, st);
+        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+        rc = project_vec<T>(&L.ps, L.kl, st);
+        if (rc) return rc;
+        e = launch_rk_stage<T>(m, H, L.kl, nullptr, 0, vl0, L.vls, vlfin, s, dt, st);
+        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+      }
     }
   }
   return EXC_OK;
@@ -170,10 +192,31 @@ static int count_kernel_nodes(cudaGraph_t g) {
   return k;
 }
 
+// sum of the workspace generations of the attached nets (a change means the
+// captured graphs point at released buffers)
+template <typename T>
+static long long net_generation(CaseImpl<T>* ci) {
+  long long g = 0;
+  for (int li = 0; li < ci->nles; ++li)
+    if (ci->les[li].net) g += net_workspace_gen(ci->les[li].net) + 1;
+  return g;
+}
+
 template <typename T>
 static int case_step(exc_case* cs, int nsteps, double dt_fixed) {
   CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
   cudaStream_t st = cs->stream;
+  for (int li = 0; li < ci->nles; ++li)
+    if (ci->les[li].net) {
+      int rc = net_reserve(ci->les[li].net, ci->les[li].M);
+      if (rc) return rc;
+    }
+  const long long gen = net_generation(ci);
+  if (gen != ci->net_gen) {
+    for (int k = 0; k < 2; ++k)
+      if (ci->graph[k]) { cudaGraphExecDestroy(ci->graph[k]); ci->graph[k] = nullptr; }
+    ci->net_gen = gen;
+  }
   for (int it = 0; it < nsteps; ++it) {
     int cur = ci->cur;
     double key = dt_fixed > 0 ? dt_fixed : -1.0;
@@ -254,7 +297,7 @@ static int case_create(exc_case* cs) {
     L.M = (long long)L.m * L.m * L.m;
     rc = poisson_init(&L.ps, cs->precision, L.m, d.l, nullptr);
     if (rc) return rc;
-    size_t nb = 14 * 3 * L.M * sizeof(T);
+    size_t nb = 20 * 3 * L.M * sizeof(T);
     if (cudaMalloc(&L.buf, nb) != cudaSuccess) { set_last_error("out of device memory (LES fields)"); return EXC_ERR_OOM; }
     cudaMemset(L.buf, 0, nb);
     size_t tbb = 3 * (size_t)d.n * L.m * L.m * sizeof(T);
@@ -264,6 +307,8 @@ static int case_create(exc_case* cs) {
     L.ub = take(); L.fk = take(); L.mcl = take(); L.mlast = take(); L.rtmp = take();
     L.ve[0] = take(); L.ve[1] = take(); L.ves = take(); L.ke = take();
     L.vn[0] = take(); L.vn[1] = take(); L.vns = take(); L.kn = take();
+    L.ublast = take();
+    L.vl[0] = take(); L.vl[1] = take(); L.vls = take(); L.kl = take(); L.nn = take();
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
@@ -284,6 +329,8 @@ static int reset_les(exc_case* cs) {
     size_t b = 3 * L.M * sizeof(T);
     cudaMemcpyAsync(L.ve[ci->cur], L.ub, b, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(L.vn[ci->cur], L.ub, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(L.vl[ci->cur], L.ub, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(L.ublast, L.ub, b, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(L.mlast, 0, b, st);
   }
   cudaMemsetAsync(ci->dscal, 0, 16 * sizeof(double), st);
@@ -358,8 +405,66 @@ static int les_field(exc_case* cs, int li, int which, double* host) {
     src = L.ub;
   } else if (which == 1) src = L.ve[ci->cur];
   else if (which == 2) src = L.vn[ci->cur];
-  else src = L.mlast;
+  else if (which == 3) src = L.mlast;
+  else if (which == 4) src = L.vl[ci->cur];
+  else src = L.ublast;
   return download<T>(cs, src, 3 * L.M, host);
+}
+
+// relative error (compute_errors, src/N.jl:1334-1349) of LES state `which`
+// (1 exact, 2 no-model, 4 learned) against the filtered DNS
+template <typename T>
+static int les_error_one(exc_case* cs, int li, int which, double* err) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  LesState<T>& L = ci->les[li];
+  cudaStream_t st = cs->stream;
+  int rc = les_target<T>(ci, L, ci->u[ci->cur], L.ub, st);
+  if (rc) return rc;
+  const T* v = which == 1 ? L.ve[ci->cur] : which == 2 ? L.vn[ci->cur] : L.vl[ci->cur];
+  double* out = ci->dscal + 4;
+  double host[6];
+  for (int c = 0; c < 3; ++c) {
+    cudaError_t e = launch_sqdiff<T>(L.M, v + c * L.M, L.ub + c * L.M, ci->part, out + 2 * c, st);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  }
+  cudaError_t e = cudaMemcpyAsync(host, out, 6 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  double s = 0;
+  for (int c = 0; c < 3; ++c) s += host[2 * c] / host[2 * c + 1];
+  *err = std::sqrt(s / 3.0);
+  return EXC_OK;
+}
+
+// copy (target, closure) at stage 0 of the last step to caller device buffers
+template <typename T>
+static int snapshot(exc_case* cs, int li, void* dev_u, void* dev_m) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  LesState<T>& L = ci->les[li];
+  size_t b = 3 * L.M * sizeof(T);
+  cudaError_t e = cudaMemcpyAsync(dev_u, L.ublast, b, cudaMemcpyDeviceToDevice, cs->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dev_m, L.mlast, b, cudaMemcpyDeviceToDevice, cs->stream);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+template <typename T>
+static int attach_net(exc_case* cs, int li, exc_net* net) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  LesState<T>& L = ci->les[li];
+  cudaStreamSynchronize(cs->stream);
+  if (net) {
+    int rc = net_reserve(net, L.M);
+    if (rc) return rc;
+  }
+  L.net = net;
+  // the step graphs change: capture again at the next step
+  for (int k = 0; k < 2; ++k)
+    if (ci->graph[k]) { cudaGraphExecDestroy(ci->graph[k]); ci->graph[k] = nullptr; }
+  ci->net_gen = net_generation(ci);
+  size_t b = 3 * L.M * sizeof(T);
+  cudaMemcpyAsync(L.vl[ci->cur], L.ve[ci->cur], b, cudaMemcpyDeviceToDevice, cs->stream);
+  return EXC_OK;
 }
 
 template <typename T>
@@ -544,8 +649,31 @@ int exc_case_get_velocity(exc_case* cs, double* host_u) {
 }
 
 int exc_case_get_les(exc_case* cs, int li, int which, double* host) {
-  if (!cs || !host || li < 0 || li >= cs->desc.nles || which < 0 || which > 3) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  if (!cs || !host || li < 0 || li >= cs->desc.nles || which < 0 || which > 5) { set_last_error("bad argument"); return EXC_ERR_ARG; }
   return DISPATCH(cs, les_field, cs, li, which, host);
+}
+
+int exc_case_reset_les(exc_case* cs) {
+  if (!cs) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, reset_les, cs);
+}
+
+int exc_case_les_error(exc_case* cs, int li, int which, double* err) {
+  if (!cs || !err || li < 0 || li >= cs->desc.nles || !(which == 1 || which == 2 || which == 4)) {
+    set_last_error("bad argument");
+    return EXC_ERR_ARG;
+  }
+  return DISPATCH(cs, les_error_one, cs, li, which, err);
+}
+
+int exc_case_snapshot(exc_case* cs, int li, void* dev_u, void* dev_m) {
+  if (!cs || !dev_u || !dev_m || li < 0 || li >= cs->desc.nles) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, snapshot, cs, li, dev_u, dev_m);
+}
+
+int exc_case_attach_net(exc_case* cs, int li, exc_net* net) {
+  if (!cs || li < 0 || li >= cs->desc.nles) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, attach_net, cs, li, net);
 }
 
 int exc_case_step(exc_case* cs, int nsteps, double dt_fixed) {

@@ -46,6 +46,10 @@ template <typename T>
 int init_random_field(exc_poisson* ps, T* u, cplx<T>* spec3, double* part, double kpeak, double energy,
                       uint64_t seed, cudaStream_t st);
 
+// Learned-closure network internals used by the case stepper (learned.cu).
+int net_reserve(exc_net* net, long long V);
+int net_workspace_gen(const exc_net* net);
+
 // Shared-memory opt-ins of every kernel that needs them, once per device;
 // called before any launch (and so before any stream capture).
 int configure_device();

@@ -1,0 +1,607 @@
+// Learned closure: a 3-D convolutional net on the LES grid (periodic 3x3x3
+// kernels, channels 3 -> 32 -> 32 -> 3, GELU after the first two layers),
+// trained on (filtered velocity, exact closure) pairs and used inside an LES.
+// No counterpart in the reference (its closures are the exact and classic
+// ones, src/N.jl:1137-1226).
+//
+// Activations are channel-last BF16 ([voxel][channel], channels padded to 16
+// or 32, outputs to 8); pre-activations are kept in FP32 for the backward
+// pass.  Forward and input-gradient convolutions are implicit GEMMs on the
+// tensor cores (mma.sync m16n8k16, BF16 inputs, FP32 accumulation): a CTA owns
+// 64 consecutive voxels and all output channels, and loops over the 27 taps
+// with the tap's input rows and weights staged in shared memory.  Weight
+// gradients are FP32 reductions with fixed-order partials.  Adam keeps FP32
+// master weights and moments and refreshes the BF16 copies.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+#include "fields.cuh"
+
+#include <cuda_bf16.h>
+
+namespace exc {
+
+constexpr int NET_TAPS = 27;
+constexpr int CONV_M = 64;  // voxels per CTA
+constexpr int CONV_THREADS = 128;
+
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad_f(float x) {
+  return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+__device__ __forceinline__ unsigned ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const unsigned*>(p); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Periodic neighbour of voxel v (linear, x fastest) on an n^3 grid per sample.
+__device__ __forceinline__ long long neighbour(long long v, int n, int dz, int dy, int dx) {
+  const long long nn = (long long)n * n, N = nn * n;
+  const long long b = v / N;
+  long long r = v - b * N;
+  int z = (int)(r / nn);
+  r -= (long long)z * nn;
+  int y = (int)(r / n), x = (int)(r - (long long)y * n);
+  z += dz; y += dy; x += dx;
+  z = z < 0 ? z + n : (z >= n ? z - n : z);
+  y = y < 0 ? y + n : (y >= n ? y - n : y);
+  x = x < 0 ? x + n : (x >= n ? x - n : x);
+  return b * N + ((long long)z * n + y) * n + x;
+}
+
+// ---------------------------------------------------------------------------
+// Implicit-GEMM convolution on the tensor cores:
+//   out[v][co] = bias[co] + sum_{tap, ci} in[v + tap][ci] * Wt[tap][co][ci]
+// KP: input channels (multiple of 16), NP: output channels (multiple of 8).
+// EPI 0: store pre (FP32) and GELU(pre) (BF16);  EPI 1: store out (FP32);
+// EPI 2: input gradient: multiply by GELU'(pre_prev[v][co]), store BF16.
+// ---------------------------------------------------------------------------
+template <int KP, int NP, int EPI>
+__global__ void __launch_bounds__(CONV_THREADS)
+conv_mma_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
+                const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
+                const float* __restrict__ pre_prev, int nout_valid) {
+  constexpr int AS = KP + 8;  // padded row stride (bf16) against bank conflicts
+  __shared__ __align__(16) __nv_bfloat16 sA[CONV_M * AS];
+  __shared__ __align__(16) __nv_bfloat16 sW[NP * AS];
+  const long long v0 = (long long)blockIdx.x * CONV_M;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  float acc[NP / 8][4];
+#pragma unroll
+  for (int j = 0; j < NP / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  for (int tap = 0; tap < NET_TAPS; ++tap) {
+    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    __syncthreads();
+    // stage the tap's input rows (16-byte chunks) and weights
+    constexpr int CH = KP / 8;  // 8 bf16 per 16-byte chunk
+    for (int t = threadIdx.x; t < CONV_M * CH; t += CONV_THREADS) {
+      const int r = t / CH, c = t - r * CH;
+      const long long v = v0 + r;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (v < V) val = *reinterpret_cast<const uint4*>(in + neighbour(v, n, dz, dy, dx) * KP + c * 8);
+      *reinterpret_cast<uint4*>(sA + r * AS + c * 8) = val;
+    }
+    for (int t = threadIdx.x; t < NP * CH; t += CONV_THREADS) {
+      const int r = t / CH, c = t - r * CH;
+      *reinterpret_cast<uint4*>(sW + r * AS + c * 8) =
+          *reinterpret_cast<const uint4*>(Wt + ((long long)tap * NP + r) * KP + c * 8);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < KP; kk += 16) {
+      unsigned a[4];
+      const __nv_bfloat16* ar = sA + (warp * 16 + gid) * AS + kk + tig * 2;
+      a[0] = ld32(ar);
+      a[1] = ld32(ar + 8 * AS);
+      a[2] = ld32(ar + 8);
+      a[3] = ld32(ar + 8 * AS + 8);
+#pragma unroll
+      for (int j = 0; j < NP / 8; ++j) {
+        const __nv_bfloat16* br = sW + (j * 8 + gid) * AS + kk + tig * 2;
+        mma_bf16(acc[j], a, ld32(br), ld32(br + 8));
+      }
+    }
+  }
+  // epilogue: C fragment rows gid / gid + 8, columns tig*2 + {0, 1}
+#pragma unroll
+  for (int j = 0; j < NP / 8; ++j)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const long long v = v0 + warp * 16 + gid + h * 8;
+      if (v >= V) continue;
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int co = j * 8 + tig * 2 + e;
+        float x = acc[j][h * 2 + e];
+        if (EPI == 0) {
+          x += bias[co];
+          pre_out[v * NP + co] = x;
+          act_out[v * NP + co] = __float2bfloat16(gelu_f(x));
+        } else if (EPI == 1) {
+          x += bias[co];
+          pre_out[v * NP + co] = co < nout_valid ? x : 0.f;
+        } else {
+          act_out[v * NP + co] = __float2bfloat16(x * gelu_grad_f(pre_prev[v * NP + co]));
+        }
+      }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradient: dW[tap][ci][co] = sum_v in[v + tap][ci] g[v][co] with
+// per-CTA partials over voxel chunks, folded in a fixed order; db[co] = sum g.
+// ---------------------------------------------------------------------------
+constexpr int WG_CHUNK = 4096;
+constexpr int WG_SUB = 32;
+
+template <int KP, int NP>
+__global__ void __launch_bounds__(256)
+wgrad_partial_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ g,
+                     float* __restrict__ part) {
+  __shared__ float sx[WG_SUB][KP];
+  __shared__ float sg[WG_SUB][NP];
+  const int tap = blockIdx.y;
+  const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+  const long long c0 = (long long)blockIdx.x * WG_CHUNK;
+  constexpr int PAIRS = KP * NP;
+  constexpr int PER = (PAIRS + 255) / 256;
+  float acc[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) acc[q] = 0.f;
+  for (long long s0 = c0; s0 < c0 + WG_CHUNK && s0 < V; s0 += WG_SUB) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < WG_SUB * KP; t += 256) {
+      const int r = t / KP, c = t - r * KP;
+      const long long v = s0 + r;
+      sx[r][c] = v < V ? __bfloat162float(in[neighbour(v, n, dz, dy, dx) * KP + c]) : 0.f;
+    }
+    for (int t = threadIdx.x; t < WG_SUB * NP; t += 256) {
+      const int r = t / NP, c = t - r * NP;
+      const long long v = s0 + r;
+      sg[r][c] = v < V ? __bfloat162float(g[v * NP + c]) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int p = threadIdx.x + q * 256;
+      if (p < PAIRS) {
+        const int ci = p / NP, co = p - ci * NP;
+        float a = acc[q];
+#pragma unroll 8
+        for (int r = 0; r < WG_SUB; ++r) a = fmaf(sx[r][ci], sg[r][co], a);
+        acc[q] = a;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int p = threadIdx.x + q * 256;
+    if (p < PAIRS) part[((long long)blockIdx.x * NET_TAPS + tap) * PAIRS + p] = acc[q];
+  }
+}
+
+// fold partials over chunks; bias gradient from the g sums of tap 13 (centre)
+template <int KP, int NP>
+__global__ void wgrad_fold_kernel(int nchunk, const float* __restrict__ part, float* __restrict__ dW) {
+  constexpr int PAIRS = KP * NP;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NET_TAPS * PAIRS) return;
+  double s = 0;
+  for (int c = 0; c < nchunk; ++c) s += part[(long long)c * NET_TAPS * PAIRS + i];
+  dW[i] = (float)s;
+}
+
+template <int NP>
+__global__ void bgrad_kernel(long long V, const __nv_bfloat16* __restrict__ g, float* __restrict__ db) {
+  // one block per channel, fixed-order tree
+  __shared__ double red[256];
+  const int co = blockIdx.x;
+  double s = 0;
+  for (long long v = threadIdx.x; v < V; v += 256) s += (double)__bfloat162float(g[v * NP + co]);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) db[co] = (float)red[0];
+}
+
+// ---------------------------------------------------------------------------
+// Packing, loss, Adam, weight layouts
+// ---------------------------------------------------------------------------
+// fields [b][3][n^3] (T) -> channel-last bf16 [b n^3][KP], scaled
+template <typename T>
+__global__ void pack_input_kernel(long long V, long long N, const T* __restrict__ f, double scale,
+                                  __nv_bfloat16* __restrict__ out, int KP) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    const long long b = v / N, r = v - b * N;
+    for (int c = 0; c < KP; ++c) {
+      float x = c < 3 ? (float)((double)f[(b * 3 + c) * N + r] * scale) : 0.f;
+      out[v * KP + c] = __float2bfloat16(x);
+    }
+  }
+}
+
+constexpr int OUTP = 16;  // padded output channels
+
+// net output [V][OUTP] (FP32, normalised) -> fields [b][3][n^3] (T) * scale
+template <typename T>
+__global__ void unpack_output_kernel(long long V, long long N, const float* __restrict__ o, double scale,
+                                     T* __restrict__ f) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    const long long b = v / N, r = v - b * N;
+    for (int c = 0; c < 3; ++c) f[(b * 3 + c) * N + r] = (T)((double)o[v * OUTP + c] * scale);
+  }
+}
+
+// g = 2 (out - target*tscale) / count (bf16, [V][OUTP]); per-block squared-error partials
+template <typename T>
+__global__ void loss_grad_kernel(long long V, long long N, const float* __restrict__ out, const T* __restrict__ tgt,
+                                 double tscale, double inv_count, __nv_bfloat16* __restrict__ g,
+                                 double* __restrict__ part) {
+  __shared__ double red[256];
+  double s = 0;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    const long long b = v / N, r = v - b * N;
+    for (int c = 0; c < OUTP; ++c) {
+      float d = 0.f;
+      if (c < 3) d = out[v * OUTP + c] - (float)((double)tgt[(b * 3 + c) * N + r] * tscale);
+      s += (double)d * d;
+      g[v * OUTP + c] = __float2bfloat16((float)(2.0 * inv_count) * d);
+    }
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void sum_kernel(int np, const double* __restrict__ part, double scale, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0;
+    for (int i = 0; i < np; ++i) s += part[i];
+    *out = s * scale;
+  }
+}
+
+// Adam (Kingma & Ba 2015): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
+// w -= lr mhat / (sqrt(vhat) + eps)
+__global__ void adam_kernel(int count, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, float lr, float b1, float b2, float c1, float c2, float eps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// master W[tap][KP][NP] (FP32, padded entries zero) -> forward
+// Wt[tap][co][ci] and input-gradient Wb[tap][ci][co] = W[26 - tap][ci][co]
+// (n = ci, k = co), both bf16
+__global__ void refresh_weights_kernel(const float* __restrict__ W, int KP, int NP, __nv_bfloat16* __restrict__ Wt,
+                                       __nv_bfloat16* __restrict__ Wb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tot = NET_TAPS * KP * NP;
+  if (i >= tot) return;
+  {
+    const int tap = i / (NP * KP), r = i - tap * NP * KP;
+    const int co = r / KP, ci = r - co * KP;
+    Wt[i] = __float2bfloat16(W[((long long)tap * KP + ci) * NP + co]);
+  }
+  {
+    const int tap = i / (KP * NP), r = i - tap * KP * NP;
+    const int ci = r / NP, co = r - ci * NP;
+    Wb[i] = __float2bfloat16(W[((long long)(26 - tap) * KP + ci) * NP + co]);
+  }
+}
+
+}  // namespace exc
+
+// ---------------------------------------------------------------------------
+// Host side: the network object and its C ABI
+// ---------------------------------------------------------------------------
+struct exc_net {
+  // padded layer shapes: (KP, NP) = (16, 32), (32, 32), (32, 16)
+  static constexpr int K1 = 16, N1 = 32, K2 = 32, N2 = 32, K3 = 32, N3 = exc::OUTP;
+  static constexpr long long W1 = 27LL * K1 * N1, W2 = 27LL * K2 * N2, W3 = 27LL * K3 * N3;
+  static constexpr long long NPARAM = W1 + N1 + W2 + N2 + W3 + N3;
+  float* params = nullptr;  // [W1 b1 W2 b2 W3 b3], FP32 master, padded entries zero
+  float* grads = nullptr;
+  float* adam_m = nullptr;
+  float* adam_v = nullptr;
+  __nv_bfloat16* wbf = nullptr;  // Wt1 Wb1 Wt2 Wb2 Wt3 Wb3
+  int adam_t = 0;
+  double in_scale = 1.0, out_scale = 1.0;
+  long long vcap = 0;  // voxel capacity of the workspace
+  int ws_gen = 0;       // bumped whenever the workspace moves (captured graphs must re-capture)
+  __nv_bfloat16 *x0 = nullptr, *a1 = nullptr, *a2 = nullptr, *g3 = nullptr, *gp2 = nullptr, *gp1 = nullptr;
+  float *pre1 = nullptr, *pre2 = nullptr, *out = nullptr, *wpart = nullptr;
+  double* lpart = nullptr;  // loss partials + result
+  float* W(int l) { return params + (l == 0 ? 0 : l == 1 ? W1 + N1 : W1 + N1 + W2 + N2); }
+  float* B(int l) { return W(l) + (l == 0 ? W1 : l == 1 ? W2 : W3); }
+  float* dW(int l) { return grads + (W(l) - params); }
+  float* dB(int l) { return grads + (B(l) - params); }
+  __nv_bfloat16* Wt(int l) { return wbf + (l == 0 ? 0 : l == 1 ? 2 * W1 : 2 * (W1 + W2)); }
+  __nv_bfloat16* Wb(int l) { return Wt(l) + (l == 0 ? W1 : l == 1 ? W2 : W3); }
+};
+
+namespace exc {
+
+static void free_workspace(exc_net* net) {
+  void* ps[] = {net->x0, net->a1, net->a2, net->g3, net->gp2, net->gp1, net->pre1, net->pre2, net->out, net->wpart,
+                net->lpart};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  net->x0 = net->a1 = net->a2 = net->g3 = net->gp2 = net->gp1 = nullptr;
+  net->pre1 = net->pre2 = net->out = net->wpart = nullptr;
+  net->lpart = nullptr;
+  net->vcap = 0;
+}
+
+static int ensure_workspace(exc_net* net, long long V) {
+  if (V <= net->vcap) return EXC_OK;
+  cudaDeviceSynchronize();
+  free_workspace(net);
+  const long long nchunk = (V + WG_CHUNK - 1) / WG_CHUNK;
+  bool ok = cudaMalloc(&net->x0, V * exc_net::K1 * 2) == cudaSuccess &&
+            cudaMalloc(&net->a1, V * exc_net::N1 * 2) == cudaSuccess &&
+            cudaMalloc(&net->a2, V * exc_net::N2 * 2) == cudaSuccess &&
+            cudaMalloc(&net->g3, V * exc_net::N3 * 2) == cudaSuccess &&
+            cudaMalloc(&net->gp2, V * exc_net::N2 * 2) == cudaSuccess &&
+            cudaMalloc(&net->gp1, V * exc_net::N1 * 2) == cudaSuccess &&
+            cudaMalloc(&net->pre1, V * exc_net::N1 * 4) == cudaSuccess &&
+            cudaMalloc(&net->pre2, V * exc_net::N2 * 4) == cudaSuccess &&
+            cudaMalloc(&net->out, V * exc_net::N3 * 4) == cudaSuccess &&
+            cudaMalloc(&net->wpart, nchunk * 27 * 32 * 32 * 4) == cudaSuccess &&
+            cudaMalloc(&net->lpart, (1024 + 8) * sizeof(double)) == cudaSuccess;
+  if (!ok) {
+    free_workspace(net);
+    set_last_error("out of device memory (network workspace)");
+    return EXC_ERR_OOM;
+  }
+  net->vcap = V;
+  net->ws_gen += 1;
+  return EXC_OK;
+}
+
+int net_reserve(exc_net* net, long long V) { return ensure_workspace(net, V); }
+int net_workspace_gen(const exc_net* net) { return net->ws_gen; }
+
+static cudaError_t refresh(exc_net* net, cudaStream_t st) {
+  const int ks[3] = {exc_net::K1, exc_net::K2, exc_net::K3}, ns[3] = {exc_net::N1, exc_net::N2, exc_net::N3};
+  for (int l = 0; l < 3; ++l) {
+    const int tot = 27 * ks[l] * ns[l];
+    refresh_weights_kernel<<<(tot + 255) / 256, 256, 0, st>>>(net->W(l), ks[l], ns[l], net->Wt(l), net->Wb(l));
+  }
+  return cudaGetLastError();
+}
+
+static inline unsigned conv_grid(long long V) { return (unsigned)((V + CONV_M - 1) / CONV_M); }
+
+// forward from the packed input x0; leaves pre1, a1, pre2, a2, out
+static cudaError_t forward_packed(exc_net* net, long long V, int n, cudaStream_t st) {
+  const unsigned g = conv_grid(V);
+  conv_mma_kernel<16, 32, 0><<<g, CONV_THREADS, 0, st>>>(V, n, net->x0, net->Wt(0), net->B(0), net->pre1, net->a1,
+                                                          nullptr, 32);
+  conv_mma_kernel<32, 32, 0><<<g, CONV_THREADS, 0, st>>>(V, n, net->a1, net->Wt(1), net->B(1), net->pre2, net->a2,
+                                                          nullptr, 32);
+  conv_mma_kernel<32, 16, 1><<<g, CONV_THREADS, 0, st>>>(V, n, net->a2, net->Wt(2), net->B(2), net->out, nullptr,
+                                                          nullptr, 3);
+  return cudaGetLastError();
+}
+
+template <int KP, int NP>
+static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* g,
+                         cudaStream_t st) {
+  const int nchunk = (int)((V + WG_CHUNK - 1) / WG_CHUNK);
+  wgrad_partial_kernel<KP, NP><<<dim3(nchunk, 27), 256, 0, st>>>(V, n, in, g, net->wpart);
+  wgrad_fold_kernel<KP, NP><<<(27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
+  bgrad_kernel<NP><<<NP, 256, 0, st>>>(V, g, net->dB(l));
+  return cudaGetLastError();
+}
+
+// loss, backward; gradients into net->grads, loss into lpart[1024]
+template <typename T>
+static cudaError_t backward(exc_net* net, long long V, int n, long long N, const T* target, cudaStream_t st) {
+  const int lb = (int)std::min<long long>((V + 255) / 256, 1024);
+  loss_grad_kernel<T><<<lb, 256, 0, st>>>(V, N, net->out, target, 1.0 / net->out_scale, 1.0 / (3.0 * (double)V),
+                                          net->g3, net->lpart);
+  sum_kernel<<<1, 32, 0, st>>>(lb, net->lpart, 1.0 / (3.0 * (double)V), net->lpart + 1024);
+  const unsigned g = conv_grid(V);
+  cudaError_t e = wgrad<32, 16>(net, 2, V, n, net->a2, net->g3, st);
+  // input gradient of layer 3 times GELU'(pre2)
+  conv_mma_kernel<16, 32, 2><<<g, CONV_THREADS, 0, st>>>(V, n, net->g3, net->Wb(2), nullptr, nullptr, net->gp2,
+                                                          net->pre2, 32);
+  if (e == cudaSuccess) e = wgrad<32, 32>(net, 1, V, n, net->a1, net->gp2, st);
+  conv_mma_kernel<32, 32, 2><<<g, CONV_THREADS, 0, st>>>(V, n, net->gp2, net->Wb(1), nullptr, nullptr, net->gp1,
+                                                          net->pre1, 32);
+  if (e == cudaSuccess) e = wgrad<16, 32>(net, 0, V, n, net->x0, net->gp1, st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e;
+}
+
+template <typename T>
+static int net_forward_t(exc_net* net, int batch, int n, const T* u, T* m, cudaStream_t st) {
+  const long long N = (long long)n * n * n, V = batch * N;
+  int rc = ensure_workspace(net, V);
+  if (rc) return rc;
+  const int gb = (int)std::min<long long>((V + 255) / 256, 152LL * 32);
+  pack_input_kernel<T><<<gb, 256, 0, st>>>(V, N, u, 1.0 / net->in_scale, net->x0, exc_net::K1);
+  cudaError_t e = forward_packed(net, V, n, st);
+  if (e == cudaSuccess) {
+    unpack_output_kernel<T><<<gb, 256, 0, st>>>(V, N, net->out, net->out_scale, m);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+template <typename T>
+static int net_grad_t(exc_net* net, int batch, int n, const T* u, const T* m, cudaStream_t st) {
+  const long long N = (long long)n * n * n, V = batch * N;
+  int rc = ensure_workspace(net, V);
+  if (rc) return rc;
+  const int gb = (int)std::min<long long>((V + 255) / 256, 152LL * 32);
+  pack_input_kernel<T><<<gb, 256, 0, st>>>(V, N, u, 1.0 / net->in_scale, net->x0, exc_net::K1);
+  cudaError_t e = forward_packed(net, V, n, st);
+  if (e == cudaSuccess) e = backward<T>(net, V, n, N, m, st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+// He-normal initial weights from the project's counter generator (host)
+static double host_normal(uint64_t seed, uint64_t i) {
+  auto sm = [](uint64_t x) {
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+  };
+  const uint64_t base = seed * 0x9E3779B97F4A7C15ull;
+  double u1 = ((double)(sm(base + 2 * i) >> 11) + 0.5) * 0x1.0p-53;
+  double u2 = ((double)(sm(base + 2 * i + 1) >> 11) + 0.5) * 0x1.0p-53;
+  return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2);
+}
+
+}  // namespace exc
+
+using namespace exc;
+
+extern "C" {
+
+int exc_net_create(uint64_t seed, exc_net** out) {
+  if (!out) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  *out = nullptr;
+  int rc = configure_device();
+  if (rc) return rc;
+  exc_net* net = new exc_net();
+  const size_t pb = exc_net::NPARAM * sizeof(float);
+  const size_t wb = 2 * (exc_net::W1 + exc_net::W2 + exc_net::W3) * sizeof(__nv_bfloat16);
+  if (cudaMalloc(&net->params, pb) != cudaSuccess || cudaMalloc(&net->grads, pb) != cudaSuccess ||
+      cudaMalloc(&net->adam_m, pb) != cudaSuccess || cudaMalloc(&net->adam_v, pb) != cudaSuccess ||
+      cudaMalloc(&net->wbf, wb) != cudaSuccess) {
+    exc_net_destroy(net);
+    set_last_error("out of device memory (network)");
+    return EXC_ERR_OOM;
+  }
+  std::vector<float> h(exc_net::NPARAM, 0.f);
+  const int cin[3] = {3, 32, 32}, cout[3] = {32, 32, 3};
+  const int ks[3] = {exc_net::K1, exc_net::K2, exc_net::K3}, ns[3] = {exc_net::N1, exc_net::N2, exc_net::N3};
+  uint64_t ctr = 0;
+  for (int l = 0; l < 3; ++l) {
+    const double std_ = std::sqrt(2.0 / (27.0 * cin[l]));
+    float* W = h.data() + (net->W(l) - net->params);
+    for (int t = 0; t < 27; ++t)
+      for (int ci = 0; ci < cin[l]; ++ci)
+        for (int co = 0; co < cout[l]; ++co) W[((size_t)t * ks[l] + ci) * ns[l] + co] = (float)(std_ * host_normal(seed, ctr++));
+  }
+  cudaMemcpy(net->params, h.data(), pb, cudaMemcpyHostToDevice);
+  cudaMemset(net->grads, 0, pb);
+  cudaMemset(net->adam_m, 0, pb);
+  cudaMemset(net->adam_v, 0, pb);
+  cudaError_t e = refresh(net, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { exc_net_destroy(net); set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  *out = net;
+  return EXC_OK;
+}
+
+int exc_net_destroy(exc_net* net) {
+  if (!net) return EXC_OK;
+  cudaDeviceSynchronize();
+  free_workspace(net);
+  if (net->params) cudaFree(net->params);
+  if (net->grads) cudaFree(net->grads);
+  if (net->adam_m) cudaFree(net->adam_m);
+  if (net->adam_v) cudaFree(net->adam_v);
+  if (net->wbf) cudaFree(net->wbf);
+  delete net;
+  return EXC_OK;
+}
+
+int exc_net_param_count(void) { return (int)exc_net::NPARAM; }
+
+int exc_net_set_scales(exc_net* net, double in_scale, double out_scale) {
+  if (!net || !(in_scale > 0) || !(out_scale > 0)) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  net->in_scale = in_scale;
+  net->out_scale = out_scale;
+  return EXC_OK;
+}
+
+int exc_net_get_params(exc_net* net, float* host, int count) {
+  if (!net || !host || count != (int)exc_net::NPARAM) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  cudaError_t e = cudaMemcpy(host, net->params, count * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+int exc_net_set_params(exc_net* net, const float* host, int count) {
+  if (!net || !host || count != (int)exc_net::NPARAM) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  cudaError_t e = cudaMemcpy(net->params, host, count * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = refresh(net, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  net->adam_t = 0;
+  if (e == cudaSuccess) e = cudaMemset(net->adam_m, 0, exc_net::NPARAM * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(net->adam_v, 0, exc_net::NPARAM * sizeof(float));
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+int exc_net_forward(exc_net* net, int precision, int batch, int n, const void* u, void* m, void* stream) {
+  if (!net || !u || !m || batch < 1 || n < 1) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == EXC_F64) return net_forward_t<double>(net, batch, n, (const double*)u, (double*)m, st);
+  if (precision == EXC_F32) return net_forward_t<float>(net, batch, n, (const float*)u, (float*)m, st);
+  set_last_error("bad precision");
+  return EXC_ERR_ARG;
+}
+
+int exc_net_gradients(exc_net* net, int precision, int batch, int n, const void* u, const void* m, float* grad_host,
+                      double* loss_host, void* stream) {
+  if (!net || !u || !m || batch < 1 || n < 1) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = precision == EXC_F64 ? net_grad_t<double>(net, batch, n, (const double*)u, (const double*)m, st)
+                                : net_grad_t<float>(net, batch, n, (const float*)u, (const float*)m, st);
+  if (rc) return rc;
+  cudaError_t e = cudaSuccess;
+  if (grad_host) e = cudaMemcpyAsync(grad_host, net->grads, exc_net::NPARAM * sizeof(float), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && loss_host) e = cudaMemcpyAsync(loss_host, net->lpart + 1024, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+int exc_net_train_step(exc_net* net, int precision, int batch, int n, const void* u, const void* m, double lr,
+                       double* loss_host, void* stream) {
+  int rc = exc_net_gradients(net, precision, batch, n, u, m, nullptr, nullptr, stream);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  net->adam_t += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)net->adam_t), c2 = 1.f - std::pow(b2, (float)net->adam_t);
+  const int cnt = (int)exc_net::NPARAM;
+  adam_kernel<<<(cnt + 255) / 256, 256, 0, st>>>(cnt, net->params, net->grads, net->adam_m, net->adam_v, (float)lr, b1,
+                                                 b2, c1, c2, 1e-8f);
+  cudaError_t e = refresh(net, st);
+  if (e == cudaSuccess && loss_host) e = cudaMemcpyAsync(loss_host, net->lpart + 1024, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+}  // extern "C"

@@ -95,7 +95,20 @@ SIGNATURES = {
     "exc_case_spectrum": [vp, dp, i32],
     "exc_case_device_ptr": [vp, i32, C.POINTER(vp)],
     "exc_case_launches_per_step": [vp, C.POINTER(i32)],
+    "exc_case_reset_les": [vp],
+    "exc_case_les_error": [vp, i32, i32, dp],
+    "exc_case_snapshot": [vp, i32, vp, vp],
+    "exc_case_attach_net": [vp, i32, vp],
     "exc_case_sync": [vp],
+    "exc_net_create": [u64, C.POINTER(vp)],
+    "exc_net_destroy": [vp],
+    "exc_net_param_count": [],
+    "exc_net_set_scales": [vp, f64, f64],
+    "exc_net_get_params": [vp, C.POINTER(C.c_float), i32],
+    "exc_net_set_params": [vp, C.POINTER(C.c_float), i32],
+    "exc_net_forward": [vp, i32, i32, i32, vp, vp, vp],
+    "exc_net_gradients": [vp, i32, i32, i32, vp, vp, C.POINTER(C.c_float), dp, vp],
+    "exc_net_train_step": [vp, i32, i32, i32, vp, vp, f64, dp, vp],
     "exc_server_create": [C.POINTER(ServerDesc), C.POINTER(vp)],
     "exc_server_destroy": [vp],
     "exc_server_submit": [vp, C.POINTER(SolveReq), C.POINTER(C.c_int64)],

@@ -214,7 +214,7 @@ class Case:
 
     def les(self, index: int, which: str = "exact") -> np.ndarray:
         """LES field: 'target' (filtered DNS), 'exact', 'nomodel' or 'closure'."""
-        w = {"target": 0, "exact": 1, "nomodel": 2, "closure": 3}[which]
+        w = {"target": 0, "exact": 1, "nomodel": 2, "closure": 3, "learned": 4, "target_last": 5}[which]
         m = self.n // self.les_list[index][0]
         a, p = self._buf((3, m, m, m))
         call("exc_case_get_les", self._h, index, w, p)
@@ -236,6 +236,27 @@ class Case:
         k = C.c_int()
         call("exc_case_launches_per_step", self._h, C.byref(k))
         return k.value
+
+    def reset_les(self):
+        """Restart every LES state from the filtered DNS (and the clock from 0)."""
+        call("exc_case_reset_les", self._h)
+
+    def les_error(self, index: int, which: str = "exact") -> float:
+        """Relative L2 error of an LES state ('exact', 'nomodel', 'learned')
+        against the filtered DNS (``compute_errors``, ``src/N.jl:1334-1349``)."""
+        e = C.c_double()
+        call("exc_case_les_error", self._h, index, {"exact": 1, "nomodel": 2, "learned": 4}[which], C.byref(e))
+        return e.value
+
+    def snapshot(self, index: int, u_dev, m_dev):
+        """Device copy of (filtered DNS, exact closure) at stage 1 of the last step
+        into CUDA tensors of the case precision, shaped (3, m, m, m)."""
+        call("exc_case_snapshot", self._h, index, C.c_void_p(u_dev.data_ptr()), C.c_void_p(m_dev.data_ptr()))
+
+    def attach_net(self, index: int, net):
+        """Drive a learned-closure LES on LES grid ``index`` (None detaches)."""
+        call("exc_case_attach_net", self._h, index, net.handle if net is not None else None)
+        self._net = net
 
     def step(self, nsteps: int = 1, dt: float = 0.0):
         call("exc_case_step", self._h, nsteps, dt)

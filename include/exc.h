@@ -175,9 +175,25 @@ int exc_case_set_velocity(exc_case* cs, const double* host_u);
 int exc_case_get_velocity(exc_case* cs, double* host_u);
 
 /* LES field `which`: 0 = filtered DNS target, 1 = exact-closure LES,
- * 2 = no-model LES, 3 = last exact closure m (stage 1 of the last step);
+ * 2 = no-model LES, 3 = last exact closure m (stage 1 of the last step),
+ * 4 = learned-closure LES (exc_case_attach_net), 5 = the filtered DNS at
+ * stage 1 of the last step (the input that goes with 3);
  * 3 (n/ratio)^3 doubles. */
 int exc_case_get_les(exc_case* cs, int les_index, int which, double* host_v);
+
+/* Restart every LES state of every LES grid from the filtered DNS
+ * (`apply_DHpi`, src/N.jl:1228-1237) and the clock from 0. */
+int exc_case_reset_les(exc_case* cs);
+
+/* Relative L2 error (compute_errors) of one LES state against the filtered
+ * DNS: which = 1 exact closure, 2 no model, 4 learned closure. */
+int exc_case_les_error(exc_case* cs, int les_index, int which, double* err);
+
+/* Device-to-device copy of the pair (filtered DNS, exact closure m) at stage
+ * 1 of the last step, 3 (n/ratio)^3 words each in the case precision: the
+ * training data of the learned closure (what the reference's driver stores
+ * with JLD2, dns_aid.jl:87-103, kept on the device here). */
+int exc_case_snapshot(exc_case* cs, int les_index, void* dev_u, void* dev_m);
 
 /* Advance `nsteps` RK4 steps.  dt_fixed > 0 uses that step, otherwise
  * propose_timestep on the device every step (no host synchronisation). */
@@ -273,6 +289,43 @@ int exc_server_drain(exc_server* sv);
 int exc_server_stats(exc_server* sv, exc_server_info* st);
 /* FFT tile shape the autotuner chose for (precision, n, slots per batch). */
 int exc_server_tuning(int precision, int n, int slots, int* col_w, int* x_rows);
+
+/* ======================================================================
+ * Learned closure (no counterpart in the reference): a 3-D convolutional
+ * net on the LES grid with periodic 3x3x3 kernels, channels 3 -> 32 -> 32 -> 3
+ * and GELU after the first two layers, trained on (filtered velocity, exact
+ * closure) pairs.  BF16 weights and activations, FP32 accumulation on the
+ * tensor cores; FP32 master weights and Adam moments.  Fields are device
+ * arrays [batch][3][n^3] of the given precision; the net sees u/in_scale and
+ * predicts m/out_scale.  Parameters are one FP32 vector in the padded layout
+ * [W1 b1 W2 b2 W3 b3], W_l[tap][KP_l][NP_l] with (KP, NP) = (16, 32),
+ * (32, 32), (32, 16) and tap = (dz+1)*9 + (dy+1)*3 + (dx+1).
+ * ====================================================================== */
+
+typedef struct exc_net exc_net;
+
+int exc_net_create(uint64_t seed, exc_net** out);
+int exc_net_destroy(exc_net* net);
+int exc_net_param_count(void);
+int exc_net_set_scales(exc_net* net, double in_scale, double out_scale);
+int exc_net_get_params(exc_net* net, float* host, int count);
+/* Also resets the Adam state. */
+int exc_net_set_params(exc_net* net, const float* host, int count);
+/* m = net(u) */
+int exc_net_forward(exc_net* net, int precision, int batch, int n, const void* u, void* m, void* stream);
+/* Gradients of the MSE loss mean((net(u) - m/out_scale)^2) (host copy in
+ * the parameter layout when grad_host != NULL) and the loss. */
+int exc_net_gradients(exc_net* net, int precision, int batch, int n, const void* u, const void* m,
+                      float* grad_host, double* loss_host, void* stream);
+/* One Adam step (b1 0.9, b2 0.999, eps 1e-8) on that loss; returns the loss
+ * before the update. */
+int exc_net_train_step(exc_net* net, int precision, int batch, int n, const void* u, const void* m, double lr,
+                       double* loss_host, void* stream);
+
+/* Drive a third LES state of LES grid `les_index` with the learned closure,
+ * k = P_H(RHS_H(v) + net(v)), starting from the exact-closure state (NULL
+ * detaches).  exc_case_get_les(which = 4) reads it. */
+int exc_case_attach_net(exc_case* cs, int les_index, exc_net* net);
 
 #ifdef __cplusplus
 }

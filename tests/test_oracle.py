@@ -186,6 +186,33 @@ def test_c_restatement_matches_numpy_oracle():
     cs.close()
 
 
+def test_net_oracle_gradients_by_finite_differences():
+    """The analytic backward of the learned-closure net (oracle/net.py)."""
+    from oracle import net as onet
+
+    rng = np.random.default_rng(0)
+    params = onet.init_params(1, hidden=4)
+    params = [(W, rng.normal(0, 0.1, b.shape)) for W, b in params]
+    x = rng.normal(size=(1, 4, 4, 4, 3))
+    t = rng.normal(size=(1, 4, 4, 4, 3))
+    loss, grads = onet.loss_and_grads(params, x, t)
+    for li, (W, b) in enumerate(params):
+        for idx in [(0, 0, 0), (13, 1, 2), (26, 2, 1)]:
+            idx = tuple(min(i, s - 1) for i, s in zip(idx, W.shape))
+            eps = 1e-6
+            Wp = W.copy()
+            Wp[idx] += eps
+            pp = list(params)
+            pp[li] = (Wp, b)
+            lp, _ = onet.loss_and_grads(pp, x, t)
+            Wm = W.copy()
+            Wm[idx] -= eps
+            pp[li] = (Wm, b)
+            lm, _ = onet.loss_and_grads(pp, x, t)
+            fd = (lp - lm) / (2 * eps)
+            assert abs(fd - grads[li][0][idx]) < 1e-6 + 1e-5 * abs(fd)
+
+
 def test_counter_normal_statistics():
     x = ns.counter_normal(0, 200000)
     assert abs(x.mean()) < 0.01 and abs(x.std() - 1) < 0.01

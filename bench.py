@@ -179,27 +179,24 @@ def serve_stream(precision=1, nreq=96, rate=20.0, nsteps=200):
         sv.submit(n, 1 / 1000, 1, seed=1)
     sv.drain()
     sv.poll()
+    ids = {}
     done = {}
     i = 0
     t0 = time.perf_counter()
-    clock0 = sv.stats()["clock"]
     while len(done) < nreq:
         now = time.perf_counter() - t0
         while i < nreq and reqs[i]["t"] <= now:
             q = reqs[i]
             rid = sv.submit(q["n"], q["visc"], q["nsteps"], seed=q["seed"], kpeak=4.0)
-            done.setdefault("_ids", {})[rid] = i
+            ids[rid] = i
             i += 1
         active, queued = sv.tick()
         for r in sv.poll():
-            if r["id"] in done.get("_ids", {}):
+            if r["id"] in ids:
                 done[r["id"]] = r
         if active == 0 and queued == 0 and i < nreq:
             time.sleep(max(0.0, min(0.01, reqs[i]["t"] - (time.perf_counter() - t0))))
-        done_count = len(done) - ("_ids" in done)
-        if done_count >= nreq:
-            break
-    res = [r for k, r in done.items() if k != "_ids"]
+    res = list(done.values())
     lat = np.array([r["t_finish"] - r["t_submit"] for r in res])
     t_first = min(r["t_submit"] for r in res)
     t_last = max(r["t_finish"] for r in res)

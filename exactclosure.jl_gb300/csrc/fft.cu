@@ -15,7 +15,7 @@ namespace exc {
 // With DIV the input line is d = div(u) (src/N.jl:222-238) computed on the fly.
 // ---------------------------------------------------------------------------
 template <typename T, bool DIV>
-__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ out, int P,
              const cplx<T>* __restrict__ tw, FftPlan plan, int rows_per_cta, SlotBatch sb) {
   using C = cplx<T>;
@@ -80,7 +80,7 @@ r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ ou
 // outer = y): a CTA loads `W` consecutive kx columns of one outer index.
 // ---------------------------------------------------------------------------
 template <typename T, bool INV>
-__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_stride,
             long long outer_stride, const cplx<T>* __restrict__ tw, FftPlan plan, SlotBatch sb) {
   using C = cplx<T>;
@@ -91,17 +91,12 @@ cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_strid
   const int ls = n + 1;
   const int kx0 = blockIdx.x * W;
   const int lines = min(W, nkx - kx0);
+  const int wlog = 31 - __clz(W);
   C* base = g + (long long)blockIdx.y * outer_stride + kx0;
-  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-    int e = t / lines, l = t - e * lines;
-    s[l * ls + e] = base[e * elem_stride + l];
-  }
+  tile_move<true>(s, ls, base, elem_stride, lines, W, wlog, n);
   __syncthreads();
   fft_lines<INV>(s, ls, lines, plan, tw, n);
-  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-    int e = t / lines, l = t - e * lines;
-    base[e * elem_stride + l] = s[l * ls + e];
-  }
+  tile_move<false>(s, ls, base, elem_stride, lines, W, wlog, n);
 }
 
 // 1/d in float64 for d in (0, 3] (a sum of three sin^2): a single-precision
@@ -122,7 +117,7 @@ __device__ __forceinline__ double recip_f64(double d) {
 // divide is computed in float64 for every precision.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<T>* __restrict__ tw,
               FftPlan plan, const double* __restrict__ sin2, double coef, const double* __restrict__ invlap,
               SlotBatch sb) {
@@ -136,11 +131,9 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
   const int ky = blockIdx.y;
   const int lines = min(W, nkx - kx0);
   const long long es = (long long)n * P;
+  const int wlog = 31 - __clz(W);
   C* base = g + (long long)ky * P + kx0;
-  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-    int e = t / lines, l = t - e * lines;
-    s[l * ls + e] = base[e * es + l];
-  }
+  tile_move<true>(s, ls, base, es, lines, W, wlog, n);
   __syncthreads();
   fft_lines<false>(s, ls, lines, plan, tw, n);
   const double sy = sin2[ky];
@@ -162,10 +155,7 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
   }
   __syncthreads();
   fft_lines<true>(s, ls, lines, plan, tw, n);
-  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-    int e = t / lines, l = t - e * lines;
-    base[e * es + l] = s[l * ls + e];
-  }
+  tile_move<false>(s, ls, base, es, lines, W, wlog, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -174,7 +164,7 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
 //   z = IDFT_{N2}(Z) (unnormalised), x_2m = Re z_m, x_2m+1 = Im z_m.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 2)
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 c2r_x_kernel(cplx<T>* __restrict__ g, int n, int P, const cplx<T>* __restrict__ tw, FftPlan plan,
              int rows_per_cta, SlotBatch sb) {
   using C = cplx<T>;

@@ -129,6 +129,50 @@ __device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns
   __syncthreads();
 }
 
+// Move a tile of `lines` columns x n rows (row stride `es` elements, columns
+// contiguous in global memory) between global memory and line-major shared
+// memory (line l, element e at s[l*ls + e]).  Full tiles of a power-of-two
+// width use shifts for the index split and, for float2 elements, 16-byte
+// accesses of column pairs; loops are unrolled so several accesses are in
+// flight per thread.
+template <bool LOAD, typename C>
+__device__ __forceinline__ void tile_move(C* s, int ls, C* base, long long es, int lines, int W, int wlog, int n) {
+  if (lines == W) {
+    if constexpr (sizeof(C) == 8) {
+      if (W >= 2) {
+        const int hl = W >> 1, hlog = wlog - 1, tot = hl * n;
+#pragma unroll 4
+        for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+          const int e = t >> hlog, l2 = t & (hl - 1);
+          float4* g = reinterpret_cast<float4*>(base + e * es + 2 * l2);
+          C* a = s + (2 * l2) * ls + e;
+          if (LOAD) {
+            const float4 v = *g;
+            a[0].x = v.x; a[0].y = v.y;
+            a[ls].x = v.z; a[ls].y = v.w;
+          } else {
+            *g = make_float4(a[0].x, a[0].y, a[ls].x, a[ls].y);
+          }
+        }
+        return;
+      }
+    }
+    const int tot = W * n;
+#pragma unroll 4
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+      const int e = t >> wlog, l = t & (W - 1);
+      if (LOAD) s[l * ls + e] = base[e * es + l];
+      else base[e * es + l] = s[l * ls + e];
+    }
+    return;
+  }
+  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+    const int e = t / lines, l = t - e * lines;
+    if (LOAD) s[l * ls + e] = base[e * es + l];
+    else base[e * es + l] = s[l * ls + e];
+  }
+}
+
 // Full transform of every line in the tile (natural-order in and out).  One
 // loop per radix keeps each pass body's registers separate.
 template <bool INV, typename C>

@@ -301,7 +301,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     import __graft_entry__  # noqa: F401  (paths)
-    from exactclosure_gb300 import _lib
+    from exactclosure_gb300 import _lib, replicas  # noqa: F401
     from exactclosure_gb300 import navierstokes as NS
 
     if args.serve_only:
@@ -335,11 +335,8 @@ def main():
         barrier()
     ms = e0.elapsed_time(e1)
     cs.sync()
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = N * args.steps * world / (ms_max / 1000.0)
+    ms_max = replicas.slowest(ms, device="cuda")
+    value = replicas.job_rate(N * args.steps, ms_max / 1000.0, world)
 
     # ---- end to end through the public API with host buffers ----
     e2e = None
@@ -361,12 +358,9 @@ def main():
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         barrier()
-        tt = torch.tensor([el], dtype=torch.float64, device="cuda")
-        if world > 1:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        el = float(tt.item())
+        el = replicas.slowest(el, device="cuda")
         state_bytes = 3 * N * 8
-        e2e = {"value": N * args.steps * world / el, "unit": "cell-updates/s",
+        e2e = {"value": replicas.job_rate(N * args.steps, el, world), "unit": "cell-updates/s",
                "h2d_bytes_per_step": state_bytes / args.steps,
                "d2h_bytes_per_step": (state_bytes + metric_bytes) / args.steps,
                "note": "initial state uploaded and final state downloaded (pinned host buffers) inside the "

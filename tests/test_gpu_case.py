@@ -114,6 +114,26 @@ def test_closure_snapshot_matches_oracle(NS):
     assert rel(m, ref) < 1e-12
 
 
+def test_snapshot_pairs_round_trip(NS, tmp_path):
+    """Pairs written every 2 steps equal the oracle's (ubar, m) at stage 1 of
+    the corresponding steps, after a binary + JSON round trip."""
+    from exactclosure_gb300 import snapshots
+
+    n, c, l, visc = 32, 4, 1.0, 1 / 1000
+    u0 = ns.randomfield(n, l, 3, 6)
+    cs = NS.Case(n, l, visc, 0.3, les=[(c, "volume")])
+    cs.set_velocity(u0)
+    hp = snapshots.write_pairs(cs, 0, tmp_path, nsnap=2, every=2, stem="run")
+    U, M, h = snapshots.read_pairs(hp)
+    assert U.shape == (2, 3, 8, 8, 8) and h["ratio"] == c
+    les = [ns.Les(c=c)]
+    _, _, closures = ns.dnsaid_rk4(u0, visc, l, 0.3, 4, les, record_closure=True)
+    for s in range(2):
+        _, ub, m = closures[2 * s + 1]  # stage 1 of steps 2 and 4
+        assert rel(U[s], ub) < 1e-12
+        assert rel(M[s], m) < 1e-12
+
+
 def test_fixed_dt_and_graph_replay(NS):
     n, l, visc = 16, 1.0, 1 / 500
     u0 = ns.randomfield(n, l, 3, 5)

@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -46,6 +47,7 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--serve-only", action="store_true")
+    ap.add_argument("--no-burgers", action="store_true")
     return ap.parse_args()
 
 
@@ -151,6 +153,60 @@ def cpu_sample(n_full: int, les, kpeak: float, visc: float, budget_s: float = 20
 
 SERVE_SIZES = (64, 96, 128, 192, 256)
 SERVE_VISC = (1 / 1000, 1 / 2000, 1 / 4000)
+
+
+def burgers_section(nsample=1000, grids=(300, 900, 2700), cpu=True):
+    """The reference's Burgers DNS-aided LES setup (src/Burgers.jl:235-265):
+    nh = 13500, 1000 samples, nu = 5e-4, k0 = 10, E = 2, Gaussian LES filter
+    Delta = 2H, t = 0.1 with CFL 0.3, forward Euler, four LES per grid.  One
+    kernel launch advances every sample to t = 0.1 (about 1470 steps each)."""
+    import torch
+
+    from exactclosure_gb300 import burgers as GB
+
+    L, nh, visc = 2 * math.pi, 13500, 5e-4
+    b = GB.Batch(GB.Grid(L, nh), nsample, visc)
+    b.randomfield(10, 2.0, 1)
+    runs = {}
+    total_units, total_s = 0.0, 0.0
+    for nH in grids:
+        b.restart()
+        b.les_setup(GB.Grid(L, nH), 2.0, "gaussian")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.advance(0.1, 0.3)
+        el = time.perf_counter() - t0
+        _, steps = b.time()
+        units = float(steps.sum()) * nh
+        total_units += units
+        total_s += el
+        err = b.errors()
+        runs[str(nH)] = {"seconds": el, "cell_updates_per_s": units / el, "sample_steps": int(steps.sum()),
+                         "errors_vs_filtered_dns": {k: err[k] for k in ("nomodel", "class_m", "class_p", "swapfil")}}
+    b.close()
+    out = {"metric": "cell-updates/s", "value": total_units / total_s, "unit": "cell-updates/s", "dtype": "f64",
+           "config": {"workload": f"1-D Burgers dns_aided_les, nh {nh}, {nsample} samples, LES grids "
+                                  f"{list(grids)}, Gaussian Delta = 2H, t = 0.1, CFL 0.3",
+                      "timing": "wall clock around each advance call (one launch runs every sample to t = 0.1)"},
+           "per_grid": runs}
+    if cpu:
+        try:
+            from oracle import build_cpu, burgers as OB, cpu_ref
+
+            build_cpu.build()
+            cores = os.cpu_count() or 1
+            ns = 2 * cores
+            u0 = OB.randomfields(ns, nh, L, 10, 2.0, 1)
+            _, les, dbl = OB.kernels(nh, grids[0], L, 2.0, "gaussian")
+            t0 = time.perf_counter()
+            _, _, _, steps = cpu_ref.burgers_dnsaid(u0, grids[0], visc, L, les[1], dbl[1], 0.1, 0.3)
+            el = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": float(steps.sum()) * nh / el, "unit": "cell-updates/s", "cores": cores,
+                                   "kind": "port", "sample": f"{ns} samples of nh {nh} to t = 0.1 with LES grid "
+                                                             f"{grids[0]} (C/OpenMP restatement, {el:.1f} s)"}
+        except Exception as ex:  # the baseline is reported, never required
+            out["cpu_baseline"] = {"value": None, "sample": f"failed: {ex}"}
+    return out
 
 
 def serve_requests(nreq=96, rate=20.0, seed=0, nsteps=200):
@@ -407,6 +463,13 @@ def main():
             except Exception as ex:
                 serving_line = {"error": str(ex)}
 
+    burgers = None
+    if rank == 0 and world == 1 and not args.no_burgers:
+        try:
+            burgers = burgers_section(cpu=not args.no_cpu)
+        except Exception as ex:
+            burgers = {"error": str(ex)}
+
     # ---- CPU baseline ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -433,6 +496,7 @@ def main():
             "e2e": e2e,
             "forms": forms,
             "serving": serving_line,
+            "burgers": burgers,
         }
         print(json.dumps(line))
     if world > 1:

@@ -35,6 +35,10 @@ class CaseDesc(C.Structure):
                 ("precision", C.c_int), ("nles", C.c_int), ("les", LesDesc * EXC_MAX_LES)]
 
 
+class BurgersDesc(C.Structure):
+    _fields_ = [("nh", C.c_int), ("nsample", C.c_int), ("l", C.c_double), ("visc", C.c_double)]
+
+
 class ServerDesc(C.Structure):
     _fields_ = [("precision", C.c_int), ("mem_fraction", C.c_double), ("max_bytes", C.c_double),
                 ("slots_per_chunk", C.c_int), ("autotune", C.c_int)]
@@ -117,6 +121,23 @@ SIGNATURES = {
     "exc_server_drain": [vp],
     "exc_server_stats": [vp, C.POINTER(ServerInfo)],
     "exc_server_tuning": [i32, i32, i32, C.POINTER(i32), C.POINTER(i32)],
+    "exc_burgers_kernels": [i32, i32, f64, f64, i32, C.POINTER(i32), dp, C.POINTER(i32), dp],
+    "exc_burgers_create": [C.POINTER(BurgersDesc), vp, C.POINTER(vp)],
+    "exc_burgers_destroy": [vp],
+    "exc_burgers_init_random": [vp, f64, f64, u64],
+    "exc_burgers_set_velocity": [vp, dp],
+    "exc_burgers_get_velocity": [vp, i32, dp],
+    "exc_burgers_time": [vp, dp, C.POINTER(i32)],
+    "exc_burgers_restart": [vp],
+    "exc_burgers_les_setup": [vp, i32, f64, i32],
+    "exc_burgers_advance": [vp, f64, f64, i32, i32, C.POINTER(i32)],
+    "exc_burgers_get_les": [vp, i32, dp],
+    "exc_burgers_filtered": [vp, dp],
+    "exc_burgers_errors": [vp, dp],
+    "exc_burgers_closure_terms": [vp, dp, dp, dp],
+    "exc_burgers_smagorinsky_fit": [vp, dp, dp],
+    "exc_burgers_smagorinsky_solve": [vp, f64, f64, f64, i32, i32, C.POINTER(i32)],
+    "exc_burgers_device_ptr": [vp, i32, C.POINTER(vp)],
 }
 _RESTYPE = {"exc_last_error": C.c_char_p}
 

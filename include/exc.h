@@ -327,6 +327,99 @@ int exc_net_train_step(exc_net* net, int precision, int batch, int n, const void
  * detaches).  exc_case_get_les(which = 4) reads it. */
 int exc_case_attach_net(exc_case* cs, int les_index, exc_net* net);
 
+/* ======================================================================
+ * 1-D Burgers, batched over samples (module `Burgers`, src/Burgers.jl)
+ *
+ * A handle holds `nsample` independent periodic samples of `nh` cells on
+ * [0, l], FP64, laid out [nsample][nh] x fastest (the reference's
+ * zeros(nh, nsample) matrices, src/Burgers.jl:273-307).  Velocities sit on
+ * the right cell faces.  Every sample advances with its own time step, as in
+ * the reference's per-sample loop (src/Burgers.jl:307).  One LES grid of nH
+ * cells (nh/nH odd) can be attached; it carries the four LES of
+ * `dns_aided_les` and a Smagorinsky LES.
+ * ====================================================================== */
+
+typedef struct exc_burgers exc_burgers;
+
+typedef struct {
+  int nh;        /* DNS cells per sample (the shared-memory resident limit is about 13,900) */
+  int nsample;   /* independent samples */
+  double l;      /* domain length (2 pi in the reference's setup) */
+  double visc;
+} exc_burgers_desc;
+
+enum exc_burgers_filter { EXC_BURGERS_GAUSSIAN = 0, EXC_BURGERS_TOPHAT = 1 };
+enum exc_burgers_scheme { EXC_BURGERS_EULER = 0, EXC_BURGERS_RK4 = 1 };
+/* Fields of exc_burgers_get_les, the `fields` of dns_aided_les
+ * (src/Burgers.jl:272-306) on the LES grid. */
+enum exc_burgers_field {
+  EXC_BURGERS_DNS_FIL = 0,  /* filtered DNS (computed from the current DNS) */
+  EXC_BURGERS_NOMODEL = 1,
+  EXC_BURGERS_CLASS_M = 2,  /* classic: vsu - sVU */
+  EXC_BURGERS_CLASS_P = 3,  /* classic + flux: vsu - svu */
+  EXC_BURGERS_SWAPFIL = 4,  /* classic + flux + div (exact): fsu - svu */
+  EXC_BURGERS_SMAG = 5      /* Smagorinsky LES (exc_burgers_smagorinsky_solve) */
+};
+
+/* LES filter kernels of one grid: `gaussian_weights`/`tophat_weights`
+ * (src/Burgers.jl:146-162) and `build_doublekernel` (src/Burgers.jl:218-233).
+ * wl gets 2*Rl+1 weights, wd 2*Rd+1 (either may be NULL to query R). */
+int exc_burgers_kernels(int nh, int nH, double l, double delta_ratio, int filter, int* Rl, double* wl, int* Rd,
+                        double* wd);
+int exc_burgers_create(const exc_burgers_desc* desc, void* stream, exc_burgers** out);
+int exc_burgers_destroy(exc_burgers* b);
+/* `randomfield` with `bump_profile` (src/Burgers.jl:192-202); sample s uses
+ * the phase stream seed + s.  Also records the initial field and resets the
+ * per-sample clocks. */
+int exc_burgers_init_random(exc_burgers* b, double kpeak, double energy, uint64_t seed);
+/* host: [nsample][nh]; records the initial field and resets the clocks. */
+int exc_burgers_set_velocity(exc_burgers* b, const double* host);
+/* initial != 0 reads the recorded initial field (`ustart`). */
+int exc_burgers_get_velocity(exc_burgers* b, int initial, double* host);
+/* Back to the recorded initial field with the clocks at zero. */
+int exc_burgers_restart(exc_burgers* b);
+/* Per-sample time and step count (either pointer may be NULL). */
+int exc_burgers_time(exc_burgers* b, double* t, int* steps);
+/* Attach an LES grid of nH cells (nH == 0 detaches) with LES filter width
+ * delta_ratio * H; its four LES start from the double-filtered current DNS
+ * (src/Burgers.jl:366-379). */
+int exc_burgers_les_setup(exc_burgers* b, int nH, double delta_ratio, int filter);
+/* Advance every sample until its time reaches tstop, at most max_steps
+ * steps this call (<= 0 or above 1,000,000: 1,000,000), with dt = min(cfl * cfl(u), tstop - t).
+ * With an LES grid: `dns_aided_les` (src/Burgers.jl:350-445, forward
+ * Euler); without: the DNS of `create_dns` with `timestep!` (EULER) or
+ * `rk4_timestep!` (RK4) (src/Burgers.jl:112-142, :522-545).  steps_max
+ * (may be NULL) gets the largest per-sample step count so far. */
+int exc_burgers_advance(exc_burgers* b, double tstop, double cfl, int scheme, int max_steps, int* steps_max);
+/* host: [nsample][nH] of the selected field. */
+int exc_burgers_get_les(exc_burgers* b, int which, double* host);
+/* The double-filtered DNS on the DNS grid, `dns_ref_fil`, host [nsample][nh]. */
+int exc_burgers_filtered(exc_burgers* b, double* host_fine);
+/* `compute_errors` (src/Burgers.jl:909-916): norm(x - dns_fil)/norm(dns_fil)
+ * over all samples for nomodel, class_m, class_p, swapfil, smag (NaN when no
+ * Smagorinsky solve ran). */
+int exc_burgers_errors(exc_burgers* b, double out[5]);
+/* Closure terms of the current DNS: terms [nsample][5][nH] = fsu, vsu, vu,
+ * sVU, svu (src/Burgers.jl:397-412); diss [nsample][3][nH] =
+ * delta_stag(vu) * sigma for classic, classic+flux, exact
+ * (`compute_dissipation`, src/Burgers.jl:447-520); fractions = the mean
+ * shares of |classic|, |flux|, |div| (`compute_fractions`,
+ * src/Burgers.jl:1022-1116).  Any output may be NULL. */
+int exc_burgers_closure_terms(exc_burgers* b, double* terms, double* diss, double fractions[3]);
+/* `smagorinsky_fields` (src/Burgers.jl:547-688) on the current DNS and the
+ * coefficient fits theta^2 = -<S,T>/<S,S> (smagorinsky.jl:32-45):
+ * theta2[0] classic, theta2[1] discrete.  fields (may be NULL):
+ * [nsample][4][nh] = Sh, Th, SH, TH. */
+int exc_burgers_smagorinsky_fit(exc_burgers* b, double theta2[2], double* fields);
+/* `solve_smagorinsky` (src/Burgers.jl:690-786) from the recorded initial
+ * field (restart != 0) or continuing the previous call, C = theta^2
+ * (Delta^2 + H^2). */
+int exc_burgers_smagorinsky_solve(exc_burgers* b, double theta, double tstop, double cfl, int max_steps,
+                                  int restart, int* steps_max);
+/* Device pointers: 0 = velocity, 1 = initial velocity, 2 = LES states
+ * [nsample][4][nH]. */
+int exc_burgers_device_ptr(exc_burgers* b, int which, void** ptr);
+
 #ifdef __cplusplus
 }
 #endif

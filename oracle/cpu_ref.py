@@ -127,3 +127,35 @@ def time_stages(n, les, kpeak, visc, budget_s=20.0, cs=None, max_stages=8):
     return {"cell_updates_per_s": n ** 3 * steps / el, "threads": threads,
             "sample": f"C/OpenMP restatement, {k} RK4 stage(s) of the {n}^3 DNS with LES ratios "
                       f"{[c for c, _ in les]} at full size ({k}/4 RK4 steps), {threads} threads"}
+
+
+def burgers_dnsaid(u0, nH, visc, l, wl, wd, tstop, cfl, max_steps=0, state=None):
+    """``dns_aided_les`` in the C restatement (``oracle/cpu_burgers.c``),
+    samples in parallel over the host cores.  ``wl``/``wd`` are the LES and
+    double kernels (``oracle.burgers.kernels``); ``nH = 0`` runs the DNS
+    alone.  Returns (u, v[ns][4][nH], t, steps)."""
+    L = lib()
+    f = L.cref_burgers_dnsaid
+    dp = C.POINTER(C.c_double)
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp, C.c_int, dp, C.c_int, C.c_double,
+                  C.c_double, C.c_int, dp, dp, dp, C.POINTER(C.c_int)]
+    f.restype = C.c_int
+    import numpy as np
+
+    ns, nh = u0.shape
+    if state is None:
+        u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+        from .burgers import coarse_filter
+
+        v0 = coarse_filter(u, (len(wd) // 2, wd), nH, True) if nH else np.zeros((ns, 1))
+        v = np.ascontiguousarray(np.repeat(v0[:, None, :], 4, axis=1)) if nH else np.zeros((ns, 4, 1))
+        t = np.zeros(ns)
+        steps = np.zeros(ns, dtype=np.int32)
+    else:
+        u, v, t, steps = (x.copy() for x in state)
+    wl = np.ascontiguousarray(wl, dtype=np.float64)
+    wd = np.ascontiguousarray(wd, dtype=np.float64)
+    f(nh, ns, nH, l, visc, wl.ctypes.data_as(dp), len(wl) // 2, wd.ctypes.data_as(dp), len(wd) // 2, tstop, cfl,
+      max_steps if max_steps > 0 else 2**31 - 1, u.ctypes.data_as(dp), v.ctypes.data_as(dp), t.ctypes.data_as(dp),
+      steps.ctypes.data_as(C.POINTER(C.c_int)))
+    return u, v, t, steps

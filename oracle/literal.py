@@ -303,3 +303,101 @@ def step_classic_flux_div(v, ubar, u, p, visc, h, H, dt, GDHi, symm=False):
         du = tensordivergence_nonsym(du, rdhi, H, True)
     du, _ = project(du, H)
     return [Field(v[i].data + dt * du[i].data) for i in range(3)]
+
+
+# ---------------------------------------------------------------------------
+# 1-D Burgers (src/Burgers.jl), one sample, 1-based indexing with mod1.
+
+class Field1:
+    """Periodic 1-D field (``Field``, ``src/Burgers.jl:33-62``)."""
+
+    def __init__(self, data, h):
+        self.data = np.asarray(data, dtype=np.float64)
+        self.n = self.data.shape[0]
+        self.h = h
+
+    def get(self, i):
+        return self.data[mod1(i, self.n) - 1]
+
+
+class Lazy1:
+    """``LazyField`` (``src/Burgers.jl:44-59``): evaluated on every access."""
+
+    def __init__(self, n, h, func):
+        self.n, self.h, self.func = n, h, func
+
+    def get(self, i):
+        return self.func(i)
+
+
+def burgers_stress(u, visc):
+    """``stress`` (``src/Burgers.jl:89-94``)."""
+    def f(i):
+        ua = u.get(i - 1)
+        ub = u.get(i)
+        return -((ua + ub) ** 2) / 8 + visc * (ub - ua) / u.h
+    return Lazy1(u.n, u.h, f)
+
+
+def burgers_lazyfilter(u, kernel):
+    """``lazyfilter`` (``src/Burgers.jl:164-172``)."""
+    R, w = kernel
+
+    def f(i):
+        s = 0.0
+        for r in range(-R, R + 1):
+            s += w[r + R] * u.get(i + r)
+        return s
+    return Lazy1(u.n, u.h, f)
+
+
+def burgers_lazycoarsegrain(nbar, hbar, u, stag):
+    """``lazycoarsegrain`` (``src/Burgers.jl:174-180``)."""
+    comp = u.n // nbar
+    a = comp // 2
+    return Lazy1(nbar, hbar, lambda i: u.get(i * comp - (0 if stag else 1) * a))
+
+
+def burgers_materialize(lz):
+    return Field1([lz.get(i) for i in range(1, lz.n + 1)], lz.h)
+
+
+def burgers_dns_aided_les(ustart, nH, visc, l, les_kernel, double_kernel, tstop, cfl_factor):
+    """``dns_aided_les`` (``src/Burgers.jl:350-445``) as written: lazy fields
+    materialised where the reference materialises them, forward Euler, the
+    LES stepped before the DNS.  Returns the DNS and the four LES fields."""
+    nh = len(ustart)
+    h, H = l / nh, l / nH
+    uh = Field1(ustart, h)
+    uH = burgers_materialize(burgers_lazycoarsegrain(nH, H, burgers_lazyfilter(uh, double_kernel), True))
+    u = {"dns_ref": Field1(uh.data.copy(), h)}
+    for k in ("nomodel", "class_m", "class_p", "swapfil"):
+        u[k] = Field1(uH.data.copy(), H)
+    t = 0.0
+    while t < tstop:
+        umax = max(abs(x) for x in u["dns_ref"].data)
+        dt = cfl_factor * min(h / umax, h * h / visc)
+        dt = min(dt, tstop - t)
+        su = burgers_stress(u["dns_ref"], visc)
+        fsu = burgers_materialize(burgers_lazycoarsegrain(nH, H, burgers_lazyfilter(su, les_kernel), False))
+        vsu = burgers_materialize(burgers_lazycoarsegrain(nH, H, burgers_lazyfilter(su, double_kernel), False))
+        VU = burgers_lazyfilter(u["dns_ref"], double_kernel)
+        vu = burgers_materialize(burgers_lazycoarsegrain(nH, H, VU, True))
+        svu = burgers_stress(vu, visc)
+        sVU = burgers_materialize(burgers_lazycoarsegrain(nH, H, burgers_stress(VU, visc), False))
+        sig = {
+            "nomodel": burgers_stress(u["nomodel"], visc),
+            "class_m": Lazy1(nH, H, (lambda s: lambda i: s.get(i) + vsu.get(i) - sVU.get(i))(
+                burgers_stress(u["class_m"], visc))),
+            "class_p": Lazy1(nH, H, (lambda s: lambda i: s.get(i) + vsu.get(i) - svu.get(i))(
+                burgers_stress(u["class_p"], visc))),
+            "swapfil": Lazy1(nH, H, (lambda s: lambda i: s.get(i) + fsu.get(i) - svu.get(i))(
+                burgers_stress(u["swapfil"], visc))),
+        }
+        for k in ("nomodel", "class_m", "class_p", "swapfil"):
+            du = [(sig[k].get(i + 1) - sig[k].get(i)) / H for i in range(1, nH + 1)]
+            u[k] = Field1(u[k].data + dt * np.array(du), H)
+        du = [(su.get(i + 1) - su.get(i)) / h for i in range(1, nh + 1)]
+        u["dns_ref"] = Field1(u["dns_ref"].data + dt * np.array(du), h)
+        t += dt
+    return {k: f.data for k, f in u.items()}

@@ -346,26 +346,30 @@ cudaError_t launch_shell_scale(int n, int P, int ncomp, cplx<T>* spec, long long
 
 // Host-side shell factors sqrt(E0/Eshell) with E0 = energy * profile(k) / sum
 // of profiles (src/N.jl:436-451); computed on the device to avoid a sync.
-__global__ void shell_factor_kernel(int nshell, double kpeak, double energy, const double* __restrict__ eshell,
-                                    double* __restrict__ factor) {
+// Shell profile: `peak_profile` k^4 exp(-2 (k/k0)^2) (src/N.jl:366) or the
+// power law (k > 0) k^p of `dnsaid_project` (src/N.jl:1245).
+__device__ __forceinline__ double shell_profile(int profile, double param, int k) {
+  if (profile == 1) return k > 0 ? pow((double)k, param) : 0.0;
+  const double q = k / param;
+  return (double)k * k * (double)k * k * exp(-2.0 * q * q);
+}
+
+__global__ void shell_factor_kernel(int nshell, int profile, double param, double energy,
+                                    const double* __restrict__ eshell, double* __restrict__ factor) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double tot = 0.0;
+    for (int k = 0; k < nshell; ++k) tot += shell_profile(profile, param, k);
     for (int k = 0; k < nshell; ++k) {
-      double q = k / kpeak;
-      tot += (double)k * k * (double)k * k * exp(-2.0 * q * q);
-    }
-    for (int k = 0; k < nshell; ++k) {
-      double q = k / kpeak;
-      double prof = (double)k * k * (double)k * k * exp(-2.0 * q * q);
+      double prof = shell_profile(profile, param, k);
       double e0 = energy * prof / tot;
       double es = eshell[k];
       factor[k] = es > 0 ? sqrt(e0 / es) : 1.0;
     }
   }
 }
-cudaError_t launch_shell_factor(int nshell, double kpeak, double energy, const double* eshell, double* factor,
-                                cudaStream_t st) {
-  shell_factor_kernel<<<1, 32, 0, st>>>(nshell, kpeak, energy, eshell, factor);
+cudaError_t launch_shell_factor(int nshell, int profile, double param, double energy, const double* eshell,
+                                double* factor, cudaStream_t st) {
+  shell_factor_kernel<<<1, 32, 0, st>>>(nshell, profile, param, energy, eshell, factor);
   return cudaGetLastError();
 }
 

@@ -25,7 +25,7 @@ cudaError_t launch_shell_energy(int n, int P, int ncomp, const cplx<T>* spec, lo
 template <typename T>
 cudaError_t launch_shell_scale(int n, int P, int ncomp, cplx<T>* spec, long long cstride, int nshell,
                                const double* factor, cudaStream_t st);
-cudaError_t launch_shell_factor(int nshell, double kpeak, double energy, const double* eshell, double* factor,
+cudaError_t launch_shell_factor(int nshell, int profile, double param, double energy, const double* eshell, double* factor,
                                 cudaStream_t st);
 template <typename T>
 cudaError_t launch_unpitch(int n, const T* src, int pitch, T* dst, T scale, cudaStream_t st);

@@ -296,7 +296,86 @@ cudaError_t filter_vector_box(int n, int c, int kind, const T* u, T* ub, T* tb, 
   return cudaGetLastError();
 }
 
+// Stress of the fine-grid filtered velocity, uf = lazyfilter(u, GDH) on the
+// DNS grid (centred box of odd width c, composed with FDelta), at fine cell
+// (x, y, z): the field that `step_ΔHπ_classic!` (src/N.jl:1137-1162) samples
+// at the LES centres and edges.  Each uf value is evaluated on the fly.
+template <typename T>
+struct FineFilteredStressSrc {
+  const T* u;
+  int n, i, j;
+  T h, visc;
+  Taps1D ft;  // centred fine-filter taps (same along every axis)
+  __device__ __forceinline__ double uf(int comp, int x, int y, int z) const {
+    const long long N = (long long)n * n * n;
+    const T* f = u + comp * N;
+    double acc = 0.0;
+    for (int tz = 0; tz < ft.cnt; ++tz) {
+      int zz = z + ft.off[tz];
+      zz = ((zz % n) + n) % n;
+      double az = 0.0;
+      for (int ty = 0; ty < ft.cnt; ++ty) {
+        int yy = y + ft.off[ty];
+        yy = ((yy % n) + n) % n;
+        double ay = 0.0;
+        for (int tx = 0; tx < ft.cnt; ++tx) {
+          int xx = x + ft.off[tx];
+          xx = ((xx % n) + n) % n;
+          ay += ft.w[tx] * (double)f[((long long)zz * n + yy) * n + xx];
+        }
+        az += ft.w[ty] * ay;
+      }
+      acc += ft.w[tz] * az;
+    }
+    return acc;
+  }
+  __device__ __forceinline__ double operator()(int x, int y, int z) const {
+    const int c[3] = {x, y, z};
+    const int off = (i != j);
+    int cr[3] = {c[0], c[1], c[2]}, cl[3] = {c[0], c[1], c[2]};
+    cr[j] = (cr[j] + off) % n;
+    cl[j] = (cl[j] + off - 1 + n) % n;
+    int dr[3] = {c[0], c[1], c[2]}, dl[3] = {c[0], c[1], c[2]};
+    dr[i] = (dr[i] + off) % n;
+    dl[i] = (dl[i] + off - 1 + n) % n;
+    const double uir = uf(i, cr[0], cr[1], cr[2]), uil = uf(i, cl[0], cl[1], cl[2]);
+    const double ujr = uf(j, dr[0], dr[1], dr[2]), ujl = uf(j, dl[0], dl[1], dl[2]);
+    const double etaj_ui = (uir + uil) / 2, etai_uj = (ujr + ujl) / 2;
+    const double dj_ui = (uir - uil) / (double)h, di_uj = (ujr - ujl) / (double)h;
+    return etaj_ui * etai_uj - (double)visc * (dj_ui + di_uj);
+  }
+};
+
+// sigma2 of `step_ΔHπ_classic!`: `lazytensorcoarsegrain(g_les,
+// stresstensor(lazyfilter(u, GDH)))` (src/N.jl:1117-1135, 1143-1145); order
+// s11, s22, s33, s12, s23, s31.  Odd ratios only (the reference's top hat).
+template <typename T>
+int classic_stress(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, T* s6,
+                   cudaStream_t st) {
+  if (c % 2 == 0) { set_last_error("the classic closure's fine-grid filter needs an odd ratio"); return EXC_ERR_RATIO; }
+  const int m = n / c;
+  const long long M = (long long)m * m * m;
+  Taps1D ft = build_taps(c, false, false, fdelta, nfd);
+  if (ft.cnt < 0) { set_last_error("filter stencil longer than MAX_TAPS"); return EXC_ERR_ARG; }
+  for (int k = 0; k < ft.cnt; ++k) ft.off[k] -= c / 2;  // centre the box on the fine cell
+  const int comps[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {2, 0}};
+  for (int k = 0; k < 6; ++k) {
+    const int i = comps[k][0], j = comps[k][1];
+    bool stag[3], point[3] = {true, true, true};
+    for (int d = 0; d < 3; ++d) stag[d] = (i != j) && (d == i || d == j);
+    Taps3 taps;
+    int rc = make_taps3(c, stag, point, nullptr, 0, &taps);
+    if (rc) return rc;
+    FineFilteredStressSrc<T> src{u, n, i, j, (T)(l / n), (T)visc, ft};
+    filter_kernel<T><<<grid_for(M), 256, 0, st>>>(src, n, c, taps, s6 + (long long)k * M);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
 #define INST(T)                                                                                          \
+  template int classic_stress<T>(int, int, double, double, const double*, int, const T*, T*, cudaStream_t); \
   template cudaError_t filter_vector_box<T>(int, int, int, const T*, T*, T*, cudaStream_t);              \
   template int filter_vector<T>(int, int, int, const double*, int, const T*, T*, cudaStream_t);          \
   template int closure_flux<T>(int, int, double, double, const double*, int, const T*, const T*, T*,     \

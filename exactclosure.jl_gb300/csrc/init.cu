@@ -17,7 +17,7 @@ namespace exc {
 //   rescaling, src/N.jl:464-469).
 template <typename T>
 int init_random_field(exc_poisson* ps, T* u, cplx<T>* spec3, double* part, double kpeak, double energy,
-                      uint64_t seed, cudaStream_t st) {
+                      uint64_t seed, cudaStream_t st, int profile) {
   using C = cplx<T>;
   const int n = ps->n, P = ps->P;
   const long long N = (long long)n * n * n;
@@ -41,7 +41,7 @@ int init_random_field(exc_poisson* ps, T* u, cplx<T>* spec3, double* part, doubl
   const double Nd = (double)N;
   if (e == cudaSuccess)
     e = launch_shell_energy<T>(n, P, 3, spec3, cstride, 1.0 / (Nd * Nd), nshell, part, SHELL_BLOCKS, eshell, st);
-  if (e == cudaSuccess) e = launch_shell_factor(nshell, kpeak, energy, eshell, factor, st);
+  if (e == cudaSuccess) e = launch_shell_factor(nshell, profile, kpeak, energy, eshell, factor, st);
   if (e == cudaSuccess) e = launch_shell_scale<T>(n, P, 3, spec3, cstride, nshell, factor, st);
   for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
     tmp.work = spec3 + c * cstride;
@@ -55,7 +55,8 @@ int init_random_field(exc_poisson* ps, T* u, cplx<T>* spec3, double* part, doubl
 }
 
 template int init_random_field<double>(exc_poisson*, double*, double2*, double*, double, double, uint64_t,
-                                       cudaStream_t);
-template int init_random_field<float>(exc_poisson*, float*, float2*, double*, double, double, uint64_t, cudaStream_t);
+                                       cudaStream_t, int);
+template int init_random_field<float>(exc_poisson*, float*, float2*, double*, double, double, uint64_t, cudaStream_t,
+                                      int);
 
 }  // namespace exc

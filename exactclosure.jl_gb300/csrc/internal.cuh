@@ -40,11 +40,12 @@ cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st);
 template <typename T>
 cudaError_t fft3d_inverse(exc_poisson* ps, cudaStream_t st);
 
-// Random solenoidal field with the peak spectrum into u (init.cu); spec3: 3
+// Random solenoidal field with a shell spectrum into u (init.cu); spec3: 3
 // spectral arrays of scratch, part: SHELL_BLOCKS*1024 + 2048 doubles.
+// profile 0: peak profile with k0 = kpeak; 1: power law (k > 0) k^kpeak.
 template <typename T>
 int init_random_field(exc_poisson* ps, T* u, cplx<T>* spec3, double* part, double kpeak, double energy,
-                      uint64_t seed, cudaStream_t st);
+                      uint64_t seed, cudaStream_t st, int profile = 0);
 
 // Learned-closure network internals used by the case stepper (learned.cu).
 int net_reserve(exc_net* net, long long V);

@@ -39,6 +39,11 @@ class BurgersDesc(C.Structure):
     _fields_ = [("nh", C.c_int), ("nsample", C.c_int), ("l", C.c_double), ("visc", C.c_double)]
 
 
+class DnsAidDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("l", C.c_double), ("visc", C.c_double), ("ratio", C.c_int),
+                ("fdelta", C.POINTER(C.c_double)), ("nfdelta", C.c_int)]
+
+
 class ServerDesc(C.Structure):
     _fields_ = [("precision", C.c_int), ("mem_fraction", C.c_double), ("max_bytes", C.c_double),
                 ("slots_per_chunk", C.c_int), ("autotune", C.c_int)]
@@ -121,6 +126,17 @@ SIGNATURES = {
     "exc_server_drain": [vp],
     "exc_server_stats": [vp, C.POINTER(ServerInfo)],
     "exc_server_tuning": [i32, i32, i32, C.POINTER(i32), C.POINTER(i32)],
+    "exc_dnsaid_create": [C.POINTER(DnsAidDesc), vp, C.POINTER(vp)],
+    "exc_dnsaid_destroy": [vp],
+    "exc_dnsaid_init_random": [vp, i32, f64, f64, u64],
+    "exc_dnsaid_set_velocity": [vp, dp],
+    "exc_dnsaid_get_velocity": [vp, dp],
+    "exc_dnsaid_warmup": [vp, f64, f64, i32, C.POINTER(i32)],
+    "exc_dnsaid_start": [vp],
+    "exc_dnsaid_step": [vp, f64, f64, i32, C.POINTER(i32)],
+    "exc_dnsaid_time": [vp, dp, C.POINTER(i32)],
+    "exc_dnsaid_get": [vp, i32, dp],
+    "exc_dnsaid_errors": [vp, dp],
     "exc_burgers_kernels": [i32, i32, f64, f64, i32, C.POINTER(i32), dp, C.POINTER(i32), dp],
     "exc_burgers_create": [C.POINTER(BurgersDesc), vp, C.POINTER(vp)],
     "exc_burgers_destroy": [vp],

@@ -301,3 +301,130 @@ class Case:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# The reference's driver `dnsaid_project` (src/N.jl:1239-1332)
+# ---------------------------------------------------------------------------
+DNSAID_FIELDS = ("u_les", "u_nomo", "u_c", "u_cf", "u_cfd", "u_cfd_symm")
+
+
+def gaussian(h: float, delta: float, nsigma: float) -> np.ndarray:
+    """``gaussian`` (``src/N.jl:599-607``), a host array like the reference's;
+    ``delta == 0`` gives ``[1]``."""
+    if delta < 1e-15:
+        return np.ones(1)
+    sig = delta / np.sqrt(12)
+    r = int(round(nsigma * sig / h))
+    x = h * np.arange(-r, r + 1)
+    w = np.exp(-(x**2) / (2 * sig**2))
+    return w / w.sum()
+
+
+class DnsAid:
+    """Handle of ``exc_dnsaid_*``: a DNS with the five LES of
+    ``dnsaid_project``, FP64."""
+
+    def __init__(self, n: int, l: float, visc: float, ratio: int, fdelta=None, stream=None):
+        from ._lib import DnsAidDesc
+
+        self.n, self.l, self.visc, self.ratio = n, l, visc, ratio
+        self.m = n // ratio
+        self._fd = None if fdelta is None or len(fdelta) <= 1 else np.ascontiguousarray(fdelta, dtype=np.float64)
+        desc = DnsAidDesc(n, l, visc, ratio,
+                          None if self._fd is None else self._fd.ctypes.data_as(C.POINTER(C.c_double)),
+                          0 if self._fd is None else len(self._fd))
+        h = C.c_void_p()
+        call("exc_dnsaid_create", C.byref(desc), stream, C.byref(h))
+        self._h = h
+
+    def init_random(self, profile: str = "power", param: float = -5 / 3, energy: float = 1.0, seed: int = 0):
+        call("exc_dnsaid_init_random", self._h, {"peak": 0, "power": 1}[profile], param, energy, seed)
+
+    def set_velocity(self, u: np.ndarray):
+        a = np.ascontiguousarray(u, dtype=np.float64)
+        call("exc_dnsaid_set_velocity", self._h, a.ctypes.data_as(C.POINTER(C.c_double)))
+
+    def velocity(self) -> np.ndarray:
+        out = np.empty((3, self.n, self.n, self.n))
+        call("exc_dnsaid_get_velocity", self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def warmup(self, twarm: float, cfl: float, max_steps: int = 0) -> int:
+        s = C.c_int()
+        call("exc_dnsaid_warmup", self._h, twarm, cfl, max_steps, C.byref(s))
+        return s.value
+
+    def start(self):
+        call("exc_dnsaid_start", self._h)
+
+    def step(self, tstop: float, cfl: float, max_steps: int = 0) -> int:
+        s = C.c_int()
+        call("exc_dnsaid_step", self._h, tstop, cfl, max_steps, C.byref(s))
+        return s.value
+
+    def time(self):
+        t, s = C.c_double(), C.c_int()
+        call("exc_dnsaid_time", self._h, C.byref(t), C.byref(s))
+        return t.value, s.value
+
+    def get(self, which: str) -> np.ndarray:
+        out = np.empty((3, self.m, self.m, self.m))
+        call("exc_dnsaid_get", self._h, DNSAID_FIELDS.index(which), out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def errors(self) -> dict:
+        e = np.empty(5)
+        call("exc_dnsaid_errors", self._h, e.ctypes.data_as(C.POINTER(C.c_double)))
+        return dict(zip(DNSAID_FIELDS[1:], e.tolist()))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().exc_dnsaid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def getsetup(**kw) -> dict:
+    """``getsetup`` (``src/N.jl:712-723``) with grid sizes the FFT of this
+    library supports (n = 2^a 3^b); keywords override."""
+    s = dict(l=1.0, n_dns=192, n_les=64, visc=2.0e-4, Δ_ratio=2, nσ=2, twarm=0.1, tstop=0.1, cfl=0.4,
+             profile=("power", -5 / 3), seed=0)
+    s.update(kw)
+    return s
+
+
+def dnsaid_project(setup: dict, stream=None) -> dict:
+    """``dnsaid_project`` (``src/N.jl:1239-1332``): warm-up, then the DNS and
+    five LES in lockstep; returns ``u_les`` (the filtered DNS) and the five
+    LES fields, plus their ``compute_errors``."""
+    n, m, l = setup["n_dns"], setup["n_les"], setup["l"]
+    ratio = n // m
+    H = l / m
+    fdelta = gaussian(l / n, setup["Δ_ratio"] * H, setup["nσ"])
+    d = DnsAid(n, l, setup["visc"], ratio, fdelta, stream)
+    kind, param = setup["profile"]
+    d.init_random(kind, param, 1.0, setup["seed"])
+    d.warmup(setup["twarm"], setup["cfl"])
+    d.start()
+    d.step(setup["tstop"], setup["cfl"])
+    out = {k: d.get(k) for k in DNSAID_FIELDS}
+    out["errors"] = d.errors()
+    d.close()
+    return out
+
+
+def compute_errors(uaid: dict) -> dict:
+    """``compute_errors`` (``src/N.jl:1334-1349``) of ``dnsaid_project``
+    output (host arrays; the GPU values come from ``DnsAid.errors``)."""
+    ref = uaid["u_les"]
+    out = {}
+    for k in DNSAID_FIELDS[1:]:
+        a = uaid[k]
+        out[k] = float(np.sqrt(sum(np.sum((a[i] - ref[i]) ** 2) / np.sum(ref[i] ** 2) for i in range(3)) / 3))
+    return out

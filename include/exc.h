@@ -328,6 +328,53 @@ int exc_net_train_step(exc_net* net, int precision, int batch, int n, const void
 int exc_case_attach_net(exc_case* cs, int les_index, exc_net* net);
 
 /* ======================================================================
+ * The reference's driver `dnsaid_project` (src/N.jl:1239-1332): a forward
+ * Euler warm-up of the DNS, then the DNS and five LES stepped in lockstep
+ * with the DNS time step -- no model (`step_forwardeuler!`), classic
+ * (`step_ΔHπ_classic!`), classic+flux, classic+flux+div (the exact closure)
+ * and its symmetrised form (src/N.jl:1137-1226).  FP64.  The ratio must be
+ * odd (the classic closure's fine-grid top hat) and n/ratio an FFT size.
+ * ====================================================================== */
+
+typedef struct exc_dnsaid exc_dnsaid;
+
+typedef struct {
+  int n;                  /* DNS cells per side */
+  double l;
+  double visc;
+  int ratio;              /* n / n_les, odd */
+  const double* fdelta;   /* optional Gaussian FDelta (odd length) or NULL */
+  int nfdelta;
+} exc_dnsaid_desc;
+
+/* Initial spectrum of exc_dnsaid_init_random: `peak_profile` with k0 = param
+ * (src/N.jl:366) or the power law (k > 0) k^param of dnsaid_project
+ * (src/N.jl:1245). */
+enum exc_profile { EXC_PROFILE_PEAK = 0, EXC_PROFILE_POWER = 1 };
+
+int exc_dnsaid_create(const exc_dnsaid_desc* desc, void* stream, exc_dnsaid** out);
+int exc_dnsaid_destroy(exc_dnsaid* d);
+/* `randomfield(profile, ...)` (src/N.jl:394-476) with the project's seeded
+ * generator. */
+int exc_dnsaid_init_random(exc_dnsaid* d, int profile, double param, double energy, uint64_t seed);
+int exc_dnsaid_set_velocity(exc_dnsaid* d, const double* host);
+int exc_dnsaid_get_velocity(exc_dnsaid* d, double* host);
+/* The warm-up loop (src/N.jl:1264-1276): step_forwardeuler! until t reaches
+ * twarm (at most max_steps steps when > 0). */
+int exc_dnsaid_warmup(exc_dnsaid* d, double twarm, double cfl, int max_steps, int* steps);
+/* LES initial states: all five = apply_ΔHπ(u) (src/N.jl:1278-1287); t = 0. */
+int exc_dnsaid_start(exc_dnsaid* d);
+/* The lockstep loop (src/N.jl:1289-1323) until t reaches tstop (at most
+ * max_steps steps when > 0). */
+int exc_dnsaid_step(exc_dnsaid* d, double tstop, double cfl, int max_steps, int* steps);
+int exc_dnsaid_time(exc_dnsaid* d, double* t, int* steps);
+/* host (3 n_les^3): 0 = apply_ΔHπ of the current DNS (`u_les`), 1 u_nomo,
+ * 2 u_c, 3 u_cf, 4 u_cfd, 5 u_cfd_symm. */
+int exc_dnsaid_get(exc_dnsaid* d, int which, double* host);
+/* `compute_errors` (src/N.jl:1334-1349) of the five LES against u_les. */
+int exc_dnsaid_errors(exc_dnsaid* d, double out[5]);
+
+/* ======================================================================
  * 1-D Burgers, batched over samples (module `Burgers`, src/Burgers.jl)
  *
  * A handle holds `nsample` independent periodic samples of `nh` cells on

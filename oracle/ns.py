@@ -269,9 +269,16 @@ def conj_weight(n: int) -> np.ndarray:
     return w
 
 
-def randomfield(n: int, l: float, kpeak: float, seed: int, totalenergy: float = 1.0):
+def power_profile(k, p):
+    """``k -> (k > 0) * k^p`` (the ``dnsaid_project`` profile, ``src/N.jl:1245``)."""
+    k = np.asarray(k, dtype=np.float64)
+    return np.where(k > 0, np.power(np.maximum(k, 1.0), p), 0.0)
+
+
+def randomfield(n: int, l: float, kpeak: float, seed: int, totalenergy: float = 1.0, profile: str = "peak"):
     """``randomfield(peak_profile, ...)`` (``src/N.jl:394-476``) with the
-    project's counter-based normals in place of ``randn!``."""
+    project's counter-based normals in place of ``randn!``; ``profile =
+    "power"`` uses ``power_profile`` with exponent ``kpeak``."""
     h = l / n
     N = n**3
     u = counter_normal(seed, 3 * N).reshape(3, n, n, n)
@@ -283,7 +290,7 @@ def randomfield(n: int, l: float, kpeak: float, seed: int, totalenergy: float = 
     kmax = n // 2
     kdiag = int(math.floor(math.sqrt(3) * kmax))
     ks = np.arange(kdiag + 1)
-    prof = peak_profile(ks, kpeak)
+    prof = peak_profile(ks, kpeak) if profile == "peak" else power_profile(ks, kpeak)
     totalprofile = prof.sum()
     for k in range(kdiag + 1):
         mask = (k * k <= kk) & (kk < (k + 1) ** 2)
@@ -698,3 +705,54 @@ def dnsaid_rk4(u: np.ndarray, visc: float, l: float, cfl: float, nsteps: int,
             les.v_exact = les.v_exact + dt / 6 * (ke[0] + 2 * ke[1] + 2 * ke[2] + ke[3])
             les.v_nomodel = les.v_nomodel + dt / 6 * (kn[0] + 2 * kn[1] + 2 * kn[2] + kn[3])
     return u, dts, closures
+
+
+# --------------------------------------------------------------------------
+# The reference's own driver: forward Euler, five LES variants in lockstep
+# --------------------------------------------------------------------------
+DNSAID_NAMES = ("u_nomo", "u_c", "u_cf", "u_cfd", "u_cfd_symm")
+
+
+def dnsaid_warmup(u, visc, l, twarm, cfl, max_steps=None, t0=0.0):
+    """The warm-up loop of ``dnsaid_project`` (``src/N.jl:1264-1276``).
+    Returns (u, t, steps)."""
+    h = l / u.shape[1]
+    t, it = t0, 0
+    while t < twarm and (max_steps is None or it < max_steps):
+        dt = min(propose_timestep(u, visc, cfl, h), twarm - t)
+        t += dt
+        it += 1
+        u = step_forwardeuler(u, visc, h, dt)
+    return u, t, it
+
+
+def dnsaid_start(u, l, c, fdelta=None):
+    """LES initial states (``src/N.jl:1278-1287``): all five equal
+    ``apply_ΔHπ(u)``."""
+    ub = apply_DHpi(u, c, l, fdelta)
+    return {k: ub.copy() for k in DNSAID_NAMES}
+
+
+def dnsaid_project_steps(u, les, visc, l, c, tstop, cfl, fdelta=None, max_steps=None, t0=0.0):
+    """The lockstep loop of ``dnsaid_project`` (``src/N.jl:1289-1323``):
+    the DNS right-hand side is projected (its pressure feeds ``r``), the
+    five LES take forward-Euler steps with the DNS time step, then the DNS
+    is updated.  Returns (u, les, t, steps)."""
+    n = u.shape[1]
+    h = l / n
+    H = l / (n // c)
+    les = {k: v.copy() for k, v in les.items()}
+    t, it = t0, 0
+    while t < tstop and (max_steps is None or it < max_steps):
+        dt = min(propose_timestep(u, visc, cfl, h), tstop - t)
+        t += dt
+        it += 1
+        du, p = project(rhs(u, visc, h), h, return_p=True)
+        ub = apply_DHpi(u, c, l, fdelta)
+        les["u_nomo"] = step_forwardeuler(les["u_nomo"], visc, H, dt)
+        les["u_c"] = step_classic(les["u_c"], u, visc, l, c, dt, fdelta)
+        les["u_cf"] = step_classic_flux(les["u_cf"], ub, u, visc, l, c, dt, fdelta)
+        les["u_cfd"] = step_classic_flux_div(les["u_cfd"], ub, u, p, visc, l, c, dt, fdelta)
+        les["u_cfd_symm"] = step_classic_flux_div(les["u_cfd_symm"], ub, u, p, visc, l, c, dt, fdelta, symm=True)
+        u = u + dt * du
+    return u, les, t, it

@@ -1,0 +1,79 @@
+"""GPU parity of the reference's own driver ``dnsaid_project``
+(``exc_dnsaid_*``, src/N.jl:1239-1332) against the oracle: the power-law
+random field, the forward-Euler warm-up, the LES start and the lockstep of
+the DNS with the five LES (no model, classic, classic+flux,
+classic+flux+div, symmetrised), 1e-12 relative per step; the exact closure
+reproduces the filtered DNS (navierstokes.jl:33 records 5.69e-15)."""
+import numpy as np
+import pytest
+
+from oracle import ns
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def NS(built_lib):
+    from exactclosure_gb300 import navierstokes
+
+    return navierstokes
+
+
+def rel(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def test_power_profile_field(NS):
+    n = 48
+    d = NS.DnsAid(n, 1.0, 1e-3, 3)
+    d.init_random("power", -5 / 3, 1.0, 4)
+    ref = ns.randomfield(n, 1.0, -5 / 3, 4, 1.0, profile="power")
+    assert rel(d.velocity(), ref) < 1e-12
+
+
+@pytest.mark.parametrize("n,c,use_fdelta", [(48, 3, False), (48, 3, True), (54, 3, True)])
+def test_warmup_start_and_lockstep_per_step(NS, n, c, use_fdelta):
+    l, visc, cfl = 1.0, 1e-3, 0.4
+    m = n // c
+    fdelta = ns.gaussian(l / n, 2 * l / m, 2) if use_fdelta else None
+    u0 = ns.randomfield(n, l, -5 / 3, 1, 1.0, profile="power")
+    d = NS.DnsAid(n, l, visc, c, fdelta)
+    d.set_velocity(u0)
+    u, t = u0, 0.0
+    for k in range(2):
+        d.warmup(0.05, cfl, max_steps=1)
+        u, t, _ = ns.dnsaid_warmup(u, visc, l, 0.05, cfl, max_steps=1, t0=t)
+        assert rel(d.velocity(), u) < 1e-12, k
+        assert abs(d.time()[0] - t) <= 1e-15
+    d.start()
+    les = ns.dnsaid_start(u, l, c, fdelta)
+    for key in ns.DNSAID_NAMES:
+        assert rel(d.get(key), les[key]) < 1e-12
+    t = 0.0
+    for k in range(3):
+        d.step(0.05, cfl, max_steps=1)
+        u, les, t, _ = ns.dnsaid_project_steps(u, les, visc, l, c, 0.05, cfl, fdelta, max_steps=1, t0=t)
+        assert rel(d.velocity(), u) < 1e-12, k
+        for key in ns.DNSAID_NAMES:
+            assert rel(d.get(key), les[key]) < 1e-12, (k, key)
+    assert rel(d.get("u_les"), ns.apply_DHpi(u, c, l, fdelta)) < 1e-12
+
+
+def test_exact_closure_invariant_and_errors(NS):
+    setup = NS.getsetup(n_dns=72, n_les=24, twarm=0.02, tstop=0.02, visc=1e-3)
+    out = NS.dnsaid_project(setup)
+    e = out["errors"]
+    assert e["u_cfd"] < 1e-13
+    for k in ("u_nomo", "u_c", "u_cf", "u_cfd_symm"):
+        assert e[k] > 1e-4, k
+    eh = NS.compute_errors(out)
+    for k in e:
+        assert abs(eh[k] - e[k]) <= 1e-10 * max(e[k], 1e-30) + 1e-15
+
+
+def test_even_ratio_rejected(NS):
+    from exactclosure_gb300 import ExcError
+
+    with pytest.raises(ExcError) as ei:
+        NS.DnsAid(48, 1.0, 1e-3, 4)
+    assert ei.value.code == 3

@@ -119,7 +119,7 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
       if (rc) return rc;
     }
     e = launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0, ci->us, ufin, s,
-                           dt, st);
+                           dt, st, SlotBatch(), 1, ci->nles > 0);
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
     for (int li = 0; li < ci->nles; ++li) {
       LesState<T>& L = ci->les[li];

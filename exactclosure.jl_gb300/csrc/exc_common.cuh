@@ -48,6 +48,34 @@ template <bool INV, typename C> __host__ __device__ __forceinline__ C mul_mi(C a
 __host__ __device__ __forceinline__ int pad8(int m) { return (m + 7) & ~7; }
 __host__ __device__ __forceinline__ int spec_pitch(int n) { return pad8(n / 2 + 1); }
 
+// Division of a linear index by a grid extent with a multiply-high
+// reciprocal m = ceil(2^64 / d): x / d exactly for every x < 2^64 / d, which
+// covers every index here.  Built once per thread (one 64-bit division), it
+// replaces the per-element 64-bit divisions of grid-stride index splits.
+struct IdxDiv {
+  unsigned long long m;
+  long long d;
+  __host__ __device__ __forceinline__ explicit IdxDiv(long long d_)
+      : m(d_ > 1 ? ~0ull / (unsigned long long)d_ + 1 : 0ull), d(d_) {}
+  __device__ __forceinline__ long long div(long long x) const {
+    return m ? (long long)__umul64hi((unsigned long long)x, m) : x;
+  }
+};
+
+// Asynchronous global -> shared copy of one 4- or 8-byte word (cp.async);
+// completion is waited for with cp_async_wait_all before a barrier.
+template <typename T>
+__device__ __forceinline__ void cp_async_word(T* smem, const T* gmem) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "word copies only");
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 // Periodic neighbour index along one axis.
 __device__ __forceinline__ int wrap_up(int i, int n) { return (i + 1 == n) ? 0 : i + 1; }
 __device__ __forceinline__ int wrap_dn(int i, int n) { return (i == 0) ? n - 1 : i - 1; }

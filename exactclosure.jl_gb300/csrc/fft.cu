@@ -26,14 +26,14 @@ r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ ou
   src += slot * sb.ustride;
   out += slot * sb.wstride;
   const int N2 = n / 2;
-  const int ls = N2 + 1;
+  const int ls = padded_len(N2);
   const long long nn = (long long)n * n;
   const long long N = nn * n;
   const long long row0 = (long long)blockIdx.x * rows_per_cta;
   const int rows = (int)min((long long)rows_per_cta, nn - row0);
   // load
   for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
-    int r = t / N2, m = t - r * N2;
+    const int r = (int)fast_div((unsigned)t, plan.rL), m = t - r * N2;
     long long row = row0 + r;
     long long base = row * n;
     T a, b;
@@ -41,7 +41,7 @@ r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ ou
       a = src[base + 2 * m];
       b = src[base + 2 * m + 1];
     } else {
-      int y = (int)(row % n), z = (int)(row / n);
+      const int z = (int)fast_div((unsigned)row, plan.r2L), y = (int)row - z * n;  // row < n^2 <= 2^20
       long long rowy = (long long)z * n + (y == 0 ? n - 1 : y - 1);
       long long rowz = (long long)(z == 0 ? n - 1 : z - 1) * n + y;
       const T* ux = src;
@@ -54,15 +54,15 @@ r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ ou
       b = ((ux[base + x1] - ux[base + x0]) + (uy[base + x1] - uy[rowy * n + x1]) +
            (uz[base + x1] - uz[rowz * n + x1])) * inv_h;
     }
-    s[r * ls + m] = mk<T>(a, b);
+    s[r * ls + pe(m)] = mk<T>(a, b);
   }
   __syncthreads();
   fft_lines<false>(s, ls, rows, plan, tw, n);
   // untangle and store k = 0..N2
   for (int t = threadIdx.x; t < rows * (N2 + 1); t += blockDim.x) {
-    int r = t / (N2 + 1), k = t - r * (N2 + 1);
-    C zk = s[r * ls + (k == N2 ? 0 : k)];
-    C zc = cconj(s[r * ls + (k == 0 ? 0 : N2 - k)]);
+    const int r = (int)fast_div((unsigned)t, plan.rL1), k = t - r * (N2 + 1);
+    C zk = s[r * ls + pe(k == N2 ? 0 : k)];
+    C zc = cconj(s[r * ls + pe(k == 0 ? 0 : N2 - k)]);
     C e = cadd(zk, zc);
     C o = csub(zk, zc);
     C w = tw[k];                  // W_n^k, k <= n/2 < n
@@ -77,26 +77,66 @@ r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ ou
 
 // ---------------------------------------------------------------------------
 // Column passes along y (elem_stride = P, outer = z) or z (elem_stride = n P,
-// outer = y): a CTA loads `W` consecutive kx columns of one outer index.
+// outer = y).  A tile is `W` consecutive kx columns of one outer index; tile
+// id = outer * ntx + kx tile.  The CTAs are persistent: each walks the tiles
+// id = blockIdx.x, + gridDim.x, ... with two shared-memory tile buffers; the
+// next tile's cp.async copies are issued before the current tile is
+// transformed, so HBM traffic continues while the shared-memory passes run.
 // ---------------------------------------------------------------------------
+struct ColTiles {
+  int nkx, W, wlog, ntx, ntiles;  // ntiles = ntx * n < 2^17
+  long long outer_stride;
+  __device__ __forceinline__ int lines(int id) const {
+    return min(W, nkx - (id % ntx) * W);
+  }
+  __device__ __forceinline__ long long offset(int id) const {
+    const int outer = id / ntx;
+    return (long long)outer * outer_stride + (id - outer * ntx) * W;
+  }
+};
+
+__device__ __forceinline__ ColTiles col_tiles(int n, int nkx, int W, long long outer_stride) {
+  ColTiles t;
+  t.nkx = nkx;
+  t.W = W;
+  t.wlog = 31 - __clz(W);
+  t.ntx = (nkx + W - 1) / W;
+  t.ntiles = t.ntx * n;
+  t.outer_stride = outer_stride;
+  return t;
+}
+
+// Shared memory: two buffers of W lines of stride n + 1.  A CTA takes the
+// tiles blockIdx.x and blockIdx.x + gridDim.x; the second tile's copies are
+// in flight while the first is transformed.
 template <typename T, bool INV>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_stride,
             long long outer_stride, const cplx<T>* __restrict__ tw, FftPlan plan, SlotBatch sb) {
   using C = cplx<T>;
   extern __shared__ unsigned char smem_raw[];
-  C* s = reinterpret_cast<C*>(smem_raw);
+  C* const buf0 = reinterpret_cast<C*>(smem_raw);
+  C* const buf1 = buf0 + W * padded_len(n);
   if (sb.active && !sb.active[blockIdx.z]) return;
   g += blockIdx.z * sb.wstride;
-  const int ls = n + 1;
-  const int kx0 = blockIdx.x * W;
-  const int lines = min(W, nkx - kx0);
-  const int wlog = 31 - __clz(W);
-  C* base = g + (long long)blockIdx.y * outer_stride + kx0;
-  tile_move<true>(s, ls, base, elem_stride, lines, W, wlog, n);
+  const int ls = padded_len(n);
+  const ColTiles ct = col_tiles(n, nkx, W, outer_stride);
+  const int a = blockIdx.x, b = blockIdx.x + gridDim.x;
+  if (a >= ct.ntiles) return;
+  const bool two = b < ct.ntiles;
+  tile_load_async(buf0, ls, g + ct.offset(a), elem_stride, ct.lines(a), W, ct.wlog, n);
+  cp_commit();
+  if (two) tile_load_async(buf1, ls, g + ct.offset(b), elem_stride, ct.lines(b), W, ct.wlog, n);
+  cp_commit();
+  cp_wait<1>();
   __syncthreads();
-  fft_lines<INV>(s, ls, lines, plan, tw, n);
-  tile_move<false>(s, ls, base, elem_stride, lines, W, wlog, n);
+  fft_lines<INV>(buf0, ls, ct.lines(a), plan, tw, n);
+  tile_move<false>(buf0, ls, g + ct.offset(a), elem_stride, ct.lines(a), W, ct.wlog, n);
+  if (!two) return;
+  cp_wait<0>();
+  __syncthreads();
+  fft_lines<INV>(buf1, ls, ct.lines(b), plan, tw, n);
+  tile_move<false>(buf1, ls, g + ct.offset(b), elem_stride, ct.lines(b), W, ct.wlog, n);
 }
 
 // 1/d in float64 for d in (0, 3] (a sum of three sin^2): a single-precision
@@ -116,29 +156,18 @@ __device__ __forceinline__ double recip_f64(double d) {
 // and the mean mode set to zero (src/N.jl:298), inverse FFT along z.  The
 // divide is computed in float64 for every precision.
 // ---------------------------------------------------------------------------
+// z forward transform, divide and inverse of one tile in shared memory.
 template <typename T>
-__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
-zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<T>* __restrict__ tw,
-              FftPlan plan, const double* __restrict__ sin2, double coef, const double* __restrict__ invlap,
-              SlotBatch sb) {
+__device__ __forceinline__ void zsolve_tile(cplx<T>* s, int ls, int lines, int wlog, int n, int nkx, int kx0, int ky,
+                                            const cplx<T>* __restrict__ tw, const FftPlan& plan,
+                                            const double* __restrict__ sin2, double coef,
+                                            const double* __restrict__ invlap) {
   using C = cplx<T>;
-  extern __shared__ unsigned char smem_raw[];
-  C* s = reinterpret_cast<C*>(smem_raw);
-  if (sb.active && !sb.active[blockIdx.z]) return;
-  g += blockIdx.z * sb.wstride;
-  const int ls = n + 1;
-  const int kx0 = blockIdx.x * W;
-  const int ky = blockIdx.y;
-  const int lines = min(W, nkx - kx0);
-  const long long es = (long long)n * P;
-  const int wlog = 31 - __clz(W);
-  C* base = g + (long long)ky * P + kx0;
-  tile_move<true>(s, ls, base, es, lines, W, wlog, n);
-  __syncthreads();
   fft_lines<false>(s, ls, lines, plan, tw, n);
   const double sy = sin2[ky];
+  const bool pow2 = lines == (1 << wlog);
   for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-    int kz = t / lines, l = t - kz * lines;
+    const int kz = pow2 ? t >> wlog : t / lines, l = t - kz * lines;
     int kx = kx0 + l;
     double f;
     if (invlap) {
@@ -148,14 +177,50 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
       double den = sin2[kx] + sy + sin2[kz];
       f = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef * recip_f64(den);
     }
-    C v = s[l * ls + kz];
+    C v = s[l * ls + pe(kz)];
     v.x = (T)((double)v.x * f);
     v.y = (T)((double)v.y * f);
-    s[l * ls + kz] = v;
+    s[l * ls + pe(kz)] = v;
   }
   __syncthreads();
   fft_lines<true>(s, ls, lines, plan, tw, n);
-  tile_move<false>(s, ls, base, es, lines, W, wlog, n);
+}
+
+// Two tiles per CTA, as in cols_kernel.
+template <typename T>
+__global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
+zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<T>* __restrict__ tw,
+              FftPlan plan, const double* __restrict__ sin2, double coef, const double* __restrict__ invlap,
+              SlotBatch sb) {
+  using C = cplx<T>;
+  extern __shared__ unsigned char smem_raw[];
+  C* const buf0 = reinterpret_cast<C*>(smem_raw);
+  C* const buf1 = buf0 + W * padded_len(n);
+  if (sb.active && !sb.active[blockIdx.z]) return;
+  g += blockIdx.z * sb.wstride;
+  const int ls = padded_len(n);
+  const long long es = (long long)n * P;
+  const ColTiles ct = col_tiles(n, nkx, W, P);
+  const int a = blockIdx.x, b = blockIdx.x + gridDim.x;
+  if (a >= ct.ntiles) return;
+  const bool two = b < ct.ntiles;
+  tile_load_async(buf0, ls, g + ct.offset(a), es, ct.lines(a), W, ct.wlog, n);
+  cp_commit();
+  if (two) tile_load_async(buf1, ls, g + ct.offset(b), es, ct.lines(b), W, ct.wlog, n);
+  cp_commit();
+  cp_wait<1>();
+  __syncthreads();
+  {
+    const int ky = a / ct.ntx;
+    zsolve_tile<T>(buf0, ls, ct.lines(a), ct.wlog, n, nkx, (a - ky * ct.ntx) * W, ky, tw, plan, sin2, coef, invlap);
+    tile_move<false>(buf0, ls, g + ct.offset(a), es, ct.lines(a), W, ct.wlog, n);
+  }
+  if (!two) return;
+  cp_wait<0>();
+  __syncthreads();
+  const int ky = b / ct.ntx;
+  zsolve_tile<T>(buf1, ls, ct.lines(b), ct.wlog, n, nkx, (b - ky * ct.ntx) * W, ky, tw, plan, sin2, coef, invlap);
+  tile_move<false>(buf1, ls, g + ct.offset(b), es, ct.lines(b), W, ct.wlog, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -173,21 +238,21 @@ c2r_x_kernel(cplx<T>* __restrict__ g, int n, int P, const cplx<T>* __restrict__ 
   if (sb.active && !sb.active[blockIdx.y]) return;
   g += blockIdx.y * sb.wstride;
   const int N2 = n / 2;
-  const int ls = N2 + 1;
+  const int ls = padded_len(N2);
   const long long nn = (long long)n * n;
   const long long row0 = (long long)blockIdx.x * rows_per_cta;
   const int rows = (int)min((long long)rows_per_cta, nn - row0);
   for (int t = threadIdx.x; t < rows * (N2 + 1); t += blockDim.x) {
-    int r = t / (N2 + 1), k = t - r * (N2 + 1);
-    s[r * ls + k] = g[(row0 + r) * P + k];
+    const int r = (int)fast_div((unsigned)t, plan.rL1), k = t - r * (N2 + 1);
+    s[r * ls + pe(k)] = g[(row0 + r) * P + k];
   }
   __syncthreads();
   // pairs (k, N2-k) handled by one thread, so the tangle is in place
   const int half = N2 / 2 + 1;
   for (int t = threadIdx.x; t < rows * half; t += blockDim.x) {
-    int r = t / half, k = t - r * half;
+    const int r = (int)fast_div((unsigned)t, plan.rhalf), k = t - r * half;
     int k2 = N2 - k;
-    C xa = s[r * ls + k], xb = s[r * ls + k2];
+    C xa = s[r * ls + pe(k)], xb = s[r * ls + pe(k2)];
     C wa = tw[k], wb = tw[k2];
     // Z_k
     C e = cadd(xa, cconj(xb));
@@ -197,15 +262,15 @@ c2r_x_kernel(cplx<T>* __restrict__ g, int n, int P, const cplx<T>* __restrict__ 
     C e2 = cadd(xb, cconj(xa));
     C o2 = cmulc(csub(xb, cconj(xa)), wb);
     C zb; zb.x = e2.x - o2.y; zb.y = e2.y + o2.x;
-    if (k < N2) s[r * ls + k] = za;
-    if (k2 < N2 && k2 != k) s[r * ls + k2] = zb;
+    if (k < N2) s[r * ls + pe(k)] = za;
+    if (k2 < N2 && k2 != k) s[r * ls + pe(k2)] = zb;
   }
   __syncthreads();
   fft_lines<true>(s, ls, rows, plan, tw, n);
   T* gr = reinterpret_cast<T*>(g);
   for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
-    int r = t / N2, m = t - r * N2;
-    C z = s[r * ls + m];
+    const int r = (int)fast_div((unsigned)t, plan.rL), m = t - r * N2;
+    C z = s[r * ls + pe(m)];
     T* row = gr + (row0 + r) * (2LL * P);
     row[2 * m] = z.x;
     row[2 * m + 1] = z.y;
@@ -244,6 +309,9 @@ static int col_width(int n, int tile) {
   return w;
 }
 
+// CTAs of a column pass: two tiles each.
+static inline unsigned column_ctas(long long ntiles) { return (unsigned)((ntiles + 1) / 2); }
+
 // Launch geometry of the passes: columns per CTA of the y/z passes and rows
 // per CTA of the x passes, from the solver's tuned values (autotuner) when
 // set and legal for the tile, else the largest that fills the 32 KB tile.
@@ -269,15 +337,16 @@ cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vec
   int W, rows;
   geometry<C>(ps, W, rows);
   // x forward
-  size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
+  size_t shx = (size_t)rows * padded_len(N2) * sizeof(C);
   dim3 gx((unsigned)((nn + rows - 1) / rows), nslots);
   if (src_is_vector)
     r2c_x_kernel<T, true><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)(1.0 / ps->h), g, P, tw, ps->plan_h, rows, sb);
   else
     r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows, sb);
   // y forward
-  dim3 gc((nkx + W - 1) / W, n, nslots);
-  size_t shc = (size_t)W * (n + 1) * sizeof(C);
+  const long long ntiles = (long long)((nkx + W - 1) / W) * n;
+  size_t shc = 2 * (size_t)W * padded_len(n) * sizeof(C);
+  dim3 gc(column_ctas(ntiles), 1, nslots);
   cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, sb);
   // z forward + divide + inverse; coef = 1/(lambda N) numerator: -h^2/(4 N)
   double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
@@ -301,11 +370,12 @@ cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st) {
   int W, rows;
   geometry<C>(ps, W, rows);
   const SlotBatch one;
-  size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
+  size_t shx = (size_t)rows * padded_len(N2) * sizeof(C);
   int gx = (int)((nn + rows - 1) / rows);
   r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows, one);
-  dim3 gc((nkx + W - 1) / W, n);
-  size_t shc = (size_t)W * (n + 1) * sizeof(C);
+  const long long ntiles = (long long)((nkx + W - 1) / W) * n;
+  size_t shc = 2 * (size_t)W * padded_len(n) * sizeof(C);
+  dim3 gc(column_ctas(ntiles));
   cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, one);
   cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n, one);
   return cudaGetLastError();
@@ -321,11 +391,12 @@ cudaError_t fft3d_inverse(exc_poisson* ps, cudaStream_t st) {
   int W, rows;
   geometry<C>(ps, W, rows);
   const SlotBatch one;
-  dim3 gc((nkx + W - 1) / W, n);
-  size_t shc = (size_t)W * (n + 1) * sizeof(C);
+  const long long ntiles = (long long)((nkx + W - 1) / W) * n;
+  size_t shc = 2 * (size_t)W * padded_len(n) * sizeof(C);
+  dim3 gc(column_ctas(ntiles));
   cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n, one);
   cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, one);
-  size_t shx = (size_t)rows * (N2 + 1) * sizeof(C);
+  size_t shx = (size_t)rows * padded_len(N2) * sizeof(C);
   int gx = (int)((nn + rows - 1) / rows);
   c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows, one);
   return cudaGetLastError();
@@ -354,13 +425,14 @@ template cudaError_t copy_pressure<float>(const exc_poisson*, float*, cudaStream
 template <typename T>
 static cudaError_t configure_fft_t() {
   using C = cplx<T>;
-  int maxsh = (int)(fft_tile<C>() + 64 * 2) * (int)sizeof(C);
+  // a tile of fft_tile elements in padded lines: at most 9/8 of it plus a slot per line
+  int maxsh = (int)(fft_tile<C>() * 9 / 8 + 1024) * (int)sizeof(C);
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(cols_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(cols_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(zsolve_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(cols_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(cols_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(zsolve_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(c2r_x_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
   return cudaSuccess;
 }

@@ -14,14 +14,30 @@ namespace exc {
 
 // Threads per CTA: one radix-8 butterfly per thread per pass over a full tile.
 template <typename C> constexpr int fft_threads() { return sizeof(C) == 16 ? 256 : 512; }
-// Max complex values per CTA (nlines * L): 32 KB of shared memory.
+// Max complex values per CTA (nlines * L): 32 KB of data.
 template <typename C> constexpr int fft_tile() { return 32768 / (int)sizeof(C); }
+// Shared-memory lines are padded with one slot after every 8 elements
+// (element e of a line at pe(e)), so the strided writes of the early
+// Stockham passes (stride R complex) and the column moves spread over all
+// banks; a line of L elements takes padded_len(L) slots.
+__host__ __device__ __forceinline__ int pe(int e) { return e + (e >> 3); }
+__host__ __device__ __forceinline__ int padded_len(int L) { return L + (L >> 3) + 1; }
 // Pass sequence of a length-L transform: n8 radix-8 passes, then at most one
 // radix-4 or radix-2 pass, then n3 radix-3 passes (L = 8^n8 4^n4 2^n2 3^n3).
+// The pass index math divides by nb = L/R and by Ns (the product of the
+// earlier radices); both divisions use multiply-high reciprocals
+// ceil(2^32/d), exact for every quotient here (dividends < 2^17, d <= 2^11;
+// checked exhaustively), and 0 marks d == 1.
+constexpr int FFT_MAX_PASSES = 12;
 struct FftPlan {
   int L;
   int n8, n4, n2, n3;
+  unsigned rnb[FFT_MAX_PASSES], rns[FFT_MAX_PASSES];
+  unsigned rL, rL1, rhalf, r2L;  // reciprocals of L, L + 1, L/2 + 1, 2L (row splits of the x passes)
 };
+
+inline unsigned fast_recip(unsigned d) { return d <= 1 ? 0u : (unsigned)((0x100000000ull + d - 1) / d); }
+__device__ __forceinline__ unsigned fast_div(unsigned x, unsigned r) { return r ? __umulhi(x, r) : x; }
 
 inline FftPlan make_plan(int L) {
   FftPlan p{};
@@ -33,6 +49,21 @@ inline FftPlan make_plan(int L) {
   p.n4 = (a % 3) == 2;
   p.n2 = (a % 3) == 1;
   p.n3 = b;
+  int radix[FFT_MAX_PASSES], np = 0;
+  for (int q = 0; q < p.n8; ++q) radix[np++] = 8;
+  if (p.n4) radix[np++] = 4;
+  if (p.n2) radix[np++] = 2;
+  for (int q = 0; q < p.n3; ++q) radix[np++] = 3;
+  int Ns = 1;
+  for (int q = 0; q < np; ++q) {
+    p.rnb[q] = fast_recip((unsigned)(L / radix[q]));
+    p.rns[q] = fast_recip((unsigned)Ns);
+    Ns *= radix[q];
+  }
+  p.rL = fast_recip((unsigned)L);
+  p.rL1 = fast_recip((unsigned)L + 1);
+  p.rhalf = fast_recip((unsigned)(L / 2 + 1));
+  p.r2L = fast_recip((unsigned)(2 * L));
   return p;
 }
 
@@ -88,7 +119,7 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft_small
 
 // One Stockham pass of radix R over all lines of the CTA's tile.
 template <int R, bool INV, typename C>
-__device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns,
+__device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns, unsigned rnb, unsigned rns,
                                          const C* __restrict__ tw, int n) {
   constexpr int NT = fft_threads<C>();
   constexpr int NB = (fft_tile<C>() / R + NT - 1) / NT;
@@ -96,17 +127,18 @@ __device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns
   const int total = nlines * nb;
   const int twmul = n / (Ns * R);
   C v[NB][R];
-  int obase[NB];
+  int obase[NB], ebase[NB];
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
     int t = threadIdx.x + b * NT;
     obase[b] = -1;
     if (t < total) {
-      int line = t / nb, j = t - line * nb;
+      const int line = (int)fast_div((unsigned)t, rnb), j = t - line * nb;
       C* ln = s + line * ls;
-      int k = j % Ns;
+      const int q = (int)fast_div((unsigned)j, rns);
+      const int k = j - q * Ns;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[b][r] = ln[j + r * nb];
+      for (int r = 0; r < R; ++r) v[b][r] = ln[pe(j + r * nb)];
       if (Ns > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) {
@@ -115,7 +147,8 @@ __device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns
         }
       }
       dft_small<R, INV, C>(v[b]);
-      obase[b] = line * ls + (j / Ns) * Ns * R + k;
+      obase[b] = line * ls;
+      ebase[b] = q * Ns * R + k;
     }
   }
   __syncthreads();
@@ -123,7 +156,7 @@ __device__ __forceinline__ void fft_pass(C* s, int ls, int nlines, int L, int Ns
   for (int b = 0; b < NB; ++b) {
     if (obase[b] >= 0) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) s[obase[b] + r * Ns] = v[b][r];
+      for (int r = 0; r < R; ++r) s[obase[b] + pe(ebase[b] + r * Ns)] = v[b][r];
     }
   }
   __syncthreads();
@@ -145,7 +178,7 @@ __device__ __forceinline__ void tile_move(C* s, int ls, C* base, long long es, i
         for (int t = threadIdx.x; t < tot; t += blockDim.x) {
           const int e = t >> hlog, l2 = t & (hl - 1);
           float4* g = reinterpret_cast<float4*>(base + e * es + 2 * l2);
-          C* a = s + (2 * l2) * ls + e;
+          C* a = s + (2 * l2) * ls + pe(e);
           if (LOAD) {
             const float4 v = *g;
             a[0].x = v.x; a[0].y = v.y;
@@ -161,15 +194,50 @@ __device__ __forceinline__ void tile_move(C* s, int ls, C* base, long long es, i
 #pragma unroll 4
     for (int t = threadIdx.x; t < tot; t += blockDim.x) {
       const int e = t >> wlog, l = t & (W - 1);
-      if (LOAD) s[l * ls + e] = base[e * es + l];
-      else base[e * es + l] = s[l * ls + e];
+      if (LOAD) s[l * ls + pe(e)] = base[e * es + l];
+      else base[e * es + l] = s[l * ls + pe(e)];
     }
     return;
   }
   for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
     const int e = t / lines, l = t - e * lines;
-    if (LOAD) s[l * ls + e] = base[e * es + l];
-    else base[e * es + l] = s[l * ls + e];
+    if (LOAD) s[l * ls + pe(e)] = base[e * es + l];
+    else base[e * es + l] = s[l * ls + pe(e)];
+  }
+}
+
+// Asynchronous copy of a column tile (`lines` columns x n rows, row stride
+// `es` elements) from global memory into line-major shared memory with
+// cp.async: one 8-byte (FP32 complex) or 16-byte (FP64 complex) copy per
+// element, consecutive threads on consecutive columns of a row, nothing held
+// in registers.  The caller commits the group and waits for it (cp_wait)
+// before a __syncthreads and the first read of the tile.
+__device__ __forceinline__ void cp_async_elem(void* smem, const void* gmem, int bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if (bytes == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory"); }
+
+template <typename C>
+__device__ __forceinline__ void tile_load_async(C* s, int ls, const C* base, long long es, int lines, int W,
+                                                int wlog, int n) {
+  if (lines == W) {
+    const int tot = W * n;
+#pragma unroll 4
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+      const int e = t >> wlog, l = t & (W - 1);
+      cp_async_elem(s + l * ls + pe(e), base + e * es + l, (int)sizeof(C));
+    }
+    return;
+  }
+  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+    const int e = t / lines, l = t - e * lines;
+    cp_async_elem(s + l * ls + pe(e), base + e * es + l, (int)sizeof(C));
   }
 }
 
@@ -178,12 +246,12 @@ __device__ __forceinline__ void tile_move(C* s, int ls, C* base, long long es, i
 template <bool INV, typename C>
 __device__ void fft_lines(C* s, int ls, int nlines, const FftPlan& plan,
                           const C* __restrict__ tw, int n) {
-  int Ns = 1;
+  int Ns = 1, p = 0;
   const int L = plan.L;
-  for (int q = 0; q < plan.n8; ++q) { fft_pass<8, INV>(s, ls, nlines, L, Ns, tw, n); Ns *= 8; }
-  if (plan.n4) { fft_pass<4, INV>(s, ls, nlines, L, Ns, tw, n); Ns *= 4; }
-  if (plan.n2) { fft_pass<2, INV>(s, ls, nlines, L, Ns, tw, n); Ns *= 2; }
-  for (int q = 0; q < plan.n3; ++q) { fft_pass<3, INV>(s, ls, nlines, L, Ns, tw, n); Ns *= 3; }
+  for (int q = 0; q < plan.n8; ++q, ++p) { fft_pass<8, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 8; }
+  if (plan.n4) { fft_pass<4, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 4; ++p; }
+  if (plan.n2) { fft_pass<2, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 2; ++p; }
+  for (int q = 0; q < plan.n3; ++q, ++p) { fft_pass<3, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 3; }
 }
 
 }  // namespace exc

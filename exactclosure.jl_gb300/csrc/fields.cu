@@ -20,7 +20,9 @@ static inline int grid_for(long long N, int threads = 256) {
 //   s = 2: xfin += dt/3 k;      xs = x0 + dt k
 //   s = 3: xfin += dt/6 k
 // ---------------------------------------------------------------------------
-template <typename T, bool GRAD>
+// With STORE_K the projected k is written back (the LES closures filter it);
+// without, k is consumed here and the write is skipped.
+template <typename T, bool GRAD, bool STORE_K = true>
 __global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __restrict__ p, int ppitch,
                                 const T* __restrict__ x0, T* __restrict__ xs, T* __restrict__ xfin, int stage,
                                 const double* __restrict__ dtp, SlotBatch sb) {
@@ -35,12 +37,13 @@ __global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __re
   const double dt = dtp[slot];
   const T cf = (T)((stage == 0 || stage == 3) ? dt / 6.0 : dt / 3.0);
   const T cs = (T)(stage == 2 ? dt : 0.5 * dt);
+  const IdxDiv dn(n);
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
     T k0 = k[g], k1 = k[N + g], k2 = k[2 * N + g];
     if (GRAD) {
-      long long r = g / n;
+      const long long r = dn.div(g);
       int x = (int)(g - r * n);
-      int z = (int)(r / n);
+      int z = (int)dn.div(r);
       int y = (int)(r - (long long)z * n);
       T pc = p[r * ppitch + x];
       T px = p[r * ppitch + wrap_up(x, n)];
@@ -49,9 +52,11 @@ __global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __re
       k0 -= (px - pc) * inv_h;
       k1 -= (py - pc) * inv_h;
       k2 -= (pz - pc) * inv_h;
-      k[g] = k0;
-      k[N + g] = k1;
-      k[2 * N + g] = k2;
+      if (STORE_K) {
+        k[g] = k0;
+        k[N + g] = k1;
+        k[2 * N + g] = k2;
+      }
     }
     T a0 = x0[g], a1 = x0[N + g], a2 = x0[2 * N + g];
     if (stage == 0) {
@@ -73,11 +78,14 @@ __global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __re
 
 template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
-                            const double* dtp, cudaStream_t st, const SlotBatch& sb, int nslots) {
+                            const double* dtp, cudaStream_t st, const SlotBatch& sb, int nslots, bool store_k) {
   long long N = (long long)n * n * n;
   dim3 grid(nslots > 1 ? std::min(grid_for(N), 152 * 8) : grid_for(N), nslots);
-  if (p)
+  if (p && store_k)
     rk_stage_kernel<T, true><<<grid, 256, 0, st>>>(n, (T)(1.0 / (double)h), k, p, ppitch, x0, xs, xfin, stage, dtp, sb);
+  else if (p)
+    rk_stage_kernel<T, true, false><<<grid, 256, 0, st>>>(n, (T)(1.0 / (double)h), k, p, ppitch, x0, xs, xfin, stage,
+                                                          dtp, sb);
   else
     rk_stage_kernel<T, false><<<grid, 256, 0, st>>>(n, (T)0, k, nullptr, 0, x0, xs, xfin, stage, dtp, sb);
   return cudaGetLastError();
@@ -190,10 +198,11 @@ __global__ void gradsq_partial_kernel(int n, const T* __restrict__ u, double* __
   __shared__ double r0[256];
   const long long N = (long long)n * n * n;
   double s = 0;
+  const IdxDiv dn(n);
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
-    long long r = g / n;
+    const long long r = dn.div(g);
     int x = (int)(g - r * n);
-    int z = (int)(r / n);
+    int z = (int)dn.div(r);
     int y = (int)(r - (long long)z * n);
     long long nb[3] = {g - x + wrap_up(x, n), ((long long)z * n + wrap_up(y, n)) * n + x,
                        ((long long)wrap_up(z, n) * n + y) * n + x};
@@ -404,7 +413,7 @@ cudaError_t launch_convert(long long count, const A* a, B* b, cudaStream_t st) {
 
 #define INST(T)                                                                                                 \
   template cudaError_t launch_rk_stage<T>(int, T, T*, const T*, int, const T*, T*, T*, int, const double*,      \
-                                          cudaStream_t, const SlotBatch&, int);                                                        \
+                                          cudaStream_t, const SlotBatch&, int, bool);                                                        \
   template cudaError_t launch_axpy<T>(long long, T*, const T*, T, cudaStream_t);                                \
   template cudaError_t launch_normals<T>(long long, unsigned long long, T*, cudaStream_t);                      \
   template cudaError_t launch_sqdiff<T>(long long, const T*, const T*, double*, double*, cudaStream_t);         \

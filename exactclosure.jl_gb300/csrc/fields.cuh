@@ -8,7 +8,8 @@ constexpr int SHELL_BLOCKS = 152;
 
 template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
-                            const double* dtp, cudaStream_t st, const SlotBatch& sb = SlotBatch(), int nslots = 1);
+                            const double* dtp, cudaStream_t st, const SlotBatch& sb = SlotBatch(), int nslots = 1,
+                            bool store_k = true);
 template <typename T>
 cudaError_t launch_axpy(long long count, T* a, const T* b, T scale, cudaStream_t st);
 cudaError_t launch_set_dt(const double* umax, double h, double visc, double cfl, double fixed, double* dt,

@@ -101,10 +101,11 @@ template <typename T, typename Src>
 __global__ void filter_kernel(Src src, int n, int c, Taps3 taps, T* __restrict__ out) {
   const int m = n / c;
   const long long M = (long long)m * m * m;
+  const IdxDiv dm(m);
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < M; g += (long long)gridDim.x * blockDim.x) {
-    long long r = g / m;
+    const long long r = dm.div(g);
     int ix = (int)(g - r * m);
-    int iz = (int)(r / m);
+    int iz = (int)dm.div(r);
     int iy = (int)(r - (long long)iz * m);
     double acc = 0.0;
     for (int tz = 0; tz < taps.a[2].cnt; ++tz) {
@@ -228,26 +229,27 @@ __global__ void tb_kernel(const T* __restrict__ f3, int n, int c, T* __restrict_
   const long long Mt = (long long)n * m * m;
   const T* __restrict__ f = f3 + comp * N;
   T* __restrict__ tb = tb3 + comp * Mt;
+  const IdxDiv dn(n), dm(m);
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < Mt; g += (long long)gridDim.x * blockDim.x) {
     T acc = (T)0;
     if (comp == 0) {
-      const int x = (int)(g % n);
-      const long long r = g / n;
-      const int Jy = (int)(r % m), Jz = (int)(r / m);
+      const long long r = dn.div(g);
+      const int x = (int)(g - r * n);
+      const int Jz = (int)dm.div(r), Jy = (int)(r - (long long)Jz * m);
       const T* p = f + ((long long)(c * Jz) * n + c * Jy) * n + x;
       for (int dz = 0; dz < c; ++dz)
         for (int dy = 0; dy < c; ++dy) acc += p[((long long)dz * n + dy) * n];
     } else if (comp == 1) {
-      const int Jx = (int)(g % m);
-      const long long r = g / m;
-      const int y = (int)(r % n), Jz = (int)(r / n);
+      const long long r = dm.div(g);
+      const int Jx = (int)(g - r * m);
+      const int Jz = (int)dn.div(r), y = (int)(r - (long long)Jz * n);
       const T* p = f + ((long long)(c * Jz) * n + y) * n + c * Jx;
       for (int dz = 0; dz < c; ++dz)
         for (int dx = 0; dx < c; ++dx) acc += p[(long long)dz * n * n + dx];
     } else {
-      const int Jx = (int)(g % m);
-      const long long r = g / m;
-      const int Jy = (int)(r % m), z = (int)(r / m);
+      const long long r = dm.div(g);
+      const int Jx = (int)(g - r * m);
+      const int z = (int)dm.div(r), Jy = (int)(r - (long long)z * m);
       const T* p = f + ((long long)z * n + c * Jy) * n + c * Jx;
       for (int dy = 0; dy < c; ++dy)
         for (int dx = 0; dx < c; ++dx) acc += p[(long long)dy * n + dx];
@@ -263,10 +265,11 @@ __global__ void oa_kernel(const T* __restrict__ tb3, int n, int c, Taps1D taps, 
   const long long M = (long long)m * m * m;
   const long long Mt = (long long)n * m * m;
   const T* __restrict__ tb = tb3 + comp * Mt;
+  const IdxDiv dm(m);
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < M; g += (long long)gridDim.x * blockDim.x) {
-    const int ix = (int)(g % m);
-    const long long r = g / m;
-    const int iy = (int)(r % m), iz = (int)(r / m);
+    const long long r = dm.div(g);
+    const int ix = (int)(g - r * m);
+    const int iz = (int)dm.div(r), iy = (int)(r - (long long)iz * m);
     const int own = comp == 0 ? ix : (comp == 1 ? iy : iz);
     double acc = 0.0;
     for (int t = 0; t < taps.cnt; ++t) {

@@ -1,8 +1,9 @@
 // RHS sweep: du = doadd*du - div sigma(u) (`stresstensor` + `tensordivergence!`,
 // src/N.jl:94-160), marching along z.
 //
-// A CTA owns a TX x TY column of cells and walks TZ planes.  Two planes of u
-// (z and z+1) with a one-cell x/y halo sit in shared memory; each thread
+// A CTA owns a TX x TY column of cells and walks TZ planes.  Three plane
+// buffers of u with a one-cell x/y halo sit in shared memory: planes z and
+// z+1 are read while plane z+2 streams in with cp.async; each thread
 // evaluates the six stress components at its own cell (the edge stresses s13,
 // s23 and the diagonal s33 of the next plane are kept in registers for the
 // next plane), four warps evaluate the halo stresses lane-parallel, and the
@@ -18,7 +19,7 @@ constexpr int PBX = PTX + 2, PBY = PTY + 2;  // plane box with one-cell halo (bo
 
 template <typename T>
 struct PlaneSmem {
-  T u[2][3][PBY][PBX];
+  T u[3][3][PBY][PBX];
   T s[5][PBY][PBX];  // s11, s22, s12, s13, s23 of the current plane
 };
 
@@ -85,19 +86,23 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   const int ca = big ? wrap(x0 - 1 + tx) : wrapm(x0 - 1 + tx);
   const int cb = big ? wrap(x0 - 1 + tx + PTX) : wrapm(x0 - 1 + tx + PTX);
   const bool xr = tx < PBX - PTX, yr = ty < PBY - PTY;
+  // asynchronous copy of plane gz (with halo) into buffer buf; the caller
+  // commits and waits (cp_async_wait_all) before the __syncthreads that
+  // publishes it
   auto load_plane = [&](int buf, int gz) {
     const long long pz = (long long)gz * n;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const T* p = u + c * N;
       const long long oa = (pz + ra) * n, ob = (pz + rb) * n;
-      sm.u[buf][c][ty][tx] = p[oa + ca];
-      if (xr) sm.u[buf][c][ty][tx + PTX] = p[oa + cb];
+      cp_async_word(&sm.u[buf][c][ty][tx], p + oa + ca);
+      if (xr) cp_async_word(&sm.u[buf][c][ty][tx + PTX], p + oa + cb);
       if (yr) {
-        sm.u[buf][c][ty + PTY][tx] = p[ob + ca];
-        if (xr) sm.u[buf][c][ty + PTY][tx + PTX] = p[ob + cb];
+        cp_async_word(&sm.u[buf][c][ty + PTY][tx], p + ob + ca);
+        if (xr) cp_async_word(&sm.u[buf][c][ty + PTY][tx + PTX], p + ob + cb);
       }
     }
+    cp_async_commit();
   };
   auto zwrap = [&](int z) { return big ? wrap(z) : wrapm(z); };
   const int bx = tx + 1, by = ty + 1;
@@ -105,21 +110,25 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   // z0-1 and s33 of plane z0 for this thread's cell
   load_plane(0, zwrap(z0 - 1));
   load_plane(1, zwrap(z0));
+  load_plane(2, zwrap(z0 + 1));
+  cp_async_wait_all();
   __syncthreads();
   T s13_prev = s13<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
   T s23_prev = s23<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
   T s33_cur = s33<T>(sm.u[1][2][by][bx], sm.u[0][2][by][bx], kd, kv2);
-  __syncthreads();
-  load_plane(0, zwrap(z0 + 1));
-  __syncthreads();
-  int cur = 1;
+  __syncthreads();  // buffer 0 is refilled by the first prefetch
+  // buffers: cur = plane z, nxt = plane z + 1, pre = the free one
+  int cur = 1, nxt = 2, pre = 0;
   const int gx = x0 + tx, gy = y0 + ty;
   const bool inside = gx < n && gy < n;
   for (int kz = 0; kz < PTZ; ++kz) {
     const int z = z0 + kz;
     if (z >= n) break;  // uniform across the CTA
+    // plane z + 2 streams into the free buffer while plane z is processed
+    // (its last reader finished before the previous iteration's barrier)
+    if (kz + 1 < PTZ && z + 1 < n) load_plane(pre, zwrap(z + 2));
     const auto& uc = sm.u[cur];
-    const auto& un = sm.u[cur ^ 1];
+    const auto& un = sm.u[nxt];
     // own-cell stresses
     const T v11 = sdiag<T, 0>(uc, bx, by, kd, kv2);
     const T v22 = sdiag<T, 1>(uc, bx, by, kd, kv2);
@@ -171,10 +180,12 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     s13_prev = v13;
     s23_prev = v23;
     s33_cur = v33n;
-    // plane z is done: its buffer receives plane z + 2
-    if (kz + 1 < PTZ && z + 1 < n) load_plane(cur, zwrap(z + 2));
+    cp_async_wait_all();
     __syncthreads();
-    cur ^= 1;
+    const int freed = cur;
+    cur = nxt;
+    nxt = pre;
+    pre = freed;
   }
 }
 

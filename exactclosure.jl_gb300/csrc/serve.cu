@@ -190,7 +190,7 @@ class Chunk : public ChunkBase {
       if (e == cudaSuccess) e = poisson_solve_inplace<T>(&ps, rhs, true, stream, sb, S);
       if (e == cudaSuccess)
         e = launch_rk_stage<T>(n, h, rhs, reinterpret_cast<const T*>(ps.work), 2 * ps.P, u0, us, ufin, s, dt, stream,
-                               sb, S);
+                               sb, S, false);
     }
     return e;
   }

@@ -8,9 +8,10 @@ namespace exc {
 // Simple per-cell kernels
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void cell_of(long long g, int n, int& x, int& y, int& z) {
-  long long r = g / n;
+  const IdxDiv dn(n);
+  const long long r = dn.div(g);
   x = (int)(g - r * n);
-  z = (int)(r / n);
+  z = (int)dn.div(r);
   y = (int)(r - (long long)z * n);
 }
 

@@ -48,6 +48,16 @@ def parse():
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--serve-only", action="store_true")
     ap.add_argument("--no-burgers", action="store_true")
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--only", default="", choices=["", "burgers", "large", "learned"],
+                    help="run one side workload alone and print its JSON object")
+    ap.add_argument("--burgers-samples", type=int, default=1000)
+    ap.add_argument("--burgers-tstop", type=float, default=0.1)
+    ap.add_argument("--large-steps", type=int, default=30)
+    ap.add_argument("--learned-steps", type=int, default=300)
+    ap.add_argument("--forms-steps", type=int, default=200,
+                    help="steps of the FP32-vs-FP64 error comparison (0: skip)")
     return ap.parse_args()
 
 
@@ -58,6 +68,16 @@ def les_list(spec):
             r, k = item.split(":")
             out.append((int(r), k))
     return out
+
+
+def measured_peaks() -> dict:
+    """MEASURED_PEAKS.json, or the fallback figures (6.8 TB/s, 1.9 PFLOP/s bf16)."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        d["source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 def peaks():
@@ -155,7 +175,139 @@ SERVE_SIZES = (64, 96, 128, 192, 256)
 SERVE_VISC = (1 / 1000, 1 / 2000, 1 / 4000)
 
 
-def burgers_section(nsample=1000, grids=(300, 900, 2700), cpu=True):
+def forms_errors(n, les, kpeak, visc, nsteps, stream):
+    """Precision comparison of the 512^3 config: the FP32 form against the FP64
+    plain path from the same initial field with the same fixed time step,
+    after `nsteps` RK4 steps: relative L2 of the velocity, of the exact closure
+    of each LES grid (stage 1 of the last step) and of the energy spectrum."""
+    import numpy as np
+
+    from exactclosure_gb300 import navierstokes as NS
+
+    ca = NS.Case(n, 1.0, visc, 0.3, precision=0, les=les, stream=stream.cuda_stream)
+    ca.init_random(kpeak, 1.0, seed=0)
+    u0 = ca.velocity()
+    ca.step(1)
+    dt = ca.time()[1]
+    ca.set_velocity(u0)
+    cb = NS.Case(n, 1.0, visc, 0.3, precision=1, les=les, stream=stream.cuda_stream)
+    cb.set_velocity(u0)
+    ca.step(nsteps, dt=dt)
+    cb.step(nsteps, dt=dt)
+    ca.sync()
+    cb.sync()
+
+    def rel(a, b):
+        return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+    out = {"steps": nsteps, "dt": dt,
+           "velocity": rel(cb.velocity(), ca.velocity()),
+           "closure": {f"{n // c}^3 {k}": rel(cb.les(i, "closure"), ca.les(i, "closure"))
+                       for i, (c, k) in enumerate(les)},
+           "spectrum": rel(cb.spectrum(), ca.spectrum()),
+           "exact_les_vs_filtered_dns_f32": {f"{n // c}^3 {k}": cb.errors(i)[0] for i, (c, k) in enumerate(les)},
+           "note": "FP32 form vs FP64 plain path, same initial field and fixed dt; relative L2"}
+    ca.close()
+    cb.close()
+    return out
+
+
+def large_section(n=1024, nsteps=30, every=10):
+    """DNS-aided LES at 1024^3 in FP32 (FP64 spectral divide), nu = 1/8000,
+    k0 = 8, exact closure at every RK4 stage for 64^3 and 128^3 LES grids with
+    both the volume and the face filter, filtered-velocity/closure pairs of
+    the 64^3 volume LES written every `every` steps (raw binary + JSON header).
+    A bounded sample of the 500-step run: `nsteps` steps."""
+    import tempfile
+
+    import torch
+
+    from exactclosure_gb300 import navierstokes as NS
+    from exactclosure_gb300 import snapshots
+
+    les = [(n // 64, "volume"), (n // 128, "volume"), (n // 64, "face"), (n // 128, "face")]
+    stream = torch.cuda.Stream()
+    cs = NS.Case(n, 1.0, 1 / 8000, 0.3, precision=1, les=les, stream=stream.cuda_stream)
+    cs.init_random(8.0, 1.0, seed=0)
+    cs.step(1)
+    cs.sync()
+    with tempfile.TemporaryDirectory() as td:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hp = snapshots.write_pairs(cs, 0, td, nsnap=max(1, nsteps // every), every=every, stem="large")
+        cs.sync()
+        el = time.perf_counter() - t0
+        nbytes = sum(f.stat().st_size for f in Path(td).iterdir())
+        nfiles = len(list(Path(td).glob("large_*.bin")))
+    steps = max(1, nsteps // every) * every
+    errs = {f"{n // c}^3 {k}": cs.errors(i)[0] for i, (c, k) in enumerate(les)}
+    out = {"metric": "cell-updates/s", "value": n ** 3 * steps / el, "unit": "cell-updates/s", "dtype": "f32",
+           "steps": steps, "seconds": el,
+           "config": {"workload": f"DNS {n}^3 FP32 (FP64 spectral divide), nu 1/8000, k0 8, exact closure every "
+                                  f"RK4 stage for LES 64^3 and 128^3 x volume/face, pairs every {every} steps",
+                      "sample": f"{steps} of the 500 steps"},
+           "snapshots": {"files": nfiles, "bytes": nbytes, "header": Path(hp).name},
+           "exact_closure_error_vs_filtered_dns": errs,
+           "timing": "wall clock around the stepping and the snapshot writes (host copies included)"}
+    cs.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def learned_section(train_steps=300, les_steps=100, peaks_json=None):
+    """Learned closure: 3 BF16 conv layers 3->32->32->3, 3^3 periodic, GELU,
+    FP32 accumulation, Adam lr 1e-3, batch 8 snapshots of 64^3 x 3, trained on
+    (filtered velocity, exact closure) pairs of a GPU DNS-aided run (256^3
+    FP32 DNS, 64^3 volume LES), then run inside the LES; errors against the
+    exact closure and the no-model LES."""
+    import torch
+
+    from exactclosure_gb300 import learned as LN
+    from exactclosure_gb300 import navierstokes as NS
+
+    n, c = 256, 4
+    cs = NS.Case(n, 1.0, 1 / 2000, 0.3, precision=1, les=[(c, "volume")])
+    cs.init_random(4.0, 1.0, 0)
+    cs.step(10)
+    U, M = LN.collect_pairs(cs, 0, nsnap=64, every=1)
+    net = LN.Net(seed=1)
+    LN.train(net, U[:8], M[:8], steps=3)  # warm-up (also fixes the scales)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = LN.train(net, U[:56], M[:56], steps=train_steps, batch=8, lr=1e-3)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    m = n // c
+    flop_fwd = 2 * 27 * (3 * 32 + 32 * 32 + 32 * 3) * m ** 3  # per sample, useful channels
+    flops = 3 * flop_fwd * 8 * train_steps  # forward + input and weight gradients
+    pred = torch.empty_like(U[56:])
+    net.forward(U[56:].contiguous(), pred)
+    torch.cuda.synchronize()
+    e_closure = float((pred - M[56:]).double().norm() / M[56:].double().norm())
+    cs.reset_les()
+    cs.attach_net(0, net)
+    cs.step(les_steps)
+    cs.sync()
+    achieved = flops / el / 1e12
+    peak = (peaks_json or {}).get("bf16_tflops")
+    out = {"metric": "training samples/s", "value": 8 * train_steps / el, "unit": "samples/s",
+           "dtype": "bf16 (fp32 accumulate)",
+           "config": {"workload": f"conv 3->32->32->3 on {m}^3 x 3, batch 8, Adam lr 1e-3, {train_steps} steps; "
+                                  f"pairs from a {n}^3 FP32 DNS-aided run"},
+           "tensor": {"achieved_tflops": achieved, "peak_tflops": peak,
+                      "frac": (achieved / peak) if peak else None,
+                      "note": "useful-channel flops (3->32->32->3) of forward + both gradients; mma.sync BF16"},
+           "loss_first_last": [losses[0], losses[-1]],
+           "held_out_closure_error": e_closure,
+           "les_error_after_steps": {"steps": les_steps, "learned": cs.les_error(0, "learned"),
+                                     "nomodel": cs.les_error(0, "nomodel"), "exact": cs.les_error(0, "exact")}}
+    net.close()
+    cs.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def burgers_section(nsample=1000, grids=(300, 900, 2700), cpu=True, tstop=0.1):
     """The reference's Burgers DNS-aided LES setup (src/Burgers.jl:235-265):
     nh = 13500, 1000 samples, nu = 5e-4, k0 = 10, E = 2, Gaussian LES filter
     Delta = 2H, t = 0.1 with CFL 0.3, forward Euler, four LES per grid.  One
@@ -174,7 +326,7 @@ def burgers_section(nsample=1000, grids=(300, 900, 2700), cpu=True):
         b.les_setup(GB.Grid(L, nH), 2.0, "gaussian")
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        b.advance(0.1, 0.3)
+        b.advance(tstop, 0.3)
         el = time.perf_counter() - t0
         _, steps = b.time()
         units = float(steps.sum()) * nh
@@ -267,18 +419,21 @@ def serve_stream(precision=1, nreq=96, rate=20.0, nsteps=200):
                       f"visc in {{1/1000, 1/2000, 1/4000}}, {nsteps} RK4 steps each"}
 
 
-def plain_fp64_stream_sample(nsolves=10, nsteps=8):
-    """The plain FP64 path on the first requests of the same stream, one solve
-    at a time through the case API (no batching)."""
+def plain_fp64_stream_sample(nsteps=8):
+    """The plain FP64 path on the same stream: each grid size of the stream
+    timed alone through the case API (one solve at a time, no batching), then
+    the stream's own mix weighted in -- total cell-updates over the sum of
+    each request's cell-updates divided by its size's rate (arrival gaps not
+    counted, which favours the plain path)."""
     import torch
 
     from exactclosure_gb300 import navierstokes as NS
 
-    reqs = serve_requests()[:nsolves]
-    cells = 0
-    el = 0.0
-    for q in reqs:
-        cs = NS.Case(q["n"], 1.0, q["visc"], 0.3, precision=0)
+    reqs = serve_requests()
+    rate = {}
+    for n in SERVE_SIZES:
+        q = next(r for r in reqs if r["n"] == n)
+        cs = NS.Case(n, 1.0, q["visc"], 0.3, precision=0)
         cs.init_random(4.0, 1.0, q["seed"])
         cs.step(1)
         cs.sync()
@@ -286,11 +441,13 @@ def plain_fp64_stream_sample(nsolves=10, nsteps=8):
         t0 = time.perf_counter()
         cs.step(nsteps)
         cs.sync()
-        el += time.perf_counter() - t0
-        cells += q["n"] ** 3 * nsteps
+        rate[n] = n ** 3 * nsteps / (time.perf_counter() - t0)
         cs.close()
-    return {"value": cells / el, "unit": "cell-updates/s",
-            "sample": f"first {nsolves} solves of the stream, {nsteps} RK4 steps each, one at a time (FP64)"}
+    cells = sum(r["n"] ** 3 * r["nsteps"] for r in reqs)
+    seconds = sum(r["n"] ** 3 * r["nsteps"] / rate[r["n"]] for r in reqs)
+    return {"value": cells / seconds, "unit": "cell-updates/s", "per_size": {str(k): v for k, v in rate.items()},
+            "sample": f"each stream size alone ({nsteps} RK4 steps, FP64), weighted by the stream's "
+                      f"{len(reqs)} requests x {reqs[0]['nsteps']} steps"}
 
 
 def run_reference(args):
@@ -360,6 +517,13 @@ def main():
     from exactclosure_gb300 import _lib, replicas  # noqa: F401
     from exactclosure_gb300 import navierstokes as NS
 
+    if args.only:
+        pk = measured_peaks()
+        fn = {"burgers": lambda: burgers_section(args.burgers_samples, cpu=not args.no_cpu, tstop=args.burgers_tstop),
+              "large": lambda: large_section(nsteps=args.large_steps),
+              "learned": lambda: learned_section(args.learned_steps, peaks_json=pk)}[args.only]
+        print(json.dumps({args.only: fn()}))
+        return
     if args.serve_only:
         served = serve_stream(precision=0 if args.precision == "f64" else 1, nsteps=args.steps)
         print(json.dumps({"serving": served}))
@@ -453,6 +617,12 @@ def main():
                 "note": "same workload; f32 = stencil/filter/RK in FP32 with FP64 spectral divide and diagnostics"}}
             c2.close()
             torch.cuda.empty_cache()
+            if args.forms_steps > 0:
+                try:
+                    forms["f32_vs_f64_error"] = forms_errors(n, les, args.kpeak, args.visc, args.forms_steps, stream)
+                except Exception as ex:
+                    forms["f32_vs_f64_error"] = {"error": str(ex)}
+                torch.cuda.empty_cache()
         if not args.no_serve:
             try:
                 served = serve_stream(precision=1)
@@ -463,6 +633,17 @@ def main():
             except Exception as ex:
                 serving_line = {"error": str(ex)}
 
+    large = learned = None
+    if rank == 0 and world == 1 and not args.no_large:
+        try:
+            large = large_section(nsteps=args.large_steps)
+        except Exception as ex:
+            large = {"error": str(ex)}
+    if rank == 0 and world == 1 and not args.no_learned:
+        try:
+            learned = learned_section(args.learned_steps, peaks_json=measured_peaks())
+        except Exception as ex:
+            learned = {"error": str(ex)}
     burgers = None
     if rank == 0 and world == 1 and not args.no_burgers:
         try:
@@ -497,6 +678,8 @@ def main():
             "forms": forms,
             "serving": serving_line,
             "burgers": burgers,
+            "large": large,
+            "learned": learned,
         }
         print(json.dumps(line))
     if world > 1:
@@ -534,7 +717,30 @@ def roofline(cs, NS, n, prec, args, stream):
     ms = e0.elapsed_time(e1) / reps
     alg_bytes = 6 * N * w  # read u (3 words), write du (3 words) per cell
     achieved = alg_bytes / (ms / 1e3) / 1e9
-    flops = 100 * N  # ~100 flops per cell (6 stresses + divergence)
+    # 6 stresses (45 flops) + their share of halo stresses (~4) + divergence
+    # and store (18): about 67 flops per cell, FMA counted as 2
+    flops = 67 * N
+    fp64 = None
+    if prec == 0:
+        # FP64 ceiling of this GB300, measured: cuBLAS DGEMM 4096^3, best of 3
+        a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        torch.matmul(a, b)
+        best = None
+        for _ in range(3):
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record()
+            torch.matmul(a, b)
+            f1.record()
+            torch.cuda.synchronize()
+            t = f0.elapsed_time(f1) / 1e3
+            best = t if best is None else min(best, t)
+        dgemm = 2 * 4096 ** 3 / best / 1e12
+        ach = flops / (ms / 1e3) / 1e12
+        fp64 = {"achieved_tflops": ach, "peak_tflops": dgemm, "frac": ach / dgemm,
+                "peak_source": "measured here: cuBLAS DGEMM 4096^3",
+                "note": "the FP64 form is bound by the FP64 pipe, not by HBM (see frac above)"}
+        del a, b
     traffic = None
     tp = ROOT / "profiles" / "rhs_traffic.json"
     if tp.exists():
@@ -544,8 +750,7 @@ def roofline(cs, NS, n, prec, args, stream):
             traffic = d[key]
     return {"kernel": "rhs_kernel (stress + divergence sweep)", "bound": "hbm", "achieved": achieved,
             "peak": hbm, "peak_source": src, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-            "ms_per_launch": ms, "algorithmic_bytes_per_launch": alg_bytes,
-            "fp64_tflops": flops / (ms / 1e3) / 1e12 if prec == 0 else None}
+            "ms_per_launch": ms, "algorithmic_bytes_per_launch": alg_bytes, "fp64": fp64}
 
 
 if __name__ == "__main__":

@@ -42,14 +42,22 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// Divisors of the voxel index split (multiply-high reciprocals, built once per
+// thread).
+struct VoxDiv {
+  IdxDiv N, nn, n;
+  __device__ __forceinline__ explicit VoxDiv(int n_)
+      : N((long long)n_ * n_ * n_), nn((long long)n_ * n_), n(n_) {}
+};
+
 // Periodic neighbour of voxel v (linear, x fastest) on an n^3 grid per sample.
-__device__ __forceinline__ long long neighbour(long long v, int n, int dz, int dy, int dx) {
+__device__ __forceinline__ long long neighbour(long long v, int n, int dz, int dy, int dx, const VoxDiv& dv) {
   const long long nn = (long long)n * n, N = nn * n;
-  const long long b = v / N;
+  const long long b = dv.N.div(v);
   long long r = v - b * N;
-  int z = (int)(r / nn);
+  int z = (int)dv.nn.div(r);
   r -= (long long)z * nn;
-  int y = (int)(r / n), x = (int)(r - (long long)y * n);
+  int y = (int)dv.n.div(r), x = (int)(r - (long long)y * n);
   z += dz; y += dy; x += dx;
   z = z < 0 ? z + n : (z >= n ? z - n : z);
   y = y < 0 ? y + n : (y >= n ? y - n : y);
@@ -78,6 +86,7 @@ conv_mma_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const 
   float acc[NP / 8][4];
 #pragma unroll
   for (int j = 0; j < NP / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  const VoxDiv dv(n);
   for (int tap = 0; tap < NET_TAPS; ++tap) {
     const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
     __syncthreads();
@@ -87,7 +96,7 @@ conv_mma_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const 
       const int r = t / CH, c = t - r * CH;
       const long long v = v0 + r;
       uint4 val = make_uint4(0, 0, 0, 0);
-      if (v < V) val = *reinterpret_cast<const uint4*>(in + neighbour(v, n, dz, dy, dx) * KP + c * 8);
+      if (v < V) val = *reinterpret_cast<const uint4*>(in + neighbour(v, n, dz, dy, dx, dv) * KP + c * 8);
       *reinterpret_cast<uint4*>(sA + r * AS + c * 8) = val;
     }
     for (int t = threadIdx.x; t < NP * CH; t += CONV_THREADS) {
@@ -137,55 +146,88 @@ conv_mma_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const 
 }
 
 // ---------------------------------------------------------------------------
-// Weight gradient: dW[tap][ci][co] = sum_v in[v + tap][ci] g[v][co] with
-// per-CTA partials over voxel chunks, folded in a fixed order; db[co] = sum g.
+// Weight gradient on the tensor cores: for one tap, the KP x NP matrix
+//   dW[tap][ci][co] = sum_v in[v + tap][ci] g[v][co]
+// is a GEMM with the voxels as the reduction axis (A = in_shifted^T, B = g).
+// A CTA reduces one chunk of WG_CHUNK voxels for one tap: blocks of WG_VB
+// voxels are staged transposed ([channel][voxel], BF16) so the mma fragments
+// are 32-bit loads of voxel pairs; each warp owns KP*NP/(16*8*4) 16x8 output
+// tiles.  Partials per (chunk, tap) are folded in a fixed order
+// (wgrad_fold_kernel), so the result is deterministic.
 // ---------------------------------------------------------------------------
 constexpr int WG_CHUNK = 4096;
-constexpr int WG_SUB = 32;
+constexpr int WG_VB = 64;
 
 template <int KP, int NP>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
 wgrad_partial_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ g,
                      float* __restrict__ part) {
-  __shared__ float sx[WG_SUB][KP];
-  __shared__ float sg[WG_SUB][NP];
+  constexpr int VS = WG_VB + 8;  // padded voxel stride (bf16)
+  constexpr int MT = KP / 16, NT = NP / 8, TILES = MT * NT, TPW = TILES / 4;
+  static_assert(TILES % 4 == 0, "tiles must split over 4 warps");
+  __shared__ __align__(16) __nv_bfloat16 sX[KP * VS];
+  __shared__ __align__(16) __nv_bfloat16 sG[NP * VS];
   const int tap = blockIdx.y;
   const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
   const long long c0 = (long long)blockIdx.x * WG_CHUNK;
-  constexpr int PAIRS = KP * NP;
-  constexpr int PER = (PAIRS + 255) / 256;
-  float acc[PER];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  const VoxDiv dv(n);
+  float acc[TPW][4];
 #pragma unroll
-  for (int q = 0; q < PER; ++q) acc[q] = 0.f;
-  for (long long s0 = c0; s0 < c0 + WG_CHUNK && s0 < V; s0 += WG_SUB) {
+  for (int q = 0; q < TPW; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+  for (long long s0 = c0; s0 < c0 + WG_CHUNK && s0 < V; s0 += WG_VB) {
     __syncthreads();
-    for (int t = threadIdx.x; t < WG_SUB * KP; t += 256) {
-      const int r = t / KP, c = t - r * KP;
+    // stage transposed: 16-byte chunks of 8 channels of one voxel
+    for (int t = threadIdx.x; t < WG_VB * (KP / 8); t += blockDim.x) {
+      const int r = t / (KP / 8), c = t - r * (KP / 8);
       const long long v = s0 + r;
-      sx[r][c] = v < V ? __bfloat162float(in[neighbour(v, n, dz, dy, dx) * KP + c]) : 0.f;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (v < V) val = *reinterpret_cast<const uint4*>(in + neighbour(v, n, dz, dy, dx, dv) * KP + c * 8);
+      const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&val);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) sX[(c * 8 + i) * VS + r] = e[i];
     }
-    for (int t = threadIdx.x; t < WG_SUB * NP; t += 256) {
-      const int r = t / NP, c = t - r * NP;
+    for (int t = threadIdx.x; t < WG_VB * (NP / 8); t += blockDim.x) {
+      const int r = t / (NP / 8), c = t - r * (NP / 8);
       const long long v = s0 + r;
-      sg[r][c] = v < V ? __bfloat162float(g[v * NP + c]) : 0.f;
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (v < V) val = *reinterpret_cast<const uint4*>(g + v * NP + c * 8);
+      const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&val);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) sG[(c * 8 + i) * VS + r] = e[i];
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int p = threadIdx.x + q * 256;
-      if (p < PAIRS) {
-        const int ci = p / NP, co = p - ci * NP;
-        float a = acc[q];
-#pragma unroll 8
-        for (int r = 0; r < WG_SUB; ++r) a = fmaf(sx[r][ci], sg[r][co], a);
-        acc[q] = a;
+    for (int kk = 0; kk < WG_VB; kk += 16) {
+#pragma unroll
+      for (int q = 0; q < TPW; ++q) {
+        const int tile = warp * TPW + q;
+        const int mt = tile / NT, nt = tile - mt * NT;
+        const __nv_bfloat16* ar = sX + (mt * 16 + gid) * VS + kk + tig * 2;
+        unsigned a[4];
+        a[0] = ld32(ar);
+        a[1] = ld32(ar + 8 * VS);
+        a[2] = ld32(ar + 8);
+        a[3] = ld32(ar + 8 * VS + 8);
+        const __nv_bfloat16* br = sG + (nt * 8 + gid) * VS + kk + tig * 2;
+        mma_bf16(acc[q], a, ld32(br), ld32(br + 8));
       }
     }
   }
+  // C fragment: rows (ci) gid / gid + 8, columns (co) tig*2 + {0, 1}
+  float* out = part + ((long long)blockIdx.x * NET_TAPS + tap) * (KP * NP);
 #pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int p = threadIdx.x + q * 256;
-    if (p < PAIRS) part[((long long)blockIdx.x * NET_TAPS + tap) * PAIRS + p] = acc[q];
+  for (int q = 0; q < TPW; ++q) {
+    const int tile = warp * TPW + q;
+    const int mt = tile / NT, nt = tile - mt * NT;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int ci = mt * 16 + gid + h * 8, co = nt * 8 + tig * 2 + e;
+        out[ci * NP + co] = acc[q][h * 2 + e];
+      }
   }
 }
 
@@ -410,7 +452,7 @@ template <int KP, int NP>
 static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* g,
                          cudaStream_t st) {
   const int nchunk = (int)((V + WG_CHUNK - 1) / WG_CHUNK);
-  wgrad_partial_kernel<KP, NP><<<dim3(nchunk, 27), 256, 0, st>>>(V, n, in, g, net->wpart);
+  wgrad_partial_kernel<KP, NP><<<dim3(nchunk, 27), 128, 0, st>>>(V, n, in, g, net->wpart);
   wgrad_fold_kernel<KP, NP><<<(27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
   bgrad_kernel<NP><<<NP, 256, 0, st>>>(V, g, net->dB(l));
   return cudaGetLastError();

@@ -76,11 +76,87 @@ __global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __re
   }
 }
 
+// FP32 form of rk_stage_kernel with GRAD for n % 4 == 0: four consecutive
+// x cells per thread with 16-byte loads and stores (same arithmetic per
+// element, so the results are bitwise those of the scalar kernel).
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+template <bool STORE_K>
+__global__ void rk_stage4_kernel(int n, float inv_h, float* __restrict__ k, const float* __restrict__ p, int ppitch,
+                                 const float* __restrict__ x0, float* __restrict__ xs, float* __restrict__ xfin,
+                                 int stage, const double* __restrict__ dtp, SlotBatch sb) {
+  const long long N = (long long)n * n * n;
+  const int slot = blockIdx.y;
+  if (sb.active && !sb.active[slot]) return;
+  k += slot * sb.ustride;
+  x0 += slot * sb.ustride;
+  xs += slot * sb.ustride;
+  xfin += slot * sb.ustride;
+  p += slot * 2 * sb.wstride;
+  const double dt = dtp[slot];
+  const float cf = (float)((stage == 0 || stage == 3) ? dt / 6.0 : dt / 3.0);
+  const float cs = (float)(stage == 2 ? dt : 0.5 * dt);
+  const IdxDiv dn(n);
+  const long long Q = N / 4;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < Q; q += (long long)gridDim.x * blockDim.x) {
+    const long long g = 4 * q;
+    const long long r = dn.div(g);
+    const int x = (int)(g - r * n);
+    const int z = (int)dn.div(r);
+    const int y = (int)(r - (long long)z * n);
+    float4 k0 = ld4(k + g), k1 = ld4(k + N + g), k2 = ld4(k + 2 * N + g);
+    const float* prow = p + r * ppitch;
+    const float4 pc = ld4(prow + x);
+    const float pn = prow[x + 4 == n ? 0 : x + 4];
+    const float4 py = ld4(p + ((long long)z * n + wrap_up(y, n)) * ppitch + x);
+    const float4 pz = ld4(p + ((long long)wrap_up(z, n) * n + y) * ppitch + x);
+    k0.x -= (pc.y - pc.x) * inv_h; k0.y -= (pc.z - pc.y) * inv_h;
+    k0.z -= (pc.w - pc.z) * inv_h; k0.w -= (pn - pc.w) * inv_h;
+    k1.x -= (py.x - pc.x) * inv_h; k1.y -= (py.y - pc.y) * inv_h;
+    k1.z -= (py.z - pc.z) * inv_h; k1.w -= (py.w - pc.w) * inv_h;
+    k2.x -= (pz.x - pc.x) * inv_h; k2.y -= (pz.y - pc.y) * inv_h;
+    k2.z -= (pz.z - pc.z) * inv_h; k2.w -= (pz.w - pc.w) * inv_h;
+    if (STORE_K) {
+      st4(k + g, k0);
+      st4(k + N + g, k1);
+      st4(k + 2 * N + g, k2);
+    }
+    const float4 kk[3] = {k0, k1, k2};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float4 a = ld4(x0 + c * N + g), kc = kk[c];
+      float4 f;
+      if (stage == 0) {
+        f = make_float4(a.x + cf * kc.x, a.y + cf * kc.y, a.z + cf * kc.z, a.w + cf * kc.w);
+      } else {
+        f = ld4(xfin + c * N + g);
+        f.x += cf * kc.x; f.y += cf * kc.y; f.z += cf * kc.z; f.w += cf * kc.w;
+      }
+      st4(xfin + c * N + g, f);
+      if (stage < 3) st4(xs + c * N + g, make_float4(a.x + cs * kc.x, a.y + cs * kc.y, a.z + cs * kc.z, a.w + cs * kc.w));
+    }
+  }
+}
+
 template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
                             const double* dtp, cudaStream_t st, const SlotBatch& sb, int nslots, bool store_k) {
   long long N = (long long)n * n * n;
   dim3 grid(nslots > 1 ? std::min(grid_for(N), 152 * 8) : grid_for(N), nslots);
+  if constexpr (sizeof(T) == 4) {
+    if (p && n % 4 == 0) {
+      dim3 g4(nslots > 1 ? std::min(grid_for(N / 4), 152 * 8) : grid_for(N / 4), nslots);
+      const float ih = (float)(1.0 / (double)h);
+      if (store_k)
+        rk_stage4_kernel<true><<<g4, 256, 0, st>>>(n, ih, (float*)k, (const float*)p, ppitch, (const float*)x0,
+                                                   (float*)xs, (float*)xfin, stage, dtp, sb);
+      else
+        rk_stage4_kernel<false><<<g4, 256, 0, st>>>(n, ih, (float*)k, (const float*)p, ppitch, (const float*)x0,
+                                                    (float*)xs, (float*)xfin, stage, dtp, sb);
+      return cudaGetLastError();
+    }
+  }
   if (p && store_k)
     rk_stage_kernel<T, true><<<grid, 256, 0, st>>>(n, (T)(1.0 / (double)h), k, p, ppitch, x0, xs, xfin, stage, dtp, sb);
   else if (p)

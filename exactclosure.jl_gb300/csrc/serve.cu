@@ -41,22 +41,23 @@ __global__ void slot_maxabs_partial(long long count, const T* __restrict__ u, lo
   const int slot = blockIdx.y;
   if (!active[slot]) return;
   const T* x = u + slot * stride;
-  double m = 0.0;
+  // maximum in the field's word type (exact; no FP64-pipe work for FP32)
+  T m = (T)0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
-    double v = fabs((double)x[i]);
+    T v = fabs(x[i]);
     m = (v > m || v != v) ? v : m;
   }
-  __shared__ double red[8];
+  __shared__ T red[8];
   for (int o = 16; o > 0; o >>= 1) {
-    double w = __shfl_xor_sync(0xffffffffu, m, o);
+    T w = __shfl_xor_sync(0xffffffffu, m, o);
     m = (w > m || w != w) ? w : m;
   }
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double r = 0.0;
+    T r = (T)0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = (red[w] > r || red[w] != red[w]) ? red[w] : r;
-    part[slot * SRV_RED + blockIdx.x] = r;
+    part[slot * SRV_RED + blockIdx.x] = (double)r;
   }
 }
 

@@ -143,25 +143,27 @@ cudaError_t launch_gradient(int n, T h, T* u, const T* p, int ppitch, cudaStream
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void maxabs_partial_kernel(size_t count, const T* __restrict__ x, double* __restrict__ partial) {
-  __shared__ double red[32];
-  double m = 0.0;
+  // the maximum is taken in the field's own word type (exact), so an FP32
+  // field costs no FP64-pipe work
+  __shared__ T red[32];
+  T m = (T)0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
-    double v = fabs((double)x[i]);
+    T v = fabs(x[i]);
     m = (v > m || v != v) ? v : m;  // NaN propagates
   }
   for (int o = 16; o > 0; o >>= 1) {
-    double w = __shfl_xor_sync(0xffffffffu, m, o);
+    T w = __shfl_xor_sync(0xffffffffu, m, o);
     m = (w > m || w != w) ? w : m;
   }
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x < 32) {
-    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : (T)0;
     for (int o = 16; o > 0; o >>= 1) {
-      double w = __shfl_xor_sync(0xffffffffu, m, o);
+      T w = __shfl_xor_sync(0xffffffffu, m, o);
       m = (w > m || w != w) ? w : m;
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+    if (threadIdx.x == 0) partial[blockIdx.x] = (double)m;
   }
 }
 

@@ -169,17 +169,27 @@ __device__ __forceinline__ void zsolve_tile(cplx<T>* s, int ls, int lines, int w
   for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
     const int kz = pow2 ? t >> wlog : t / lines, l = t - kz * lines;
     int kx = kx0 + l;
-    double f;
-    if (invlap) {
-      // precomputed 1/(lambda N), one float64 per mode ([kz][ky][kx])
-      f = invlap[((long long)kz * n + ky) * nkx + kx];
-    } else {
-      double den = sin2[kx] + sy + sin2[kz];
-      f = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef * recip_f64(den);
-    }
     C v = s[l * ls + pe(kz)];
-    v.x = (T)((double)v.x * f);
-    v.y = (T)((double)v.y * f);
+    const long long mi = ((long long)kz * n + ky) * nkx + kx;
+    if (sizeof(T) == 4 && invlap) {
+      // FP32 form: the float64 factor 1/(lambda N) stored as hi + lo floats;
+      // v (hi + lo) with one FMA keeps the factor's float64 precision up to
+      // the final float rounding, without FP64-pipe work
+      const float2 f2 = reinterpret_cast<const float2*>(invlap)[mi];
+      v.x = (T)fmaf((float)v.x, f2.x, (float)v.x * f2.y);
+      v.y = (T)fmaf((float)v.y, f2.x, (float)v.y * f2.y);
+    } else {
+      double f;
+      if (invlap) {
+        // precomputed 1/(lambda N), one float64 per mode ([kz][ky][kx])
+        f = invlap[mi];
+      } else {
+        double den = sin2[kx] + sy + sin2[kz];
+        f = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef * recip_f64(den);
+      }
+      v.x = (T)((double)v.x * f);
+      v.y = (T)((double)v.y * f);
+    }
     s[l * ls + pe(kz)] = v;
   }
   __syncthreads();
@@ -289,6 +299,17 @@ __global__ void copy_pitched_kernel(const T* __restrict__ src, int pitch, T* __r
 }
 
 // 1/(lambda N) on the half spectrum [kz][ky][kx], 0 for the mean mode.
+// In place: each float64 factor f becomes the float pair (hi, lo) with
+// hi = fl32(f), lo = fl32(f - hi) (FP32 solvers).
+__global__ void invlap_split_kernel(long long tot, double* __restrict__ t) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
+    const double f = t[g];
+    const float hi = (float)f;
+    const float lo = (float)(f - (double)hi);
+    reinterpret_cast<float2*>(t)[g] = make_float2(hi, lo);
+  }
+}
+
 __global__ void invlap_kernel(int n, const double* __restrict__ sin2, double coef, double* __restrict__ out) {
   const int nkx = n / 2 + 1;
   const long long tot = (long long)n * n * nkx;
@@ -489,6 +510,8 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
     const double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
     const long long tot = (long long)n * n * (n / 2 + 1);
     invlap_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152LL * 32), 256>>>(n, ps->sin2, coef, ps->invlap);
+    if (precision == EXC_F32)
+      invlap_split_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152LL * 32), 256>>>(tot, ps->invlap);
   }
   size_t wbytes = (size_t)n * n * ps->P * csz;
   if (work) {

@@ -58,7 +58,12 @@ __global__ void rk_stage_kernel(int n, T inv_h, T* __restrict__ k, const T* __re
         k[2 * N + g] = k2;
       }
     }
-    T a0 = x0[g], a1 = x0[N + g], a2 = x0[2 * N + g];
+    T a0 = 0, a1 = 0, a2 = 0;  // x0 is not read at stage 3
+    if (stage < 3) {
+      a0 = x0[g];
+      a1 = x0[N + g];
+      a2 = x0[2 * N + g];
+    }
     if (stage == 0) {
       xfin[g] = a0 + cf * k0;
       xfin[N + g] = a1 + cf * k1;
@@ -125,7 +130,8 @@ __global__ void rk_stage4_kernel(int n, float inv_h, float* __restrict__ k, cons
     const float4 kk[3] = {k0, k1, k2};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const float4 a = ld4(x0 + c * N + g), kc = kk[c];
+      const float4 kc = kk[c];
+      const float4 a = stage < 3 ? ld4(x0 + c * N + g) : make_float4(0.f, 0.f, 0.f, 0.f);  // unused at stage 3
       float4 f;
       if (stage == 0) {
         f = make_float4(a.x + cf * kc.x, a.y + cf * kc.y, a.z + cf * kc.z, a.w + cf * kc.w);

@@ -271,7 +271,8 @@ __global__ void oa_kernel(const T* __restrict__ tb3, int n, int c, Taps1D taps, 
     const int ix = (int)(g - r * m);
     const int iz = (int)dm.div(r), iy = (int)(r - (long long)iz * m);
     const int own = comp == 0 ? ix : (comp == 1 ? iy : iz);
-    double acc = 0.0;
+    // accumulate in the field's word type (FP32 form: no FP64-pipe work)
+    T acc = (T)0;
     for (int t = 0; t < taps.cnt; ++t) {
       int fi = c * own + taps.off[t];
       fi = fi >= n ? fi - n : (fi < 0 ? fi + n : fi);
@@ -279,9 +280,9 @@ __global__ void oa_kernel(const T* __restrict__ tb3, int n, int c, Taps1D taps, 
       if (comp == 0) idx = ((long long)iz * m + iy) * n + fi;
       else if (comp == 1) idx = ((long long)iz * n + fi) * m + ix;
       else idx = ((long long)fi * m + iy) * m + ix;
-      acc += taps.w[t] * (double)tb[idx];
+      acc += (T)taps.w[t] * tb[idx];
     }
-    out3[comp * M + g] = (T)(acc * scale);
+    out3[comp * M + g] = acc * (T)scale;
   }
 }
 

@@ -13,7 +13,7 @@ struct exc_poisson {
   void* work = nullptr;    // complex [n][n][P]; real view [n][n][2P]
   void* tw = nullptr;      // W_n^m, m < n (precision's complex type)
   double* sin2 = nullptr;  // sin^2(pi k / n), k < n
-  double* invlap = nullptr;  // 1/(lambda N) per half-spectrum mode, or null (computed on the fly)
+  double* invlap = nullptr;  // 1/(lambda N) per half-spectrum mode (FP32 solvers: float (hi, lo) pairs), or null
   exc::FftPlan plan_n{}, plan_h{};
   bool external_work = false;
   int col_w = 0, x_rows = 0;  // tuned launch geometry (0 = default)

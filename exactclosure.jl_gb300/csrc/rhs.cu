@@ -16,16 +16,22 @@ namespace exc {
 
 constexpr int PTX = 32, PTY = 8, PTZ = 32;
 constexpr int PBX = PTX + 2, PBY = PTY + 2;  // plane box with one-cell halo (box x = x - x0 + 1)
+// u rows in shared memory: box x index xb sits at xb + SH<T>, so the 32
+// interior cells start on a 16-byte boundary and arrive by 16-byte copies
+template <typename T> constexpr int SH = 16 / (int)sizeof(T) - 1;
+template <typename T> constexpr int UROW = ((SH<T> + PBX) + 16 / (int)sizeof(T) - 1) / (16 / (int)sizeof(T)) *
+                                           (16 / (int)sizeof(T));
 
 template <typename T>
 struct PlaneSmem {
-  T u[3][3][PBY][PBX];
+  __align__(16) T u[3][3][PBY][UROW<T>];
   T s[5][PBY][PBX];  // s11, s22, s12, s13, s23 of the current plane
 };
 
 // sigma_ii at box (bx, by) of plane buffer b (uses u_i at the cell and at -e_i)
 template <typename T, int I>
-__device__ __forceinline__ T sdiag(const T (&u)[3][PBY][PBX], int bx, int by, T kd, T kv2) {
+__device__ __forceinline__ T sdiag(const T (&u)[3][PBY][UROW<T>], int bx, int by, T kd, T kv2) {
+  bx += SH<T>;
   const T a = u[I][by][bx];
   const T b = I == 0 ? u[0][by][bx - 1] : u[1][by - 1][bx];
   const T s = a + b, d = a - b;
@@ -33,21 +39,24 @@ __device__ __forceinline__ T sdiag(const T (&u)[3][PBY][PBX], int bx, int by, T 
 }
 // sigma_12 at box (bx, by): u1, u1(+y), u2, u2(+x)
 template <typename T>
-__device__ __forceinline__ T s12(const T (&u)[3][PBY][PBX], int bx, int by, T kd, T kv) {
+__device__ __forceinline__ T s12(const T (&u)[3][PBY][UROW<T>], int bx, int by, T kd, T kv) {
+  bx += SH<T>;
   const T a = u[0][by][bx], b = u[0][by + 1][bx], c = u[1][by][bx], d = u[1][by][bx + 1];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
 }
 // sigma_13 at box (bx, by): u1, u1(+z) [next plane], u3, u3(+x)
 template <typename T>
-__device__ __forceinline__ T s13(const T (&uc)[3][PBY][PBX], const T (&un)[3][PBY][PBX], int bx, int by, T kd,
-                                 T kv) {
+__device__ __forceinline__ T s13(const T (&uc)[3][PBY][UROW<T>], const T (&un)[3][PBY][UROW<T>], int bx, int by,
+                                 T kd, T kv) {
+  bx += SH<T>;
   const T a = uc[0][by][bx], b = un[0][by][bx], c = uc[2][by][bx], d = uc[2][by][bx + 1];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
 }
 // sigma_23 at box (bx, by): u2, u2(+z) [next plane], u3, u3(+y)
 template <typename T>
-__device__ __forceinline__ T s23(const T (&uc)[3][PBY][PBX], const T (&un)[3][PBY][PBX], int bx, int by, T kd,
-                                 T kv) {
+__device__ __forceinline__ T s23(const T (&uc)[3][PBY][UROW<T>], const T (&un)[3][PBY][UROW<T>], int bx, int by,
+                                 T kd, T kv) {
+  bx += SH<T>;
   const T a = uc[1][by][bx], b = un[1][by][bx], c = uc[2][by][bx], d = uc[2][by + 1][bx];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
 }
@@ -89,17 +98,38 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   // asynchronous copy of plane gz (with halo) into buffer buf; the caller
   // commits and waits (cp_async_wait_all) before the __syncthreads that
   // publishes it
+  // full x tiles of a grid whose rows are 16-byte multiples take the row
+  // interiors as 16-byte copies (VE words each) and the two halo cells as
+  // words; other tiles copy word by word
+  constexpr int VE = 16 / (int)sizeof(T), NV = PTX / VE;
+  const bool vec = big && x0 + PTX <= n && (n % VE) == 0;
+  const int cl = wrap(x0 - 1), cr = wrap(x0 + PTX);
+  const int tid = ty * PTX + tx;
   auto load_plane = [&](int buf, int gz) {
     const long long pz = (long long)gz * n;
+    if (vec) {
+      for (int t = tid; t < 3 * PBY * (NV + 2); t += PTX * PTY) {
+        const int c = t / (PBY * (NV + 2));
+        const int rem = t - c * (PBY * (NV + 2));
+        const int rr = rem / (NV + 2), j = rem - rr * (NV + 2);
+        const int gy = wrap(y0 - 1 + rr);
+        const T* row = u + c * N + (pz + gy) * n;
+        T* srow = &sm.u[buf][c][rr][SH<T>];
+        if (j < NV) cp_async_16(srow + 1 + j * VE, row + x0 + j * VE);
+        else if (j == NV) cp_async_word(srow, row + cl);
+        else cp_async_word(srow + PTX + 1, row + cr);
+      }
+    } else {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const T* p = u + c * N;
-      const long long oa = (pz + ra) * n, ob = (pz + rb) * n;
-      cp_async_word(&sm.u[buf][c][ty][tx], p + oa + ca);
-      if (xr) cp_async_word(&sm.u[buf][c][ty][tx + PTX], p + oa + cb);
-      if (yr) {
-        cp_async_word(&sm.u[buf][c][ty + PTY][tx], p + ob + ca);
-        if (xr) cp_async_word(&sm.u[buf][c][ty + PTY][tx + PTX], p + ob + cb);
+      for (int c = 0; c < 3; ++c) {
+        const T* p = u + c * N;
+        const long long oa = (pz + ra) * n, ob = (pz + rb) * n;
+        cp_async_word(&sm.u[buf][c][ty][tx + SH<T>], p + oa + ca);
+        if (xr) cp_async_word(&sm.u[buf][c][ty][tx + PTX + SH<T>], p + oa + cb);
+        if (yr) {
+          cp_async_word(&sm.u[buf][c][ty + PTY][tx + SH<T>], p + ob + ca);
+          if (xr) cp_async_word(&sm.u[buf][c][ty + PTY][tx + PTX + SH<T>], p + ob + cb);
+        }
       }
     }
     cp_async_commit();
@@ -115,7 +145,7 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   __syncthreads();
   T s13_prev = s13<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
   T s23_prev = s23<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
-  T s33_cur = s33<T>(sm.u[1][2][by][bx], sm.u[0][2][by][bx], kd, kv2);
+  T s33_cur = s33<T>(sm.u[1][2][by][bx + SH<T>], sm.u[0][2][by][bx + SH<T>], kd, kv2);
   __syncthreads();  // buffer 0 is refilled by the first prefetch
   // buffers: cur = plane z, nxt = plane z + 1, pre = the free one
   int cur = 1, nxt = 2, pre = 0;
@@ -135,7 +165,7 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     const T v12 = s12<T>(uc, bx, by, kd, kv);
     const T v13 = s13<T>(uc, un, bx, by, kd, kv);
     const T v23 = s23<T>(uc, un, bx, by, kd, kv);
-    const T v33n = s33<T>(un[2][by][bx], uc[2][by][bx], kd, kv2);
+    const T v33n = s33<T>(un[2][by][bx + SH<T>], uc[2][by][bx + SH<T>], kd, kv2);
     sm.s[0][by][bx] = v11;
     sm.s[1][by][bx] = v22;
     sm.s[2][by][bx] = v12;

@@ -465,7 +465,7 @@ cudaError_t configure_fft() {
 }
 
 int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
-  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
   if (!(l > 0)) { set_last_error("domain size must be positive"); return EXC_ERR_ARG; }
   if (precision != EXC_F64 && precision != EXC_F32) { set_last_error("bad precision"); return EXC_ERR_ARG; }
   ps->precision = precision;

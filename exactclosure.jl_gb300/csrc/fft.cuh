@@ -23,7 +23,8 @@ template <typename C> constexpr int fft_tile() { return 32768 / (int)sizeof(C); 
 __host__ __device__ __forceinline__ int pe(int e) { return e + (e >> 3); }
 __host__ __device__ __forceinline__ int padded_len(int L) { return L + (L >> 3) + 1; }
 // Pass sequence of a length-L transform: n8 radix-8 passes, then at most one
-// radix-4 or radix-2 pass, then n3 radix-3 passes (L = 8^n8 4^n4 2^n2 3^n3).
+// radix-4 or radix-2 pass, then n3 radix-3 and n5 radix-5 passes
+// (L = 8^n8 4^n4 2^n2 3^n3 5^n5).
 // The pass index math divides by nb = L/R and by Ns (the product of the
 // earlier radices); both divisions use multiply-high reciprocals
 // ceil(2^32/d), exact for every quotient here (dividends < 2^17, d <= 2^11;
@@ -31,7 +32,7 @@ __host__ __device__ __forceinline__ int padded_len(int L) { return L + (L >> 3) 
 constexpr int FFT_MAX_PASSES = 12;
 struct FftPlan {
   int L;
-  int n8, n4, n2, n3;
+  int n8, n4, n2, n3, n5;
   unsigned rnb[FFT_MAX_PASSES], rns[FFT_MAX_PASSES];
   unsigned rL, rL1, rhalf, r2L;  // reciprocals of L, L + 1, L/2 + 1, 2L (row splits of the x passes)
 };
@@ -42,18 +43,21 @@ __device__ __forceinline__ unsigned fast_div(unsigned x, unsigned r) { return r 
 inline FftPlan make_plan(int L) {
   FftPlan p{};
   p.L = L;
-  int m = L, a = 0, b = 0;
+  int m = L, a = 0, b = 0, c5 = 0;
   while (m % 2 == 0) { m /= 2; ++a; }
   while (m % 3 == 0) { m /= 3; ++b; }
+  while (m % 5 == 0) { m /= 5; ++c5; }
   p.n8 = a / 3;
   p.n4 = (a % 3) == 2;
   p.n2 = (a % 3) == 1;
   p.n3 = b;
+  p.n5 = c5;
   int radix[FFT_MAX_PASSES], np = 0;
   for (int q = 0; q < p.n8; ++q) radix[np++] = 8;
   if (p.n4) radix[np++] = 4;
   if (p.n2) radix[np++] = 2;
   for (int q = 0; q < p.n3; ++q) radix[np++] = 3;
+  for (int q = 0; q < p.n5; ++q) radix[np++] = 5;
   int Ns = 1;
   for (int q = 0; q < np; ++q) {
     p.rnb[q] = fast_recip((unsigned)(L / radix[q]));
@@ -85,6 +89,23 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft_small
     v[0] = cadd(v[0], t1);
     v[1] = cadd(t2, t3);
     v[2] = csub(t2, t3);
+  } else if constexpr (R == 5) {
+    // X1 = a1 - i b1, X4 = a1 + i b1, X2 = a2 - i b2, X3 = a2 + i b2 (forward)
+    const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;  // cos(2 pi/5), cos(4 pi/5)
+    const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;   // sin(2 pi/5), sin(4 pi/5)
+    const C t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+    const C t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+    C a1, a2, b1, b2;
+    a1.x = v[0].x + c1 * t1.x + c2 * t2.x; a1.y = v[0].y + c1 * t1.y + c2 * t2.y;
+    a2.x = v[0].x + c2 * t1.x + c1 * t2.x; a2.y = v[0].y + c2 * t1.y + c1 * t2.y;
+    b1.x = s1 * t3.x + s2 * t4.x; b1.y = s1 * t3.y + s2 * t4.y;
+    b2.x = s2 * t3.x - s1 * t4.x; b2.y = s2 * t3.y - s1 * t4.y;
+    const C ib1 = mul_mi<INV>(b1), ib2 = mul_mi<INV>(b2);
+    v[0] = cadd(v[0], cadd(t1, t2));
+    v[1] = cadd(a1, ib1);
+    v[4] = csub(a1, ib1);
+    v[2] = cadd(a2, ib2);
+    v[3] = csub(a2, ib2);
   } else if constexpr (R == 4) {
     C t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
     C t2 = cadd(v[1], v[3]), t3 = mul_mi<INV>(csub(v[1], v[3]));
@@ -252,6 +273,7 @@ __device__ void fft_lines(C* s, int ls, int nlines, const FftPlan& plan,
   if (plan.n4) { fft_pass<4, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 4; ++p; }
   if (plan.n2) { fft_pass<2, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 2; ++p; }
   for (int q = 0; q < plan.n3; ++q, ++p) { fft_pass<3, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 3; }
+  for (int q = 0; q < plan.n5; ++q, ++p) { fft_pass<5, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 5; }
 }
 
 }  // namespace exc

@@ -77,3 +77,25 @@ def test_even_ratio_rejected(NS):
     with pytest.raises(ExcError) as ei:
         NS.DnsAid(48, 1.0, 1e-3, 4)
     assert ei.value.code == 3
+
+
+def test_reference_ratio_5_grid(NS):
+    """The reference's own dnsaid_project setup uses n_dns = 500, n_les = 100
+    (ratio 5, src/N.jl:718); the radix-5 FFT runs the same ratio here at
+    n = 50 -> 10 against the oracle, one warm-up and two lockstep steps."""
+    n, c, l, visc, cfl = 50, 5, 1.0, 2e-4, 0.4
+    m = n // c
+    fdelta = ns.gaussian(l / n, 2 * l / m, 2)
+    u0 = ns.randomfield(n, l, -5 / 3, 3, 1.0, profile="power")
+    d = NS.DnsAid(n, l, visc, c, fdelta)
+    d.set_velocity(u0)
+    d.warmup(1.0, cfl, max_steps=1)
+    u, t, _ = ns.dnsaid_warmup(u0, visc, l, 1.0, cfl, max_steps=1)
+    assert rel(d.velocity(), u) < 1e-12
+    d.start()
+    les = ns.dnsaid_start(u, l, c, fdelta)
+    d.step(1.0, cfl, max_steps=2)
+    u, les, _, _ = ns.dnsaid_project_steps(u, les, visc, l, c, 1.0, cfl, fdelta, max_steps=2)
+    assert rel(d.velocity(), u) < 1e-12
+    for key in ns.DNSAID_NAMES:
+        assert rel(d.get(key), les[key]) < 1e-12, key

@@ -146,6 +146,123 @@ conv_mma_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const 
 }
 
 // ---------------------------------------------------------------------------
+// The same convolution with the input staged once per CTA: a CTA owns a
+// 4 x 4 x 4 voxel block of one sample and loads its 6 x 6 x 6 halo tile
+// (all input channels) into shared memory once; the 27 taps then read their
+// shifted rows from the tile, and the weights arrive one 3 x 3 tap plane
+// (9 taps) at a time.  Used when n % 4 == 0.
+// ---------------------------------------------------------------------------
+constexpr int TB = 4;            // block edge (voxels)
+constexpr int TH = TB + 2;       // halo tile edge
+constexpr int TVOX = TH * TH * TH;
+
+template <int KP, int NP, int EPI>
+__global__ void __launch_bounds__(CONV_THREADS)
+conv_tile_kernel(int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
+                 const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
+                 const float* __restrict__ pre_prev, int nout_valid) {
+  constexpr int AS = KP + 8;  // padded row stride (bf16) against bank conflicts
+  constexpr int CH = KP / 8;  // 16-byte chunks per voxel row
+  __shared__ __align__(16) __nv_bfloat16 sT[TVOX * AS];
+  __shared__ __align__(16) __nv_bfloat16 sW[9 * NP * AS];
+  const int nb = n / TB;
+  const long long N = (long long)n * n * n;
+  int blk = blockIdx.x;
+  const int bxb = blk % nb; blk /= nb;
+  const int byb = blk % nb; blk /= nb;
+  const int bzb = blk % nb;
+  const int b = blk / nb;
+  const int x0 = bxb * TB, y0 = byb * TB, z0 = bzb * TB;
+  const __nv_bfloat16* inb = in + (long long)b * N * KP;
+  // halo tile
+  for (int t = threadIdx.x; t < TVOX * CH; t += CONV_THREADS) {
+    const int vox = t / CH, c = t - vox * CH;
+    const int tx = vox % TH, ty = (vox / TH) % TH, tz = vox / (TH * TH);
+    int gx = x0 - 1 + tx, gy = y0 - 1 + ty, gz = z0 - 1 + tz;
+    gx = gx < 0 ? gx + n : (gx >= n ? gx - n : gx);
+    gy = gy < 0 ? gy + n : (gy >= n ? gy - n : gy);
+    gz = gz < 0 ? gz + n : (gz >= n ? gz - n : gz);
+    const long long gv = ((long long)gz * n + gy) * n + gx;
+    *reinterpret_cast<uint4*>(sT + vox * AS + c * 8) = *reinterpret_cast<const uint4*>(inb + gv * KP + c * 8);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  // the two output rows of this lane: voxels r0 = warp*16 + gid and r0 + 8
+  const int r0 = warp * 16 + gid, r1 = r0 + 8;
+  const int l0x = r0 % TB, l0y = (r0 / TB) % TB, l0z = r0 / (TB * TB);
+  const int l1x = r1 % TB, l1y = (r1 / TB) % TB, l1z = r1 / (TB * TB);
+  float acc[NP / 8][4];
+#pragma unroll
+  for (int j = 0; j < NP / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  for (int dzp = 0; dzp < 3; ++dzp) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < 9 * NP * CH; t += CONV_THREADS) {
+      const int row = t / CH, c = t - row * CH;  // row = tap9 * NP + co
+      *reinterpret_cast<uint4*>(sW + row * AS + c * 8) =
+          *reinterpret_cast<const uint4*>(Wt + ((long long)(dzp * 9) * NP + row) * KP + c * 8);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int t9 = 0; t9 < 9; ++t9) {
+      const int dy = t9 / 3, dx = t9 - dy * 3;  // offsets + 1
+      const __nv_bfloat16* a0r = sT + (((l0z + dzp) * TH + (l0y + dy)) * TH + (l0x + dx)) * AS;
+      const __nv_bfloat16* a1r = sT + (((l1z + dzp) * TH + (l1y + dy)) * TH + (l1x + dx)) * AS;
+#pragma unroll
+      for (int kk = 0; kk < KP; kk += 16) {
+        unsigned a[4];
+        a[0] = ld32(a0r + kk + tig * 2);
+        a[1] = ld32(a1r + kk + tig * 2);
+        a[2] = ld32(a0r + kk + 8 + tig * 2);
+        a[3] = ld32(a1r + kk + 8 + tig * 2);
+#pragma unroll
+        for (int j = 0; j < NP / 8; ++j) {
+          const __nv_bfloat16* br = sW + (t9 * NP + j * 8 + gid) * AS + kk + tig * 2;
+          mma_bf16(acc[j], a, ld32(br), ld32(br + 8));
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NP / 8; ++j)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int lx = h ? l1x : l0x, ly = h ? l1y : l0y, lz = h ? l1z : l0z;
+      const long long v = (long long)b * N + ((long long)(z0 + lz) * n + (y0 + ly)) * n + (x0 + lx);
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int co = j * 8 + tig * 2 + e;
+        float x = acc[j][h * 2 + e];
+        if (EPI == 0) {
+          x += bias[co];
+          pre_out[v * NP + co] = x;
+          act_out[v * NP + co] = __float2bfloat16(gelu_f(x));
+        } else if (EPI == 1) {
+          x += bias[co];
+          pre_out[v * NP + co] = co < nout_valid ? x : 0.f;
+        } else {
+          act_out[v * NP + co] = __float2bfloat16(x * gelu_grad_f(pre_prev[v * NP + co]));
+        }
+      }
+    }
+}
+
+// Launch the tiled convolution when the grid allows it, else the row form.
+template <int KP, int NP, int EPI>
+static void conv_launch(long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* W, const float* bias,
+                        float* pre_out, __nv_bfloat16* act_out, const float* pre_prev, int nout_valid,
+                        cudaStream_t st) {
+  if (n % TB == 0) {
+    const long long N = (long long)n * n * n;
+    const long long blocks = (V / N) * (N / (TB * TB * TB));
+    conv_tile_kernel<KP, NP, EPI><<<(unsigned)blocks, CONV_THREADS, 0, st>>>(n, in, W, bias, pre_out, act_out,
+                                                                          pre_prev, nout_valid);
+  } else {
+    conv_mma_kernel<KP, NP, EPI><<<(unsigned)((V + CONV_M - 1) / CONV_M), CONV_THREADS, 0, st>>>(
+        V, n, in, W, bias, pre_out, act_out, pre_prev, nout_valid);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Weight gradient on the tensor cores: for one tap, the KP x NP matrix
 //   dW[tap][ci][co] = sum_v in[v + tap][ci] g[v][co]
 // is a GEMM with the voxels as the reduction axis (A = in_shifted^T, B = g).
@@ -242,20 +359,37 @@ __global__ void wgrad_fold_kernel(int nchunk, const float* __restrict__ part, fl
   dW[i] = (float)s;
 }
 
+// Bias gradient db[co] = sum_v g[v][co]: BG_BLOCKS blocks, each thread one
+// channel of 256/NP voxel lanes (coalesced rows of g), FP64 sums folded in a
+// fixed order (block tree, then blocks in order), so the result is
+// deterministic.
+constexpr int BG_BLOCKS = 304;
+
 template <int NP>
-__global__ void bgrad_kernel(long long V, const __nv_bfloat16* __restrict__ g, float* __restrict__ db) {
-  // one block per channel, fixed-order tree
+__global__ void __launch_bounds__(256) bgrad_partial_kernel(long long V, const __nv_bfloat16* __restrict__ g,
+                                                            double* __restrict__ part) {
+  constexpr int LANES = 256 / NP;
   __shared__ double red[256];
-  const int co = blockIdx.x;
+  const int co = threadIdx.x % NP, vl = threadIdx.x / NP;
   double s = 0;
-  for (long long v = threadIdx.x; v < V; v += 256) s += (double)__bfloat162float(g[v * NP + co]);
+  for (long long v = (long long)blockIdx.x * LANES + vl; v < V; v += (long long)gridDim.x * LANES)
+    s += (double)__bfloat162float(g[v * NP + co]);
   red[threadIdx.x] = s;
   __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+  for (int o = LANES / 2; o > 0; o >>= 1) {
+    if (vl < o) red[threadIdx.x] += red[threadIdx.x + o * NP];
     __syncthreads();
   }
-  if (threadIdx.x == 0) db[co] = (float)red[0];
+  if (vl == 0) part[(long long)blockIdx.x * NP + co] = red[threadIdx.x];
+}
+
+template <int NP>
+__global__ void bgrad_fold_kernel(int nblk, const double* __restrict__ part, float* __restrict__ db) {
+  const int co = threadIdx.x;
+  if (co >= NP) return;
+  double s = 0;
+  for (int b = 0; b < nblk; ++b) s += part[(long long)b * NP + co];
+  db[co] = (float)s;
 }
 
 // ---------------------------------------------------------------------------
@@ -434,17 +568,12 @@ static cudaError_t refresh(exc_net* net, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-static inline unsigned conv_grid(long long V) { return (unsigned)((V + CONV_M - 1) / CONV_M); }
 
 // forward from the packed input x0; leaves pre1, a1, pre2, a2, out
 static cudaError_t forward_packed(exc_net* net, long long V, int n, cudaStream_t st) {
-  const unsigned g = conv_grid(V);
-  conv_mma_kernel<16, 32, 0><<<g, CONV_THREADS, 0, st>>>(V, n, net->x0, net->Wt(0), net->B(0), net->pre1, net->a1,
-                                                          nullptr, 32);
-  conv_mma_kernel<32, 32, 0><<<g, CONV_THREADS, 0, st>>>(V, n, net->a1, net->Wt(1), net->B(1), net->pre2, net->a2,
-                                                          nullptr, 32);
-  conv_mma_kernel<32, 16, 1><<<g, CONV_THREADS, 0, st>>>(V, n, net->a2, net->Wt(2), net->B(2), net->out, nullptr,
-                                                          nullptr, 3);
+  conv_launch<16, 32, 0>(V, n, net->x0, net->Wt(0), net->B(0), net->pre1, net->a1, nullptr, 32, st);
+  conv_launch<32, 32, 0>(V, n, net->a1, net->Wt(1), net->B(1), net->pre2, net->a2, nullptr, 32, st);
+  conv_launch<32, 16, 1>(V, n, net->a2, net->Wt(2), net->B(2), net->out, nullptr, nullptr, 3, st);
   return cudaGetLastError();
 }
 
@@ -454,7 +583,10 @@ static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfl
   const int nchunk = (int)((V + WG_CHUNK - 1) / WG_CHUNK);
   wgrad_partial_kernel<KP, NP><<<dim3(nchunk, 27), 128, 0, st>>>(V, n, in, g, net->wpart);
   wgrad_fold_kernel<KP, NP><<<(27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
-  bgrad_kernel<NP><<<NP, 256, 0, st>>>(V, g, net->dB(l));
+  // the weight-gradient partials are folded by now: reuse their buffer
+  double* bpart = reinterpret_cast<double*>(net->wpart);
+  bgrad_partial_kernel<NP><<<BG_BLOCKS, 256, 0, st>>>(V, g, bpart);
+  bgrad_fold_kernel<NP><<<1, 32, 0, st>>>(BG_BLOCKS, bpart, net->dB(l));
   return cudaGetLastError();
 }
 
@@ -465,14 +597,11 @@ static cudaError_t backward(exc_net* net, long long V, int n, long long N, const
   loss_grad_kernel<T><<<lb, 256, 0, st>>>(V, N, net->out, target, 1.0 / net->out_scale, 1.0 / (3.0 * (double)V),
                                           net->g3, net->lpart);
   sum_kernel<<<1, 32, 0, st>>>(lb, net->lpart, 1.0 / (3.0 * (double)V), net->lpart + 1024);
-  const unsigned g = conv_grid(V);
   cudaError_t e = wgrad<32, 16>(net, 2, V, n, net->a2, net->g3, st);
   // input gradient of layer 3 times GELU'(pre2)
-  conv_mma_kernel<16, 32, 2><<<g, CONV_THREADS, 0, st>>>(V, n, net->g3, net->Wb(2), nullptr, nullptr, net->gp2,
-                                                          net->pre2, 32);
+  conv_launch<16, 32, 2>(V, n, net->g3, net->Wb(2), nullptr, nullptr, net->gp2, net->pre2, 32, st);
   if (e == cudaSuccess) e = wgrad<32, 32>(net, 1, V, n, net->a1, net->gp2, st);
-  conv_mma_kernel<32, 32, 2><<<g, CONV_THREADS, 0, st>>>(V, n, net->gp2, net->Wb(1), nullptr, nullptr, net->gp1,
-                                                          net->pre1, 32);
+  conv_launch<32, 32, 2>(V, n, net->gp2, net->Wb(1), nullptr, nullptr, net->gp1, net->pre1, 32, st);
   if (e == cudaSuccess) e = wgrad<16, 32>(net, 0, V, n, net->x0, net->gp1, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;

@@ -130,6 +130,13 @@ int exc_poisson_destroy(exc_poisson* ps) {
   return EXC_OK;
 }
 
+int exc_poisson_set_engine(exc_poisson* ps, int engine) {
+  if (!ps) { set_last_error("null solver"); return EXC_ERR_ARG; }
+  if (engine != 0 && engine != 1) { set_last_error("engine must be 0 (register passes where planned) or 1 (Stockham)"); return EXC_ERR_ARG; }
+  ps->engine = engine;
+  return EXC_OK;
+}
+
 int exc_poisson_solve(exc_poisson* ps, const void* d, void* p, void* stream) {
   if (!ps || !d || !p) { set_last_error("null argument"); return EXC_ERR_ARG; }
   cudaStream_t st = (cudaStream_t)stream;

@@ -170,7 +170,7 @@ __device__ __forceinline__ void zsolve_tile(cplx<T>* s, int ls, int lines, int w
     const int kz = pow2 ? t >> wlog : t / lines, l = t - kz * lines;
     int kx = kx0 + l;
     C v = s[l * ls + pe(kz)];
-    const long long mi = ((long long)kz * n + ky) * nkx + kx;
+    const long long mi = invlap_index(n, kz, ky, kx);
     if (sizeof(T) == 4 && invlap) {
       // FP32 form: the float64 factor 1/(lambda N) stored as hi + lo floats;
       // v (hi + lo) with one FMA keeps the factor's float64 precision up to
@@ -298,9 +298,8 @@ __global__ void copy_pitched_kernel(const T* __restrict__ src, int pitch, T* __r
   }
 }
 
-// 1/(lambda N) on the half spectrum [kz][ky][kx], 0 for the mean mode.
-// In place: each float64 factor f becomes the float pair (hi, lo) with
-// hi = fl32(f), lo = fl32(f - hi) (FP32 solvers).
+// In place: each float64 factor f of the 1/(lambda N) table becomes the
+// float pair (hi, lo) with hi = fl32(f), lo = fl32(f - hi) (FP32 solvers).
 __global__ void invlap_split_kernel(long long tot, double* __restrict__ t) {
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
     const double f = t[g];
@@ -310,13 +309,16 @@ __global__ void invlap_split_kernel(long long tot, double* __restrict__ t) {
   }
 }
 
+// 1/(lambda N) for kz, ky <= n/2 and kx <= n/2 ([kz][ky][kx], invlap_index),
+// 0 for the mean mode; sin2 is mirrored (sin2[n-k] == sin2[k]), so these
+// entries are the factors of every mode.
 __global__ void invlap_kernel(int n, const double* __restrict__ sin2, double coef, double* __restrict__ out) {
   const int nkx = n / 2 + 1;
-  const long long tot = (long long)n * n * nkx;
+  const long long tot = (long long)nkx * nkx * nkx;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
     const int kx = (int)(g % nkx);
     const long long r = g / nkx;
-    const int ky = (int)(r % n), kz = (int)(r / n);
+    const int ky = (int)(r % nkx), kz = (int)(r / nkx);
     out[g] = (kx == 0 && ky == 0 && kz == 0) ? 0.0 : coef / (sin2[kx] + sin2[ky] + sin2[kz]);
   }
 }
@@ -351,6 +353,8 @@ template <typename T>
 cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st,
                                   const SlotBatch& sb, int nslots) {
   using C = cplx<T>;
+  if (ps->engine == 0 && ps->twl_n && ps->twl_h && ps->invlap)
+    return fftreg_solve(ps, src, src_is_vector, st, sb, nslots);
   const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
   C* g = reinterpret_cast<C*>(ps->work);
   const C* tw = reinterpret_cast<const C*>(ps->tw);
@@ -461,7 +465,42 @@ static cudaError_t configure_fft_t() {
 cudaError_t configure_fft() {
   cudaError_t e = configure_fft_t<double>();
   if (e == cudaSuccess) e = configure_fft_t<float>();
+  if (e == cudaSuccess) e = configure_fftreg_f64();
+  if (e == cudaSuccess) e = configure_fftreg_f32();
   return e;
+}
+
+// Level twiddles of a length-L register plan with first factor N1:
+// tl[k1 N2 + m2] = W_L^(m2 k1), from long double.
+template <typename C>
+static std::vector<C> level_table(int L, int N1) {
+  const int N2 = L / N1;
+  std::vector<C> t((size_t)L);
+  const long double pi_l = 3.141592653589793238462643383279502884L;
+  for (int k1 = 0; k1 < N1; ++k1)
+    for (int m2 = 0; m2 < N2; ++m2) {
+      const long double a = -2.0L * pi_l * (long double)((m2 * k1) % L) / (long double)L;
+      C w;
+      w.x = (decltype(w.x))cosl(a);
+      w.y = (decltype(w.y))sinl(a);
+      t[(size_t)k1 * N2 + m2] = w;
+    }
+  return t;
+}
+
+template <typename C>
+static int alloc_level_tables(exc_poisson* ps) {
+  const int n = ps->n;
+  const std::vector<C> tn = level_table<C>(n, reg_split_host(n));
+  const std::vector<C> th = level_table<C>(n / 2, reg_split_host(n / 2));
+  if (cudaMalloc(&ps->twl_n, tn.size() * sizeof(C)) != cudaSuccess ||
+      cudaMalloc(&ps->twl_h, th.size() * sizeof(C)) != cudaSuccess) {
+    set_last_error("out of device memory (poisson level twiddles)");
+    return EXC_ERR_OOM;
+  }
+  cudaMemcpy(ps->twl_n, tn.data(), tn.size() * sizeof(C), cudaMemcpyHostToDevice);
+  cudaMemcpy(ps->twl_h, th.data(), th.size() * sizeof(C), cudaMemcpyHostToDevice);
+  return EXC_OK;
 }
 
 int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
@@ -488,8 +527,8 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
     double c = (double)cosl(a), s = (double)sinl(a);
     twd[m] = make_double2(c, s);
     twf[m] = make_float2((float)cosl(a), (float)sinl(a));
-    long double sn = sinl(pi_l * (long double)m / (long double)n);
-    s2[m] = (double)(sn * sn);
+    long double sn = sinl(pi_l * (long double)std::min(m, n - m) / (long double)n);
+    s2[m] = (double)(sn * sn);  // mirrored: s2[n - m] == s2[m]
   }
   if (cudaMalloc(&ps->tw, n * csz) != cudaSuccess || cudaMalloc(&ps->sin2, n * sizeof(double)) != cudaSuccess) {
     set_last_error("out of device memory (poisson tables)");
@@ -500,18 +539,23 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
              cudaMemcpyHostToDevice);
   cudaMemcpy(ps->sin2, s2.data(), n * sizeof(double), cudaMemcpyHostToDevice);
   {
-    // 1/(lambda N) per half-spectrum mode, from an exact float64 division
-    const size_t tb = (size_t)n * n * (n / 2 + 1) * sizeof(double);
+    // 1/(lambda N) per mode with ky, kz folded to <= n/2 (lambda is even in
+    // each wavenumber), from an exact float64 division
+    const size_t tb = (size_t)(n / 2 + 1) * (n / 2 + 1) * (n / 2 + 1) * sizeof(double);
     if (cudaMalloc(&ps->invlap, tb) != cudaSuccess) {
       set_last_error("out of device memory (poisson inverse symbol)");
       poisson_free(ps);
       return EXC_ERR_OOM;
     }
     const double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
-    const long long tot = (long long)n * n * (n / 2 + 1);
+    const long long tot = (long long)(n / 2 + 1) * (n / 2 + 1) * (n / 2 + 1);
     invlap_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152LL * 32), 256>>>(n, ps->sin2, coef, ps->invlap);
     if (precision == EXC_F32)
       invlap_split_kernel<<<(int)std::min<long long>((tot + 255) / 256, 152LL * 32), 256>>>(tot, ps->invlap);
+  }
+  if (fftreg_supported(n, precision)) {
+    const int rc = precision == EXC_F64 ? alloc_level_tables<double2>(ps) : alloc_level_tables<float2>(ps);
+    if (rc) { poisson_free(ps); return rc; }
   }
   size_t wbytes = (size_t)n * n * ps->P * csz;
   if (work) {
@@ -535,6 +579,9 @@ void poisson_free(exc_poisson* ps) {
   if (ps->sin2) cudaFree(ps->sin2);
   if (ps->invlap) cudaFree(ps->invlap);
   ps->invlap = nullptr;
+  if (ps->twl_n) cudaFree(ps->twl_n);
+  if (ps->twl_h) cudaFree(ps->twl_h);
+  ps->twl_n = ps->twl_h = nullptr;
   if (ps->work && !ps->external_work) cudaFree(ps->work);
   ps->tw = nullptr;
   ps->sin2 = nullptr;

@@ -1,0 +1,38 @@
+// Register-resident FFT Poisson solve, FP32 instantiations (grids 32..1024).
+#include "fftreg.cuh"
+
+namespace exc {
+
+// Grids n with register plans for both the columns (L = n) and the x lines
+// (L = n/2): FP32 up to 1024, FP64 up to 256 (longer FP64 lines exceed the
+// register budget of one thread).
+int reg_split_host(int L) { return reg_split(L); }
+
+bool fftreg_supported(int n, int precision) {
+  if (n < 4 || (n & 1) || !reg_split(n) || !reg_split(n / 2)) return false;
+  return precision == EXC_F32 ? n <= 1024 : n <= 256;
+}
+
+#define EXC_REG_SIZES_F32(X) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024)
+
+cudaError_t fftreg_solve(exc_poisson* ps, const float* src, bool vec, cudaStream_t st, const SlotBatch& sb,
+                         int ns) {
+  switch (ps->n) {
+#define EXC_CASE(N) \
+  case N: return RegSolve<float, N>::solve(ps, src, vec, st, sb, ns);
+    EXC_REG_SIZES_F32(EXC_CASE)
+#undef EXC_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t configure_fftreg_f32() {
+  cudaError_t e = cudaSuccess;
+#define EXC_CONF(N) \
+  if (e == cudaSuccess) e = RegSolve<float, N>::configure();
+  EXC_REG_SIZES_F32(EXC_CONF)
+#undef EXC_CONF
+  return e;
+}
+
+}  // namespace exc

@@ -1,0 +1,28 @@
+// Register-resident FFT Poisson solve, FP64 instantiations (grids 32..256).
+#include "fftreg.cuh"
+
+namespace exc {
+
+#define EXC_REG_SIZES_F64(X) X(32) X(48) X(64) X(96) X(128) X(192) X(256)
+
+cudaError_t fftreg_solve(exc_poisson* ps, const double* src, bool vec, cudaStream_t st, const SlotBatch& sb,
+                         int ns) {
+  switch (ps->n) {
+#define EXC_CASE(N) \
+  case N: return RegSolve<double, N>::solve(ps, src, vec, st, sb, ns);
+    EXC_REG_SIZES_F64(EXC_CASE)
+#undef EXC_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t configure_fftreg_f64() {
+  cudaError_t e = cudaSuccess;
+#define EXC_CONF(N) \
+  if (e == cudaSuccess) e = RegSolve<double, N>::configure();
+  EXC_REG_SIZES_F64(EXC_CONF)
+#undef EXC_CONF
+  return e;
+}
+
+}  // namespace exc

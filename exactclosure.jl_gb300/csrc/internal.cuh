@@ -13,13 +13,29 @@ struct exc_poisson {
   void* work = nullptr;    // complex [n][n][P]; real view [n][n][2P]
   void* tw = nullptr;      // W_n^m, m < n (precision's complex type)
   double* sin2 = nullptr;  // sin^2(pi k / n), k < n
-  double* invlap = nullptr;  // 1/(lambda N) per half-spectrum mode (FP32 solvers: float (hi, lo) pairs), or null
+  double* invlap = nullptr;  // 1/(lambda N) per mode at invlap_index (FP32 solvers: float (hi, lo) pairs), or null
   exc::FftPlan plan_n{}, plan_h{};
   bool external_work = false;
-  int col_w = 0, x_rows = 0;  // tuned launch geometry (0 = default)
+  int col_w = 0, x_rows = 0;  // tuned launch geometry of the shared-memory passes (0 = default)
+  // register-resident passes (fftreg.cuh): level twiddle tables of the
+  // column lines (L = n) and the x lines (L = n/2), null when the grid has
+  // no register plan; engine 0 uses them when present, 1 forces the
+  // shared-memory passes
+  void* twl_n = nullptr;
+  void* twl_h = nullptr;
+  int engine = 0;
 };
 
 namespace exc {
+
+// Entry of mode (kz, ky, kx) in the 1/(lambda N) table: lambda depends on
+// sin^2(pi k/n), even in k, so ky and kz fold to min(k, n - k) and the table
+// holds (n/2 + 1)^3 entries [kz][ky][kx].
+__host__ __device__ __forceinline__ long long invlap_index(int n, int kz, int ky, int kx) {
+  const int h = n / 2;
+  const int fz = kz <= h ? kz : n - kz, fy = ky <= h ? ky : n - ky;
+  return ((long long)fz * (h + 1) + fy) * (h + 1) + kx;
+}
 
 // Allocate/free the device tables of a solver; `work` may be supplied by the
 // caller (external_work) and is otherwise allocated here.
@@ -32,6 +48,17 @@ void poisson_free(exc_poisson* ps);
 template <typename T>
 cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st,
                                   const SlotBatch& sb = SlotBatch(), int nslots = 1);
+
+// The same solve on the register-resident passes (fftreg_f32.cu,
+// fftreg_f64.cu); only for grids with fftreg_supported(n, precision).
+bool fftreg_supported(int n, int precision);
+int reg_split_host(int L);  // first factor N1 of a line length L with a register plan, else 0
+cudaError_t fftreg_solve(exc_poisson* ps, const float* src, bool src_is_vector, cudaStream_t st, const SlotBatch& sb,
+                         int nslots);
+cudaError_t fftreg_solve(exc_poisson* ps, const double* src, bool src_is_vector, cudaStream_t st, const SlotBatch& sb,
+                         int nslots);
+cudaError_t configure_fftreg_f32();
+cudaError_t configure_fftreg_f64();
 
 // Plain forward (half spectrum into ps->work) and unnormalised inverse (reals
 // at pitch 2P in ps->work) 3-D transforms.

@@ -99,12 +99,14 @@ class PoissonSolver:
     """``poissonsolver(grid, backend)`` (``src/N.jl:202-220``): owns the
     spectral work array and FFT tables of one grid on the device."""
 
-    def __init__(self, grid: Grid, precision: int = EXC_F64):
+    def __init__(self, grid: Grid, precision: int = EXC_F64, engine: int = 0):
         self.grid = grid
         self.precision = precision
         h = C.c_void_p()
         call("exc_poisson_create", precision, grid.n, grid.l, C.byref(h))
         self._h = h
+        if engine:
+            call("exc_poisson_set_engine", h, engine)
 
     def solve(self, p, d):
         """``p`` with ``L_h p = d`` and zero mean (``src/N.jl:262-301``)."""
@@ -129,8 +131,8 @@ class PoissonSolver:
             pass
 
 
-def poissonsolver(grid: Grid, precision: int = EXC_F64) -> PoissonSolver:
-    return PoissonSolver(grid, precision)
+def poissonsolver(grid: Grid, precision: int = EXC_F64, engine: int = 0) -> PoissonSolver:
+    return PoissonSolver(grid, precision, engine)
 
 
 def project(u, poisson: PoissonSolver, p=None):

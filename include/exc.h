@@ -87,6 +87,12 @@ int exc_pressuregradient(int precision, int n, double l, void* u, const void* p,
 typedef struct exc_poisson exc_poisson;
 int exc_poisson_create(int precision, int n, double l, exc_poisson** out);
 int exc_poisson_destroy(exc_poisson* ps);
+/* FFT engine of a solver (no counterpart in the reference): 0 = register-
+ * resident two-level passes where the grid has a plan (n = 32, 48, 64, 96,
+ * 128, 192, 256 and, in FP32, 384, 512, 1024), shared-memory Stockham passes
+ * otherwise (the default); 1 = Stockham passes for every grid.  Results agree
+ * to round-off; the autotuner of the serving form picks per grid. */
+int exc_poisson_set_engine(exc_poisson* ps, int engine);
 /* p with L_h p = d, mean(p) = 0 (src/N.jl:262-301).  d and p may alias. */
 int exc_poisson_solve(exc_poisson* ps, const void* d, void* p, void* stream);
 /* In-place projection u <- u - grad L^-1 div u (`project!`, src/N.jl:256-307).

@@ -1,36 +1,46 @@
 // RHS sweep: du = doadd*du - div sigma(u) (`stresstensor` + `tensordivergence!`,
 // src/N.jl:94-160), marching along z.
 //
-// A CTA owns a TX x TY column of cells and walks TZ planes.  Three plane
-// buffers of u with a one-cell x/y halo sit in shared memory: planes z and
-// z+1 are read while plane z+2 streams in with cp.async; each thread
-// evaluates the six stress components at its own cell (the edge stresses s13,
-// s23 and the diagonal s33 of the next plane are kept in registers for the
-// next plane), four warps evaluate the halo stresses lane-parallel, and the
-// divergence is formed from shared memory and registers.  Every stress value
-// is computed once (plus the x/y halo), index arithmetic is per plane, and
-// global loads and stores are row-contiguous.  Stresses are kept divided by h.
+// A CTA of 32 x 8 threads owns a PTX x PTY column of cells (PTY = 8 CY, CY
+// cells per thread along y) and walks PTZ planes.  Three plane buffers of u
+// with a one-cell x/y halo sit in shared memory: planes z and z+1 are read
+// while plane z+2 streams in with cp.async; each thread evaluates the six
+// stress components at its own cells (the edge stresses s13, s23 and the
+// diagonal s33 of the next plane are kept in registers for the next plane),
+// six warps evaluate the halo stresses lane-parallel (one task per warp), and
+// the divergence is formed from shared memory and registers.  Every stress
+// value is computed once (plus the x/y halo), copy offsets are computed once
+// per thread, and global loads and stores are row-contiguous.  Stresses are
+// kept divided by h.
 #include "internal.cuh"
 
 namespace exc {
 
-constexpr int PTX = 32, PTY = 8, PTZ = 32;
-constexpr int PBX = PTX + 2, PBY = PTY + 2;  // plane box with one-cell halo (box x = x - x0 + 1)
+constexpr int PTX = 32, PTZ = 32, NWARP = 8;
+constexpr int PBX = PTX + 2;  // plane box with one-cell halo (box x = x - x0 + 1)
 // u rows in shared memory: box x index xb sits at xb + SH<T>, so the 32
 // interior cells start on a 16-byte boundary and arrive by 16-byte copies
 template <typename T> constexpr int SH = 16 / (int)sizeof(T) - 1;
 template <typename T> constexpr int UROW = ((SH<T> + PBX) + 16 / (int)sizeof(T) - 1) / (16 / (int)sizeof(T)) *
                                            (16 / (int)sizeof(T));
+// cells per thread along y: two in FP32 (16-row tiles), one in FP64 (whose
+// three plane buffers of a 16-row tile would exceed 48 KB of static shared
+// memory)
+template <typename T> constexpr int CY = sizeof(T) == 4 ? 2 : 1;
+template <typename T> constexpr int PTYT = NWARP * CY<T>;
+template <typename T> constexpr int PBYT = PTYT<T> + 2;
 
 template <typename T>
 struct PlaneSmem {
-  __align__(16) T u[3][3][PBY][UROW<T>];
-  T s[5][PBY][PBX];  // s11, s22, s12, s13, s23 of the current plane
+  __align__(16) T u[3][3][PBYT<T>][UROW<T>];
+  T s[5][PBYT<T>][PBX];  // s11, s22, s12, s13, s23 of the current plane
 };
+
+template <typename T> using UPlane = T[3][PBYT<T>][UROW<T>];
 
 // sigma_ii at box (bx, by) of plane buffer b (uses u_i at the cell and at -e_i)
 template <typename T, int I>
-__device__ __forceinline__ T sdiag(const T (&u)[3][PBY][UROW<T>], int bx, int by, T kd, T kv2) {
+__device__ __forceinline__ T sdiag(const UPlane<T>& u, int bx, int by, T kd, T kv2) {
   bx += SH<T>;
   const T a = u[I][by][bx];
   const T b = I == 0 ? u[0][by][bx - 1] : u[1][by - 1][bx];
@@ -39,23 +49,21 @@ __device__ __forceinline__ T sdiag(const T (&u)[3][PBY][UROW<T>], int bx, int by
 }
 // sigma_12 at box (bx, by): u1, u1(+y), u2, u2(+x)
 template <typename T>
-__device__ __forceinline__ T s12(const T (&u)[3][PBY][UROW<T>], int bx, int by, T kd, T kv) {
+__device__ __forceinline__ T s12(const UPlane<T>& u, int bx, int by, T kd, T kv) {
   bx += SH<T>;
   const T a = u[0][by][bx], b = u[0][by + 1][bx], c = u[1][by][bx], d = u[1][by][bx + 1];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
 }
 // sigma_13 at box (bx, by): u1, u1(+z) [next plane], u3, u3(+x)
 template <typename T>
-__device__ __forceinline__ T s13(const T (&uc)[3][PBY][UROW<T>], const T (&un)[3][PBY][UROW<T>], int bx, int by,
-                                 T kd, T kv) {
+__device__ __forceinline__ T s13(const UPlane<T>& uc, const UPlane<T>& un, int bx, int by, T kd, T kv) {
   bx += SH<T>;
   const T a = uc[0][by][bx], b = un[0][by][bx], c = uc[2][by][bx], d = uc[2][by][bx + 1];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
 }
 // sigma_23 at box (bx, by): u2, u2(+z) [next plane], u3, u3(+y)
 template <typename T>
-__device__ __forceinline__ T s23(const T (&uc)[3][PBY][UROW<T>], const T (&un)[3][PBY][UROW<T>], int bx, int by,
-                                 T kd, T kv) {
+__device__ __forceinline__ T s23(const UPlane<T>& uc, const UPlane<T>& un, int bx, int by, T kd, T kv) {
   bx += SH<T>;
   const T a = uc[1][by][bx], b = un[1][by][bx], c = uc[2][by][bx], d = uc[2][by + 1][bx];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
@@ -67,10 +75,10 @@ __device__ __forceinline__ T s33(T up, T lo, T kd, T kv2) {
   return s * s * kd - kv2 * d;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(PTX * PTY)
-rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, int doadd, SlotBatch sb,
-           int zblocks) {
+template <typename T, bool DOADD>
+__global__ void __launch_bounds__(PTX * NWARP)
+rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks) {
+  constexpr int NC = CY<T>, PTY = PTYT<T>, PBY = PBYT<T>;
   __shared__ PlaneSmem<T> sm;
   const long long N = (long long)n * n * n;
   // slot of a batch of same-size solves (serving form): blockIdx.z = slot * zblocks + zb
@@ -88,69 +96,86 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   const T kv2 = (T)2 * kv;
   auto wrap = [n](int g) { return g < 0 ? g + n : (g >= n ? g - n : g); };
   auto wrapm = [n](int g) { return ((g % n) + n) % n; };
-  // per-thread load offsets within a plane: rows ty and ty + 8, columns tx and tx + 32
   const bool big = n >= PBX;
-  const int ra = big ? wrap(y0 - 1 + ty) : wrapm(y0 - 1 + ty);
-  const int rb = big ? wrap(y0 - 1 + ty + PTY) : wrapm(y0 - 1 + ty + PTY);
-  const int ca = big ? wrap(x0 - 1 + tx) : wrapm(x0 - 1 + tx);
-  const int cb = big ? wrap(x0 - 1 + tx + PTX) : wrapm(x0 - 1 + tx + PTX);
-  const bool xr = tx < PBX - PTX, yr = ty < PBY - PTY;
   // asynchronous copy of plane gz (with halo) into buffer buf; the caller
   // commits and waits (cp_async_wait_all) before the __syncthreads that
-  // publishes it
-  // full x tiles of a grid whose rows are 16-byte multiples take the row
-  // interiors as 16-byte copies (VE words each) and the two halo cells as
-  // words; other tiles copy word by word
+  // publishes it.  Full x tiles of a grid whose rows are 16-byte multiples
+  // copy each box row as NV + 2 aligned 16-byte pieces: the interior, the
+  // piece ending at x0 - 1 (left halo in its last word) and the piece starting
+  // at x0 + PTX (right halo in its first word).  Each thread's pieces are the
+  // same in every plane: their offsets are computed once, and a plane adds
+  // gz n^2.  Other tiles copy word by word.
   constexpr int VE = 16 / (int)sizeof(T), NV = PTX / VE;
-  const bool vec = big && x0 + PTX <= n && (n % VE) == 0;
-  const int cl = wrap(x0 - 1), cr = wrap(x0 + PTX);
+  constexpr int NPIECE = 3 * PBY * (NV + 2);
+  constexpr int NSLOT = (NPIECE + PTX * NWARP - 1) / (PTX * NWARP);
+  const bool vec = big && x0 + PTX <= n && (n % VE) == 0 && (reinterpret_cast<uintptr_t>(u) & 15) == 0;
   const int tid = ty * PTX + tx;
-  auto load_plane = [&](int buf, int gz) {
-    const long long pz = (long long)gz * n;
-    if (vec) {
-      for (int t = tid; t < 3 * PBY * (NV + 2); t += PTX * PTY) {
+  long long goff[NSLOT];
+  int soff[NSLOT];
+  if (vec) {
+#pragma unroll
+    for (int i = 0; i < NSLOT; ++i) {
+      const int t = tid + i * PTX * NWARP;
+      goff[i] = -1;
+      soff[i] = 0;
+      if (t < NPIECE) {
         const int c = t / (PBY * (NV + 2));
         const int rem = t - c * (PBY * (NV + 2));
         const int rr = rem / (NV + 2), j = rem - rr * (NV + 2);
         const int gy = wrap(y0 - 1 + rr);
-        const T* row = u + c * N + (pz + gy) * n;
-        T* srow = &sm.u[buf][c][rr][SH<T>];
-        if (j < NV) cp_async_16(srow + 1 + j * VE, row + x0 + j * VE);
-        else if (j == NV) cp_async_word(srow, row + cl);
-        else cp_async_word(srow + PTX + 1, row + cr);
+        const int gx = j < NV ? x0 + j * VE : (j == NV ? wrap(x0 - VE) : wrap(x0 + PTX));
+        const int bx0 = j < NV ? SH<T> + 1 + j * VE : (j == NV ? 0 : SH<T> + 1 + PTX);
+        goff[i] = c * N + (long long)gy * n + gx;
+        soff[i] = (c * PBY + rr) * UROW<T> + bx0;
       }
-    } else {
+    }
+  }
+  const long long nn = (long long)n * n;
+  auto load_plane = [&](int buf, int gz) {
+    if (vec) {
+      T* const sb0 = &sm.u[buf][0][0][0];
+      const T* const ub = u + gz * nn;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const T* p = u + c * N;
-        const long long oa = (pz + ra) * n, ob = (pz + rb) * n;
-        cp_async_word(&sm.u[buf][c][ty][tx + SH<T>], p + oa + ca);
-        if (xr) cp_async_word(&sm.u[buf][c][ty][tx + PTX + SH<T>], p + oa + cb);
-        if (yr) {
-          cp_async_word(&sm.u[buf][c][ty + PTY][tx + SH<T>], p + ob + ca);
-          if (xr) cp_async_word(&sm.u[buf][c][ty + PTY][tx + PTX + SH<T>], p + ob + cb);
+      for (int i = 0; i < NSLOT; ++i)
+        if (goff[i] >= 0) cp_async_16(sb0 + soff[i], ub + goff[i]);
+    } else {
+      const long long pz = (long long)gz * n;
+      for (int rr = ty; rr < PBY; rr += NWARP) {
+        const int gy = big ? wrap(y0 - 1 + rr) : wrapm(y0 - 1 + rr);
+        for (int bxx = tx; bxx < PBX; bxx += PTX) {
+          const int gx = big ? wrap(x0 - 1 + bxx) : wrapm(x0 - 1 + bxx);
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            cp_async_word(&sm.u[buf][c][rr][bxx + SH<T>], u + c * N + (pz + gy) * n + gx);
         }
       }
     }
     cp_async_commit();
   };
   auto zwrap = [&](int z) { return big ? wrap(z) : wrapm(z); };
-  const int bx = tx + 1, by = ty + 1;
+  const int bx = tx + 1;
   // prologue: planes z0-1 (buffer 0) and z0 (buffer 1) give s13, s23 of plane
-  // z0-1 and s33 of plane z0 for this thread's cell
+  // z0-1 and s33 of plane z0 for this thread's cells
   load_plane(0, zwrap(z0 - 1));
   load_plane(1, zwrap(z0));
   load_plane(2, zwrap(z0 + 1));
   cp_async_wait_all();
   __syncthreads();
-  T s13_prev = s13<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
-  T s23_prev = s23<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
-  T s33_cur = s33<T>(sm.u[1][2][by][bx + SH<T>], sm.u[0][2][by][bx + SH<T>], kd, kv2);
+  T s13_prev[NC], s23_prev[NC], s33_cur[NC];
+#pragma unroll
+  for (int i = 0; i < NC; ++i) {
+    const int by = ty + 1 + NWARP * i;
+    s13_prev[i] = s13<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
+    s23_prev[i] = s23<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
+    s33_cur[i] = s33<T>(sm.u[1][2][by][bx + SH<T>], sm.u[0][2][by][bx + SH<T>], kd, kv2);
+  }
   __syncthreads();  // buffer 0 is refilled by the first prefetch
   // buffers: cur = plane z, nxt = plane z + 1, pre = the free one
   int cur = 1, nxt = 2, pre = 0;
-  const int gx = x0 + tx, gy = y0 + ty;
-  const bool inside = gx < n && gy < n;
+  const int gx = x0 + tx;
+  T* const du1 = du;
+  T* const du2 = du + N;
+  T* const du3 = du + 2 * N;
   for (int kz = 0; kz < PTZ; ++kz) {
     const int z = z0 + kz;
     if (z >= n) break;  // uniform across the CTA
@@ -160,19 +185,25 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     const auto& uc = sm.u[cur];
     const auto& un = sm.u[nxt];
     // own-cell stresses
-    const T v11 = sdiag<T, 0>(uc, bx, by, kd, kv2);
-    const T v22 = sdiag<T, 1>(uc, bx, by, kd, kv2);
-    const T v12 = s12<T>(uc, bx, by, kd, kv);
-    const T v13 = s13<T>(uc, un, bx, by, kd, kv);
-    const T v23 = s23<T>(uc, un, bx, by, kd, kv);
-    const T v33n = s33<T>(un[2][by][bx + SH<T>], uc[2][by][bx + SH<T>], kd, kv2);
-    sm.s[0][by][bx] = v11;
-    sm.s[1][by][bx] = v22;
-    sm.s[2][by][bx] = v12;
-    sm.s[3][by][bx] = v13;
-    sm.s[4][by][bx] = v23;
-    // halo stresses, lane-parallel: s12 on the lower row, s23 on the lower
-    // row, s22 on the upper row, and the column halos (s12, s13 left; s11 right)
+    T v11[NC], v22[NC], v12[NC], v13[NC], v23[NC], v33n[NC];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+      const int by = ty + 1 + NWARP * i;
+      v11[i] = sdiag<T, 0>(uc, bx, by, kd, kv2);
+      v22[i] = sdiag<T, 1>(uc, bx, by, kd, kv2);
+      v12[i] = s12<T>(uc, bx, by, kd, kv);
+      v13[i] = s13<T>(uc, un, bx, by, kd, kv);
+      v23[i] = s23<T>(uc, un, bx, by, kd, kv);
+      v33n[i] = s33<T>(un[2][by][bx + SH<T>], uc[2][by][bx + SH<T>], kd, kv2);
+      sm.s[0][by][bx] = v11[i];
+      sm.s[1][by][bx] = v22[i];
+      sm.s[2][by][bx] = v12[i];
+      sm.s[3][by][bx] = v13[i];
+      sm.s[4][by][bx] = v23[i];
+    }
+    // halo stresses, one task per warp: s12, s23 on the lower halo row, s22
+    // on the upper halo row, s12 and s13 on the left halo column, s11 on the
+    // right halo column
     if (warp == 0) {
       sm.s[2][0][lane + 1] = s12<T>(uc, lane + 1, 0, kd, kv);
     } else if (warp == 1) {
@@ -180,36 +211,39 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     } else if (warp == 2) {
       sm.s[1][PTY + 1][lane + 1] = sdiag<T, 1>(uc, lane + 1, PTY + 1, kd, kv2);
     } else if (warp == 3) {
-      if (lane <= PTY) {
-        sm.s[2][lane][0] = s12<T>(uc, 0, lane, kd, kv);
-      } else if (lane <= 2 * PTY) {
-        const int r = lane - PTY;
-        sm.s[3][r][0] = s13<T>(uc, un, 0, r, kd, kv);
-      } else if (lane <= 3 * PTY) {
-        const int r = lane - 2 * PTY;
-        sm.s[0][r][PTX + 1] = sdiag<T, 0>(uc, PTX + 1, r, kd, kv2);
-      }
+      if (lane <= PTY) sm.s[2][lane][0] = s12<T>(uc, 0, lane, kd, kv);
+    } else if (warp == 4) {
+      if (lane < PTY) sm.s[3][lane + 1][0] = s13<T>(uc, un, 0, lane + 1, kd, kv);
+    } else if (warp == 5) {
+      if (lane < PTY) sm.s[0][lane + 1][PTX + 1] = sdiag<T, 0>(uc, PTX + 1, lane + 1, kd, kv2);
     }
     __syncthreads();
-    if (inside) {
+    if (gx < n) {
       const auto& S = sm.s;
-      const T d1 = (S[0][by][bx + 1] - v11) + (v12 - S[2][by - 1][bx]) + (v13 - s13_prev);
-      const T d2 = (v12 - S[2][by][bx - 1]) + (S[1][by + 1][bx] - v22) + (v23 - s23_prev);
-      const T d3 = (v13 - S[3][by][bx - 1]) + (v23 - S[4][by - 1][bx]) + (v33n - s33_cur);
-      const long long g = ((long long)z * n + gy) * n + gx;
-      if (doadd) {
-        du[g] -= d1;
-        du[N + g] -= d2;
-        du[2 * N + g] -= d3;
-      } else {
-        du[g] = -d1;
-        du[N + g] = -d2;
-        du[2 * N + g] = -d3;
+#pragma unroll
+      for (int i = 0; i < NC; ++i) {
+        const int by = ty + 1 + NWARP * i;
+        const int gy = y0 + by - 1;
+        if (gy < n) {
+          const T d1 = (S[0][by][bx + 1] - v11[i]) + (v12[i] - S[2][by - 1][bx]) + (v13[i] - s13_prev[i]);
+          const T d2 = (v12[i] - S[2][by][bx - 1]) + (S[1][by + 1][bx] - v22[i]) + (v23[i] - s23_prev[i]);
+          const T d3 = (v13[i] - S[3][by][bx - 1]) + (v23[i] - S[4][by - 1][bx]) + (v33n[i] - s33_cur[i]);
+          const long long g = ((long long)z * n + gy) * n + gx;
+          if (DOADD) {
+            du1[g] -= d1;
+            du2[g] -= d2;
+            du3[g] -= d3;
+          } else {
+            du1[g] = -d1;
+            du2[g] = -d2;
+            du3[g] = -d3;
+          }
+        }
+        s13_prev[i] = v13[i];
+        s23_prev[i] = v23[i];
+        s33_cur[i] = v33n[i];
       }
     }
-    s13_prev = v13;
-    s23_prev = v23;
-    s33_cur = v33n;
     cp_async_wait_all();
     __syncthreads();
     const int freed = cur;
@@ -223,8 +257,11 @@ template <typename T>
 cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st, const SlotBatch& sb,
                        int nslots) {
   const int zblocks = (n + PTZ - 1) / PTZ;
-  dim3 grid((n + PTX - 1) / PTX, (n + PTY - 1) / PTY, zblocks * nslots);
-  rhs_kernel<T><<<grid, dim3(PTX, PTY), 0, st>>>(n, (T)(1.0 / (double)h), visc, u, du, doadd ? 1 : 0, sb, zblocks);
+  dim3 grid((n + PTX - 1) / PTX, (n + PTYT<T> - 1) / PTYT<T>, zblocks * nslots);
+  if (doadd)
+    rhs_kernel<T, true><<<grid, dim3(PTX, NWARP), 0, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks);
+  else
+    rhs_kernel<T, false><<<grid, dim3(PTX, NWARP), 0, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks);
   return cudaGetLastError();
 }
 

@@ -23,24 +23,21 @@ constexpr int PBX = PTX + 2;  // plane box with one-cell halo (box x = x - x0 + 
 template <typename T> constexpr int SH = 16 / (int)sizeof(T) - 1;
 template <typename T> constexpr int UROW = ((SH<T> + PBX) + 16 / (int)sizeof(T) - 1) / (16 / (int)sizeof(T)) *
                                            (16 / (int)sizeof(T));
-// cells per thread along y: two in FP32 (16-row tiles), one in FP64 (whose
-// three plane buffers of a 16-row tile would exceed 48 KB of static shared
-// memory)
-template <typename T> constexpr int CY = sizeof(T) == 4 ? 2 : 1;
-template <typename T> constexpr int PTYT = NWARP * CY<T>;
-template <typename T> constexpr int PBYT = PTYT<T> + 2;
+// NC cells per thread along y: a tile is PTY = 8 NC rows
+template <int NC> constexpr int PTYT = NWARP * NC;
+template <int NC> constexpr int PBYT = PTYT<NC> + 2;
 
-template <typename T>
+template <typename T, int NC>
 struct PlaneSmem {
-  __align__(16) T u[3][3][PBYT<T>][UROW<T>];
-  T s[5][PBYT<T>][PBX];  // s11, s22, s12, s13, s23 of the current plane
+  __align__(16) T u[3][3][PBYT<NC>][UROW<T>];
+  T s[5][PBYT<NC>][PBX];  // s11, s22, s12, s13, s23 of the current plane
 };
 
-template <typename T> using UPlane = T[3][PBYT<T>][UROW<T>];
+template <typename T, int NC> using UPlane = T[3][PBYT<NC>][UROW<T>];
 
 // sigma_ii at box (bx, by) of plane buffer b (uses u_i at the cell and at -e_i)
-template <typename T, int I>
-__device__ __forceinline__ T sdiag(const UPlane<T>& u, int bx, int by, T kd, T kv2) {
+template <typename T, int I, typename U>
+__device__ __forceinline__ T sdiag(const U& u, int bx, int by, T kd, T kv2) {
   bx += SH<T>;
   const T a = u[I][by][bx];
   const T b = I == 0 ? u[0][by][bx - 1] : u[1][by - 1][bx];
@@ -48,22 +45,22 @@ __device__ __forceinline__ T sdiag(const UPlane<T>& u, int bx, int by, T kd, T k
   return s * s * kd - kv2 * d;
 }
 // sigma_12 at box (bx, by): u1, u1(+y), u2, u2(+x)
-template <typename T>
-__device__ __forceinline__ T s12(const UPlane<T>& u, int bx, int by, T kd, T kv) {
+template <typename T, typename U>
+__device__ __forceinline__ T s12(const U& u, int bx, int by, T kd, T kv) {
   bx += SH<T>;
   const T a = u[0][by][bx], b = u[0][by + 1][bx], c = u[1][by][bx], d = u[1][by][bx + 1];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
 }
 // sigma_13 at box (bx, by): u1, u1(+z) [next plane], u3, u3(+x)
-template <typename T>
-__device__ __forceinline__ T s13(const UPlane<T>& uc, const UPlane<T>& un, int bx, int by, T kd, T kv) {
+template <typename T, typename U>
+__device__ __forceinline__ T s13(const U& uc, const U& un, int bx, int by, T kd, T kv) {
   bx += SH<T>;
   const T a = uc[0][by][bx], b = un[0][by][bx], c = uc[2][by][bx], d = uc[2][by][bx + 1];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
 }
 // sigma_23 at box (bx, by): u2, u2(+z) [next plane], u3, u3(+y)
-template <typename T>
-__device__ __forceinline__ T s23(const UPlane<T>& uc, const UPlane<T>& un, int bx, int by, T kd, T kv) {
+template <typename T, typename U>
+__device__ __forceinline__ T s23(const U& uc, const U& un, int bx, int by, T kd, T kv) {
   bx += SH<T>;
   const T a = uc[1][by][bx], b = un[1][by][bx], c = uc[2][by][bx], d = uc[2][by + 1][bx];
   return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
@@ -75,11 +72,12 @@ __device__ __forceinline__ T s33(T up, T lo, T kd, T kv2) {
   return s * s * kd - kv2 * d;
 }
 
-template <typename T, bool DOADD>
+template <typename T, int NC, bool DOADD>
 __global__ void __launch_bounds__(PTX * NWARP)
 rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks) {
-  constexpr int NC = CY<T>, PTY = PTYT<T>, PBY = PBYT<T>;
-  __shared__ PlaneSmem<T> sm;
+  constexpr int PTY = PTYT<NC>, PBY = PBYT<NC>;
+  extern __shared__ __align__(16) unsigned char rhs_smem[];
+  PlaneSmem<T, NC>& sm = *reinterpret_cast<PlaneSmem<T, NC>*>(rhs_smem);
   const long long N = (long long)n * n * n;
   // slot of a batch of same-size solves (serving form): blockIdx.z = slot * zblocks + zb
   const int slot = blockIdx.z / zblocks;
@@ -211,11 +209,11 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     } else if (warp == 2) {
       sm.s[1][PTY + 1][lane + 1] = sdiag<T, 1>(uc, lane + 1, PTY + 1, kd, kv2);
     } else if (warp == 3) {
-      if (lane <= PTY) sm.s[2][lane][0] = s12<T>(uc, 0, lane, kd, kv);
+      for (int r = lane; r <= PTY; r += 32) sm.s[2][r][0] = s12<T>(uc, 0, r, kd, kv);
     } else if (warp == 4) {
-      if (lane < PTY) sm.s[3][lane + 1][0] = s13<T>(uc, un, 0, lane + 1, kd, kv);
+      for (int r = lane + 1; r <= PTY; r += 32) sm.s[3][r][0] = s13<T>(uc, un, 0, r, kd, kv);
     } else if (warp == 5) {
-      if (lane < PTY) sm.s[0][lane + 1][PTX + 1] = sdiag<T, 0>(uc, PTX + 1, lane + 1, kd, kv2);
+      for (int r = lane + 1; r <= PTY; r += 32) sm.s[0][r][PTX + 1] = sdiag<T, 0>(uc, PTX + 1, r, kd, kv2);
     }
     __syncthreads();
     if (gx < n) {
@@ -253,19 +251,40 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   }
 }
 
+// Cells per thread along y: two in FP32 (16-row tiles; four ran slower at
+// 94 registers, two CTAs per SM), one in FP64 (where the sweep is bound by the
+// FP64 pipe, not by per-plane overhead).
+template <typename T> constexpr int CYT = sizeof(T) == 4 ? 2 : 1;
+
 template <typename T>
 cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st, const SlotBatch& sb,
                        int nslots) {
+  constexpr int NC = CYT<T>;
   const int zblocks = (n + PTZ - 1) / PTZ;
-  dim3 grid((n + PTX - 1) / PTX, (n + PTYT<T> - 1) / PTYT<T>, zblocks * nslots);
+  dim3 grid((n + PTX - 1) / PTX, (n + PTYT<NC> - 1) / PTYT<NC>, zblocks * nslots);
+  const size_t sh = sizeof(PlaneSmem<T, NC>);
   if (doadd)
-    rhs_kernel<T, true><<<grid, dim3(PTX, NWARP), 0, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks);
+    rhs_kernel<T, NC, true><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks);
   else
-    rhs_kernel<T, false><<<grid, dim3(PTX, NWARP), 0, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks);
+    rhs_kernel<T, NC, false><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks);
   return cudaGetLastError();
 }
 
-cudaError_t configure_stencil() { return cudaSuccess; }
+template <typename T>
+static cudaError_t configure_rhs_t() {
+  constexpr int NC = CYT<T>;
+  const int sh = (int)sizeof(PlaneSmem<T, NC>);
+  cudaError_t e = cudaFuncSetAttribute(rhs_kernel<T, NC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(rhs_kernel<T, NC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
+  return e;
+}
+
+cudaError_t configure_stencil() {
+  cudaError_t e = configure_rhs_t<float>();
+  if (e == cudaSuccess) e = configure_rhs_t<double>();
+  return e;
+}
 
 template cudaError_t launch_rhs<double>(int, double, double, const double*, double*, bool, cudaStream_t,
                                         const SlotBatch&, int);

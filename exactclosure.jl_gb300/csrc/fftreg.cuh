@@ -188,6 +188,10 @@ struct ColGeom {
   static constexpr int MINB0 = 65536 / (NT * REGS);
   static constexpr int MINB = MINB0 < 1 ? 1 : MINB0 > 4 ? 4 : MINB0;
   static constexpr int MINB_Z = MINB > 3 ? 3 : MINB;  // z pass: one more set of twiddles live
+  // z pass: the tile's 1/(lambda N) entries (8 bytes each) are prefetched
+  // into shared memory at kernel start when they fit in 32 KB
+  static constexpr bool TABS = (size_t)W * L * 8 <= 32768;
+  static constexpr size_t SMEM_Z = SMEM + (TABS ? (size_t)W * L * 8 : 0);
 };
 
 constexpr int pow2_floor(int x) {
@@ -209,6 +213,14 @@ struct XGeom {
   static constexpr int XS0 = N1 * (N2 + 1);
   static constexpr int XS = XS0 + (((N2 - XS0) % 16) + 16) % 16;
   static constexpr size_t SMEM = (size_t)RW * XS * 2 * sizeof(T);
+  // FP32 divergence pass: the RW rows (one z plane when RW divides n) of
+  // u_x, u_z, u_z(z-1) and RW + 1 rows of u_y are staged in shared memory by
+  // 16-byte cp.async copies, which keep every load in flight without holding
+  // registers; the exchange buffer reuses the staging area afterwards
+  static constexpr int NX = 2 * L;
+  static constexpr size_t STAGE_BYTES = (size_t)(4 * RW + 1) * NX * sizeof(T);
+  static constexpr bool STAGE = sizeof(T) == 4 && NX % RW == 0 && STAGE_BYTES <= 100 * 1024;
+  static constexpr size_t SMEM_DIV = STAGE && STAGE_BYTES > SMEM ? STAGE_BYTES : SMEM;
 };
 
 // ---------------------------------------------------------------------------
@@ -275,9 +287,10 @@ rzsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int ntx, int P, const cp
                const double* __restrict__ invlap, SlotBatch sb) {
   using C = cplx<T>;
   using G = ColGeom<T, N1, N2>;
-  constexpr int W = G::W;
+  constexpr int W = G::W, L = N1 * N2;
   extern __shared__ unsigned char smem_raw[];
   C* xs = reinterpret_cast<C*>(smem_raw);
+  double* tab = reinterpret_cast<double*>(smem_raw + G::SMEM);  // [kz][line], 8-byte entries
   if (sb.active && !sb.active[blockIdx.z]) return;
   g += blockIdx.z * sb.wstride;
   const long long es = (long long)n * P;
@@ -286,6 +299,13 @@ rzsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int ntx, int P, const cp
   C* const base = g + (long long)ky * P + kx0;
   const int tid = threadIdx.x, line = tid % W;
   const bool lv = line < lines;
+  if constexpr (G::TABS) {
+    for (int t = tid; t < L * W; t += G::NT) {
+      const int kz = t / W, l = t - kz * W;
+      if (l < lines) cp_async_word(&tab[t], invlap + invlap_index(n, kz, ky, kx0 + l));
+    }
+    cp_async_commit();
+  }
   if (tid < W * N2) {
     const int m2 = tid / W;
     const C* p = base + m2 * es + line;
@@ -299,6 +319,7 @@ rzsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int ntx, int P, const cp
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) xs[(k1 * N2 + m2) * W + line] = v[k1];
   }
+  if constexpr (G::TABS) cp_async_wait_all();
   __syncthreads();
   C v[N2];
   const int k1 = tid / W;
@@ -312,15 +333,17 @@ rzsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int ntx, int P, const cp
       const int kx = kx0 + line;
 #pragma unroll
       for (int k2 = 0; k2 < N2; ++k2) {
-        const long long mi = invlap_index(n, k1 + N1 * k2, ky, kx);
+        const int kz = k1 + N1 * k2;
+        const long long mi = G::TABS ? (long long)kz * W + line : invlap_index(n, kz, ky, kx);
+        const double* src_f = G::TABS ? tab : invlap;
         if constexpr (sizeof(T) == 4) {
           // float64 factor as hi + lo floats: v (hi + lo) with one FMA keeps
           // the factor's float64 precision up to the final float rounding
-          const float2 f = __ldg(reinterpret_cast<const float2*>(invlap) + mi);
+          const float2 f = reinterpret_cast<const float2*>(src_f)[mi];
           v[k2].x = fmaf(v[k2].x, f.x, v[k2].x * f.y);
           v[k2].y = fmaf(v[k2].y, f.x, v[k2].y * f.y);
         } else {
-          const double f = __ldg(invlap + mi);
+          const double f = src_f[mi];
           v[k2].x = (T)((double)v[k2].x * f);
           v[k2].y = (T)((double)v[k2].y * f);
         }
@@ -357,7 +380,7 @@ rzsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int ntx, int P, const cp
 // k = 0..L).  With DIV the row is d = div(u) (src/N.jl:222-238) computed on
 // the fly.  blockIdx.x = row block, blockIdx.y = slot.
 // ---------------------------------------------------------------------------
-template <typename T, int N1, int N2, bool DIV>
+template <typename T, int N1, int N2, bool DIV, bool STAGE = false>
 __global__ void __launch_bounds__(XGeom<T, N1, N2>::NT)
 rr2c_kernel(const T* __restrict__ src, T inv_h, cplx<T>* __restrict__ out, int P, const cplx<T>* __restrict__ tw,
             const cplx<T>* __restrict__ tl, SlotBatch sb) {
@@ -374,11 +397,56 @@ rr2c_kernel(const T* __restrict__ src, T inv_h, cplx<T>* __restrict__ out, int P
   constexpr long long nn = (long long)n * n, N = nn * n;
   const long long row0 = (long long)blockIdx.x * RW;
   const int tid = threadIdx.x;
+  if constexpr (STAGE) {
+    // rows row0 .. row0 + RW - 1: one z plane, y = y0 .. y0 + RW - 1
+    static_assert(DIV && G::STAGE, "staging is the FP32 divergence pass");
+    T* const sux = reinterpret_cast<T*>(smem_raw);
+    T* const suy = sux + RW * n;            // rows y0 - 1 .. y0 + RW - 1
+    T* const suz = suy + (RW + 1) * n;
+    T* const szm = suz + RW * n;            // u_z of plane z - 1
+    const int z = (int)(row0 / n), y0 = (int)(row0 - (long long)z * n);
+    const int zm = z == 0 ? n - 1 : z - 1;
+    const T* gx = src + row0 * n;
+    const T* gy = src + N + row0 * n;
+    const T* gz = src + 2 * N + row0 * n;
+    const T* gzm = src + 2 * N + ((long long)zm * n + y0) * n;
+    constexpr int PR = RW * n / 4;  // 16-byte pieces of RW rows
+    for (int t = tid; t < PR; t += G::NT) {
+      cp_async_16(sux + 4 * t, gx + 4 * t);
+      cp_async_16(suy + n + 4 * t, gy + 4 * t);
+      cp_async_16(suz + 4 * t, gz + 4 * t);
+      cp_async_16(szm + 4 * t, gzm + 4 * t);
+    }
+    const T* gyd = src + N + ((long long)z * n + (y0 == 0 ? n - 1 : y0 - 1)) * n;
+    for (int t = tid; t < n / 4; t += G::NT) cp_async_16(suy + 4 * t, gyd + 4 * t);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  C v[N1];
+  const int line = tid / N2, m2 = tid - line * N2;
   if (tid < RW * N2) {
-    const int line = tid / N2, m2 = tid - line * N2;
     const long long row = row0 + line;
-    C v[N1];
-    if (row < nn) {
+    if (STAGE) {
+      const T* ux = reinterpret_cast<const T*>(smem_raw) + line * n;
+      const T* uy = ux + RW * n;          // row y - 1 of the staged u_y
+      const T* uz = uy + (RW + 1) * n;
+      const T* uzm = uz + RW * n;
+      const T2* ux2 = reinterpret_cast<const T2*>(ux);
+      const T2* uy2 = reinterpret_cast<const T2*>(uy + n);
+      const T2* uyd = reinterpret_cast<const T2*>(uy);
+      const T2* uz2 = reinterpret_cast<const T2*>(uz);
+      const T2* uzd = reinterpret_cast<const T2*>(uzm);
+#pragma unroll
+      for (int m1 = 0; m1 < N1; ++m1) {
+        const int m = m2 + N2 * m1;
+        const int xm = (m == 0) ? n - 1 : 2 * m - 1;
+        const T2 a0 = ux2[m], b0 = uy2[m], b1 = uyd[m], c0 = uz2[m], c1 = uzd[m];
+        const T uxm = ux[xm];
+        v[m1].x = ((a0.x - uxm) + (b0.x - b1.x) + (c0.x - c1.x)) * inv_h;
+        v[m1].y = ((a0.y - a0.x) + (b0.y - b1.y) + (c0.y - c1.y)) * inv_h;
+      }
+    } else if (row < nn) {
       const long long base = row * n;
       if constexpr (!DIV) {
         const T2* s2 = reinterpret_cast<const T2*>(src + base);
@@ -413,6 +481,9 @@ rr2c_kernel(const T* __restrict__ src, T inv_h, cplx<T>* __restrict__ out, int P
     dft_reg<N1, false>(v);
 #pragma unroll
     for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], __ldg(&tl[k1 * N2 + m2]));
+  }
+  if constexpr (STAGE) __syncthreads();  // the staged rows are read; xs reuses them
+  if (tid < RW * N2) {
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) xs[line * XS + k1 * (N2 + 1) + m2] = v[k1];
   }
@@ -536,8 +607,9 @@ struct RegSolve {
     };
     set((const void*)rcols_kernel<T, A1, A2, false>, CG::SMEM);
     set((const void*)rcols_kernel<T, A1, A2, true>, CG::SMEM);
-    set((const void*)rzsolve_kernel<T, A1, A2>, CG::SMEM);
+    set((const void*)rzsolve_kernel<T, A1, A2>, CG::SMEM_Z);
     set((const void*)rr2c_kernel<T, B1, B2, true>, XG::SMEM);
+    if constexpr (XG::STAGE) set((const void*)rr2c_kernel<T, B1, B2, true, true>, XG::SMEM_DIV);
     set((const void*)rr2c_kernel<T, B1, B2, false>, XG::SMEM);
     set((const void*)rc2r_kernel<T, B1, B2>, XG::SMEM);
     return e;
@@ -553,14 +625,23 @@ struct RegSolve {
     const C* tlh = reinterpret_cast<const C*>(ps->twl_h);
     const long long nn = (long long)n * n;
     const dim3 gx((unsigned)((nn + XG::RW - 1) / XG::RW), ns);
-    if (vec)
+    bool staged = false;
+    if constexpr (XG::STAGE) {
+      // 16-byte copies need a 16-byte aligned field (slot strides 3 n^3 words keep it)
+      if (vec && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+        rr2c_kernel<T, B1, B2, true, true><<<gx, XG::NT, XG::SMEM_DIV, st>>>(src, (T)(1.0 / ps->h), g, P, tw, tlh, sb);
+        staged = true;
+      }
+    }
+    if (staged) {
+    } else if (vec)
       rr2c_kernel<T, B1, B2, true><<<gx, XG::NT, XG::SMEM, st>>>(src, (T)(1.0 / ps->h), g, P, tw, tlh, sb);
     else
       rr2c_kernel<T, B1, B2, false><<<gx, XG::NT, XG::SMEM, st>>>(src, (T)1, g, P, tw, tlh, sb);
     const int ntx = (nkx + CG::W - 1) / CG::W;
     const dim3 gc((unsigned)(ntx * n), 1, ns);
     rcols_kernel<T, A1, A2, false><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, sb);
-    rzsolve_kernel<T, A1, A2><<<gc, CG::NT, CG::SMEM, st>>>(g, n, nkx, ntx, P, tln, ps->invlap, sb);
+    rzsolve_kernel<T, A1, A2><<<gc, CG::NT, CG::SMEM_Z, st>>>(g, n, nkx, ntx, P, tln, ps->invlap, sb);
     rcols_kernel<T, A1, A2, true><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, sb);
     rc2r_kernel<T, B1, B2><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, sb);
     return cudaGetLastError();

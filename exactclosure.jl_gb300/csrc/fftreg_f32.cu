@@ -8,6 +8,13 @@ namespace exc {
 // register budget of one thread).
 int reg_split_host(int L) { return reg_split(L); }
 
+void fftreg_geometry_f64(int n, int* col_w, int* x_rows);
+void fftreg_geometry_f32(int n, int* col_w, int* x_rows);
+void fftreg_geometry(int n, int precision, int* col_w, int* x_rows) {
+  if (precision == EXC_F32) fftreg_geometry_f32(n, col_w, x_rows);
+  else fftreg_geometry_f64(n, col_w, x_rows);
+}
+
 bool fftreg_supported(int n, int precision) {
   if (n < 4 || (n & 1) || !reg_split(n) || !reg_split(n / 2)) return false;
   return precision == EXC_F32 ? n <= 1024 : n <= 256;
@@ -23,6 +30,20 @@ cudaError_t fftreg_solve(exc_poisson* ps, const float* src, bool vec, cudaStream
     EXC_REG_SIZES_F32(EXC_CASE)
 #undef EXC_CASE
     default: return cudaErrorInvalidValue;
+  }
+}
+
+void fftreg_geometry_f32(int n, int* col_w, int* x_rows) {
+  switch (n) {
+#define EXC_GEOM(N) \
+  case N:                                          \
+    *col_w = RegSolve<float, N>::CG::W;              \
+    *x_rows = RegSolve<float, N>::XG::RW;            \
+    return;
+    EXC_REG_SIZES_F32(EXC_GEOM)
+#undef EXC_GEOM
+    default:
+      *col_w = *x_rows = 0;
   }
 }
 

@@ -16,6 +16,20 @@ cudaError_t fftreg_solve(exc_poisson* ps, const double* src, bool vec, cudaStrea
   }
 }
 
+void fftreg_geometry_f64(int n, int* col_w, int* x_rows) {
+  switch (n) {
+#define EXC_GEOM(N) \
+  case N:                                          \
+    *col_w = RegSolve<double, N>::CG::W;              \
+    *x_rows = RegSolve<double, N>::XG::RW;            \
+    return;
+    EXC_REG_SIZES_F64(EXC_GEOM)
+#undef EXC_GEOM
+    default:
+      *col_w = *x_rows = 0;
+  }
+}
+
 cudaError_t configure_fftreg_f64() {
   cudaError_t e = cudaSuccess;
 #define EXC_CONF(N) \

@@ -57,6 +57,8 @@ cudaError_t fftreg_solve(exc_poisson* ps, const float* src, bool src_is_vector, 
                          int nslots);
 cudaError_t fftreg_solve(exc_poisson* ps, const double* src, bool src_is_vector, cudaStream_t st, const SlotBatch& sb,
                          int nslots);
+// Lines per column tile and rows per x-pass CTA of a grid's register plan.
+void fftreg_geometry(int n, int precision, int* col_w, int* x_rows);
 cudaError_t configure_fftreg_f32();
 cudaError_t configure_fftreg_f64();
 

@@ -1,8 +1,8 @@
 // RHS sweep: du = doadd*du - div sigma(u) (`stresstensor` + `tensordivergence!`,
 // src/N.jl:94-160), marching along z.
 //
-// A CTA of 32 x 8 threads owns a PTX x PTY column of cells (PTY = 8 CY, CY
-// cells per thread along y) and walks PTZ planes.  Three plane buffers of u
+// A CTA of 32 x 8 threads owns a PTX x PTY column of cells (PTY = 8 NC, NC
+// consecutive rows per thread) and walks PTZ planes.  Three plane buffers of u
 // with a one-cell x/y halo sit in shared memory: planes z and z+1 are read
 // while plane z+2 streams in with cp.async; each thread evaluates the six
 // stress components at its own cells (the edge stresses s13, s23 and the
@@ -73,7 +73,7 @@ __device__ __forceinline__ T s33(T up, T lo, T kd, T kv2) {
 }
 
 template <typename T, int NC, bool DOADD>
-__global__ void __launch_bounds__(PTX * NWARP)
+__global__ void __launch_bounds__(PTX * NWARP, 4)
 rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks) {
   constexpr int PTY = PTYT<NC>, PBY = PBYT<NC>;
   extern __shared__ __align__(16) unsigned char rhs_smem[];
@@ -162,7 +162,7 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   T s13_prev[NC], s23_prev[NC], s33_cur[NC];
 #pragma unroll
   for (int i = 0; i < NC; ++i) {
-    const int by = ty + 1 + NWARP * i;
+    const int by = NC * ty + 1 + i;
     s13_prev[i] = s13<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
     s23_prev[i] = s23<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
     s33_cur[i] = s33<T>(sm.u[1][2][by][bx + SH<T>], sm.u[0][2][by][bx + SH<T>], kd, kv2);
@@ -186,18 +186,20 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     T v11[NC], v22[NC], v12[NC], v13[NC], v23[NC], v33n[NC];
 #pragma unroll
     for (int i = 0; i < NC; ++i) {
-      const int by = ty + 1 + NWARP * i;
+      const int by = NC * ty + 1 + i;
       v11[i] = sdiag<T, 0>(uc, bx, by, kd, kv2);
       v22[i] = sdiag<T, 1>(uc, bx, by, kd, kv2);
       v12[i] = s12<T>(uc, bx, by, kd, kv);
       v13[i] = s13<T>(uc, un, bx, by, kd, kv);
       v23[i] = s23<T>(uc, un, bx, by, kd, kv);
       v33n[i] = s33<T>(un[2][by][bx + SH<T>], uc[2][by][bx + SH<T>], kd, kv2);
+      // s22 is read from the row above and s23 from the row below: inside a
+      // thread's rows they stay in registers
       sm.s[0][by][bx] = v11[i];
-      sm.s[1][by][bx] = v22[i];
+      if (i == 0) sm.s[1][by][bx] = v22[i];
       sm.s[2][by][bx] = v12[i];
       sm.s[3][by][bx] = v13[i];
-      sm.s[4][by][bx] = v23[i];
+      if (i == NC - 1) sm.s[4][by][bx] = v23[i];
     }
     // halo stresses, one task per warp: s12, s23 on the lower halo row, s22
     // on the upper halo row, s12 and s13 on the left halo column, s11 on the
@@ -220,12 +222,17 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
       const auto& S = sm.s;
 #pragma unroll
       for (int i = 0; i < NC; ++i) {
-        const int by = ty + 1 + NWARP * i;
+        const int by = NC * ty + 1 + i;
         const int gy = y0 + by - 1;
         if (gy < n) {
-          const T d1 = (S[0][by][bx + 1] - v11[i]) + (v12[i] - S[2][by - 1][bx]) + (v13[i] - s13_prev[i]);
-          const T d2 = (v12[i] - S[2][by][bx - 1]) + (S[1][by + 1][bx] - v22[i]) + (v23[i] - s23_prev[i]);
-          const T d3 = (v13[i] - S[3][by][bx - 1]) + (v23[i] - S[4][by - 1][bx]) + (v33n[i] - s33_cur[i]);
+          // a thread's cells are consecutive rows: the stresses of the row
+          // below and above come from registers where the thread owns them
+          const T s12_below = i > 0 ? v12[i > 0 ? i - 1 : 0] : S[2][by - 1][bx];
+          const T s22_above = i < NC - 1 ? v22[i < NC - 1 ? i + 1 : 0] : S[1][by + 1][bx];
+          const T s23_below = i > 0 ? v23[i > 0 ? i - 1 : 0] : S[4][by - 1][bx];
+          const T d1 = (S[0][by][bx + 1] - v11[i]) + (v12[i] - s12_below) + (v13[i] - s13_prev[i]);
+          const T d2 = (v12[i] - S[2][by][bx - 1]) + (s22_above - v22[i]) + (v23[i] - s23_prev[i]);
+          const T d3 = (v13[i] - S[3][by][bx - 1]) + (v23[i] - s23_below) + (v33n[i] - s33_cur[i]);
           const long long g = ((long long)z * n + gy) * n + gx;
           if (DOADD) {
             du1[g] -= d1;

@@ -197,9 +197,12 @@ class Chunk : public ChunkBase {
   }
 };
 
-// autotuned (col_w, x_rows) per (n, precision, S)
+// autotuned FFT engine and Stockham tile shape per (n, precision, S)
+struct Tuned {
+  int engine, col_w, x_rows;
+};
 static std::mutex g_tune_mu;
-static std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tuned;
+static std::map<std::tuple<int, int, int>, Tuned> g_tuned;
 
 }  // namespace exc
 
@@ -234,8 +237,9 @@ static int tune_chunk(exc_server* sv, Chunk<T>* ck) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
     if (it != g_tuned.end()) {
-      ck->ps.col_w = it->second.first;
-      ck->ps.x_rows = it->second.second;
+      ck->ps.engine = it->second.engine;
+      ck->ps.col_w = it->second.col_w;
+      ck->ps.x_rows = it->second.x_rows;
       return EXC_OK;
     }
   }
@@ -249,30 +253,37 @@ static int tune_chunk(exc_server* sv, Chunk<T>* ck) {
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  float best = 1e30f;
-  int bw = wmax, br = rmax;
+  // candidates: the register-resident passes (where the grid has a plan) and
+  // the Stockham passes over the tile shapes above
+  std::vector<Tuned> cands;
+  if (ck->ps.twl_n && ck->ps.twl_h) cands.push_back({0, 0, 0});
   for (int w : ws)
-    for (int r : rs) {
-      ck->ps.col_w = w;
-      ck->ps.x_rows = r;
-      poisson_solve_inplace<T>(&ck->ps, ck->rhs, true, ck->stream, ck->batch(), ck->S);  // warm
-      cudaEventRecord(a, ck->stream);
-      for (int rep = 0; rep < 3; ++rep) poisson_solve_inplace<T>(&ck->ps, ck->rhs, true, ck->stream, ck->batch(), ck->S);
-      cudaEventRecord(b, ck->stream);
-      cudaEventSynchronize(b);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, a, b);
-      if (ms < best) { best = ms; bw = w; br = r; }
-    }
+    for (int r : rs) cands.push_back({1, w, r});
+  float best = 1e30f;
+  Tuned bc = cands.front();
+  for (const Tuned& c : cands) {
+    ck->ps.engine = c.engine;
+    ck->ps.col_w = c.col_w;
+    ck->ps.x_rows = c.x_rows;
+    poisson_solve_inplace<T>(&ck->ps, ck->rhs, true, ck->stream, ck->batch(), ck->S);  // warm
+    cudaEventRecord(a, ck->stream);
+    for (int rep = 0; rep < 3; ++rep) poisson_solve_inplace<T>(&ck->ps, ck->rhs, true, ck->stream, ck->batch(), ck->S);
+    cudaEventRecord(b, ck->stream);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) { best = ms; bc = c; }
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   set_active_kernel<<<1, 64, 0, ck->stream>>>(ck->S, 0ull, ck->active);
-  ck->ps.col_w = bw;
-  ck->ps.x_rows = br;
+  ck->ps.engine = bc.engine;
+  ck->ps.col_w = bc.col_w;
+  ck->ps.x_rows = bc.x_rows;
   cudaError_t e = cudaStreamSynchronize(ck->stream);
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tuned[key] = {bw, br};
+  g_tuned[key] = bc;
   return EXC_OK;
 }
 
@@ -651,13 +662,18 @@ int exc_server_stats(exc_server* sv, exc_server_info* st) {
   return EXC_OK;
 }
 
-int exc_server_tuning(int precision, int n, int slots, int* col_w, int* x_rows) {
-  if (!col_w || !x_rows) { set_last_error("null argument"); return EXC_ERR_ARG; }
+int exc_server_tuning(int precision, int n, int slots, int* engine, int* col_w, int* x_rows) {
+  if (!engine || !col_w || !x_rows) { set_last_error("null argument"); return EXC_ERR_ARG; }
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tuned.find(std::make_tuple(n, precision, slots));
   if (it == g_tuned.end()) { set_last_error("no tuning recorded for this size"); return EXC_ERR_STATE; }
-  *col_w = it->second.first;
-  *x_rows = it->second.second;
+  *engine = it->second.engine;
+  if (it->second.engine == 0) {
+    fftreg_geometry(n, precision, col_w, x_rows);
+  } else {
+    *col_w = it->second.col_w;
+    *x_rows = it->second.x_rows;
+  }
   return EXC_OK;
 }
 

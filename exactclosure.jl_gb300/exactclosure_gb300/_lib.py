@@ -126,7 +126,7 @@ SIGNATURES = {
     "exc_server_poll": [vp, C.POINTER(SolveResult), i32, C.POINTER(i32)],
     "exc_server_drain": [vp],
     "exc_server_stats": [vp, C.POINTER(ServerInfo)],
-    "exc_server_tuning": [i32, i32, i32, C.POINTER(i32), C.POINTER(i32)],
+    "exc_server_tuning": [i32, i32, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)],
     "exc_dnsaid_create": [C.POINTER(DnsAidDesc), vp, C.POINTER(vp)],
     "exc_dnsaid_destroy": [vp],
     "exc_dnsaid_init_random": [vp, i32, f64, f64, u64],

@@ -69,9 +69,11 @@ class Server:
 
     @staticmethod
     def tuning(precision: int, n: int, slots: int):
-        w, r = C.c_int(), C.c_int()
-        call("exc_server_tuning", precision, n, slots, C.byref(w), C.byref(r))
-        return w.value, r.value
+        """(engine, col_w, x_rows) the autotuner chose: engine 0 = register-
+        resident FFT passes, 1 = Stockham passes."""
+        e, w, r = C.c_int(), C.c_int(), C.c_int()
+        call("exc_server_tuning", precision, n, slots, C.byref(e), C.byref(w), C.byref(r))
+        return e.value, w.value, r.value
 
     def close(self):
         if getattr(self, "_h", None):

@@ -293,8 +293,11 @@ int exc_server_poll(exc_server* sv, exc_solve_result* out, int max, int* count);
 /* Tick until every submitted solve has finished; synchronises the device. */
 int exc_server_drain(exc_server* sv);
 int exc_server_stats(exc_server* sv, exc_server_info* st);
-/* FFT tile shape the autotuner chose for (precision, n, slots per batch). */
-int exc_server_tuning(int precision, int n, int slots, int* col_w, int* x_rows);
+/* FFT engine and tile shape the autotuner chose for (precision, n, slots per
+ * batch): engine 0 = register-resident passes (col_w = kx columns per column
+ * tile, x_rows = rows per x-pass CTA of its plan), 1 = Stockham passes with
+ * the tuned col_w and x_rows. */
+int exc_server_tuning(int precision, int n, int slots, int* engine, int* col_w, int* x_rows);
 
 /* ======================================================================
  * Learned closure (no counterpart in the reference): a 3-D convolutional

@@ -174,11 +174,13 @@ constexpr int reg_split(int L) {
   }
 }
 
-// Column tile geometry: W lines (kx columns) of 128 bytes per element row.
+// Column tile geometry: W lines (kx columns) per tile, 128 bytes per element
+// row; FP32 lines of 512 and more take 8 columns, so the CTA of a 32-point
+// level stays at 256 threads (two CTAs per SM at 128 registers).
 template <typename T, int N1, int N2>
 struct ColGeom {
   static constexpr int L = N1 * N2;
-  static constexpr int W = sizeof(T) == 4 ? (L >= 1024 ? 8 : 16) : 8;
+  static constexpr int W = sizeof(T) == 4 ? (L >= 512 ? 8 : 16) : 8;
   static constexpr int NR = N1 > N2 ? N1 : N2;
   static constexpr int NT = W * NR;
   static constexpr size_t SMEM = (size_t)W * L * 2 * sizeof(T);

@@ -73,7 +73,7 @@ __device__ __forceinline__ T s33(T up, T lo, T kd, T kv2) {
 }
 
 template <typename T, int NC, bool DOADD>
-__global__ void __launch_bounds__(PTX * NWARP, 4)
+__global__ void __launch_bounds__(PTX * NWARP, sizeof(T) == 4 ? 4 : 3)
 rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks) {
   constexpr int PTY = PTYT<NC>, PBY = PBYT<NC>;
   extern __shared__ __align__(16) unsigned char rhs_smem[];
@@ -258,10 +258,10 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   }
 }
 
-// Cells per thread along y: two in FP32 (16-row tiles; four ran slower at
-// 94 registers, two CTAs per SM), one in FP64 (where the sweep is bound by the
-// FP64 pipe, not by per-plane overhead).
-template <typename T> constexpr int CYT = sizeof(T) == 4 ? 2 : 1;
+// Cells per thread along y: two (16-row tiles: the halo stresses are
+// recomputed for fewer cells and adjacent rows share their u reads); four ran
+// slower in FP32 (94 registers, two CTAs per SM).
+template <typename T> constexpr int CYT = 2;
 
 template <typename T>
 cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st, const SlotBatch& sb,

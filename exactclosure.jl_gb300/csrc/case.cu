@@ -31,6 +31,11 @@ struct LesState {
   exc_poisson ps;
   T* buf = nullptr;  // one allocation, sliced below (3M words each)
   T* tb = nullptr;   // filter scratch: 3 n (n/c)^2 words (transverse box sums)
+  // source of the transverse sums: -1 = the fine field; otherwise LES tb_from,
+  // whose ratio divides c (coarsened into tb) or equals it (tb_same: its
+  // buffer is used as is)
+  int tb_from = -1;
+  bool tb_same = false;
   T *ub, *fk, *mcl, *mlast, *rtmp;
   T *ve[2], *ves, *ke;  // exact LES: state (ping-pong), stage, k
   T *vn[2], *vns, *kn;  // no-model LES
@@ -82,14 +87,53 @@ static int project_vec(exc_poisson* ps, T* u, cudaStream_t st) {
   return EXC_OK;
 }
 
-// ubar = target(src): filter, then project for the volume filter.
+// Transverse box sums of src for every LES: one pass over the fine field per
+// LES whose ratio has no divisor among the other ratios, coarsening passes for
+// the multiples (in increasing ratio), nothing for repeated ratios.
 template <typename T>
-static int les_target(CaseImpl<T>* ci, LesState<T>& L, const T* src, T* out, cudaStream_t st) {
-  cudaError_t e = filter_vector_box<T>(ci->n, L.c, L.kind, src, out, L.tb, st);
+static int les_tb_fill(CaseImpl<T>* ci, const T* src, cudaStream_t st) {
+  int order[EXC_MAX_LES];
+  for (int i = 0; i < ci->nles; ++i) order[i] = i;
+  for (int i = 1; i < ci->nles; ++i)
+    for (int j = i; j > 0 && ci->les[order[j]].c < ci->les[order[j - 1]].c; --j) {
+      const int t = order[j];
+      order[j] = order[j - 1];
+      order[j - 1] = t;
+    }
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < ci->nles && e == cudaSuccess; ++k) {
+    LesState<T>& L = ci->les[order[k]];
+    if (L.tb_same) continue;
+    if (L.tb_from < 0) e = box_tb<T>(ci->n, L.c, src, L.tb, st);
+    else e = box_tb_coarsen<T>(ci->n, ci->les[L.tb_from].c, L.c, ci->les[L.tb_from].tb, L.tb, st);
+  }
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+template <typename T>
+static const T* les_tb(const CaseImpl<T>* ci, const LesState<T>& L) {
+  return L.tb_same ? ci->les[L.tb_from].tb : L.tb;
+}
+
+// ubar from the filled transverse sums: own-axis taps, then the projection
+// for the volume filter.
+template <typename T>
+static int les_target_tb(CaseImpl<T>* ci, LesState<T>& L, T* out, cudaStream_t st) {
+  cudaError_t e = box_oa<T>(ci->n, L.c, L.kind, les_tb(ci, L), out, st);
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   int rc = EXC_OK;
   if (L.kind == EXC_FILTER_VOLUME) rc = project_vec<T>(&L.ps, out, st);
   return rc;
+}
+
+// ubar = target(src) for one LES (the sums of every LES are refreshed, so the
+// result has the same bits as in the stepper).
+template <typename T>
+static int les_target(CaseImpl<T>* ci, LesState<T>& L, const T* src, T* out, cudaStream_t st) {
+  int rc = les_tb_fill<T>(ci, src, st);
+  if (rc) return rc;
+  return les_target_tb<T>(ci, L, out, st);
 }
 
 // Enqueue one RK4 step (no host synchronisation).
@@ -113,20 +157,28 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
     if (e == cudaSuccess) e = poisson_solve_inplace<T>(&ci->ps, ci->rhs, true, st);
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
     // LES targets use the stage state before it is overwritten
+    if (ci->nles > 0) {
+      int rc = les_tb_fill<T>(ci, src, st);
+      if (rc) return rc;
+    }
     for (int li = 0; li < ci->nles; ++li) {
       LesState<T>& L = ci->les[li];
-      int rc = les_target<T>(ci, L, src, L.ub, st);
+      int rc = les_target_tb<T>(ci, L, L.ub, st);
       if (rc) return rc;
     }
     e = launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0, ci->us, ufin, s,
                            dt, st, SlotBatch(), 1, ci->nles > 0);
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    if (ci->nles > 0) {
+      int rc = les_tb_fill<T>(ci, ci->rhs, st);
+      if (rc) return rc;
+    }
     for (int li = 0; li < ci->nles; ++li) {
       LesState<T>& L = ci->les[li];
       const int m = L.m;
       const T H = (T)(cs->desc.l / m);
       // m_s = P_H(filter(k_s) - RHS_H(ubar_s))
-      e = filter_vector_box<T>(n, L.c, L.kind, ci->rhs, L.mcl, L.tb, st);
+      e = box_oa<T>(n, L.c, L.kind, les_tb(ci, L), L.mcl, st);
       if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
       int rc;
       e = launch_rhs<T>(m, H, visc, L.ub, L.rtmp, false, st);
@@ -309,6 +361,23 @@ static int case_create(exc_case* cs) {
     L.vn[0] = take(); L.vn[1] = take(); L.vns = take(); L.kn = take();
     L.ublast = take();
     L.vl[0] = take(); L.vl[1] = take(); L.vls = take(); L.kl = take(); L.nn = take();
+  }
+  // sources of the transverse box sums: an earlier LES of the same ratio, else
+  // the LES with the largest ratio that divides this one, else the fine field
+  for (int li = 0; li < d.nles; ++li) {
+    LesState<T>& L = ci->les[li];
+    for (int lj = 0; lj < li; ++lj)
+      if (ci->les[lj].c == L.c && !ci->les[lj].tb_same) {
+        L.tb_from = lj;
+        L.tb_same = true;
+        break;
+      }
+    if (L.tb_same) continue;
+    for (int lj = 0; lj < d.nles; ++lj) {
+      const LesState<T>& S = ci->les[lj];
+      if (lj == li || S.tb_same || S.c >= L.c || L.c % S.c != 0) continue;
+      if (L.tb_from < 0 || S.c > ci->les[L.tb_from].c) L.tb_from = lj;
+    }
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }

@@ -286,18 +286,76 @@ __global__ void oa_kernel(const T* __restrict__ tb3, int n, int c, Taps1D taps, 
   }
 }
 
+// Transverse sums of ratio cf * r from those of ratio cf: an r x r block of
+// the cf-sums (block order a, b; each cf-sum in its own fixed order), so a
+// case with several LES reads the fine field once per filtered quantity.
 template <typename T>
-cudaError_t filter_vector_box(int n, int c, int kind, const T* u, T* ub, T* tb, cudaStream_t st) {
+__global__ void tb_coarsen_kernel(const T* __restrict__ tf3, int n, int cf, int r, T* __restrict__ tt3) {
+  const int comp = blockIdx.y;
+  const int mf = n / cf, mt = mf / r;
+  const long long Mtf = (long long)n * mf * mf;
+  const long long Mtt = (long long)n * mt * mt;
+  const T* __restrict__ tf = tf3 + comp * Mtf;
+  T* __restrict__ tt = tt3 + comp * Mtt;
+  const IdxDiv dn(n), dmt(mt);
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < Mtt; g += (long long)gridDim.x * blockDim.x) {
+    T acc = (T)0;
+    if (comp == 0) {  // [(Kz mt + Ky) n + x]
+      const long long q = dn.div(g);
+      const int x = (int)(g - q * n);
+      const int Kz = (int)dmt.div(q), Ky = (int)(q - (long long)Kz * mt);
+      for (int a = 0; a < r; ++a)
+        for (int b = 0; b < r; ++b) acc += tf[((long long)(r * Kz + a) * mf + r * Ky + b) * n + x];
+    } else if (comp == 1) {  // [(Kz n + y) mt + Kx]
+      const long long q = dmt.div(g);
+      const int Kx = (int)(g - q * mt);
+      const int Kz = (int)dn.div(q), y = (int)(q - (long long)Kz * n);
+      for (int a = 0; a < r; ++a)
+        for (int b = 0; b < r; ++b) acc += tf[((long long)(r * Kz + a) * n + y) * mf + r * Kx + b];
+    } else {  // [(z mt + Ky) mt + Kx]
+      const long long q = dmt.div(g);
+      const int Kx = (int)(g - q * mt);
+      const int z = (int)dmt.div(q), Ky = (int)(q - (long long)z * mt);
+      for (int a = 0; a < r; ++a)
+        for (int b = 0; b < r; ++b) acc += tf[((long long)z * mf + r * Ky + a) * mf + r * Kx + b];
+    }
+    tt[g] = acc;
+  }
+}
+
+template <typename T>
+cudaError_t box_tb(int n, int c, const T* u, T* tb, cudaStream_t st) {
   const int m = n / c;
   const long long Mt = (long long)n * m * m;
+  tb_kernel<T><<<dim3(grid_for(Mt), 3), 256, 0, st>>>(u, n, c, tb);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t box_tb_coarsen(int n, int cf, int ct, const T* tbf, T* tbt, cudaStream_t st) {
+  const int mt = n / ct;
+  const long long Mtt = (long long)n * mt * mt;
+  tb_coarsen_kernel<T><<<dim3(grid_for(Mtt), 3), 256, 0, st>>>(tbf, n, cf, ct / cf, tbt);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t box_oa(int n, int c, int kind, const T* tb, T* ub, cudaStream_t st) {
+  const int m = n / c;
   const long long M = (long long)m * m * m;
   Taps1D taps = build_taps(c, true, kind == EXC_FILTER_FACE, nullptr, 0);
   // the transverse box weight 1/c is applied once per axis here; the own-axis
   // taps already carry their 1/c
   const double scale = 1.0 / ((double)c * c);
-  tb_kernel<T><<<dim3(grid_for(Mt), 3), 256, 0, st>>>(u, n, c, tb);
   oa_kernel<T><<<dim3(grid_for(M), 3), 256, 0, st>>>(tb, n, c, taps, scale, ub);
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t filter_vector_box(int n, int c, int kind, const T* u, T* ub, T* tb, cudaStream_t st) {
+  cudaError_t e = box_tb<T>(n, c, u, tb, st);
+  if (e == cudaSuccess) e = box_oa<T>(n, c, kind, tb, ub, st);
+  return e;
 }
 
 // Stress of the fine-grid filtered velocity, uf = lazyfilter(u, GDH) on the
@@ -381,6 +439,9 @@ int classic_stress(int n, int c, double l, double visc, const double* fdelta, in
 #define INST(T)                                                                                          \
   template int classic_stress<T>(int, int, double, double, const double*, int, const T*, T*, cudaStream_t); \
   template cudaError_t filter_vector_box<T>(int, int, int, const T*, T*, T*, cudaStream_t);              \
+  template cudaError_t box_tb<T>(int, int, const T*, T*, cudaStream_t);                                  \
+  template cudaError_t box_tb_coarsen<T>(int, int, int, const T*, T*, cudaStream_t);                     \
+  template cudaError_t box_oa<T>(int, int, int, const T*, T*, cudaStream_t);                             \
   template int filter_vector<T>(int, int, int, const double*, int, const T*, T*, cudaStream_t);          \
   template int closure_flux<T>(int, int, double, double, const double*, int, const T*, const T*, T*,     \
                                cudaStream_t);                                                            \

@@ -24,6 +24,14 @@ int filter_vector(int n, int c, int kind, const double* fdelta, int nfd, const T
 // of scratch.
 template <typename T>
 cudaError_t filter_vector_box(int n, int c, int kind, const T* u, T* ub, T* tb, cudaStream_t st);
+// Its passes: transverse c x c sums of the fine field (tb), the same sums of
+// ratio ct = r cf from those of ratio cf, and the own-axis taps into ub.
+template <typename T>
+cudaError_t box_tb(int n, int c, const T* u, T* tb, cudaStream_t st);
+template <typename T>
+cudaError_t box_tb_coarsen(int n, int cf, int ct, const T* tbf, T* tbt, cudaStream_t st);
+template <typename T>
+cudaError_t box_oa(int n, int c, int kind, const T* tb, T* ub, cudaStream_t st);
 template <typename T>
 int closure_flux(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, const T* p,
                  T* r9, cudaStream_t st);

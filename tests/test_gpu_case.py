@@ -34,8 +34,11 @@ def test_init_random_matches_oracle(NS, n, kpeak, seed):
     assert abs(cs.dissipation() - eps) < 1e-12 * eps
 
 
+# ratio 8 after ratio 4: transverse sums coarsened from the ratio-4 ones; two
+# LES of ratio 4 share one set of sums
 @pytest.mark.parametrize("n,les", [(32, [(4, "volume")]), (24, [(3, "volume"), (2, "face")]),
-                                   (32, [(8, "volume"), (4, "face")])])
+                                   (32, [(8, "volume"), (4, "face")]),
+                                   (32, [(4, "volume"), (8, "volume"), (4, "face")])])
 def test_rk4_steps_match_oracle_per_step(NS, n, les):
     l, visc, cfl = 1.0, 1 / 2000, 0.3
     u0 = ns.randomfield(n, l, 4, 3)

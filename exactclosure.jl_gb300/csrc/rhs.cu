@@ -2,7 +2,7 @@
 // src/N.jl:94-160), marching along z.
 //
 // A CTA of 32 x 8 threads owns a PTX x PTY column of cells (PTY = 8 NC, NC
-// consecutive rows per thread) and walks PTZ planes.  Three plane buffers of u
+// consecutive rows per thread) and walks ptz planes (8 to 32).  Three plane buffers of u
 // with a one-cell x/y halo sit in shared memory: planes z and z+1 are read
 // while plane z+2 streams in with cp.async; each thread evaluates the six
 // stress components at its own cells (the edge stresses s13, s23 and the
@@ -16,7 +16,7 @@
 
 namespace exc {
 
-constexpr int PTX = 32, PTZ = 32, NWARP = 8;
+constexpr int PTX = 32, NWARP = 8;
 constexpr int PBX = PTX + 2;  // plane box with one-cell halo (box x = x - x0 + 1)
 // u rows in shared memory: box x index xb sits at xb + SH<T>, so the 32
 // interior cells start on a 16-byte boundary and arrive by 16-byte copies
@@ -74,7 +74,7 @@ __device__ __forceinline__ T s33(T up, T lo, T kd, T kv2) {
 
 template <typename T, int NC, bool DOADD>
 __global__ void __launch_bounds__(PTX * NWARP, sizeof(T) == 4 ? 4 : 3)
-rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks) {
+rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks, int ptz) {
   constexpr int PTY = PTYT<NC>, PBY = PBYT<NC>;
   extern __shared__ __align__(16) unsigned char rhs_smem[];
   PlaneSmem<T, NC>& sm = *reinterpret_cast<PlaneSmem<T, NC>*>(rhs_smem);
@@ -88,7 +88,7 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   if (sb.visc) visc = reinterpret_cast<const T*>(sb.visc)[slot];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int lane = tx, warp = ty;
-  const int x0 = blockIdx.x * PTX, y0 = blockIdx.y * PTY, z0 = zb * PTZ;
+  const int x0 = blockIdx.x * PTX, y0 = blockIdx.y * PTY, z0 = zb * ptz;
   const T kd = (T)0.25 * inv_h;
   const T kv = visc * inv_h * inv_h;
   const T kv2 = (T)2 * kv;
@@ -174,12 +174,12 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   T* const du1 = du;
   T* const du2 = du + N;
   T* const du3 = du + 2 * N;
-  for (int kz = 0; kz < PTZ; ++kz) {
+  for (int kz = 0; kz < ptz; ++kz) {
     const int z = z0 + kz;
     if (z >= n) break;  // uniform across the CTA
     // plane z + 2 streams into the free buffer while plane z is processed
     // (its last reader finished before the previous iteration's barrier)
-    if (kz + 1 < PTZ && z + 1 < n) load_plane(pre, zwrap(z + 2));
+    if (kz + 1 < ptz && z + 1 < n) load_plane(pre, zwrap(z + 2));
     const auto& uc = sm.u[cur];
     const auto& un = sm.u[nxt];
     // own-cell stresses
@@ -258,6 +258,239 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 sweep with 2 x 2 cells per thread (64 x 16 tiles, grids that are
+// multiples of 64): each thread reads its u rows as aligned float pairs, takes
+// the x and y neighbour stresses of its own cells from registers and stores
+// float pairs, which halves the shared-memory and global instructions per
+// cell.  Same stress and divergence arithmetic, in the same order, as
+// rhs_kernel: the results are bit-identical.
+// ---------------------------------------------------------------------------
+constexpr int QX = 64, QY = 16, QBX = QX + 2, QBY = QY + 2;
+constexpr int QROW = 72;  // box x b at b + 3: left piece [0, 4), interior [4, 68), right piece [68, 72)
+
+struct QuadSmem {
+  __align__(16) float u[3][3][QBY][QROW];
+  float s[5][QBY][QBX];  // s11, s22, s12, s13, s23 of the current plane
+};
+
+__device__ __forceinline__ float qdiag(float a, float b, float kd, float kv2) {
+  const float s = a + b, d = a - b;
+  return s * s * kd - kv2 * d;
+}
+__device__ __forceinline__ float qoff(float a, float b, float c, float d, float kd, float kv) {
+  return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
+}
+
+template <bool DOADD>
+__global__ void __launch_bounds__(256, 3)
+rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, float* __restrict__ du, SlotBatch sb,
+                int zblocks, int ptz) {
+  extern __shared__ __align__(16) unsigned char quad_smem[];
+  QuadSmem& sm = *reinterpret_cast<QuadSmem*>(quad_smem);
+  const long long N = (long long)n * n * n;
+  const int slot = blockIdx.z / zblocks;
+  const int zb = blockIdx.z - slot * zblocks;
+  if (sb.active && !sb.active[slot]) return;
+  u += slot * sb.ustride;
+  du += slot * sb.ustride;
+  if (sb.visc) visc = reinterpret_cast<const float*>(sb.visc)[slot];
+  const int tx = threadIdx.x, ty = threadIdx.y, lane = tx, warp = ty;
+  const int x0 = blockIdx.x * QX, y0 = blockIdx.y * QY, z0 = zb * ptz;
+  const float kd = 0.25f * inv_h, kv = visc * inv_h * inv_h, kv2 = 2.0f * kv;
+  auto wrap = [n](int g) { return g < 0 ? g + n : (g >= n ? g - n : g); };
+  // 16-byte copy pieces of a plane: 18 pieces per box row (left, 16 interior,
+  // right), offsets computed once
+  constexpr int NPQ = 3 * QBY * 18, NSQ = (NPQ + 255) / 256;
+  const int tid = ty * 32 + tx;
+  long long goff[NSQ];
+  int soff[NSQ];
+#pragma unroll
+  for (int i = 0; i < NSQ; ++i) {
+    const int t = tid + i * 256;
+    goff[i] = -1;
+    soff[i] = 0;
+    if (t < NPQ) {
+      const int c = t / (QBY * 18), rem = t - c * (QBY * 18);
+      const int rr = rem / 18, j = rem - rr * 18;
+      const int gy = wrap(y0 - 1 + rr);
+      const int gx = j == 0 ? wrap(x0 - 4) : (j == 17 ? wrap(x0 + QX) : x0 + 4 * (j - 1));
+      goff[i] = c * N + (long long)gy * n + gx;
+      soff[i] = (c * QBY + rr) * QROW + 4 * j;
+    }
+  }
+  const long long nn = (long long)n * n;
+  auto load_plane = [&](int buf, int gz) {
+    float* const s0 = &sm.u[buf][0][0][0];
+    const float* const ub = u + gz * nn;
+#pragma unroll
+    for (int i = 0; i < NSQ; ++i)
+      if (goff[i] >= 0) cp_async_16(s0 + soff[i], ub + goff[i]);
+    cp_async_commit();
+  };
+  // this thread: box columns c0 = 2 tx + 1, c0 + 1 and rows r0 = 2 ty + 1, r0 + 1
+  const int c0 = 2 * tx + 1, r0 = 2 * ty + 1;
+  const int sc = c0 + 3;  // smem column of c0 (even: float2 aligned)
+  auto f2 = [&](const float* row) { return *reinterpret_cast<const float2*>(row + sc); };
+  load_plane(0, wrap(z0 - 1));
+  load_plane(1, wrap(z0));
+  load_plane(2, wrap(z0 + 1));
+  cp_async_wait_all();
+  __syncthreads();
+  float p13[2][2], p23[2][2], p33[2][2];  // [row j][col i]
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const auto& ua = sm.u[0];  // plane z0 - 1
+    const auto& ub = sm.u[1];  // plane z0
+    const int r = r0 + j;
+    const float2 a1 = f2(ua[0][r]), b1 = f2(ub[0][r]), a3 = f2(ua[2][r]), a2 = f2(ua[1][r]), b2 = f2(ub[1][r]);
+    const float a3r = ua[2][r][sc + 2];
+    const float2 a3u = f2(ua[2][r + 1]);
+    const float2 b3 = f2(ub[2][r]);
+    p13[j][0] = qoff(a1.x, b1.x, a3.x, a3.y, kd, kv);
+    p13[j][1] = qoff(a1.y, b1.y, a3.y, a3r, kd, kv);
+    p23[j][0] = qoff(a2.x, b2.x, a3.x, a3u.x, kd, kv);
+    p23[j][1] = qoff(a2.y, b2.y, a3.y, a3u.y, kd, kv);
+    p33[j][0] = qdiag(b3.x, a3.x, kd, kv2);
+    p33[j][1] = qdiag(b3.y, a3.y, kd, kv2);
+  }
+  __syncthreads();  // buffer 0 is refilled by the first prefetch
+  int cur = 1, nxt = 2, pre = 0;
+  const int gx = x0 + 2 * tx, gy = y0 + 2 * ty;
+  float* const du1 = du;
+  float* const du2 = du + N;
+  float* const du3 = du + 2 * N;
+  for (int kz = 0; kz < ptz; ++kz) {
+    const int z = z0 + kz;
+    if (z >= n) break;  // uniform across the CTA
+    if (kz + 1 < ptz && z + 1 < n) load_plane(pre, wrap(z + 2));
+    const auto& uc = sm.u[cur];
+    const auto& un = sm.u[nxt];
+    // register patch: u1 rows r0, r0+1, r0+2 and column c0-1; u2 rows r0-1,
+    // r0, r0+1 and column c0+2; u3 rows r0, r0+1, r0+2 and column c0+2; the
+    // next plane's u1, u2, u3 on the thread's rows
+    float2 u1r[3], u2r[3], u3r[3], u1n[2], u2n[2], u3n[2];
+    float u1l[2], u2r2[2], u3r2[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      u1r[k] = f2(uc[0][r0 + k]);
+      u2r[k] = f2(uc[1][r0 - 1 + k]);
+      u3r[k] = f2(uc[2][r0 + k]);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      u1l[j] = uc[0][r0 + j][sc - 1];
+      u2r2[j] = uc[1][r0 + j][sc + 2];
+      u3r2[j] = uc[2][r0 + j][sc + 2];
+      u1n[j] = f2(un[0][r0 + j]);
+      u2n[j] = f2(un[1][r0 + j]);
+      u3n[j] = f2(un[2][r0 + j]);
+    }
+    float v11[2][2], v22[2][2], v12[2][2], v13[2][2], v23[2][2], v33[2][2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const float2 a1 = u1r[j], a1u = u1r[j + 1];
+      const float2 a2 = u2r[j + 1], a2d = u2r[j];
+      const float2 a3 = u3r[j], a3u = u3r[j + 1];
+      v11[j][0] = qdiag(a1.x, u1l[j], kd, kv2);
+      v11[j][1] = qdiag(a1.y, a1.x, kd, kv2);
+      v22[j][0] = qdiag(a2.x, a2d.x, kd, kv2);
+      v22[j][1] = qdiag(a2.y, a2d.y, kd, kv2);
+      v12[j][0] = qoff(a1.x, a1u.x, a2.x, a2.y, kd, kv);
+      v12[j][1] = qoff(a1.y, a1u.y, a2.y, u2r2[j], kd, kv);
+      v13[j][0] = qoff(a1.x, u1n[j].x, a3.x, a3.y, kd, kv);
+      v13[j][1] = qoff(a1.y, u1n[j].y, a3.y, u3r2[j], kd, kv);
+      v23[j][0] = qoff(a2.x, u2n[j].x, a3.x, a3u.x, kd, kv);
+      v23[j][1] = qoff(a2.y, u2n[j].y, a3.y, a3u.y, kd, kv);
+      v33[j][0] = qdiag(u3n[j].x, a3.x, kd, kv2);
+      v33[j][1] = qdiag(u3n[j].y, a3.y, kd, kv2);
+    }
+    // stresses other threads read: s11 of column c0 (left neighbour), s12 of
+    // column c0+1 and of row r0+1 (right neighbour, row above), s13 of column
+    // c0+1, s22 of row r0 (row below), s23 of row r0+1 (row above)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      sm.s[0][r0 + j][c0] = v11[j][0];
+      sm.s[3][r0 + j][c0 + 1] = v13[j][1];
+    }
+    sm.s[2][r0][c0 + 1] = v12[0][1];
+    sm.s[2][r0 + 1][c0] = v12[1][0];
+    sm.s[2][r0 + 1][c0 + 1] = v12[1][1];
+    sm.s[1][r0][c0] = v22[0][0];
+    sm.s[1][r0][c0 + 1] = v22[0][1];
+    sm.s[4][r0 + 1][c0] = v23[1][0];
+    sm.s[4][r0 + 1][c0 + 1] = v23[1][1];
+    // halo stresses, one task per warp (box row 0, row QY+1, column 0,
+    // column QX+1)
+    if (warp == 0) {
+      for (int c = lane + 1; c <= QX; c += 32)
+        sm.s[2][0][c] = qoff(uc[0][0][c + 3], uc[0][1][c + 3], uc[1][0][c + 3], uc[1][0][c + 4], kd, kv);
+    } else if (warp == 1) {
+      for (int c = lane + 1; c <= QX; c += 32)
+        sm.s[4][0][c] = qoff(uc[1][0][c + 3], un[1][0][c + 3], uc[2][0][c + 3], uc[2][1][c + 3], kd, kv);
+    } else if (warp == 2) {
+      for (int c = lane + 1; c <= QX; c += 32)
+        sm.s[1][QY + 1][c] = qdiag(uc[1][QY + 1][c + 3], uc[1][QY][c + 3], kd, kv2);
+    } else if (warp == 3) {
+      if (lane <= QY) sm.s[2][lane][0] = qoff(uc[0][lane][3], uc[0][lane + 1][3], uc[1][lane][3], uc[1][lane][4], kd, kv);
+    } else if (warp == 4) {
+      if (lane < QY) {
+        const int r = lane + 1;
+        sm.s[3][r][0] = qoff(uc[0][r][3], un[0][r][3], uc[2][r][3], uc[2][r][4], kd, kv);
+      }
+    } else if (warp == 5) {
+      if (lane < QY) {
+        const int r = lane + 1;
+        sm.s[0][r][QX + 1] = qdiag(uc[0][r][QX + 4], uc[0][r][QX + 3], kd, kv2);
+      }
+    }
+    __syncthreads();
+    const auto& S = sm.s;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int r = r0 + j;
+      float d1[2], d2[2], d3[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int c = c0 + i;
+        const float s11_right = i == 0 ? v11[j][1] : S[0][r][c + 1];
+        const float s12_below = j == 1 ? v12[0][i] : S[2][r - 1][c];
+        const float s12_left = i == 1 ? v12[j][0] : S[2][r][c - 1];
+        const float s22_above = j == 0 ? v22[1][i] : S[1][r + 1][c];
+        const float s13_left = i == 1 ? v13[j][0] : S[3][r][c - 1];
+        const float s23_below = j == 1 ? v23[0][i] : S[4][r - 1][c];
+        d1[i] = (s11_right - v11[j][i]) + (v12[j][i] - s12_below) + (v13[j][i] - p13[j][i]);
+        d2[i] = (v12[j][i] - s12_left) + (s22_above - v22[j][i]) + (v23[j][i] - p23[j][i]);
+        d3[i] = (v13[j][i] - s13_left) + (v23[j][i] - s23_below) + (v33[j][i] - p33[j][i]);
+        p13[j][i] = v13[j][i];
+        p23[j][i] = v23[j][i];
+        p33[j][i] = v33[j][i];
+      }
+      const long long g = ((long long)z * n + gy + j) * n + gx;
+      float2* o1 = reinterpret_cast<float2*>(du1 + g);
+      float2* o2 = reinterpret_cast<float2*>(du2 + g);
+      float2* o3 = reinterpret_cast<float2*>(du3 + g);
+      if (DOADD) {
+        float2 a = *o1, b = *o2, c = *o3;
+        a.x -= d1[0]; a.y -= d1[1];
+        b.x -= d2[0]; b.y -= d2[1];
+        c.x -= d3[0]; c.y -= d3[1];
+        *o1 = a; *o2 = b; *o3 = c;
+      } else {
+        *o1 = make_float2(-d1[0], -d1[1]);
+        *o2 = make_float2(-d2[0], -d2[1]);
+        *o3 = make_float2(-d3[0], -d3[1]);
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int freed = cur;
+    cur = nxt;
+    nxt = pre;
+    pre = freed;
+  }
+}
+
 // Cells per thread along y: two (16-row tiles: the halo stresses are
 // recomputed for fewer cells and adjacent rows share their u reads); four ran
 // slower in FP32 (94 registers, two CTAs per SM).
@@ -267,13 +500,43 @@ template <typename T>
 cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st, const SlotBatch& sb,
                        int nslots) {
   constexpr int NC = CYT<T>;
-  const int zblocks = (n + PTZ - 1) / PTZ;
-  dim3 grid((n + PTX - 1) / PTX, (n + PTYT<NC> - 1) / PTYT<NC>, zblocks * nslots);
+  // planes per CTA: 32, halved (down to 8) while the launch would give fewer
+  // than two waves of resident CTAs (`per_sm` per SM), so small grids and
+  // single solves still fill the GPU (each CTA re-reads three planes to start)
+  auto zsplit = [&](long long columns, int per_sm, int& ptz, int& zblocks) {
+    ptz = 32;
+    zblocks = (n + ptz - 1) / ptz;
+    while (ptz > 8 && columns * zblocks * nslots < 2LL * per_sm * 152) {
+      ptz /= 2;
+      zblocks = (n + ptz - 1) / ptz;
+    }
+    return columns * zblocks * nslots;
+  };
+  int ptz, zblocks;
+  if constexpr (sizeof(T) == 4) {
+    // grids of 64-multiples with 16-byte aligned fields and at least one full
+    // wave of CTAs (three per SM): the 2 x 2 kernel
+    if (n % QX == 0 && (reinterpret_cast<uintptr_t>(u) & 15) == 0 && (reinterpret_cast<uintptr_t>(du) & 15) == 0 &&
+        zsplit((long long)(n / QX) * (n / QY), 3, ptz, zblocks) >= 3LL * 152) {
+      dim3 gq(n / QX, n / QY, zblocks * nslots);
+      const float ih = (float)(1.0 / (double)h);
+      if (doadd)
+        rhs_quad_kernel<true><<<gq, dim3(32, 8), sizeof(QuadSmem), st>>>(n, ih, (float)visc, (const float*)u, (float*)du,
+                                                                         sb, zblocks, ptz);
+      else
+        rhs_quad_kernel<false><<<gq, dim3(32, 8), sizeof(QuadSmem), st>>>(n, ih, (float)visc, (const float*)u,
+                                                                          (float*)du, sb, zblocks, ptz);
+      return cudaGetLastError();
+    }
+  }
+  const int gxb = (n + PTX - 1) / PTX, gyb = (n + PTYT<NC> - 1) / PTYT<NC>;
+  zsplit((long long)gxb * gyb, sizeof(T) == 4 ? 4 : 3, ptz, zblocks);
+  dim3 grid(gxb, gyb, zblocks * nslots);
   const size_t sh = sizeof(PlaneSmem<T, NC>);
   if (doadd)
-    rhs_kernel<T, NC, true><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks);
+    rhs_kernel<T, NC, true><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks, ptz);
   else
-    rhs_kernel<T, NC, false><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks);
+    rhs_kernel<T, NC, false><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks, ptz);
   return cudaGetLastError();
 }
 
@@ -289,6 +552,10 @@ static cudaError_t configure_rhs_t() {
 
 cudaError_t configure_stencil() {
   cudaError_t e = configure_rhs_t<float>();
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(rhs_quad_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(QuadSmem));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(rhs_quad_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(QuadSmem));
   if (e == cudaSuccess) e = configure_rhs_t<double>();
   return e;
 }

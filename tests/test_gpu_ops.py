@@ -102,6 +102,24 @@ def test_poisson_solve_and_divergence(NS, n):
     assert rel(host(ut), ns.pressuregradient(u, ns.poisson_solve(dref, l / n), l / n)) < TOL64
 
 
+@pytest.mark.parametrize("n", [64, 128])
+def test_f32_rhs_two_by_two_cells(NS, n):
+    """FP32 sweep of 64-multiple grids (2 x 2 cells per thread), both modes."""
+    import torch
+
+    l, visc = 1.0, 1 / 900
+    u = seeded_field(n, l, 11)
+    g = NS.Grid(l, n)
+    ref = ns.rhs(u, visc, l / n)
+    du = torch.empty((3, n, n, n), dtype=torch.float32, device="cuda")
+    NS.tensordivergence(du, dev(u, "float32"), visc, g)
+    assert rel(host(du), ref) < TOL32
+    base = np.random.default_rng(2).standard_normal(ref.shape)
+    du2 = dev(base, "float32")
+    NS.tensordivergence(du2, dev(u, "float32"), visc, g, doadd=True)
+    assert rel(host(du2), base + ref) < TOL32
+
+
 @pytest.mark.parametrize("n", [16, 64])
 def test_f32_form_operators(NS, n):
     import torch

@@ -175,12 +175,12 @@ constexpr int reg_split(int L) {
 }
 
 // Column tile geometry: W lines (kx columns) per tile, 128 bytes per element
-// row; FP32 lines of 512 and more take 8 columns, so the CTA of a 32-point
-// level stays at 256 threads (two CTAs per SM at 128 registers).
+// row; FP32 lines of 384 and more take 8 columns, so the CTA of a 24- or
+// 32-point level stays at 192-256 threads (two CTAs per SM at 128 registers).
 template <typename T, int N1, int N2>
 struct ColGeom {
   static constexpr int L = N1 * N2;
-  static constexpr int W = sizeof(T) == 4 ? (L >= 512 ? 8 : 16) : 8;
+  static constexpr int W = sizeof(T) == 4 ? (L >= 384 ? 8 : 16) : 8;
   static constexpr int NR = N1 > N2 ? N1 : N2;
   static constexpr int NT = W * NR;
   static constexpr size_t SMEM = (size_t)W * L * 2 * sizeof(T);

@@ -145,6 +145,67 @@ __global__ void rk_stage4_kernel(int n, float inv_h, float* __restrict__ k, cons
   }
 }
 
+// FP64 form: two consecutive x cells per thread with 16-byte accesses (same
+// arithmetic per element as the scalar kernel).
+__device__ __forceinline__ double2 ld2(const double* p) { return *reinterpret_cast<const double2*>(p); }
+__device__ __forceinline__ void st2(double* p, double2 v) { *reinterpret_cast<double2*>(p) = v; }
+
+template <bool STORE_K>
+__global__ void rk_stage2_kernel(int n, double inv_h, double* __restrict__ k, const double* __restrict__ p, int ppitch,
+                                 const double* __restrict__ x0, double* __restrict__ xs, double* __restrict__ xfin,
+                                 int stage, const double* __restrict__ dtp, SlotBatch sb) {
+  const long long N = (long long)n * n * n;
+  const int slot = blockIdx.y;
+  if (sb.active && !sb.active[slot]) return;
+  k += slot * sb.ustride;
+  x0 += slot * sb.ustride;
+  xs += slot * sb.ustride;
+  xfin += slot * sb.ustride;
+  p += slot * 2 * sb.wstride;
+  const double dt = dtp[slot];
+  const double cf = (stage == 0 || stage == 3) ? dt / 6.0 : dt / 3.0;
+  const double cs = stage == 2 ? dt : 0.5 * dt;
+  const IdxDiv dn(n);
+  const long long Q = N / 2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < Q; q += (long long)gridDim.x * blockDim.x) {
+    const long long g = 2 * q;
+    const long long r = dn.div(g);
+    const int x = (int)(g - r * n);
+    const int z = (int)dn.div(r);
+    const int y = (int)(r - (long long)z * n);
+    double2 k0 = ld2(k + g), k1 = ld2(k + N + g), k2 = ld2(k + 2 * N + g);
+    const double* prow = p + r * ppitch;
+    const double2 pc = ld2(prow + x);
+    const double pn = prow[x + 2 == n ? 0 : x + 2];
+    const double2 py = ld2(p + ((long long)z * n + wrap_up(y, n)) * ppitch + x);
+    const double2 pz = ld2(p + ((long long)wrap_up(z, n) * n + y) * ppitch + x);
+    k0.x -= (pc.y - pc.x) * inv_h; k0.y -= (pn - pc.y) * inv_h;
+    k1.x -= (py.x - pc.x) * inv_h; k1.y -= (py.y - pc.y) * inv_h;
+    k2.x -= (pz.x - pc.x) * inv_h; k2.y -= (pz.y - pc.y) * inv_h;
+    if (STORE_K) {
+      st2(k + g, k0);
+      st2(k + N + g, k1);
+      st2(k + 2 * N + g, k2);
+    }
+    const double2 kk[3] = {k0, k1, k2};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double2 kc = kk[c];
+      const double2 a = stage < 3 ? ld2(x0 + c * N + g) : make_double2(0.0, 0.0);  // unused at stage 3
+      double2 f;
+      if (stage == 0) {
+        f = make_double2(a.x + cf * kc.x, a.y + cf * kc.y);
+      } else {
+        f = ld2(xfin + c * N + g);
+        f.x += cf * kc.x;
+        f.y += cf * kc.y;
+      }
+      st2(xfin + c * N + g, f);
+      if (stage < 3) st2(xs + c * N + g, make_double2(a.x + cs * kc.x, a.y + cs * kc.y));
+    }
+  }
+}
+
 template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
                             const double* dtp, cudaStream_t st, const SlotBatch& sb, int nslots, bool store_k) {
@@ -160,6 +221,18 @@ cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x
       else
         rk_stage4_kernel<false><<<g4, 256, 0, st>>>(n, ih, (float*)k, (const float*)p, ppitch, (const float*)x0,
                                                     (float*)xs, (float*)xfin, stage, dtp, sb);
+      return cudaGetLastError();
+    }
+  } else {
+    if (p && n % 2 == 0) {
+      dim3 g2(nslots > 1 ? std::min(grid_for(N / 2), 152 * 8) : grid_for(N / 2), nslots);
+      const double ih = 1.0 / (double)h;
+      if (store_k)
+        rk_stage2_kernel<true><<<g2, 256, 0, st>>>(n, ih, (double*)k, (const double*)p, ppitch, (const double*)x0,
+                                                   (double*)xs, (double*)xfin, stage, dtp, sb);
+      else
+        rk_stage2_kernel<false><<<g2, 256, 0, st>>>(n, ih, (double*)k, (const double*)p, ppitch, (const double*)x0,
+                                                    (double*)xs, (double*)xfin, stage, dtp, sb);
       return cudaGetLastError();
     }
   }

@@ -348,6 +348,155 @@ wgrad_partial_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, c
   }
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient over 8 x 2 x 4 voxel blocks (x, y, z), every tap in one
+// CTA:
+//   dW[tap][ci][co] = sum_v in[v + shift(tap)][ci] * g[v][co].
+// A persistent CTA of 9 warps walks the blocks of the batch; each block's
+// 10 x 4 x 6 halo of `in` and its 64 rows of `g` arrive by 16-byte cp.async
+// into one of two buffers while the other is consumed, so both tensors are
+// read once per block (the halo of `in` from L2).  Voxel rows in shared memory
+// are padded to an odd number of 16-byte units, so the 8 rows of an ldmatrix
+// (8 consecutive x) fall in distinct banks.  Warp w owns the three taps
+// (dz, dy) = (w / 3 - 1, w % 3 - 1), dx = -1, 0, 1, and accumulates them over
+// all of its blocks in registers; its A fragments (in^T, channels x voxels)
+// and B fragments (g, voxels x channels) come from the [voxel][channel]
+// layouts by ldmatrix.trans.  The partials of a CTA go to part[cta] and are
+// folded in a fixed order (wgrad_fold_kernel).
+// ---------------------------------------------------------------------------
+constexpr int WT_WARPS = 9, WT_THREADS = 32 * WT_WARPS, WT_CTAS = 152;
+constexpr int WT_HX = 10, WT_HY = 4, WT_HZ = 6, WT_HALO = WT_HX * WT_HY * WT_HZ;
+
+// shared memory of wgrad_tile_kernel: two buffers of the halo rows (stride
+// KP + 8 halves) and of the g rows (stride NP + 8 halves)
+template <int KP, int NP>
+constexpr size_t wgrad_tile_smem() {
+  return 2 * ((size_t)WT_HALO * (KP + 8) + 64 * (size_t)(NP + 8)) * sizeof(__nv_bfloat16);
+}
+
+__device__ __forceinline__ void ldsm_x4_trans(unsigned (&r)[4], const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+template <int KP, int NP>
+__global__ void __launch_bounds__(WT_THREADS, 1)
+wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ g,
+                  float* __restrict__ part) {
+  constexpr int MT = KP / 16, NTL = NP / 8, KS = KP + 8, NS = NP + 8;
+  static_assert(NTL % 2 == 0, "B fragments load two n-tiles at a time");
+  extern __shared__ __align__(16) unsigned char wt_smem[];
+  __nv_bfloat16* const sX0 = reinterpret_cast<__nv_bfloat16*>(wt_smem);
+  __nv_bfloat16* const sG0 = sX0 + 2 * WT_HALO * KS;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wdz = warp / 3, wdy = warp % 3;  // dz + 1, dy + 1 of this warp's taps
+  const int nbx = n / 8, nby = n / 2, nbz = n / 4;
+  const long long nb3 = (long long)nbx * nby * nbz;
+  const long long nblk = (long long)batch * nb3;
+  const long long N = (long long)n * n * n;
+  float acc[3][MT][NTL][4];
+#pragma unroll
+  for (int t = 0; t < 3; ++t)
+#pragma unroll
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+      for (int q = 0; q < NTL; ++q) acc[t][m][q][0] = acc[t][m][q][1] = acc[t][m][q][2] = acc[t][m][q][3] = 0.f;
+  // copies of block b into buffer buf: halo voxels (hx, hy, hz) at origin
+  // (8 bx, 2 by, 4 bz) - 1 (periodic in the sample), KP / 8 pieces each; g
+  // rows of the 64 block voxels (v = x + 8 y + 16 z), NP / 8 pieces each
+  auto load_block = [&](long long b, int buf) {
+    const long long s = b / nb3;
+    const long long r = b - s * nb3;
+    const int bz = (int)(r / ((long long)nbx * nby)), by = (int)((r / nbx) % nby), bx = (int)(r % nbx);
+    const __nv_bfloat16* ins = in + s * N * KP;
+    __nv_bfloat16* const sX = sX0 + buf * WT_HALO * KS;
+    for (int t = threadIdx.x; t < WT_HALO * (KP / 8); t += WT_THREADS) {
+      const int h = t / (KP / 8), c = t - h * (KP / 8);
+      const int hz = h / (WT_HX * WT_HY), hy = (h / WT_HX) % WT_HY, hx = h % WT_HX;
+      int x = 8 * bx - 1 + hx, y = 2 * by - 1 + hy, z = 4 * bz - 1 + hz;
+      x = x < 0 ? x + n : (x >= n ? x - n : x);
+      y = y < 0 ? y + n : (y >= n ? y - n : y);
+      z = z < 0 ? z + n : (z >= n ? z - n : z);
+      cp_async_16(sX + h * KS + c * 8, ins + (((long long)z * n + y) * n + x) * KP + c * 8);
+    }
+    const __nv_bfloat16* gs = g + s * N * NP;
+    __nv_bfloat16* const sG = sG0 + buf * 64 * NS;
+    for (int t = threadIdx.x; t < 64 * (NP / 8); t += WT_THREADS) {
+      const int v = t / (NP / 8), c = t - v * (NP / 8);
+      const int x = 8 * bx + (v & 7), y = 2 * by + ((v >> 3) & 1), z = 4 * bz + (v >> 4);
+      cp_async_16(sG + v * NS + c * 8, gs + (((long long)z * n + y) * n + x) * NP + c * 8);
+    }
+    cp_async_commit();
+  };
+  // ldmatrix lane roles: matrix mat = lane / 8, row r = lane % 8
+  const int mat = lane >> 3, lr = lane & 7;
+  long long b = blockIdx.x;
+  int buf = 0;
+  if (b < nblk) load_block(b, 0);
+  for (; b < nblk; b += gridDim.x, buf ^= 1) {
+    const long long nxt = b + gridDim.x;
+    if (nxt < nblk) {
+      load_block(nxt, buf ^ 1);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      cp_async_wait_all();
+    }
+    __syncthreads();
+    const __nv_bfloat16* X = sX0 + buf * WT_HALO * KS;
+    const __nv_bfloat16* G = sG0 + buf * 64 * NS;
+#pragma unroll
+    for (int kz = 0; kz < 4; ++kz) {
+      // B: voxels k = x + 8 y of slice kz; two n-tiles per ldmatrix.x4
+      unsigned bf[NTL][2];
+#pragma unroll
+      for (int p = 0; p < NTL / 2; ++p) {
+        const int k = lr + 8 * (mat & 1);
+        unsigned r[4];
+        ldsm_x4_trans(r, G + (16 * kz + k) * NS + 16 * p + 8 * (mat >> 1));
+        bf[2 * p][0] = r[0];
+        bf[2 * p][1] = r[1];
+        bf[2 * p + 1][0] = r[2];
+        bf[2 * p + 1][1] = r[3];
+      }
+      // A: in at the shifted voxel of each tap, channels 16 mt ..
+      const int ka = lr + 8 * (mat >> 1);
+      const int hy = (ka >> 3) + wdy, hz = kz + wdz;
+#pragma unroll
+      for (int t = 0; t < 3; ++t) {
+        const int h = (ka & 7) + t + WT_HX * hy + WT_HX * WT_HY * hz;
+#pragma unroll
+        for (int m = 0; m < MT; ++m) {
+          unsigned a[4];
+          ldsm_x4_trans(a, X + h * KS + 16 * m + 8 * (mat & 1));
+#pragma unroll
+          for (int q = 0; q < NTL; ++q) mma_bf16(acc[t][m][q], a, bf[q][0], bf[q][1]);
+        }
+      }
+    }
+    __syncthreads();  // this buffer is refilled by the next iteration's prefetch
+  }
+  // C fragment: rows (ci) gid / gid + 8, columns (co) tig * 2 + {0, 1}
+  const int gid = lane >> 2, tig = lane & 3;
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const int tap = wdz * 9 + wdy * 3 + t;
+    float* out = part + ((long long)blockIdx.x * NET_TAPS + tap) * (KP * NP);
+#pragma unroll
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+      for (int q = 0; q < NTL; ++q)
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int ci = m * 16 + gid + hh * 8, co = q * 8 + tig * 2 + e;
+            out[ci * NP + co] = acc[t][m][q][hh * 2 + e];
+          }
+  }
+}
+
 // fold partials over chunks; bias gradient from the g sums of tap 13 (centre)
 template <int KP, int NP>
 __global__ void wgrad_fold_kernel(int nchunk, const float* __restrict__ part, float* __restrict__ dW) {
@@ -534,7 +683,7 @@ static int ensure_workspace(exc_net* net, long long V) {
   if (V <= net->vcap) return EXC_OK;
   cudaDeviceSynchronize();
   free_workspace(net);
-  const long long nchunk = (V + WG_CHUNK - 1) / WG_CHUNK;
+  const long long nchunk = std::max<long long>((V + WG_CHUNK - 1) / WG_CHUNK, WT_CTAS);
   bool ok = cudaMalloc(&net->x0, V * exc_net::K1 * 2) == cudaSuccess &&
             cudaMalloc(&net->a1, V * exc_net::N1 * 2) == cudaSuccess &&
             cudaMalloc(&net->a2, V * exc_net::N2 * 2) == cudaSuccess &&
@@ -580,8 +729,18 @@ static cudaError_t forward_packed(exc_net* net, long long V, int n, cudaStream_t
 template <int KP, int NP>
 static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* g,
                          cudaStream_t st) {
-  const int nchunk = (int)((V + WG_CHUNK - 1) / WG_CHUNK);
-  wgrad_partial_kernel<KP, NP><<<dim3(nchunk, 27), 128, 0, st>>>(V, n, in, g, net->wpart);
+  int nchunk;
+  const long long N = (long long)n * n * n;
+  if (n % 8 == 0) {
+    // all taps per CTA over 8 x 2 x 4 voxel blocks, one persistent CTA per SM
+    const long long nblk = V / 64;
+    nchunk = (int)std::min<long long>(nblk, WT_CTAS);
+    wgrad_tile_kernel<KP, NP><<<nchunk, WT_THREADS, wgrad_tile_smem<KP, NP>(), st>>>((int)(V / N), n, in, g,
+                                                                                      net->wpart);
+  } else {
+    nchunk = (int)((V + WG_CHUNK - 1) / WG_CHUNK);
+    wgrad_partial_kernel<KP, NP><<<dim3(nchunk, 27), 128, 0, st>>>(V, n, in, g, net->wpart);
+  }
   wgrad_fold_kernel<KP, NP><<<(27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
   // the weight-gradient partials are folded by now: reuse their buffer
   double* bpart = reinterpret_cast<double*>(net->wpart);

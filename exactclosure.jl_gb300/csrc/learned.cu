@@ -16,6 +16,8 @@
 #include <cstring>
 #include <vector>
 
+#include <mutex>
+
 #include "internal.cuh"
 #include "fields.cuh"
 
@@ -246,12 +248,164 @@ conv_tile_kernel(int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat1
     }
 }
 
+// ---------------------------------------------------------------------------
+// Convolution with the weights resident in shared memory (grids n % 8 == 0):
+// a persistent CTA of 4 warps loads all 27 taps of the weights once, then
+// walks 8 x 2 x 4 voxel blocks (x, y, z) of the batch; each block's
+// 10 x 4 x 6 halo (all input channels) arrives by 16-byte cp.async into one
+// of two buffers while the other is consumed.  Warp w computes the 16 voxels
+// of slice z = w (rows m = x + 8 y), A fragments by ldmatrix from the halo
+// rows, B fragments by ldmatrix from the weight rows ([tap][co][ci]); rows are
+// padded to an odd number of 16-byte units, so the 8 rows of an ldmatrix fall
+// in distinct banks.  Same epilogues as conv_tile_kernel.
+// ---------------------------------------------------------------------------
+constexpr int CR_HX = 10, CR_HY = 4, CR_HZ = 6, CR_HALO = CR_HX * CR_HY * CR_HZ;
+
+template <int KP, int NP>
+constexpr size_t conv_res_smem() {
+  return ((size_t)NET_TAPS * NP * (KP + 8) + 2 * (size_t)CR_HALO * (KP + 8)) * sizeof(__nv_bfloat16);
+}
+template <int KP, int NP>
+constexpr int conv_res_per_sm() {
+  return (int)((227 * 1024) / (conv_res_smem<KP, NP>() + 1024)) < 4 ? (int)((227 * 1024) / (conv_res_smem<KP, NP>() + 1024)) : 4;
+}
+
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+template <int KP, int NP, int EPI>
+__global__ void __launch_bounds__(CONV_THREADS)
+conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
+                const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
+                const float* __restrict__ pre_prev, int nout_valid) {
+  constexpr int AS = KP + 8, NTL = NP / 8;
+  static_assert(NTL % 2 == 0, "B fragments load two n-tiles at a time");
+  extern __shared__ __align__(16) unsigned char cr_smem[];
+  __nv_bfloat16* const sW = reinterpret_cast<__nv_bfloat16*>(cr_smem);
+  __nv_bfloat16* const sT0 = sW + NET_TAPS * NP * AS;
+  for (int t = threadIdx.x; t < NET_TAPS * NP * (KP / 8); t += CONV_THREADS) {
+    const int row = t / (KP / 8), c = t - row * (KP / 8);
+    cp_async_16(sW + row * AS + c * 8, Wt + (long long)row * KP + c * 8);
+  }
+  cp_async_commit();
+  const int nbx = n / 8, nby = n / 2, nbz = n / 4;
+  const long long nb3 = (long long)nbx * nby * nbz;
+  const long long nblk = (long long)batch * nb3;
+  const long long N = (long long)n * n * n;
+  auto origin = [&](long long b, long long& s, int& x0, int& y0, int& z0) {
+    s = b / nb3;
+    const long long r = b - s * nb3;
+    z0 = 4 * (int)(r / ((long long)nbx * nby));
+    y0 = 2 * (int)((r / nbx) % nby);
+    x0 = 8 * (int)(r % nbx);
+  };
+  auto load_block = [&](long long b, int buf) {
+    long long s;
+    int x0, y0, z0;
+    origin(b, s, x0, y0, z0);
+    const __nv_bfloat16* ins = in + s * N * KP;
+    __nv_bfloat16* const sT = sT0 + buf * CR_HALO * AS;
+    for (int t = threadIdx.x; t < CR_HALO * (KP / 8); t += CONV_THREADS) {
+      const int h = t / (KP / 8), c = t - h * (KP / 8);
+      const int hz = h / (CR_HX * CR_HY), hy = (h / CR_HX) % CR_HY, hx = h % CR_HX;
+      int x = x0 - 1 + hx, y = y0 - 1 + hy, z = z0 - 1 + hz;
+      x = x < 0 ? x + n : (x >= n ? x - n : x);
+      y = y < 0 ? y + n : (y >= n ? y - n : y);
+      z = z < 0 ? z + n : (z >= n ? z - n : z);
+      cp_async_16(sT + h * AS + c * 8, ins + (((long long)z * n + y) * n + x) * KP + c * 8);
+    }
+    cp_async_commit();
+  };
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3, mat = lane >> 3, lr = lane & 7;
+  // this lane's ldmatrix rows: A voxel m = lr + 8 (mat & 1) of slice z = warp
+  const int am = lr + 8 * (mat & 1);
+  const int ah = (am & 7) + CR_HX * (am >> 3) + CR_HX * CR_HY * warp;  // halo row at tap offsets 0
+  const int ak = 8 * (mat >> 1);
+  long long b = blockIdx.x;
+  int buf = 0;
+  if (b < nblk) load_block(b, 0);
+  for (; b < nblk; b += gridDim.x, buf ^= 1) {
+    const long long nxt = b + gridDim.x;
+    if (nxt < nblk) {
+      load_block(nxt, buf ^ 1);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      cp_async_wait_all();
+    }
+    __syncthreads();
+    const __nv_bfloat16* T = sT0 + buf * CR_HALO * AS;
+    float acc[NTL][4];
+#pragma unroll
+    for (int j = 0; j < NTL; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll 1
+    for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+      for (int t9 = 0; t9 < 9; ++t9) {
+        const int tap = dz * 9 + t9, dy = t9 / 3, dx = t9 - dy * 3;
+        const __nv_bfloat16* arow = T + (ah + dx + CR_HX * dy + CR_HX * CR_HY * dz) * AS + ak;
+#pragma unroll
+        for (int kk = 0; kk < KP; kk += 16) {
+          unsigned a[4];
+          ldsm_x4(a, arow + kk);
+#pragma unroll
+          for (int p = 0; p < NTL / 2; ++p) {
+            unsigned r[4];
+            ldsm_x4(r, sW + (tap * NP + 16 * p + 8 * (mat >> 1) + lr) * AS + kk + 8 * (mat & 1));
+            mma_bf16(acc[2 * p], a, r[0], r[1]);
+            mma_bf16(acc[2 * p + 1], a, r[2], r[3]);
+          }
+        }
+      }
+    long long s;
+    int x0, y0, z0;
+    origin(b, s, x0, y0, z0);
+#pragma unroll
+    for (int h2 = 0; h2 < 2; ++h2) {
+      const int m = gid + 8 * h2;
+      const long long v = s * N + ((long long)(z0 + warp) * n + (y0 + (m >> 3))) * n + (x0 + (m & 7));
+#pragma unroll
+      for (int j = 0; j < NTL; ++j) {
+        const int co = j * 8 + tig * 2;
+        float x0v = acc[j][h2 * 2], x1v = acc[j][h2 * 2 + 1];
+        if (EPI == 0) {
+          x0v += bias[co];
+          x1v += bias[co + 1];
+          *reinterpret_cast<float2*>(pre_out + v * NP + co) = make_float2(x0v, x1v);
+          *reinterpret_cast<__nv_bfloat162*>(act_out + v * NP + co) =
+              __halves2bfloat162(__float2bfloat16(gelu_f(x0v)), __float2bfloat16(gelu_f(x1v)));
+        } else if (EPI == 1) {
+          x0v += bias[co];
+          x1v += bias[co + 1];
+          *reinterpret_cast<float2*>(pre_out + v * NP + co) =
+              make_float2(co < nout_valid ? x0v : 0.f, co + 1 < nout_valid ? x1v : 0.f);
+        } else {
+          const float2 pp = *reinterpret_cast<const float2*>(pre_prev + v * NP + co);
+          *reinterpret_cast<__nv_bfloat162*>(act_out + v * NP + co) =
+              __halves2bfloat162(__float2bfloat16(x0v * gelu_grad_f(pp.x)), __float2bfloat16(x1v * gelu_grad_f(pp.y)));
+        }
+      }
+    }
+    __syncthreads();  // this buffer is refilled by the next iteration's prefetch
+  }
+}
+
 // Launch the tiled convolution when the grid allows it, else the row form.
 template <int KP, int NP, int EPI>
 static void conv_launch(long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* W, const float* bias,
                         float* pre_out, __nv_bfloat16* act_out, const float* pre_prev, int nout_valid,
                         cudaStream_t st) {
-  if (n % TB == 0) {
+  if (n % 8 == 0) {
+    const long long N = (long long)n * n * n;
+    const long long nblk = V / 64;
+    const long long ctas = std::min<long long>(nblk, (long long)conv_res_per_sm<KP, NP>() * 152);
+    conv_res_kernel<KP, NP, EPI><<<(unsigned)ctas, CONV_THREADS, conv_res_smem<KP, NP>(), st>>>(
+        (int)(V / N), n, in, W, bias, pre_out, act_out, pre_prev, nout_valid);
+  } else if (n % TB == 0) {
     const long long N = (long long)n * n * n;
     const long long blocks = (V / N) * (N / (TB * TB * TB));
     conv_tile_kernel<KP, NP, EPI><<<(unsigned)blocks, CONV_THREADS, 0, st>>>(n, in, W, bias, pre_out, act_out,
@@ -812,12 +966,44 @@ static double host_normal(uint64_t seed, uint64_t i) {
 
 using namespace exc;
 
+namespace exc {
+
+// Shared-memory opt-in of the weight-resident convolutions (before any
+// stream capture).
+template <int KP, int NP, int EPI>
+static cudaError_t conv_res_attr() {
+  return cudaFuncSetAttribute(conv_res_kernel<KP, NP, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)conv_res_smem<KP, NP>());
+}
+static int configure_learned() {
+  static std::mutex mu;
+  static bool done[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    set_last_error("no usable CUDA device");
+    return EXC_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev]) return EXC_OK;
+  cudaError_t e = conv_res_attr<16, 32, 0>();
+  if (e == cudaSuccess) e = conv_res_attr<32, 32, 0>();
+  if (e == cudaSuccess) e = conv_res_attr<32, 16, 1>();
+  if (e == cudaSuccess) e = conv_res_attr<16, 32, 2>();
+  if (e == cudaSuccess) e = conv_res_attr<32, 32, 2>();
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  done[dev] = true;
+  return EXC_OK;
+}
+
+}  // namespace exc
+
 extern "C" {
 
 int exc_net_create(uint64_t seed, exc_net** out) {
   if (!out) { set_last_error("null argument"); return EXC_ERR_ARG; }
   *out = nullptr;
   int rc = configure_device();
+  if (rc == EXC_OK) rc = configure_learned();
   if (rc) return rc;
   exc_net* net = new exc_net();
   const size_t pb = exc_net::NPARAM * sizeof(float);

@@ -538,7 +538,7 @@ __device__ __forceinline__ void ldsm_x4_trans(unsigned (&r)[4], const void* p) {
 template <int KP, int NP>
 __global__ void __launch_bounds__(WT_THREADS, 1)
 wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ g,
-                  float* __restrict__ part) {
+                  float* __restrict__ part, double* __restrict__ bpart) {
   constexpr int MT = KP / 16, NTL = NP / 8, KS = KP + 8, NS = NP + 8;
   static_assert(NTL % 2 == 0, "B fragments load two n-tiles at a time");
   extern __shared__ __align__(16) unsigned char wt_smem[];
@@ -586,6 +586,11 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
   };
   // ldmatrix lane roles: matrix mat = lane / 8, row r = lane % 8
   const int mat = lane >> 3, lr = lane & 7;
+  // bias gradient db[co] = sum_v g[v][co] from the same g rows: thread
+  // t < 2 NP sums rows 32 (t / NP) .. + 31 of channel t % NP per block in
+  // FP32 and the block sums in FP64, in the CTA's fixed block order
+  const int bco = threadIdx.x % NP, bhalf = threadIdx.x / NP;
+  double bsum = 0.0;
   long long b = blockIdx.x;
   int buf = 0;
   if (b < nblk) load_block(b, 0);
@@ -600,6 +605,12 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
     __syncthreads();
     const __nv_bfloat16* X = sX0 + buf * WT_HALO * KS;
     const __nv_bfloat16* G = sG0 + buf * 64 * NS;
+    if (bhalf < 2) {
+      float fs = 0.f;
+#pragma unroll 8
+      for (int v = 32 * bhalf; v < 32 * bhalf + 32; ++v) fs += __bfloat162float(G[v * NS + bco]);
+      bsum += (double)fs;
+    }
 #pragma unroll
     for (int kz = 0; kz < 4; ++kz) {
       // B: voxels k = x + 8 y of slice kz; two n-tiles per ldmatrix.x4
@@ -631,6 +642,7 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
     }
     __syncthreads();  // this buffer is refilled by the next iteration's prefetch
   }
+  if (bhalf < 2) bpart[((long long)blockIdx.x * 2 + bhalf) * NP + bco] = bsum;
   // C fragment: rows (ci) gid / gid + 8, columns (co) tig * 2 + {0, 1}
   const int gid = lane >> 2, tig = lane & 3;
 #pragma unroll
@@ -702,12 +714,17 @@ __global__ void bgrad_fold_kernel(int nblk, const double* __restrict__ part, flo
 template <typename T>
 __global__ void pack_input_kernel(long long V, long long N, const T* __restrict__ f, double scale,
                                   __nv_bfloat16* __restrict__ out, int KP) {
+  // one voxel row per thread, written as 16-byte pieces (KP % 8 == 0)
+  const IdxDiv dN(N);
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    const long long b = v / N, r = v - b * N;
-    for (int c = 0; c < KP; ++c) {
-      float x = c < 3 ? (float)((double)f[(b * 3 + c) * N + r] * scale) : 0.f;
-      out[v * KP + c] = __float2bfloat16(x);
-    }
+    const long long b = dN.div(v), r = v - b * N;
+    __nv_bfloat16 row[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      row[c] = __float2bfloat16(c < 3 ? (float)((double)f[(b * 3 + c) * N + r] * scale) : 0.f);
+    uint4* o = reinterpret_cast<uint4*>(out + v * KP);
+    o[0] = *reinterpret_cast<const uint4*>(row);
+    for (int c = 1; c < KP / 8; ++c) o[c] = make_uint4(0, 0, 0, 0);
   }
 }
 
@@ -730,14 +747,25 @@ __global__ void loss_grad_kernel(long long V, long long N, const float* __restri
                                  double* __restrict__ part) {
   __shared__ double red[256];
   double s = 0;
+  const IdxDiv dN(N);
+  const float gs = (float)(2.0 * inv_count);
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    const long long b = v / N, r = v - b * N;
-    for (int c = 0; c < OUTP; ++c) {
+    const long long b = dN.div(v), r = v - b * N;
+    // the output row's first 4 words in one 16-byte load; the gradient row
+    // (3 values, then zeros) in 16-byte pieces
+    const float4 o4 = *reinterpret_cast<const float4*>(out + v * OUTP);
+    const float oc[3] = {o4.x, o4.y, o4.z};
+    __nv_bfloat16 row[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
       float d = 0.f;
-      if (c < 3) d = out[v * OUTP + c] - (float)((double)tgt[(b * 3 + c) * N + r] * tscale);
-      s += (double)d * d;
-      g[v * OUTP + c] = __float2bfloat16((float)(2.0 * inv_count) * d);
+      if (c < 3) d = oc[c] - (float)((double)tgt[(b * 3 + c) * N + r] * tscale);
+      if (c < 3) s += (double)d * d;
+      row[c] = __float2bfloat16(gs * d);
     }
+    uint4* gr = reinterpret_cast<uint4*>(g + v * OUTP);
+    gr[0] = *reinterpret_cast<const uint4*>(row);
+    gr[1] = make_uint4(0, 0, 0, 0);
   }
   red[threadIdx.x] = s;
   __syncthreads();
@@ -847,7 +875,7 @@ static int ensure_workspace(exc_net* net, long long V) {
             cudaMalloc(&net->pre1, V * exc_net::N1 * 4) == cudaSuccess &&
             cudaMalloc(&net->pre2, V * exc_net::N2 * 4) == cudaSuccess &&
             cudaMalloc(&net->out, V * exc_net::N3 * 4) == cudaSuccess &&
-            cudaMalloc(&net->wpart, nchunk * 27 * 32 * 32 * 4) == cudaSuccess &&
+            cudaMalloc(&net->wpart, nchunk * 27 * 32 * 32 * 4 + (long long)WT_CTAS * 2 * 32 * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&net->lpart, (1024 + 8) * sizeof(double)) == cudaSuccess;
   if (!ok) {
     free_workspace(net);
@@ -886,11 +914,16 @@ static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfl
   int nchunk;
   const long long N = (long long)n * n * n;
   if (n % 8 == 0) {
-    // all taps per CTA over 8 x 2 x 4 voxel blocks, one persistent CTA per SM
+    // all taps per CTA over 8 x 2 x 4 voxel blocks, one persistent CTA per
+    // SM; the bias partials follow the weight partials in the buffer
     const long long nblk = V / 64;
     nchunk = (int)std::min<long long>(nblk, WT_CTAS);
+    double* bpart = reinterpret_cast<double*>(net->wpart + (size_t)WT_CTAS * NET_TAPS * 32 * 32);
     wgrad_tile_kernel<KP, NP><<<nchunk, WT_THREADS, wgrad_tile_smem<KP, NP>(), st>>>((int)(V / N), n, in, g,
-                                                                                      net->wpart);
+                                                                                      net->wpart, bpart);
+    wgrad_fold_kernel<KP, NP><<<(27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
+    bgrad_fold_kernel<NP><<<1, 32, 0, st>>>(2 * nchunk, bpart, net->dB(l));
+    return cudaGetLastError();
   } else {
     nchunk = (int)((V + WG_CHUNK - 1) / WG_CHUNK);
     wgrad_partial_kernel<KP, NP><<<dim3(nchunk, 27), 128, 0, st>>>(V, n, in, g, net->wpart);

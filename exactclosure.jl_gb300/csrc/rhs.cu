@@ -12,6 +12,11 @@
 // value is computed once (plus the x/y halo), copy offsets are computed once
 // per thread, and global loads and stores are row-contiguous.  Stresses are
 // kept divided by h.
+#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's driver entry point)
+
+#include <cstring>
+#include <mutex>
+
 #include "internal.cuh"
 
 namespace exc {
@@ -268,11 +273,51 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
 // ---------------------------------------------------------------------------
 constexpr int QX = 64, QY = 16, QBX = QX + 2, QBY = QY + 2;
 constexpr int QROW = 72;  // box x b at b + 3: left piece [0, 4), interior [4, 68), right piece [68, 72)
+constexpr int QPLANE = QBY * QROW;                 // words of one component plane
+constexpr int QCOMP = (QPLANE + 31) / 32 * 32;     // padded to 128 bytes (TMA destinations)
 
-struct QuadSmem {
-  __align__(16) float u[3][3][QBY][QROW];
-  float s[5][QBY][QBX];  // s11, s22, s12, s13, s23 of the current plane
+struct QuadComp {
+  float r[QBY][QROW];
+  float pad[QCOMP - QPLANE];
 };
+struct QuadSmem {
+  QuadComp u[3][3];      // [plane buffer][component]
+  float s[5][QBY][QBX];  // s11, s22, s12, s13, s23 of the current plane
+  unsigned long long bar[3];  // TMA completion of each plane buffer
+};
+// dynamic shared memory of rhs_quad_kernel: the struct plus room to align it
+// to 128 bytes
+constexpr size_t QUAD_SMEM = sizeof(QuadSmem) + 128;
+
+// Set when a wait for a TMA plane gave up (the copy never completed): the
+// sweep then ran on incomplete data; read and cleared by exc_device_faults.
+__device__ int g_rhs_tma_fault = 0;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// 3-D tiled TMA load of one box (x, y, z) of the tensor map into shared memory
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
 
 __device__ __forceinline__ float qdiag(float a, float b, float kd, float kv2) {
   const float s = a + b, d = a - b;
@@ -285,9 +330,9 @@ __device__ __forceinline__ float qoff(float a, float b, float c, float d, float 
 template <bool DOADD>
 __global__ void __launch_bounds__(256, 3)
 rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, float* __restrict__ du, SlotBatch sb,
-                int zblocks, int ptz) {
-  extern __shared__ __align__(16) unsigned char quad_smem[];
-  QuadSmem& sm = *reinterpret_cast<QuadSmem*>(quad_smem);
+                int zblocks, int ptz, const __grid_constant__ CUtensorMap umap, int have_map) {
+  extern __shared__ __align__(128) unsigned char quad_smem[];
+  QuadSmem& sm = *reinterpret_cast<QuadSmem*>(quad_smem + ((128u - (smem_u32(quad_smem) & 127u)) & 127u));
   const long long N = (long long)n * n * n;
   const int slot = blockIdx.z / zblocks;
   const int zb = blockIdx.z - slot * zblocks;
@@ -316,17 +361,57 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
       const int gy = wrap(y0 - 1 + rr);
       const int gx = j == 0 ? wrap(x0 - 4) : (j == 17 ? wrap(x0 + QX) : x0 + 4 * (j - 1));
       goff[i] = c * N + (long long)gy * n + gx;
-      soff[i] = (c * QBY + rr) * QROW + 4 * j;
+      soff[i] = c * QCOMP + rr * QROW + 4 * j;
     }
   }
   const long long nn = (long long)n * n;
+  // tiles whose box (x0 - 4 .. x0 + 67, y0 - 1 .. y0 + 16) lies inside the
+  // grid take each component plane as one TMA box, completed on the
+  // buffer's mbarrier; the others (their halo wraps around the periodic
+  // boundary) use the cp.async pieces
+  const bool tma = have_map && x0 >= 4 && x0 + QX + 4 <= n && y0 >= 1 && y0 + QY + 1 <= n;
+  unsigned parity = 0;  // bit b: phase of buffer b's mbarrier to wait for
+  if (tma) {
+    if (tid == 0) {
+#pragma unroll
+      for (int b = 0; b < 3; ++b) mbar_init(&sm.bar[b], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+  }
   auto load_plane = [&](int buf, int gz) {
-    float* const s0 = &sm.u[buf][0][0][0];
+    if (tma) {
+      if (tid == 0) {
+        mbar_expect_tx(&sm.bar[buf], 3u * QPLANE * sizeof(float));
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          tma_load_3d(&sm.u[buf][c].r[0][0], &umap, x0 - 4, y0 - 1, (slot * 3 + c) * n + gz, &sm.bar[buf]);
+      }
+      return;
+    }
+    float* const s0 = &sm.u[buf][0].r[0][0];
     const float* const ub = u + gz * nn;
 #pragma unroll
     for (int i = 0; i < NSQ; ++i)
       if (goff[i] >= 0) cp_async_16(s0 + soff[i], ub + goff[i]);
     cp_async_commit();
+  };
+  // completion of the loads of buffer buf (its mbarrier phase, or every
+  // cp.async of this thread); a TMA wait gives up after about 2^20 polls,
+  // records the fault and goes on
+  auto wait_plane = [&](int buf) {
+    if (!tma) {
+      cp_async_wait_all();
+      return;
+    }
+    int polls = 0;
+    while (!mbar_try_wait(&sm.bar[buf], (parity >> buf) & 1u)) {
+      if (++polls > (1 << 20)) {
+        if (tid == 0) atomicExch(&g_rhs_tma_fault, 1);
+        break;
+      }
+    }
+    parity ^= 1u << buf;
   };
   // this thread: box columns c0 = 2 tx + 1, c0 + 1 and rows r0 = 2 ty + 1, r0 + 1
   const int c0 = 2 * tx + 1, r0 = 2 * ty + 1;
@@ -335,7 +420,9 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
   load_plane(0, wrap(z0 - 1));
   load_plane(1, wrap(z0));
   load_plane(2, wrap(z0 + 1));
-  cp_async_wait_all();
+  wait_plane(0);
+  wait_plane(1);
+  wait_plane(2);
   __syncthreads();
   float p13[2][2], p23[2][2], p33[2][2];  // [row j][col i]
 #pragma unroll
@@ -343,10 +430,10 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
     const auto& ua = sm.u[0];  // plane z0 - 1
     const auto& ub = sm.u[1];  // plane z0
     const int r = r0 + j;
-    const float2 a1 = f2(ua[0][r]), b1 = f2(ub[0][r]), a3 = f2(ua[2][r]), a2 = f2(ua[1][r]), b2 = f2(ub[1][r]);
-    const float a3r = ua[2][r][sc + 2];
-    const float2 a3u = f2(ua[2][r + 1]);
-    const float2 b3 = f2(ub[2][r]);
+    const float2 a1 = f2(ua[0].r[r]), b1 = f2(ub[0].r[r]), a3 = f2(ua[2].r[r]), a2 = f2(ua[1].r[r]), b2 = f2(ub[1].r[r]);
+    const float a3r = ua[2].r[r][sc + 2];
+    const float2 a3u = f2(ua[2].r[r + 1]);
+    const float2 b3 = f2(ub[2].r[r]);
     p13[j][0] = qoff(a1.x, b1.x, a3.x, a3.y, kd, kv);
     p13[j][1] = qoff(a1.y, b1.y, a3.y, a3r, kd, kv);
     p23[j][0] = qoff(a2.x, b2.x, a3.x, a3u.x, kd, kv);
@@ -373,18 +460,18 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
     float u1l[2], u2r2[2], u3r2[2];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      u1r[k] = f2(uc[0][r0 + k]);
-      u2r[k] = f2(uc[1][r0 - 1 + k]);
-      u3r[k] = f2(uc[2][r0 + k]);
+      u1r[k] = f2(uc[0].r[r0 + k]);
+      u2r[k] = f2(uc[1].r[r0 - 1 + k]);
+      u3r[k] = f2(uc[2].r[r0 + k]);
     }
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
-      u1l[j] = uc[0][r0 + j][sc - 1];
-      u2r2[j] = uc[1][r0 + j][sc + 2];
-      u3r2[j] = uc[2][r0 + j][sc + 2];
-      u1n[j] = f2(un[0][r0 + j]);
-      u2n[j] = f2(un[1][r0 + j]);
-      u3n[j] = f2(un[2][r0 + j]);
+      u1l[j] = uc[0].r[r0 + j][sc - 1];
+      u2r2[j] = uc[1].r[r0 + j][sc + 2];
+      u3r2[j] = uc[2].r[r0 + j][sc + 2];
+      u1n[j] = f2(un[0].r[r0 + j]);
+      u2n[j] = f2(un[1].r[r0 + j]);
+      u3n[j] = f2(un[2].r[r0 + j]);
     }
     float v11[2][2], v22[2][2], v12[2][2], v13[2][2], v23[2][2], v33[2][2];
 #pragma unroll
@@ -424,24 +511,24 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
     // column QX+1)
     if (warp == 0) {
       for (int c = lane + 1; c <= QX; c += 32)
-        sm.s[2][0][c] = qoff(uc[0][0][c + 3], uc[0][1][c + 3], uc[1][0][c + 3], uc[1][0][c + 4], kd, kv);
+        sm.s[2][0][c] = qoff(uc[0].r[0][c + 3], uc[0].r[1][c + 3], uc[1].r[0][c + 3], uc[1].r[0][c + 4], kd, kv);
     } else if (warp == 1) {
       for (int c = lane + 1; c <= QX; c += 32)
-        sm.s[4][0][c] = qoff(uc[1][0][c + 3], un[1][0][c + 3], uc[2][0][c + 3], uc[2][1][c + 3], kd, kv);
+        sm.s[4][0][c] = qoff(uc[1].r[0][c + 3], un[1].r[0][c + 3], uc[2].r[0][c + 3], uc[2].r[1][c + 3], kd, kv);
     } else if (warp == 2) {
       for (int c = lane + 1; c <= QX; c += 32)
-        sm.s[1][QY + 1][c] = qdiag(uc[1][QY + 1][c + 3], uc[1][QY][c + 3], kd, kv2);
+        sm.s[1][QY + 1][c] = qdiag(uc[1].r[QY + 1][c + 3], uc[1].r[QY][c + 3], kd, kv2);
     } else if (warp == 3) {
-      if (lane <= QY) sm.s[2][lane][0] = qoff(uc[0][lane][3], uc[0][lane + 1][3], uc[1][lane][3], uc[1][lane][4], kd, kv);
+      if (lane <= QY) sm.s[2][lane][0] = qoff(uc[0].r[lane][3], uc[0].r[lane + 1][3], uc[1].r[lane][3], uc[1].r[lane][4], kd, kv);
     } else if (warp == 4) {
       if (lane < QY) {
         const int r = lane + 1;
-        sm.s[3][r][0] = qoff(uc[0][r][3], un[0][r][3], uc[2][r][3], uc[2][r][4], kd, kv);
+        sm.s[3][r][0] = qoff(uc[0].r[r][3], un[0].r[r][3], uc[2].r[r][3], uc[2].r[r][4], kd, kv);
       }
     } else if (warp == 5) {
       if (lane < QY) {
         const int r = lane + 1;
-        sm.s[0][r][QX + 1] = qdiag(uc[0][r][QX + 4], uc[0][r][QX + 3], kd, kv2);
+        sm.s[0][r][QX + 1] = qdiag(uc[0].r[r][QX + 4], uc[0].r[r][QX + 3], kd, kv2);
       }
     }
     __syncthreads();
@@ -482,7 +569,7 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
         *o3 = make_float2(-d3[0], -d3[1]);
       }
     }
-    cp_async_wait_all();
+    if (kz + 1 < ptz && z + 1 < n) wait_plane(pre);
     __syncthreads();
     const int freed = cur;
     cur = nxt;
@@ -495,6 +582,43 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
 // recomputed for fewer cells and adjacent rows share their u reads); four ran
 // slower in FP32 (94 registers, two CTAs per SM).
 template <typename T> constexpr int CYT = 2;
+
+// The driver's tensor-map encoder, reached through the runtime (no link to
+// the driver library); null when the driver does not provide it.
+using TensorMapEncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                          const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                          CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                          CUtensorMapFloatOOBfill);
+static TensorMapEncodeTiled tensor_map_encoder() {
+  static std::once_flag once;
+  static TensorMapEncodeTiled fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<TensorMapEncodeTiled>(p);
+  });
+  return fn;
+}
+
+// Tensor map of the FP32 vector fields of nslots solves as one 3-D tensor
+// (x, y, (slot * 3 + component) * n + z) with QROW x QBY x 1 boxes; false when
+// it cannot be made (the sweep then copies with cp.async).
+static bool quad_tensor_map(const float* u, int n, int nslots, const SlotBatch& sb, CUtensorMap* map) {
+  std::memset(map, 0, sizeof(*map));
+  const long long N = (long long)n * n * n;
+  if (nslots > 1 && sb.ustride != 3 * N) return false;
+  TensorMapEncodeTiled enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)nslots * 3 * n};
+  const cuuint64_t strides[2] = {(cuuint64_t)n * sizeof(float), (cuuint64_t)n * n * sizeof(float)};
+  const cuuint32_t box[3] = {QROW, QBY, 1};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(u), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 template <typename T>
 cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st, const SlotBatch& sb,
@@ -520,12 +644,14 @@ cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaSt
         zsplit((long long)(n / QX) * (n / QY), 3, ptz, zblocks) >= 3LL * 152) {
       dim3 gq(n / QX, n / QY, zblocks * nslots);
       const float ih = (float)(1.0 / (double)h);
+      CUtensorMap map;
+      const int have = quad_tensor_map((const float*)u, n, nslots, sb, &map) ? 1 : 0;
       if (doadd)
-        rhs_quad_kernel<true><<<gq, dim3(32, 8), sizeof(QuadSmem), st>>>(n, ih, (float)visc, (const float*)u, (float*)du,
-                                                                         sb, zblocks, ptz);
+        rhs_quad_kernel<true><<<gq, dim3(32, 8), QUAD_SMEM, st>>>(n, ih, (float)visc, (const float*)u, (float*)du, sb,
+                                                                  zblocks, ptz, map, have);
       else
-        rhs_quad_kernel<false><<<gq, dim3(32, 8), sizeof(QuadSmem), st>>>(n, ih, (float)visc, (const float*)u,
-                                                                          (float*)du, sb, zblocks, ptz);
+        rhs_quad_kernel<false><<<gq, dim3(32, 8), QUAD_SMEM, st>>>(n, ih, (float)visc, (const float*)u, (float*)du, sb,
+                                                                   zblocks, ptz, map, have);
       return cudaGetLastError();
     }
   }
@@ -553,9 +679,9 @@ static cudaError_t configure_rhs_t() {
 cudaError_t configure_stencil() {
   cudaError_t e = configure_rhs_t<float>();
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rhs_quad_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(QuadSmem));
+    e = cudaFuncSetAttribute(rhs_quad_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUAD_SMEM);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rhs_quad_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(QuadSmem));
+    e = cudaFuncSetAttribute(rhs_quad_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUAD_SMEM);
   if (e == cudaSuccess) e = configure_rhs_t<double>();
   return e;
 }
@@ -566,3 +692,13 @@ template cudaError_t launch_rhs<float>(int, float, float, const float*, float*, 
                                        int);
 
 }  // namespace exc
+
+extern "C" int exc_device_faults(int* flags) {
+  if (!flags) { exc::set_last_error("null argument"); return EXC_ERR_ARG; }
+  int v = 0, zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, exc::g_rhs_tma_fault, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(exc::g_rhs_tma_fault, &zero, sizeof(int));
+  if (e != cudaSuccess) { exc::set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  *flags = v;
+  return EXC_OK;
+}

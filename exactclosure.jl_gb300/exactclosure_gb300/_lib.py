@@ -83,6 +83,7 @@ SIGNATURES = {
     "exc_poisson_create": [i32, i32, f64, C.POINTER(vp)],
     "exc_poisson_destroy": [vp],
     "exc_poisson_set_engine": [vp, i32],
+    "exc_device_faults": [C.POINTER(i32)],
     "exc_poisson_solve": [vp, vp, vp, vp],
     "exc_project": [vp, vp, vp, vp],
     "exc_project_noalloc": [i32, i32, f64, vp, vp, vp],

@@ -131,6 +131,13 @@ class PoissonSolver:
             pass
 
 
+def device_faults() -> int:
+    """Device fault flags recorded since the last call (0 = none)."""
+    v = C.c_int()
+    call("exc_device_faults", C.byref(v))
+    return v.value
+
+
 def poissonsolver(grid: Grid, precision: int = EXC_F64, engine: int = 0) -> PoissonSolver:
     return PoissonSolver(grid, precision, engine)
 

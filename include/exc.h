@@ -87,6 +87,12 @@ int exc_pressuregradient(int precision, int n, double l, void* u, const void* p,
 typedef struct exc_poisson exc_poisson;
 int exc_poisson_create(int precision, int n, double l, exc_poisson** out);
 int exc_poisson_destroy(exc_poisson* ps);
+/* Device faults recorded by kernels since the last call (and cleared): bit 0
+ * = a wait for a TMA plane of the FP32 RHS sweep gave up after its poll
+ * limit (the copy never completed; that sweep's output is not valid).  0 in
+ * normal operation. */
+int exc_device_faults(int* flags);
+
 /* FFT engine of a solver (no counterpart in the reference): 0 = register-
  * resident two-level passes where the grid has a plan (n = 32, 48, 64, 96,
  * 128, 192, 256 and, in FP32, 384, 512, 1024), shared-memory Stockham passes

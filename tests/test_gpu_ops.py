@@ -102,9 +102,10 @@ def test_poisson_solve_and_divergence(NS, n):
     assert rel(host(ut), ns.pressuregradient(u, ns.poisson_solve(dref, l / n), l / n)) < TOL64
 
 
-@pytest.mark.parametrize("n", [64, 128])
+@pytest.mark.parametrize("n", [64, 128, 256])
 def test_f32_rhs_two_by_two_cells(NS, n):
-    """FP32 sweep of 64-multiple grids (2 x 2 cells per thread), both modes."""
+    """FP32 sweep of 64-multiple grids (2 x 2 cells per thread), both modes;
+    at 256^3 the interior tiles arrive by TMA."""
     import torch
 
     l, visc = 1.0, 1 / 900
@@ -118,6 +119,7 @@ def test_f32_rhs_two_by_two_cells(NS, n):
     du2 = dev(base, "float32")
     NS.tensordivergence(du2, dev(u, "float32"), visc, g, doadd=True)
     assert rel(host(du2), base + ref) < TOL32
+    assert NS.device_faults() == 0
 
 
 @pytest.mark.parametrize("n", [16, 64])

@@ -21,6 +21,36 @@
 
 namespace exc {
 
+// Set when a wait for a TMA plane gave up (the copy never completed): the
+// sweep then ran on incomplete data; read and cleared by exc_device_faults.
+__device__ int g_rhs_tma_fault = 0;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// 3-D tiled TMA load of one box (x, y, z) of the tensor map into shared memory
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
 constexpr int PTX = 32, NWARP = 8;
 constexpr int PBX = PTX + 2;  // plane box with one-cell halo (box x = x - x0 + 1)
 // u rows in shared memory: box x index xb sits at xb + SH<T>, so the 32
@@ -32,13 +62,30 @@ template <typename T> constexpr int UROW = ((SH<T> + PBX) + 16 / (int)sizeof(T) 
 template <int NC> constexpr int PTYT = NWARP * NC;
 template <int NC> constexpr int PBYT = PTYT<NC> + 2;
 
+// One component plane of a buffer: PBY rows of UROW words, padded to a
+// multiple of 128 bytes (TMA destinations); u[c][row] is the row's pointer.
 template <typename T, int NC>
-struct PlaneSmem {
-  __align__(16) T u[3][3][PBYT<NC>][UROW<T>];
-  T s[5][PBYT<NC>][PBX];  // s11, s22, s12, s13, s23 of the current plane
+struct CompPlane {
+  static constexpr int WORDS = PBYT<NC> * UROW<T>;
+  static constexpr int PADDED = (WORDS * (int)sizeof(T) + 127) / 128 * 128 / (int)sizeof(T);
+  T r[PBYT<NC>][UROW<T>];
+  T pad[PADDED > WORDS ? PADDED - WORDS : 128 / (int)sizeof(T)];
+  __device__ __forceinline__ const T* operator[](int row) const { return r[row]; }
+  __device__ __forceinline__ T* operator[](int row) { return r[row]; }
 };
 
-template <typename T, int NC> using UPlane = T[3][PBYT<NC>][UROW<T>];
+template <typename T, int NC>
+struct PlaneSmem {
+  CompPlane<T, NC> u[3][3];  // [plane buffer][component]
+  T s[5][PBYT<NC>][PBX];     // s11, s22, s12, s13, s23 of the current plane
+  unsigned long long bar[3];  // TMA completion of each plane buffer
+};
+// dynamic shared memory of rhs_kernel: the struct plus room to align it to
+// 128 bytes
+template <typename T, int NC>
+constexpr size_t plane_smem_bytes() {
+  return sizeof(PlaneSmem<T, NC>) + 128;
+}
 
 // sigma_ii at box (bx, by) of plane buffer b (uses u_i at the cell and at -e_i)
 template <typename T, int I, typename U>
@@ -79,10 +126,13 @@ __device__ __forceinline__ T s33(T up, T lo, T kd, T kv2) {
 
 template <typename T, int NC, bool DOADD>
 __global__ void __launch_bounds__(PTX * NWARP, sizeof(T) == 4 ? 4 : 3)
-rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks, int ptz) {
+rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks, int ptz,
+           const __grid_constant__ CUtensorMap umap, int have_map) {
   constexpr int PTY = PTYT<NC>, PBY = PBYT<NC>;
-  extern __shared__ __align__(16) unsigned char rhs_smem[];
-  PlaneSmem<T, NC>& sm = *reinterpret_cast<PlaneSmem<T, NC>*>(rhs_smem);
+  constexpr int CSTRIDE = (int)(sizeof(CompPlane<T, NC>) / sizeof(T));
+  extern __shared__ __align__(128) unsigned char rhs_smem[];
+  PlaneSmem<T, NC>& sm =
+      *reinterpret_cast<PlaneSmem<T, NC>*>(rhs_smem + ((128u - (smem_u32(rhs_smem) & 127u)) & 127u));
   const long long N = (long long)n * n * n;
   // slot of a batch of same-size solves (serving form): blockIdx.z = slot * zblocks + zb
   const int slot = blockIdx.z / zblocks;
@@ -129,14 +179,36 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
         const int gx = j < NV ? x0 + j * VE : (j == NV ? wrap(x0 - VE) : wrap(x0 + PTX));
         const int bx0 = j < NV ? SH<T> + 1 + j * VE : (j == NV ? 0 : SH<T> + 1 + PTX);
         goff[i] = c * N + (long long)gy * n + gx;
-        soff[i] = (c * PBY + rr) * UROW<T> + bx0;
+        soff[i] = c * CSTRIDE + rr * UROW<T> + bx0;
       }
     }
   }
   const long long nn = (long long)n * n;
+  // full tiles whose box (x0 - VE .. x0 - VE + UROW - 1, y0 - 1 .. y0 + PTY)
+  // lies inside the grid take each component plane as one TMA box, completed
+  // on the buffer's mbarrier; the others use the cp.async pieces
+  const bool tma = vec && have_map && x0 >= VE && x0 - VE + UROW<T> <= n && y0 >= 1 && y0 + PTY + 1 <= n;
+  unsigned parity = 0;  // bit b: phase of buffer b's mbarrier to wait for
+  if (tma) {
+    if (tid == 0) {
+#pragma unroll
+      for (int b = 0; b < 3; ++b) mbar_init(&sm.bar[b], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+  }
   auto load_plane = [&](int buf, int gz) {
+    if (tma) {
+      if (tid == 0) {
+        mbar_expect_tx(&sm.bar[buf], 3u * CompPlane<T, NC>::WORDS * sizeof(T));
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          tma_load_3d(&sm.u[buf][c].r[0][0], &umap, x0 - VE, y0 - 1, (slot * 3 + c) * n + gz, &sm.bar[buf]);
+      }
+      return;
+    }
     if (vec) {
-      T* const sb0 = &sm.u[buf][0][0][0];
+      T* const sb0 = &sm.u[buf][0].r[0][0];
       const T* const ub = u + gz * nn;
 #pragma unroll
       for (int i = 0; i < NSLOT; ++i)
@@ -159,10 +231,29 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   const int bx = tx + 1;
   // prologue: planes z0-1 (buffer 0) and z0 (buffer 1) give s13, s23 of plane
   // z0-1 and s33 of plane z0 for this thread's cells
+  // completion of the loads of buffer buf (its mbarrier phase, or every
+  // cp.async of this thread); a TMA wait gives up after about 2^20 polls,
+  // records the fault and goes on
+  auto wait_plane = [&](int buf) {
+    if (!tma) {
+      cp_async_wait_all();
+      return;
+    }
+    int polls = 0;
+    while (!mbar_try_wait(&sm.bar[buf], (parity >> buf) & 1u)) {
+      if (++polls > (1 << 20)) {
+        if (tid == 0) atomicExch(&g_rhs_tma_fault, 1);
+        break;
+      }
+    }
+    parity ^= 1u << buf;
+  };
   load_plane(0, zwrap(z0 - 1));
   load_plane(1, zwrap(z0));
   load_plane(2, zwrap(z0 + 1));
-  cp_async_wait_all();
+  wait_plane(0);
+  wait_plane(1);
+  wait_plane(2);
   __syncthreads();
   T s13_prev[NC], s23_prev[NC], s33_cur[NC];
 #pragma unroll
@@ -254,7 +345,7 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
         s33_cur[i] = v33n[i];
       }
     }
-    cp_async_wait_all();
+    if (kz + 1 < ptz && z + 1 < n) wait_plane(pre);
     __syncthreads();
     const int freed = cur;
     cur = nxt;
@@ -289,35 +380,7 @@ struct QuadSmem {
 // to 128 bytes
 constexpr size_t QUAD_SMEM = sizeof(QuadSmem) + 128;
 
-// Set when a wait for a TMA plane gave up (the copy never completed): the
-// sweep then ran on incomplete data; read and cleared by exc_device_faults.
-__device__ int g_rhs_tma_fault = 0;
 
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// 3-D tiled TMA load of one box (x, y, z) of the tensor map into shared memory
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
-                                            unsigned long long* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
-          smem_u32(dst)),
-      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
-}
 
 __device__ __forceinline__ float qdiag(float a, float b, float kd, float kv2) {
   const float s = a + b, d = a - b;
@@ -602,22 +665,25 @@ static TensorMapEncodeTiled tensor_map_encoder() {
   return fn;
 }
 
-// Tensor map of the FP32 vector fields of nslots solves as one 3-D tensor
-// (x, y, (slot * 3 + component) * n + z) with QROW x QBY x 1 boxes; false when
-// it cannot be made (the sweep then copies with cp.async).
-static bool quad_tensor_map(const float* u, int n, int nslots, const SlotBatch& sb, CUtensorMap* map) {
+// Tensor map of the vector fields of nslots solves as one 3-D tensor
+// (x, y, (slot * 3 + component) * n + z) with boxes of bx x by x 1 words;
+// false when it cannot be made (the sweep then copies with cp.async).
+template <typename T>
+static bool field_tensor_map(const T* u, int n, int nslots, const SlotBatch& sb, unsigned bx, unsigned by,
+                             CUtensorMap* map) {
   std::memset(map, 0, sizeof(*map));
   const long long N = (long long)n * n * n;
   if (nslots > 1 && sb.ustride != 3 * N) return false;
+  if ((reinterpret_cast<uintptr_t>(u) & 15) != 0 || (n * sizeof(T)) % 16 != 0) return false;
   TensorMapEncodeTiled enc = tensor_map_encoder();
   if (!enc) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)nslots * 3 * n};
-  const cuuint64_t strides[2] = {(cuuint64_t)n * sizeof(float), (cuuint64_t)n * n * sizeof(float)};
-  const cuuint32_t box[3] = {QROW, QBY, 1};
+  const cuuint64_t strides[2] = {(cuuint64_t)n * sizeof(T), (cuuint64_t)n * n * sizeof(T)};
+  const cuuint32_t box[3] = {bx, by, 1};
   const cuuint32_t es[3] = {1, 1, 1};
-  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(u), dims, strides, box, es,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return enc(map, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+             const_cast<T*>(u), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <typename T>
@@ -645,7 +711,7 @@ cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaSt
       dim3 gq(n / QX, n / QY, zblocks * nslots);
       const float ih = (float)(1.0 / (double)h);
       CUtensorMap map;
-      const int have = quad_tensor_map((const float*)u, n, nslots, sb, &map) ? 1 : 0;
+      const int have = field_tensor_map<float>((const float*)u, n, nslots, sb, QROW, QBY, &map) ? 1 : 0;
       if (doadd)
         rhs_quad_kernel<true><<<gq, dim3(32, 8), QUAD_SMEM, st>>>(n, ih, (float)visc, (const float*)u, (float*)du, sb,
                                                                   zblocks, ptz, map, have);
@@ -658,18 +724,22 @@ cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaSt
   const int gxb = (n + PTX - 1) / PTX, gyb = (n + PTYT<NC> - 1) / PTYT<NC>;
   zsplit((long long)gxb * gyb, sizeof(T) == 4 ? 4 : 3, ptz, zblocks);
   dim3 grid(gxb, gyb, zblocks * nslots);
-  const size_t sh = sizeof(PlaneSmem<T, NC>);
+  const size_t sh = plane_smem_bytes<T, NC>();
+  CUtensorMap map;
+  const int have = field_tensor_map<T>(u, n, nslots, sb, UROW<T>, PBYT<NC>, &map) ? 1 : 0;
   if (doadd)
-    rhs_kernel<T, NC, true><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks, ptz);
+    rhs_kernel<T, NC, true><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks, ptz,
+                                                                map, have);
   else
-    rhs_kernel<T, NC, false><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks, ptz);
+    rhs_kernel<T, NC, false><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks,
+                                                                 ptz, map, have);
   return cudaGetLastError();
 }
 
 template <typename T>
 static cudaError_t configure_rhs_t() {
   constexpr int NC = CYT<T>;
-  const int sh = (int)sizeof(PlaneSmem<T, NC>);
+  const int sh = (int)plane_smem_bytes<T, NC>();
   cudaError_t e = cudaFuncSetAttribute(rhs_kernel<T, NC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(rhs_kernel<T, NC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh);

@@ -63,6 +63,7 @@ def test_rhs_f64(NS, n):
     du2 = dev(base)
     NS.tensordivergence(du2, dev(u), visc, g, doadd=True)
     assert rel(host(du2), base + ref) < TOL64
+    assert NS.device_faults() == 0  # interior tiles of n >= 96 arrive by TMA
 
 
 @pytest.mark.parametrize("n", SIZES)

@@ -250,16 +250,20 @@ conv_tile_kernel(int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat1
 
 // ---------------------------------------------------------------------------
 // Convolution with the weights resident in shared memory (grids n % 8 == 0):
-// a persistent CTA of 4 warps loads all 27 taps of the weights once, then
-// walks 8 x 2 x 4 voxel blocks (x, y, z) of the batch; each block's
-// 10 x 4 x 6 halo (all input channels) arrives by 16-byte cp.async into one
-// of two buffers while the other is consumed.  Warp w computes the 16 voxels
-// of slice z = w (rows m = x + 8 y), A fragments by ldmatrix from the halo
-// rows, B fragments by ldmatrix from the weight rows ([tap][co][ci]); rows are
-// padded to an odd number of 16-byte units, so the 8 rows of an ldmatrix fall
-// in distinct banks.  Same epilogues as conv_tile_kernel.
+// a persistent CTA of 8 warps loads all 27 taps of the weights once, then
+// walks 8 x 8 x 4 voxel blocks (x, y, z) of the batch; each block's
+// 10 x 10 x 6 halo (all input channels) arrives by 16-byte cp.async into one
+// of two buffers while the other is consumed.  Warp w computes the 32 voxels
+// of slice z = w / 2, rows y = 4 (w % 2) .. + 3, as two 16-voxel m-tiles
+// (m = x + 8 y'), so it keeps 2 x NP / 8 independent accumulators; A
+// fragments by ldmatrix from the halo rows, B fragments by ldmatrix from the
+// weight rows ([tap][co][ci]); rows are padded to an odd number of 16-byte
+// units, so the 8 rows of an ldmatrix fall in distinct banks.  Same epilogues
+// as conv_tile_kernel.
 // ---------------------------------------------------------------------------
-constexpr int CR_HX = 10, CR_HY = 4, CR_HZ = 6, CR_HALO = CR_HX * CR_HY * CR_HZ;
+constexpr int CR_WARPS = 8, CR_THREADS = 32 * CR_WARPS;
+constexpr int CR_BV = 256;  // block 8 x 8 x 4 voxels
+constexpr int CR_HX = 10, CR_HY = 10, CR_HZ = 6, CR_HALO = CR_HX * CR_HY * CR_HZ;
 
 template <int KP, int NP>
 constexpr size_t conv_res_smem() {
@@ -278,7 +282,7 @@ __device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void* p) {
 }
 
 template <int KP, int NP, int EPI>
-__global__ void __launch_bounds__(CONV_THREADS)
+__global__ void __launch_bounds__(CR_THREADS)
 conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
                 const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
                 const float* __restrict__ pre_prev, int nout_valid) {
@@ -287,12 +291,12 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
   extern __shared__ __align__(16) unsigned char cr_smem[];
   __nv_bfloat16* const sW = reinterpret_cast<__nv_bfloat16*>(cr_smem);
   __nv_bfloat16* const sT0 = sW + NET_TAPS * NP * AS;
-  for (int t = threadIdx.x; t < NET_TAPS * NP * (KP / 8); t += CONV_THREADS) {
+  for (int t = threadIdx.x; t < NET_TAPS * NP * (KP / 8); t += CR_THREADS) {
     const int row = t / (KP / 8), c = t - row * (KP / 8);
     cp_async_16(sW + row * AS + c * 8, Wt + (long long)row * KP + c * 8);
   }
   cp_async_commit();
-  const int nbx = n / 8, nby = n / 2, nbz = n / 4;
+  const int nbx = n / 8, nby = n / 8, nbz = n / 4;
   const long long nb3 = (long long)nbx * nby * nbz;
   const long long nblk = (long long)batch * nb3;
   const long long N = (long long)n * n * n;
@@ -300,7 +304,7 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
     s = b / nb3;
     const long long r = b - s * nb3;
     z0 = 4 * (int)(r / ((long long)nbx * nby));
-    y0 = 2 * (int)((r / nbx) % nby);
+    y0 = 8 * (int)((r / nbx) % nby);
     x0 = 8 * (int)(r % nbx);
   };
   auto load_block = [&](long long b, int buf) {
@@ -309,7 +313,7 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
     origin(b, s, x0, y0, z0);
     const __nv_bfloat16* ins = in + s * N * KP;
     __nv_bfloat16* const sT = sT0 + buf * CR_HALO * AS;
-    for (int t = threadIdx.x; t < CR_HALO * (KP / 8); t += CONV_THREADS) {
+    for (int t = threadIdx.x; t < CR_HALO * (KP / 8); t += CR_THREADS) {
       const int h = t / (KP / 8), c = t - h * (KP / 8);
       const int hz = h / (CR_HX * CR_HY), hy = (h / CR_HX) % CR_HY, hx = h % CR_HX;
       int x = x0 - 1 + hx, y = y0 - 1 + hy, z = z0 - 1 + hz;
@@ -322,9 +326,11 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
   };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3, mat = lane >> 3, lr = lane & 7;
-  // this lane's ldmatrix rows: A voxel m = lr + 8 (mat & 1) of slice z = warp
+  // this lane's ldmatrix rows: A voxel m = lr + 8 (mat & 1) of m-tile t:
+  // x = m % 8, y = 4 (warp % 2) + 2 t + m / 8, z = warp / 2
   const int am = lr + 8 * (mat & 1);
-  const int ah = (am & 7) + CR_HX * (am >> 3) + CR_HX * CR_HY * warp;  // halo row at tap offsets 0
+  const int wz = warp >> 1, wy = 4 * (warp & 1);
+  const int ah = (am & 7) + CR_HX * (wy + (am >> 3)) + CR_HX * CR_HY * wz;  // halo row of m-tile 0, tap offsets 0
   const int ak = 8 * (mat >> 1);
   long long b = blockIdx.x;
   int buf = 0;
@@ -339,9 +345,11 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
     }
     __syncthreads();
     const __nv_bfloat16* T = sT0 + buf * CR_HALO * AS;
-    float acc[NTL][4];
+    float acc[2][NTL][4];
 #pragma unroll
-    for (int j = 0; j < NTL; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int j = 0; j < NTL; ++j) acc[mt][j][0] = acc[mt][j][1] = acc[mt][j][2] = acc[mt][j][3] = 0.f;
 #pragma unroll 1
     for (int dz = 0; dz < 3; ++dz)
 #pragma unroll
@@ -350,14 +358,17 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
         const __nv_bfloat16* arow = T + (ah + dx + CR_HX * dy + CR_HX * CR_HY * dz) * AS + ak;
 #pragma unroll
         for (int kk = 0; kk < KP; kk += 16) {
-          unsigned a[4];
-          ldsm_x4(a, arow + kk);
+          unsigned a0[4], a1[4];
+          ldsm_x4(a0, arow + kk);
+          ldsm_x4(a1, arow + 2 * CR_HX * AS + kk);  // m-tile 1: two rows further in y
 #pragma unroll
           for (int p = 0; p < NTL / 2; ++p) {
             unsigned r[4];
             ldsm_x4(r, sW + (tap * NP + 16 * p + 8 * (mat >> 1) + lr) * AS + kk + 8 * (mat & 1));
-            mma_bf16(acc[2 * p], a, r[0], r[1]);
-            mma_bf16(acc[2 * p + 1], a, r[2], r[3]);
+            mma_bf16(acc[0][2 * p], a0, r[0], r[1]);
+            mma_bf16(acc[0][2 * p + 1], a0, r[2], r[3]);
+            mma_bf16(acc[1][2 * p], a1, r[0], r[1]);
+            mma_bf16(acc[1][2 * p + 1], a1, r[2], r[3]);
           }
         }
       }
@@ -365,13 +376,14 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
     int x0, y0, z0;
     origin(b, s, x0, y0, z0);
 #pragma unroll
-    for (int h2 = 0; h2 < 2; ++h2) {
+    for (int q = 0; q < 4; ++q) {
+      const int mt = q >> 1, h2 = q & 1;
       const int m = gid + 8 * h2;
-      const long long v = s * N + ((long long)(z0 + warp) * n + (y0 + (m >> 3))) * n + (x0 + (m & 7));
+      const long long v = s * N + ((long long)(z0 + wz) * n + (y0 + wy + 2 * mt + (m >> 3))) * n + (x0 + (m & 7));
 #pragma unroll
       for (int j = 0; j < NTL; ++j) {
         const int co = j * 8 + tig * 2;
-        float x0v = acc[j][h2 * 2], x1v = acc[j][h2 * 2 + 1];
+        float x0v = acc[mt][j][h2 * 2], x1v = acc[mt][j][h2 * 2 + 1];
         if (EPI == 0) {
           x0v += bias[co];
           x1v += bias[co + 1];
@@ -401,9 +413,9 @@ static void conv_launch(long long V, int n, const __nv_bfloat16* in, const __nv_
                         cudaStream_t st) {
   if (n % 8 == 0) {
     const long long N = (long long)n * n * n;
-    const long long nblk = V / 64;
+    const long long nblk = V / CR_BV;
     const long long ctas = std::min<long long>(nblk, (long long)conv_res_per_sm<KP, NP>() * 152);
-    conv_res_kernel<KP, NP, EPI><<<(unsigned)ctas, CONV_THREADS, conv_res_smem<KP, NP>(), st>>>(
+    conv_res_kernel<KP, NP, EPI><<<(unsigned)ctas, CR_THREADS, conv_res_smem<KP, NP>(), st>>>(
         (int)(V / N), n, in, W, bias, pre_out, act_out, pre_prev, nout_valid);
   } else if (n % TB == 0) {
     const long long N = (long long)n * n * n;
@@ -519,13 +531,14 @@ wgrad_partial_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, c
 // folded in a fixed order (wgrad_fold_kernel).
 // ---------------------------------------------------------------------------
 constexpr int WT_WARPS = 9, WT_THREADS = 32 * WT_WARPS, WT_CTAS = 152;
-constexpr int WT_HX = 10, WT_HY = 4, WT_HZ = 6, WT_HALO = WT_HX * WT_HY * WT_HZ;
+constexpr int WT_BY = 4, WT_BV = 8 * WT_BY * 4;  // block 8 x WT_BY x 4 voxels
+constexpr int WT_HX = 10, WT_HY = WT_BY + 2, WT_HZ = 6, WT_HALO = WT_HX * WT_HY * WT_HZ;
 
 // shared memory of wgrad_tile_kernel: two buffers of the halo rows (stride
 // KP + 8 halves) and of the g rows (stride NP + 8 halves)
 template <int KP, int NP>
 constexpr size_t wgrad_tile_smem() {
-  return 2 * ((size_t)WT_HALO * (KP + 8) + 64 * (size_t)(NP + 8)) * sizeof(__nv_bfloat16);
+  return 2 * ((size_t)WT_HALO * (KP + 8) + WT_BV * (size_t)(NP + 8)) * sizeof(__nv_bfloat16);
 }
 
 __device__ __forceinline__ void ldsm_x4_trans(unsigned (&r)[4], const void* p) {
@@ -546,7 +559,7 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
   __nv_bfloat16* const sG0 = sX0 + 2 * WT_HALO * KS;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wdz = warp / 3, wdy = warp % 3;  // dz + 1, dy + 1 of this warp's taps
-  const int nbx = n / 8, nby = n / 2, nbz = n / 4;
+  const int nbx = n / 8, nby = n / WT_BY, nbz = n / 4;
   const long long nb3 = (long long)nbx * nby * nbz;
   const long long nblk = (long long)batch * nb3;
   const long long N = (long long)n * n * n;
@@ -558,8 +571,8 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
 #pragma unroll
       for (int q = 0; q < NTL; ++q) acc[t][m][q][0] = acc[t][m][q][1] = acc[t][m][q][2] = acc[t][m][q][3] = 0.f;
   // copies of block b into buffer buf: halo voxels (hx, hy, hz) at origin
-  // (8 bx, 2 by, 4 bz) - 1 (periodic in the sample), KP / 8 pieces each; g
-  // rows of the 64 block voxels (v = x + 8 y + 16 z), NP / 8 pieces each
+  // (8 bx, WT_BY by, 4 bz) - 1 (periodic in the sample), KP / 8 pieces each;
+  // g rows of the block voxels (v = x + 8 y + 8 WT_BY z), NP / 8 pieces each
   auto load_block = [&](long long b, int buf) {
     const long long s = b / nb3;
     const long long r = b - s * nb3;
@@ -569,17 +582,17 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
     for (int t = threadIdx.x; t < WT_HALO * (KP / 8); t += WT_THREADS) {
       const int h = t / (KP / 8), c = t - h * (KP / 8);
       const int hz = h / (WT_HX * WT_HY), hy = (h / WT_HX) % WT_HY, hx = h % WT_HX;
-      int x = 8 * bx - 1 + hx, y = 2 * by - 1 + hy, z = 4 * bz - 1 + hz;
+      int x = 8 * bx - 1 + hx, y = WT_BY * by - 1 + hy, z = 4 * bz - 1 + hz;
       x = x < 0 ? x + n : (x >= n ? x - n : x);
       y = y < 0 ? y + n : (y >= n ? y - n : y);
       z = z < 0 ? z + n : (z >= n ? z - n : z);
       cp_async_16(sX + h * KS + c * 8, ins + (((long long)z * n + y) * n + x) * KP + c * 8);
     }
     const __nv_bfloat16* gs = g + s * N * NP;
-    __nv_bfloat16* const sG = sG0 + buf * 64 * NS;
-    for (int t = threadIdx.x; t < 64 * (NP / 8); t += WT_THREADS) {
+    __nv_bfloat16* const sG = sG0 + buf * WT_BV * NS;
+    for (int t = threadIdx.x; t < WT_BV * (NP / 8); t += WT_THREADS) {
       const int v = t / (NP / 8), c = t - v * (NP / 8);
-      const int x = 8 * bx + (v & 7), y = 2 * by + ((v >> 3) & 1), z = 4 * bz + (v >> 4);
+      const int x = 8 * bx + (v & 7), y = WT_BY * by + ((v >> 3) % WT_BY), z = 4 * bz + v / (8 * WT_BY);
       cp_async_16(sG + v * NS + c * 8, gs + (((long long)z * n + y) * n + x) * NP + c * 8);
     }
     cp_async_commit();
@@ -604,22 +617,25 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
     }
     __syncthreads();
     const __nv_bfloat16* X = sX0 + buf * WT_HALO * KS;
-    const __nv_bfloat16* G = sG0 + buf * 64 * NS;
+    const __nv_bfloat16* G = sG0 + buf * WT_BV * NS;
     if (bhalf < 2) {
       float fs = 0.f;
 #pragma unroll 8
-      for (int v = 32 * bhalf; v < 32 * bhalf + 32; ++v) fs += __bfloat162float(G[v * NS + bco]);
+      for (int v = (WT_BV / 2) * bhalf; v < (WT_BV / 2) * (bhalf + 1); ++v) fs += __bfloat162float(G[v * NS + bco]);
       bsum += (double)fs;
     }
-#pragma unroll
-    for (int kz = 0; kz < 4; ++kz) {
-      // B: voxels k = x + 8 y of slice kz; two n-tiles per ldmatrix.x4
+#pragma unroll 2
+    for (int ks = 0; ks < WT_BV / 16; ++ks) {
+      // step ks: the 16 voxels x = 0..7, y = 2 (ks % (WT_BY / 2)) + {0, 1},
+      // z = ks / (WT_BY / 2) (rows 16 ks .. 16 ks + 15 of the g block)
+      const int kz = ks / (WT_BY / 2), ky0 = 2 * (ks % (WT_BY / 2));
+      // B: voxels k = x + 8 y of the step; two n-tiles per ldmatrix.x4
       unsigned bf[NTL][2];
 #pragma unroll
       for (int p = 0; p < NTL / 2; ++p) {
         const int k = lr + 8 * (mat & 1);
         unsigned r[4];
-        ldsm_x4_trans(r, G + (16 * kz + k) * NS + 16 * p + 8 * (mat >> 1));
+        ldsm_x4_trans(r, G + (16 * ks + k) * NS + 16 * p + 8 * (mat >> 1));
         bf[2 * p][0] = r[0];
         bf[2 * p][1] = r[1];
         bf[2 * p + 1][0] = r[2];
@@ -627,7 +643,7 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
       }
       // A: in at the shifted voxel of each tap, channels 16 mt ..
       const int ka = lr + 8 * (mat >> 1);
-      const int hy = (ka >> 3) + wdy, hz = kz + wdz;
+      const int hy = ky0 + (ka >> 3) + wdy, hz = kz + wdz;
 #pragma unroll
       for (int t = 0; t < 3; ++t) {
         const int h = (ka & 7) + t + WT_HX * hy + WT_HX * WT_HY * hz;
@@ -916,7 +932,7 @@ static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfl
   if (n % 8 == 0) {
     // all taps per CTA over 8 x 2 x 4 voxel blocks, one persistent CTA per
     // SM; the bias partials follow the weight partials in the buffer
-    const long long nblk = V / 64;
+    const long long nblk = V / WT_BV;
     nchunk = (int)std::min<long long>(nblk, WT_CTAS);
     double* bpart = reinterpret_cast<double*>(net->wpart + (size_t)WT_CTAS * NET_TAPS * 32 * 32);
     wgrad_tile_kernel<KP, NP><<<nchunk, WT_THREADS, wgrad_tile_smem<KP, NP>(), st>>>((int)(V / N), n, in, g,
@@ -1008,6 +1024,11 @@ static cudaError_t conv_res_attr() {
   return cudaFuncSetAttribute(conv_res_kernel<KP, NP, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)conv_res_smem<KP, NP>());
 }
+template <int KP, int NP>
+static cudaError_t wgrad_tile_attr() {
+  return cudaFuncSetAttribute(wgrad_tile_kernel<KP, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)wgrad_tile_smem<KP, NP>());
+}
 static int configure_learned() {
   static std::mutex mu;
   static bool done[64];
@@ -1019,6 +1040,9 @@ static int configure_learned() {
   std::lock_guard<std::mutex> lock(mu);
   if (done[dev]) return EXC_OK;
   cudaError_t e = conv_res_attr<16, 32, 0>();
+  if (e == cudaSuccess) e = wgrad_tile_attr<16, 32>();
+  if (e == cudaSuccess) e = wgrad_tile_attr<32, 32>();
+  if (e == cudaSuccess) e = wgrad_tile_attr<32, 16>();
   if (e == cudaSuccess) e = conv_res_attr<32, 32, 0>();
   if (e == cudaSuccess) e = conv_res_attr<32, 16, 1>();
   if (e == cudaSuccess) e = conv_res_attr<16, 32, 2>();

@@ -36,6 +36,7 @@ struct LesState {
   // buffer is used as is)
   int tb_from = -1;
   bool tb_same = false;
+  T* tb2 = nullptr;  // root LES of a fused stepper: sums of the stage state
   T *ub, *fk, *mcl, *mlast, *rtmp;
   T *ve[2], *ves, *ke;  // exact LES: state (ping-pong), stage, k
   T *vn[2], *vns, *kn;  // no-model LES
@@ -60,6 +61,7 @@ namespace exc {
 
 template <typename T>
 struct CaseImpl {
+  int fuse_root = -1;  // LES whose ratio the fused RK stage sums (-1: separate passes)
   int n = 0;
   long long N = 0;
   double h = 0;
@@ -116,6 +118,38 @@ static const T* les_tb(const CaseImpl<T>* ci, const LesState<T>& L) {
   return L.tb_same ? ci->les[L.tb_from].tb : L.tb;
 }
 
+// Fused stepper (one root ratio for every LES): the root's sums come from
+// rk_stage_sums_kernel in `root`; the other LES coarsen from them (in
+// increasing ratio) into their own buffers.
+template <typename T>
+static int les_tb_coarsen(CaseImpl<T>* ci, const T* root, cudaStream_t st) {
+  int order[EXC_MAX_LES];
+  for (int i = 0; i < ci->nles; ++i) order[i] = i;
+  for (int i = 1; i < ci->nles; ++i)
+    for (int j = i; j > 0 && ci->les[order[j]].c < ci->les[order[j - 1]].c; --j) {
+      const int t = order[j];
+      order[j] = order[j - 1];
+      order[j - 1] = t;
+    }
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < ci->nles && e == cudaSuccess; ++k) {
+    LesState<T>& L = ci->les[order[k]];
+    if (L.tb_same || L.tb_from < 0) continue;
+    const T* src = ci->les[L.tb_from].tb_from < 0 && !ci->les[L.tb_from].tb_same ? root : ci->les[L.tb_from].tb;
+    e = box_tb_coarsen<T>(ci->n, ci->les[L.tb_from].c, L.c, src, L.tb, st);
+  }
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+// Sums used by LES L when the root's sums are in `root`.
+template <typename T>
+static const T* les_tb_from_root(const CaseImpl<T>* ci, const LesState<T>& L, const T* root) {
+  const int r = ci->fuse_root;
+  if (&L == &ci->les[r] || (L.tb_same && L.tb_from == r)) return root;
+  return les_tb(ci, L);
+}
+
 // ubar from the filled transverse sums: own-axis taps, then the projection
 // for the volume filter.
 template <typename T>
@@ -151,26 +185,50 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
   if (e == cudaSuccess)
     e = launch_set_dt(ci->dscal + 2, ci->h, cs->desc.visc, cs->desc.cfl, dt_fixed, dt, ci->dscal + 1, ci->dflag, st);
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  const bool fused = ci->fuse_root >= 0;
+  T* const root_k = fused ? ci->les[ci->fuse_root].tb : nullptr;   // sums of k_s
+  T* const root_s = fused ? ci->les[ci->fuse_root].tb2 : nullptr;  // sums of the stage state
   for (int s = 0; s < 4; ++s) {
     const T* src = s == 0 ? u0 : ci->us;
     e = launch_rhs<T>(n, h, visc, src, ci->rhs, false, st);
     if (e == cudaSuccess) e = poisson_solve_inplace<T>(&ci->ps, ci->rhs, true, st);
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-    // LES targets use the stage state before it is overwritten
+    // LES targets use the stage state before it is overwritten; the fused
+    // stepper has the sums of stages 1-3 from the previous RK stage kernel
+    const T* troot = nullptr;
     if (ci->nles > 0) {
-      int rc = les_tb_fill<T>(ci, src, st);
+      int rc;
+      if (fused && s > 0) {
+        troot = root_s;
+        rc = les_tb_coarsen<T>(ci, troot, st);
+      } else {
+        rc = les_tb_fill<T>(ci, src, st);
+        if (fused) troot = root_k;
+      }
       if (rc) return rc;
     }
     for (int li = 0; li < ci->nles; ++li) {
       LesState<T>& L = ci->les[li];
-      int rc = les_target_tb<T>(ci, L, L.ub, st);
+      int rc;
+      if (fused) {
+        e = box_oa<T>(n, L.c, L.kind, les_tb_from_root(ci, L, troot), L.ub, st);
+        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+        rc = L.kind == EXC_FILTER_VOLUME ? project_vec<T>(&L.ps, L.ub, st) : EXC_OK;
+      } else {
+        rc = les_target_tb<T>(ci, L, L.ub, st);
+      }
       if (rc) return rc;
     }
-    e = launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0, ci->us, ufin, s,
-                           dt, st, SlotBatch(), 1, ci->nles > 0);
+    if (fused) {
+      e = launch_rk_stage_sums<T>(n, ci->les[ci->fuse_root].c, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work),
+                                  2 * ci->ps.P, u0, ci->us, ufin, s, dt, root_k, s < 3 ? root_s : nullptr, st);
+    } else {
+      e = launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0, ci->us, ufin,
+                             s, dt, st, SlotBatch(), 1, ci->nles > 0);
+    }
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
     if (ci->nles > 0) {
-      int rc = les_tb_fill<T>(ci, ci->rhs, st);
+      int rc = fused ? les_tb_coarsen<T>(ci, root_k, st) : les_tb_fill<T>(ci, ci->rhs, st);
       if (rc) return rc;
     }
     for (int li = 0; li < ci->nles; ++li) {
@@ -178,7 +236,7 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
       const int m = L.m;
       const T H = (T)(cs->desc.l / m);
       // m_s = P_H(filter(k_s) - RHS_H(ubar_s))
-      e = box_oa<T>(n, L.c, L.kind, les_tb(ci, L), L.mcl, st);
+      e = box_oa<T>(n, L.c, L.kind, fused ? les_tb_from_root(ci, L, root_k) : les_tb(ci, L), L.mcl, st);
       if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
       int rc;
       e = launch_rhs<T>(m, H, visc, L.ub, L.rtmp, false, st);
@@ -308,6 +366,7 @@ static void case_destroy(exc_case* cs) {
     poisson_free(&ci->les[li].ps);
     if (ci->les[li].buf) cudaFree(ci->les[li].buf);
     if (ci->les[li].tb) cudaFree(ci->les[li].tb);
+    if (ci->les[li].tb2) cudaFree(ci->les[li].tb2);
   }
   delete ci;
   cs->impl = nullptr;
@@ -377,6 +436,26 @@ static int case_create(exc_case* cs) {
       const LesState<T>& S = ci->les[lj];
       if (lj == li || S.tb_same || S.c >= L.c || L.c % S.c != 0) continue;
       if (L.tb_from < 0 || S.c > ci->les[L.tb_from].c) L.tb_from = lj;
+    }
+  }
+  // fused RK stage: one root ratio among the LES (every other LES shares or
+  // coarsens from its sums) with a rk_stage_sums_kernel for the grid
+  ci->fuse_root = -1;
+  {
+    int roots = 0, root = -1;
+    for (int li = 0; li < d.nles; ++li)
+      if (ci->les[li].tb_from < 0 && !ci->les[li].tb_same) {
+        ++roots;
+        root = li;
+      }
+    if (roots == 1) {
+      const int xcw = rk_sums_chunk<T>(ci->les[root].c);
+      if (xcw && d.n % xcw == 0) {
+        LesState<T>& R = ci->les[root];
+        const size_t tbb = 3 * (size_t)d.n * R.m * R.m * sizeof(T);
+        if (cudaMalloc(&R.tb2, tbb) != cudaSuccess) { set_last_error("out of device memory (LES filter scratch)"); return EXC_ERR_OOM; }
+        ci->fuse_root = root;
+      }
     }
   }
   cudaError_t e = cudaGetLastError();

@@ -206,6 +206,133 @@ __global__ void rk_stage2_kernel(int n, double inv_h, double* __restrict__ k, co
   }
 }
 
+// ---------------------------------------------------------------------------
+// RK stage that also forms the transverse box sums of the LES filters (the
+// first pass of filter_vector_box, tb_kernel) of k and of the stage output:
+// a CTA owns one coarse column (Jz, Jy) of ratio C0 (C0^2 fine rows of n
+// cells) and walks it in chunks of XC cells per row; after the RK arithmetic
+// of rk_stage4_kernel / rk_stage2_kernel (same expressions, V cells per
+// thread), k and the stage output of the chunk sit in shared memory and are
+// summed over the C0 x C0 transverse boxes in tb_kernel's order, so the sums
+// are bit-identical to tb_kernel's on the stored fields.  k itself is not
+// stored.  tbs (sums of xs, stages 0-2) may be null.
+// ---------------------------------------------------------------------------
+template <typename T, int C0>
+__global__ void __launch_bounds__(256)
+rk_stage_sums_kernel(int n, T inv_h, const T* __restrict__ k, const T* __restrict__ p, int ppitch,
+                     const T* __restrict__ x0, T* __restrict__ xs, T* __restrict__ xfin, int stage,
+                     const double* __restrict__ dtp, T* __restrict__ tbk, T* __restrict__ tbs) {
+  constexpr int V = 16 / (int)sizeof(T);
+  constexpr int ROWS = C0 * C0;
+  constexpr int LANES = 256 / ROWS;
+  constexpr int XC = LANES * V;
+  constexpr int JC = XC / C0;  // coarse x cells per chunk
+  static_assert(ROWS <= 256 && XC % C0 == 0, "chunk must hold whole coarse cells");
+  __shared__ __align__(16) T sk[3][ROWS][XC];
+  __shared__ __align__(16) T ss[3][ROWS][XC];
+  const int m = n / C0;
+  const long long N = (long long)n * n * n;
+  const long long Mt = (long long)n * m * m;
+  const int Jy = blockIdx.x % m, Jz = blockIdx.x / m;
+  const int tid = threadIdx.x, r = tid / LANES, lane = tid - r * LANES;
+  const int z = C0 * Jz + r / C0, y = C0 * Jy + r % C0;
+  const double dt = dtp[0];
+  const T cf = (T)((stage == 0 || stage == 3) ? dt / 6.0 : dt / 3.0);
+  const T cs = (T)(stage == 2 ? dt : 0.5 * dt);
+  const long long rowbase = ((long long)z * n + y) * n;
+  const T* prow = p + ((long long)z * n + y) * ppitch;
+  const T* prowy = p + ((long long)z * n + wrap_up(y, n)) * ppitch;
+  const T* prowz = p + ((long long)wrap_up(z, n) * n + y) * ppitch;
+  const bool sums_s = tbs != nullptr && stage < 3;
+  for (int xc = 0; xc < n; xc += XC) {
+    const int x = xc + V * lane;
+    const long long g = rowbase + x;
+    T kk[3][V], pc[V], py[V], pz[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      kk[0][i] = k[g + i];
+      kk[1][i] = k[N + g + i];
+      kk[2][i] = k[2 * N + g + i];
+      pc[i] = prow[x + i];
+      py[i] = prowy[x + i];
+      pz[i] = prowz[x + i];
+    }
+    const T pn = prow[x + V == n ? 0 : x + V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      kk[0][i] -= ((i + 1 < V ? pc[i + 1] : pn) - pc[i]) * inv_h;
+      kk[1][i] -= (py[i] - pc[i]) * inv_h;
+      kk[2][i] -= (pz[i] - pc[i]) * inv_h;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      T a[V], f[V];
+#pragma unroll
+      for (int i = 0; i < V; ++i) a[i] = stage < 3 ? x0[c * N + g + i] : (T)0;  // x0 unused at stage 3
+#pragma unroll
+      for (int i = 0; i < V; ++i) f[i] = stage == 0 ? a[i] + cf * kk[c][i] : xfin[c * N + g + i] + cf * kk[c][i];
+#pragma unroll
+      for (int i = 0; i < V; ++i) xfin[c * N + g + i] = f[i];
+      if (stage < 3) {
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          const T sv = a[i] + cs * kk[c][i];
+          xs[c * N + g + i] = sv;
+          ss[c][r][V * lane + i] = sv;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < V; ++i) sk[c][r][V * lane + i] = kk[c][i];
+    }
+    __syncthreads();
+    // box sums of the chunk: component 0 over the C0^2 rows at each x;
+    // component 1 over (dz, dx) for each dy; component 2 over (dy, dx) for
+    // each dz (tb_kernel's orders)
+    for (int q = 0; q < (sums_s ? 2 : 1); ++q) {
+      const T(*src)[ROWS][XC] = q == 0 ? sk : ss;
+      T* const out = q == 0 ? tbk : tbs;
+      for (int o = tid; o < 3 * XC; o += 256) {
+        const int c = o / XC, i = o - c * XC;
+        T acc = (T)0;
+        if (c == 0) {
+#pragma unroll 4
+          for (int rr = 0; rr < ROWS; ++rr) acc += src[0][rr][i];
+          out[((long long)Jz * m + Jy) * n + xc + i] = acc;
+        } else if (c == 1) {
+          const int ddy = i / JC, jx = i - ddy * JC;
+          for (int ddz = 0; ddz < C0; ++ddz)
+#pragma unroll
+            for (int dx = 0; dx < C0; ++dx) acc += src[1][ddz * C0 + ddy][C0 * jx + dx];
+          out[Mt + ((long long)Jz * n + C0 * Jy + ddy) * m + xc / C0 + jx] = acc;
+        } else {
+          const int ddz = i / JC, jx = i - ddz * JC;
+          for (int ddy = 0; ddy < C0; ++ddy)
+#pragma unroll
+            for (int dx = 0; dx < C0; ++dx) acc += src[2][ddz * C0 + ddy][C0 * jx + dx];
+          out[2 * Mt + ((long long)(C0 * Jz + ddz) * m + Jy) * m + xc / C0 + jx] = acc;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+cudaError_t launch_rk_stage_sums(int n, int c0, T h, const T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin,
+                                 int stage, const double* dtp, T* tbk, T* tbs, cudaStream_t st) {
+  const int xcw = rk_sums_chunk<T>(c0);
+  if (!xcw || n % xcw != 0 || n % c0 != 0) return cudaErrorInvalidValue;
+  const int m = n / c0;
+  const T ih = (T)(1.0 / (double)h);
+  const dim3 grid((unsigned)(m * m));
+  switch (c0) {
+    case 2: rk_stage_sums_kernel<T, 2><<<grid, 256, 0, st>>>(n, ih, k, p, ppitch, x0, xs, xfin, stage, dtp, tbk, tbs); break;
+    case 4: rk_stage_sums_kernel<T, 4><<<grid, 256, 0, st>>>(n, ih, k, p, ppitch, x0, xs, xfin, stage, dtp, tbk, tbs); break;
+    default: rk_stage_sums_kernel<T, 8><<<grid, 256, 0, st>>>(n, ih, k, p, ppitch, x0, xs, xfin, stage, dtp, tbk, tbs); break;
+  }
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
                             const double* dtp, cudaStream_t st, const SlotBatch& sb, int nslots, bool store_k) {
@@ -567,6 +694,8 @@ cudaError_t launch_convert(long long count, const A* a, B* b, cudaStream_t st) {
 }
 
 #define INST(T)                                                                                                 \
+  template cudaError_t launch_rk_stage_sums<T>(int, int, T, const T*, const T*, int, const T*, T*, T*, int,     \
+                                               const double*, T*, T*, cudaStream_t);                           \
   template cudaError_t launch_rk_stage<T>(int, T, T*, const T*, int, const T*, T*, T*, int, const double*,      \
                                           cudaStream_t, const SlotBatch&, int, bool);                                                        \
   template cudaError_t launch_axpy<T>(long long, T*, const T*, T, cudaStream_t);                                \

@@ -10,6 +10,27 @@ template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
                             const double* dtp, cudaStream_t st, const SlotBatch& sb = SlotBatch(), int nslots = 1,
                             bool store_k = true);
+// RK stage (GRAD form, k not stored) that also writes the transverse box sums
+// of ratio c0 of k into tbk and of the stage output xs (stages 0-2) into tbs
+// (may be null), bit-identical to tb_kernel's (fields.cu); for grids with
+// n % rk_sums_chunk<T>(c0) == 0.
+template <typename T>
+cudaError_t launch_rk_stage_sums(int n, int c0, T h, const T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin,
+                                 int stage, const double* dtp, T* tbk, T* tbs, cudaStream_t st);
+// Chunk width (cells per row) of rk_stage_sums_kernel for ratio c0; 0 when
+// the fused stage is not used: FP64 (measured slower than the separate
+// passes: 512^3 with LES ratios 8 and 4, 197.6 against 196.2 ms per RK4
+// step), ratios without a kernel, or rows under 128 bytes wide (poorly
+// coalesced).
+template <typename T>
+inline int rk_sums_chunk(int c0) {
+  const int V = 16 / (int)sizeof(T);
+  if (sizeof(T) != 4 || (c0 != 2 && c0 != 4 && c0 != 8)) return 0;
+  const int xc = 256 * V / (c0 * c0);
+  return xc * (int)sizeof(T) >= 128 ? xc : 0;
+}
+
+
 template <typename T>
 cudaError_t launch_axpy(long long count, T* a, const T* b, T scale, cudaStream_t st);
 cudaError_t launch_set_dt(const double* umax, double h, double visc, double cfl, double fixed, double* dt,

@@ -184,10 +184,11 @@ def test_nonfinite_is_flagged(NS):
     assert ei.value.code == 6
 
 
-@pytest.mark.parametrize("n", [32, 48, 64])
+@pytest.mark.parametrize("n", [32, 48, 64, 128])
 def test_f32_dns_unaffected_by_les(NS, n):
     """An LES grid does not act on the DNS: with and without one (the RK stage
-    then stores or skips the projected k) the FP32 DNS matches bit for bit."""
+    then stores or skips the projected k, or forms the filter sums itself at
+    n = 64, 128) the FP32 DNS matches bit for bit."""
     cf = NS.Case(n, 1.0, 1 / 2000, 0.3, precision=1)
     cu = NS.Case(n, 1.0, 1 / 2000, 0.3, precision=1, les=[(4, "volume")])
     u0 = ns.randomfield(n, 1.0, 4, 9)
@@ -197,3 +198,22 @@ def test_f32_dns_unaffected_by_les(NS, n):
     cu.step(5)
     assert np.array_equal(cf.velocity(), cu.velocity())
     assert cf.time() == cu.time()
+
+
+def test_f32_fused_filter_sums_match_separate_passes(NS):
+    """FP32, 192^3: an LES of ratio 4 alone takes its filter sums from the RK
+    stage kernel; next to an LES of ratio 3 (two root ratios) the same LES uses
+    the separate box-sum passes.  Its exact-closure and no-model states agree
+    bit for bit."""
+    n = 192
+    u0 = ns.randomfield(n, 1.0, 4, 5)
+    fused = NS.Case(n, 1.0, 1 / 2000, 0.3, precision=1, les=[(4, "volume")])
+    sep = NS.Case(n, 1.0, 1 / 2000, 0.3, precision=1, les=[(4, "volume"), (3, "volume")])
+    for cs in (fused, sep):
+        cs.set_velocity(u0)
+        cs.step(2)
+    assert np.array_equal(fused.velocity(), sep.velocity())
+    for which in ("exact", "nomodel"):
+        assert np.array_equal(fused.les(0, which), sep.les(0, which)), which
+    fused.close()
+    sep.close()

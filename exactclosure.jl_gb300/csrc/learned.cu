@@ -682,12 +682,17 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
 // fold partials over chunks; bias gradient from the g sums of tap 13 (centre)
 template <int KP, int NP>
 __global__ void wgrad_fold_kernel(int nchunk, const float* __restrict__ part, float* __restrict__ dW) {
+  // four lanes per output: lane q sums chunks q, q + 4, ... in order, then
+  // the four sums combine in a fixed order (deterministic)
   constexpr int PAIRS = KP * NP;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= NET_TAPS * PAIRS) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t >> 2, q = t & 3;
   double s = 0;
-  for (int c = 0; c < nchunk; ++c) s += part[(long long)c * NET_TAPS * PAIRS + i];
-  dW[i] = (float)s;
+  if (i < NET_TAPS * PAIRS)
+    for (int c = q; c < nchunk; c += 4) s += (double)part[(long long)c * NET_TAPS * PAIRS + i];
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  if (q == 0 && i < NET_TAPS * PAIRS) dW[i] = (float)s;
 }
 
 // Bias gradient db[co] = sum_v g[v][co]: BG_BLOCKS blocks, each thread one
@@ -716,11 +721,14 @@ __global__ void __launch_bounds__(256) bgrad_partial_kernel(long long V, const _
 
 template <int NP>
 __global__ void bgrad_fold_kernel(int nblk, const double* __restrict__ part, float* __restrict__ db) {
-  const int co = threadIdx.x;
+  // one warp per channel: lane l sums partials l, l + 32, ... in order, then
+  // a fixed shuffle tree (deterministic)
+  const int co = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (co >= NP) return;
   double s = 0;
-  for (int b = 0; b < nblk; ++b) s += part[(long long)b * NP + co];
-  db[co] = (float)s;
+  for (int b = lane; b < nblk; b += 32) s += part[(long long)b * NP + co];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) db[co] = (float)s;
 }
 
 // ---------------------------------------------------------------------------
@@ -792,12 +800,20 @@ __global__ void loss_grad_kernel(long long V, long long N, const float* __restri
   if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
-__global__ void sum_kernel(int np, const double* __restrict__ part, double scale, double* __restrict__ out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0;
-    for (int i = 0; i < np; ++i) s += part[i];
-    *out = s * scale;
+// Sum of np partials in a fixed order: one block of 256 threads, each thread
+// a strided subset in order, then a fixed tree.
+__global__ void __launch_bounds__(256) sum_kernel(int np, const double* __restrict__ part, double scale,
+                                                  double* __restrict__ out) {
+  __shared__ double red[256];
+  double s = 0;
+  for (int i = threadIdx.x; i < np; i += 256) s += part[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) *out = red[0] * scale;
 }
 
 // Adam (Kingma & Ba 2015): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
@@ -937,18 +953,18 @@ static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfl
     double* bpart = reinterpret_cast<double*>(net->wpart + (size_t)WT_CTAS * NET_TAPS * 32 * 32);
     wgrad_tile_kernel<KP, NP><<<nchunk, WT_THREADS, wgrad_tile_smem<KP, NP>(), st>>>((int)(V / N), n, in, g,
                                                                                       net->wpart, bpart);
-    wgrad_fold_kernel<KP, NP><<<(27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
-    bgrad_fold_kernel<NP><<<1, 32, 0, st>>>(2 * nchunk, bpart, net->dB(l));
+    wgrad_fold_kernel<KP, NP><<<(4 * 27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
+    bgrad_fold_kernel<NP><<<1, 32 * NP, 0, st>>>(2 * nchunk, bpart, net->dB(l));
     return cudaGetLastError();
   } else {
     nchunk = (int)((V + WG_CHUNK - 1) / WG_CHUNK);
     wgrad_partial_kernel<KP, NP><<<dim3(nchunk, 27), 128, 0, st>>>(V, n, in, g, net->wpart);
   }
-  wgrad_fold_kernel<KP, NP><<<(27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
+  wgrad_fold_kernel<KP, NP><<<(4 * 27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
   // the weight-gradient partials are folded by now: reuse their buffer
   double* bpart = reinterpret_cast<double*>(net->wpart);
   bgrad_partial_kernel<NP><<<BG_BLOCKS, 256, 0, st>>>(V, g, bpart);
-  bgrad_fold_kernel<NP><<<1, 32, 0, st>>>(BG_BLOCKS, bpart, net->dB(l));
+  bgrad_fold_kernel<NP><<<1, 32 * NP, 0, st>>>(BG_BLOCKS, bpart, net->dB(l));
   return cudaGetLastError();
 }
 
@@ -958,7 +974,7 @@ static cudaError_t backward(exc_net* net, long long V, int n, long long N, const
   const int lb = (int)std::min<long long>((V + 255) / 256, 1024);
   loss_grad_kernel<T><<<lb, 256, 0, st>>>(V, N, net->out, target, 1.0 / net->out_scale, 1.0 / (3.0 * (double)V),
                                           net->g3, net->lpart);
-  sum_kernel<<<1, 32, 0, st>>>(lb, net->lpart, 1.0 / (3.0 * (double)V), net->lpart + 1024);
+  sum_kernel<<<1, 256, 0, st>>>(lb, net->lpart, 1.0 / (3.0 * (double)V), net->lpart + 1024);
   cudaError_t e = wgrad<32, 16>(net, 2, V, n, net->a2, net->g3, st);
   // input gradient of layer 3 times GELU'(pre2)
   conv_launch<16, 32, 2>(V, n, net->g3, net->Wb(2), nullptr, nullptr, net->gp2, net->pre2, 32, st);

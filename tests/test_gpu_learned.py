@@ -65,7 +65,10 @@ def setup_net(LN, seed=3):
     return net, params
 
 
-@pytest.mark.parametrize("n,batch", [(8, 2), (12, 1)])
+# n = 8: weight-resident convolutions and per-block weight gradients; 12: the
+# 4^3-tile convolution and per-tap weight gradients; 10: the row-form
+# convolution
+@pytest.mark.parametrize("n,batch", [(8, 2), (12, 1), (10, 1)])
 def test_forward_and_gradients_match_oracle(LN, n, batch):
     import torch
 

@@ -67,22 +67,24 @@ def test_served_solve_equals_case_path(SV, prec, built_lib):
     assert r["sim_time"] == t
 
 
-def test_large_grid_batch_equals_alone_and_case(SV, built_lib):
-    """192^3 FP32: the RHS sweep takes its interior tiles by TMA through a
-    tensor map over the batched slots; a solve gives the same bytes alone,
-    batched with another solve of its size, and on the case path."""
+@pytest.mark.parametrize("prec", [1, 0])
+def test_large_grid_batch_equals_alone_and_case(SV, prec, built_lib):
+    """192^3: the RHS sweep (FP32: 2 x 2 kernel, FP64: generic kernel) takes
+    its interior tiles by TMA through a tensor map over the batched slots; a
+    solve gives the same bytes alone, batched with another solve of its size,
+    and on the case path."""
     from exactclosure_gb300 import navierstokes as NS
 
     n, visc, seed, nsteps = 192, 1 / 2000, 11, 3
-    alone = run_alone(SV, 1, n, visc, seed, nsteps)
-    sv = SV.Server(precision=1)
+    alone = run_alone(SV, prec, n, visc, seed, nsteps)
+    sv = SV.Server(precision=prec)
     a = sv.submit(n, visc, nsteps, seed=seed, keep_field=True)
     sv.submit(n, 1 / 1000, nsteps, seed=12)
     sv.drain()
     res = {r["id"]: r for r in sv.poll()}
     sv.close()
     assert np.array_equal(res[a]["field"], alone["field"])
-    cs = NS.Case(n, 1.0, visc, 0.3, precision=1)
+    cs = NS.Case(n, 1.0, visc, 0.3, precision=prec)
     cs.init_random(4.0, 1.0, seed)
     cs.step(nsteps)
     assert np.array_equal(alone["field"], cs.velocity())

@@ -67,34 +67,21 @@ struct FieldSrc {
   }
 };
 
-// r_ij = sigma_ij(u) + delta_ij p at fine cell (x, y, z) (src/N.jl:106-118, 1022-1036)
+// Launch the filter of one flux component with compile-time (i, j).
+template <typename T, int I, int J>
+static void launch_flux_filter(const T* u, const T* p, int n, T inv_h, T visc, int c, const Taps3& taps, T* out,
+                               long long M, cudaStream_t st);
+
 template <typename T>
-struct FluxSrc {
-  const T* u;
-  const T* p;  // may be null: sigma only
-  int n;
-  int i, j;
-  T h, visc;
-  __device__ __forceinline__ long long at(int x, int y, int z) const { return ((long long)z * n + y) * n + x; }
-  __device__ __forceinline__ double operator()(int x, int y, int z) const {
-    const long long N = (long long)n * n * n;
-    int c[3] = {x, y, z};
-    int off = (i != j);
-    int cr[3] = {c[0], c[1], c[2]}, cl[3] = {c[0], c[1], c[2]};
-    cr[j] = (cr[j] + off) % n;
-    cl[j] = (cl[j] + off - 1 + n) % n;
-    T uir = u[i * N + at(cr[0], cr[1], cr[2])], uil = u[i * N + at(cl[0], cl[1], cl[2])];
-    int dr[3] = {c[0], c[1], c[2]}, dl[3] = {c[0], c[1], c[2]};
-    dr[i] = (dr[i] + off) % n;
-    dl[i] = (dl[i] + off - 1 + n) % n;
-    T ujr = u[j * N + at(dr[0], dr[1], dr[2])], ujl = u[j * N + at(dl[0], dl[1], dl[2])];
-    T etaj_ui = (uir + uil) / 2, etai_uj = (ujr + ujl) / 2;
-    T dj_ui = (uir - uil) / h, di_uj = (ujr - ujl) / h;
-    T s = etaj_ui * etai_uj - visc * (dj_ui + di_uj);
-    if (i == j && p) s += p[at(x, y, z)];
-    return (double)s;
-  }
-};
+static void launch_flux_filter_rt(int i, int j, const T* u, const T* p, int n, T inv_h, T visc, int c,
+                                  const Taps3& taps, T* out, long long M, cudaStream_t st) {
+#define EXC_FLUX(I, J) \
+  if (i == I && j == J) return launch_flux_filter<T, I, J>(u, p, n, inv_h, visc, c, taps, out, M, st);
+  EXC_FLUX(0, 0) EXC_FLUX(0, 1) EXC_FLUX(0, 2)
+  EXC_FLUX(1, 0) EXC_FLUX(1, 1) EXC_FLUX(1, 2)
+  EXC_FLUX(2, 0) EXC_FLUX(2, 1) EXC_FLUX(2, 2)
+#undef EXC_FLUX
+}
 
 // One thread per coarse cell: separable sum over the three tap lists.
 template <typename T, typename Src>
@@ -108,17 +95,16 @@ __global__ void filter_kernel(Src src, int n, int c, Taps3 taps, T* __restrict__
     int iz = (int)dm.div(r);
     int iy = (int)(r - (long long)iz * m);
     double acc = 0.0;
+    // tap offsets stay within (-n, 2n): wrap by comparison
+    auto wrapc = [n](int q) { return q < 0 ? q + n : (q >= n ? q - n : q); };
     for (int tz = 0; tz < taps.a[2].cnt; ++tz) {
-      int z = c * iz + taps.a[2].off[tz];
-      z = ((z % n) + n) % n;
+      const int z = wrapc(c * iz + taps.a[2].off[tz]);
       double az = 0.0;
       for (int ty = 0; ty < taps.a[1].cnt; ++ty) {
-        int y = c * iy + taps.a[1].off[ty];
-        y = ((y % n) + n) % n;
+        const int y = wrapc(c * iy + taps.a[1].off[ty]);
         double ay = 0.0;
         for (int tx = 0; tx < taps.a[0].cnt; ++tx) {
-          int x = c * ix + taps.a[0].off[tx];
-          x = ((x % n) + n) % n;
+          const int x = wrapc(c * ix + taps.a[0].off[tx]);
           ay += taps.a[0].w[tx] * src(x, y, z);
         }
         az += taps.a[1].w[ty] * ay;
@@ -132,6 +118,90 @@ __global__ void filter_kernel(Src src, int n, int c, Taps3 taps, T* __restrict__
 static inline int grid_for(long long M) {
   long long b = (M + 255) / 256;
   return (int)(b < 152LL * 32 ? b : 152LL * 32);
+}
+
+// Filter of one closure-flux component r_ij = sigma_ij(u) + delta_ij p with
+// compile-time (I, J).  The flux splits into an advective product and a
+// viscous difference,
+//   r = a b / 4 - (visc / h) d + delta_ij p,
+//   a = u_i(x + o e_j) + u_i(x + (o - 1) e_j),  b = the same for u_j along i,
+//   d = [u_i(x + o e_j) - u_i(x + (o - 1) e_j)] + [the same for u_j along i],
+// o = (i != j); the taps sum a b, d and p separately and the three sums are
+// combined once per coarse cell.  That is 8 FP64 operations per fine cell off
+// the diagonal and 5 on it (the diagonal has a = b and d = 2 d_i), against 12
+// for summing r itself; the results differ from summing r only by rounding.
+template <typename T, int I, int J, bool P>
+__global__ void __launch_bounds__(256, 2) flux_filter_kernel(const T* __restrict__ u, const T* __restrict__ p, int n,
+                                                          int c, double vh, Taps3 taps, T* __restrict__ out) {
+  const int m = n / c;
+  const long long M = (long long)m * m * m, N = (long long)n * n * n;
+  const IdxDiv dm(m);
+  const T* __restrict__ ui = u + I * N;
+  const T* __restrict__ uj = u + J * N;
+  constexpr int o = (I != J);
+  auto wrapc = [n](int q) { return q < 0 ? q + n : (q >= n ? q - n : q); };
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < M; g += (long long)gridDim.x * blockDim.x) {
+    const long long r = dm.div(g);
+    const int ix = (int)(g - r * m);
+    const int iz = (int)dm.div(r);
+    const int iy = (int)(r - (long long)iz * m);
+    double sab = 0.0, sd = 0.0, sp = 0.0;
+    for (int tz = 0; tz < taps.a[2].cnt; ++tz) {
+      const int z = wrapc(c * iz + taps.a[2].off[tz]);
+      double zab = 0.0, zd = 0.0, zp = 0.0;
+      for (int ty = 0; ty < taps.a[1].cnt; ++ty) {
+        const int y = wrapc(c * iy + taps.a[1].off[ty]);
+        // the rows of u_i and u_j at (y, z) and their neighbours along j and i
+        auto row = [&](int axis, int s) -> long long {
+          const int yy = axis == 1 ? wrapc(y + s) : y, zz = axis == 2 ? wrapc(z + s) : z;
+          return ((long long)zz * n + yy) * n;
+        };
+        const long long ri_r = row(J, o), ri_l = row(J, o - 1);
+        const long long rj_r = row(I, o), rj_l = row(I, o - 1);
+        const long long rc = ((long long)z * n + y) * n;
+        double yab = 0.0, yd = 0.0, yp = 0.0;
+        for (int tx = 0; tx < taps.a[0].cnt; ++tx) {
+          const int x = wrapc(c * ix + taps.a[0].off[tx]);
+          const int xi_r = J == 0 ? wrapc(x + o) : x, xi_l = J == 0 ? wrapc(x + o - 1) : x;
+          const double w = taps.a[0].w[tx];
+          const T air = ui[ri_r + xi_r], ail = ui[ri_l + xi_l];
+          if constexpr (I == J) {
+            const T a = air + ail, d = air - ail;
+            yab = fma(w, (double)(a * a), yab);
+            yd = fma(w, (double)d, yd);
+          } else {
+            const int xj_r = I == 0 ? wrapc(x + o) : x, xj_l = I == 0 ? wrapc(x + o - 1) : x;
+            const T ajr = uj[rj_r + xj_r], ajl = uj[rj_l + xj_l];
+            const T a = air + ail, b = ajr + ajl, d = (air + ajr) - (ail + ajl);
+            yab = fma(w, (double)(a * b), yab);
+            yd = fma(w, (double)d, yd);
+          }
+          if constexpr (P) yp = fma(w, (double)p[rc + x], yp);
+        }
+        const double wy = taps.a[1].w[ty];
+        zab = fma(wy, yab, zab);
+        zd = fma(wy, yd, zd);
+        if constexpr (P) zp = fma(wy, yp, zp);
+      }
+      const double wz = taps.a[2].w[tz];
+      sab = fma(wz, zab, sab);
+      sd = fma(wz, zd, sd);
+      if constexpr (P) sp = fma(wz, zp, sp);
+    }
+    // the diagonal's d is half the viscous difference
+    const double k = I == J ? 2.0 * vh : vh;
+    out[g] = (T)(fma(0.25, sab, -k * sd) + sp);
+  }
+}
+
+template <typename T, int I, int J>
+static void launch_flux_filter(const T* u, const T* p, int n, T inv_h, T visc, int c, const Taps3& taps, T* out,
+                               long long M, cudaStream_t st) {
+  const double vh = (double)visc * (double)inv_h;
+  if (I == J && p)
+    flux_filter_kernel<T, I, J, true><<<grid_for(M), 256, 0, st>>>(u, p, n, c, vh, taps, out);
+  else
+    flux_filter_kernel<T, I, J, false><<<grid_for(M), 256, 0, st>>>(u, p, n, c, vh, taps, out);
 }
 
 int make_taps3(int c, const bool stag[3], const bool point[3], const double* fdelta, int nfd, Taps3* out) {
@@ -180,8 +250,8 @@ int closure_flux(int n, int c, double l, double visc, const double* fdelta, int 
       Taps3 taps;
       int rc = make_taps3(c, stag, point, fdelta, nfd, &taps);
       if (rc) return rc;
-      FluxSrc<T> src{u, p, n, i, j, (T)(l / n), (T)visc};
-      filter_kernel<T><<<grid_for(M), 256, 0, st>>>(src, n, c, taps, r9 + (long long)(3 * j + i) * M);
+      launch_flux_filter_rt<T>(i, j, u, p, n, (T)(1.0 / (l / n)), (T)visc, c, taps, r9 + (long long)(3 * j + i) * M, M,
+                               st);
     }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
@@ -203,8 +273,8 @@ int filtered_stress(int n, int c, double l, double visc, const double* fdelta, i
     Taps3 taps;
     int rc = make_taps3(c, stag, point, fdelta, nfd, &taps);
     if (rc) return rc;
-    FluxSrc<T> src{u, nullptr, n, i, j, (T)(l / n), (T)visc};
-    filter_kernel<T><<<grid_for(M), 256, 0, st>>>(src, n, c, taps, s6 + (long long)k * M);
+    launch_flux_filter_rt<T>(i, j, u, (const T*)nullptr, n, (T)(1.0 / (l / n)), (T)visc, c, taps, s6 + (long long)k * M,
+                             M, st);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
@@ -362,51 +432,56 @@ cudaError_t filter_vector_box(int n, int c, int kind, const T* u, T* ub, T* tb, 
 // DNS grid (centred box of odd width c, composed with FDelta), at fine cell
 // (x, y, z): the field that `step_ΔHπ_classic!` (src/N.jl:1137-1162) samples
 // at the LES centres and edges.  Each uf value is evaluated on the fly.
-template <typename T>
+// sigma_ij of the fine-filtered velocity GDH u at fine cell (x, y, z); the
+// components (I, J) are compile-time and every index wraps by comparison (tap
+// offsets stay within (-n, 2n)).
+template <typename T, int I, int J>
 struct FineFilteredStressSrc {
   const T* u;
-  int n, i, j;
-  T h, visc;
+  int n;
+  T inv_h, visc;
   Taps1D ft;  // centred fine-filter taps (same along every axis)
+  __device__ __forceinline__ int wrap(int q) const { return q < 0 ? q + n : (q >= n ? q - n : q); }
   __device__ __forceinline__ double uf(int comp, int x, int y, int z) const {
     const long long N = (long long)n * n * n;
     const T* f = u + comp * N;
     double acc = 0.0;
     for (int tz = 0; tz < ft.cnt; ++tz) {
-      int zz = z + ft.off[tz];
-      zz = ((zz % n) + n) % n;
+      const int zz = wrap(z + ft.off[tz]);
       double az = 0.0;
       for (int ty = 0; ty < ft.cnt; ++ty) {
-        int yy = y + ft.off[ty];
-        yy = ((yy % n) + n) % n;
+        const T* row = f + ((long long)zz * n + wrap(y + ft.off[ty])) * n;
         double ay = 0.0;
-        for (int tx = 0; tx < ft.cnt; ++tx) {
-          int xx = x + ft.off[tx];
-          xx = ((xx % n) + n) % n;
-          ay += ft.w[tx] * (double)f[((long long)zz * n + yy) * n + xx];
-        }
+        for (int tx = 0; tx < ft.cnt; ++tx) ay += ft.w[tx] * (double)row[wrap(x + ft.off[tx])];
         az += ft.w[ty] * ay;
       }
       acc += ft.w[tz] * az;
     }
     return acc;
   }
+  template <int A>
+  __device__ __forceinline__ double uf_at(int comp, int x, int y, int z, int s) const {
+    if (A == 0) x = wrap(x + s);
+    if (A == 1) y = wrap(y + s);
+    if (A == 2) z = wrap(z + s);
+    return uf(comp, x, y, z);
+  }
   __device__ __forceinline__ double operator()(int x, int y, int z) const {
-    const int c[3] = {x, y, z};
-    const int off = (i != j);
-    int cr[3] = {c[0], c[1], c[2]}, cl[3] = {c[0], c[1], c[2]};
-    cr[j] = (cr[j] + off) % n;
-    cl[j] = (cl[j] + off - 1 + n) % n;
-    int dr[3] = {c[0], c[1], c[2]}, dl[3] = {c[0], c[1], c[2]};
-    dr[i] = (dr[i] + off) % n;
-    dl[i] = (dl[i] + off - 1 + n) % n;
-    const double uir = uf(i, cr[0], cr[1], cr[2]), uil = uf(i, cl[0], cl[1], cl[2]);
-    const double ujr = uf(j, dr[0], dr[1], dr[2]), ujl = uf(j, dl[0], dl[1], dl[2]);
+    constexpr int off = (I != J);
+    const double uir = uf_at<J>(I, x, y, z, off), uil = uf_at<J>(I, x, y, z, off - 1);
+    const double ujr = uf_at<I>(J, x, y, z, off), ujl = uf_at<I>(J, x, y, z, off - 1);
     const double etaj_ui = (uir + uil) / 2, etai_uj = (ujr + ujl) / 2;
-    const double dj_ui = (uir - uil) / (double)h, di_uj = (ujr - ujl) / (double)h;
+    const double dj_ui = (uir - uil) * (double)inv_h, di_uj = (ujr - ujl) * (double)inv_h;
     return etaj_ui * etai_uj - (double)visc * (dj_ui + di_uj);
   }
 };
+
+template <typename T, int I, int J>
+static void launch_classic(const T* u, int n, T inv_h, T visc, const Taps1D& ft, int c, const Taps3& taps, T* out,
+                           long long M, cudaStream_t st) {
+  FineFilteredStressSrc<T, I, J> src{u, n, inv_h, visc, ft};
+  filter_kernel<T><<<grid_for(M), 256, 0, st>>>(src, n, c, taps, out);
+}
 
 // sigma2 of `step_ΔHπ_classic!`: `lazytensorcoarsegrain(g_les,
 // stresstensor(lazyfilter(u, GDH)))` (src/N.jl:1117-1135, 1143-1145); order
@@ -428,8 +503,12 @@ int classic_stress(int n, int c, double l, double visc, const double* fdelta, in
     Taps3 taps;
     int rc = make_taps3(c, stag, point, nullptr, 0, &taps);
     if (rc) return rc;
-    FineFilteredStressSrc<T> src{u, n, i, j, (T)(l / n), (T)visc, ft};
-    filter_kernel<T><<<grid_for(M), 256, 0, st>>>(src, n, c, taps, s6 + (long long)k * M);
+    const T inv_h = (T)(1.0 / (l / n));
+    T* out = s6 + (long long)k * M;
+#define EXC_CLASSIC(I, J) \
+  if (i == I && j == J) launch_classic<T, I, J>(u, n, inv_h, (T)visc, ft, c, taps, out, M, st);
+    EXC_CLASSIC(0, 0) EXC_CLASSIC(1, 1) EXC_CLASSIC(2, 2) EXC_CLASSIC(0, 1) EXC_CLASSIC(1, 2) EXC_CLASSIC(2, 0)
+#undef EXC_CLASSIC
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }

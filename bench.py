@@ -296,7 +296,7 @@ def learned_section(train_steps=300, les_steps=100, peaks_json=None):
                                   f"pairs from a {n}^3 FP32 DNS-aided run"},
            "tensor": {"achieved_tflops": achieved, "peak_tflops": peak,
                       "frac": (achieved / peak) if peak else None,
-                      "note": "useful-channel flops (3->32->32->3) of forward + both gradients; mma.sync BF16"},
+                      "note": "useful-channel flops (3->32->32->3) of forward + both gradients; BF16 on tcgen05 (32-channel-input convolutions, tensor-memory accumulators) and mma.sync (the rest)"},
            "loss_first_last": [losses[0], losses[-1]],
            "held_out_closure_error": e_closure,
            "les_error_after_steps": {"steps": les_steps, "learned": cs.les_error(0, "learned"),

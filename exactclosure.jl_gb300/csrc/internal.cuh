@@ -59,6 +59,8 @@ cudaError_t fftreg_solve(exc_poisson* ps, const double* src, bool src_is_vector,
                          int nslots);
 // Lines per column tile and rows per x-pass CTA of a grid's register plan.
 void fftreg_geometry(int n, int precision, int* col_w, int* x_rows);
+// Read and clear the learned closure's tensor-core wait fault flag.
+int learned_fault_take(int* flag);
 cudaError_t configure_fftreg_f32();
 cudaError_t configure_fftreg_f64();
 

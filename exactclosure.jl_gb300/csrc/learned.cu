@@ -7,11 +7,12 @@
 // Activations are channel-last BF16 ([voxel][channel], channels padded to 16
 // or 32, outputs to 8); pre-activations are kept in FP32 for the backward
 // pass.  Forward and input-gradient convolutions are implicit GEMMs on the
-// tensor cores (mma.sync m16n8k16, BF16 inputs, FP32 accumulation): a CTA owns
-// 64 consecutive voxels and all output channels, and loops over the 27 taps
-// with the tap's input rows and weights staged in shared memory.  Weight
-// gradients are FP32 reductions with fixed-order partials.  Adam keeps FP32
-// master weights and moments and refreshes the BF16 copies.
+// tensor cores, BF16 inputs with FP32 accumulation: on 64^3 grids with 32
+// input channels tcgen05.mma with tensor-memory accumulators (conv_umma_kernel),
+// otherwise mma.sync m16n8k16 with the taps' input rows and the weights staged
+// in shared memory.  Weight gradients are FP32 reductions with fixed-order
+// partials.  Adam keeps FP32 master weights and moments and refreshes the BF16
+// copies.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -406,11 +407,345 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
   }
 }
 
-// Launch the tiled convolution when the grid allows it, else the row form.
+// ---------------------------------------------------------------------------
+// The convolution on the fifth-generation tensor cores (tcgen05), for 64^3
+// grids: tcgen05.mma kind::f16 (BF16 operands in shared memory, FP32
+// accumulators in tensor memory) issued by one thread per CTA.
+//
+// The x taps ride on the N side of the product.  For the nine (dy, dz) tap
+// pairs, one instruction multiplies M = 128 voxels (two consecutive output
+// rows of 64, the input rows shifted by (dy, dz)) by all three dx taps' weights
+// at once, N = 3 NP columns (dx, co), K = 16 input channels:
+//   D[v][dx][co] = sum_{dy, dz, ci} in[v + (dy - 1, dz - 1)][ci] W[dx, dy, dz][co][ci],
+// and the epilogue forms out[x][co] = D[x - 1][0][co] + D[x][1][co] + D[x + 1][2][co]
+// with x periodic along the row.  Input rows therefore need no x halo: a
+// block's halo (4 + 2 rows, 3 planes, 64 voxels each) is stored channel-chunk
+// major, [KP/8][plane][row][x][8 channels], so 128 consecutive voxels (two
+// rows) form the A operand with 8-row groups 128 bytes apart and channel
+// chunks one plane apart (no swizzle).  Weights sit as [dy, dz][KP/8][dx, co][8].
+// A block of 4 rows takes 2 x 9 x KP/16 instructions.
+//
+// A persistent CTA of 16 warps keeps the weights resident and walks blocks
+// (sample, z, 4 rows) with two halo buffers and two accumulator sets:
+// thread 0 issues block i's instructions and commits them to an mbarrier;
+// all warps then wait for block i-1's commit, refill the halo buffer it
+// freed with block i+1 (cp.async), and run block i-1's epilogue.  Warp w reads
+// tensor-memory sub-partition w % 4 (M = 128: output voxel m sits in lane m),
+// i.e. 32 voxels of one row, for half of the channels; the x neighbours'
+// D come by shuffles within the warp and, at the ends of its 32 voxels, from
+// the warp holding the other half of the row through shared memory.  Every
+// wait is bounded; a wait that gives up records a fault flag (read by
+// exc_device_faults) and the CTA stops after its copies have landed and frees
+// its tensor memory.
+// ---------------------------------------------------------------------------
+constexpr int CU_N = 64;    // grid edge this kernel serves (the row is 64 voxels)
+constexpr int CU_ROWS = 4;  // output rows per block: two M = 128 tiles
+constexpr int CU_HY = CU_ROWS + 2, CU_HZ = 3;
+constexpr int CU_HVOX = CU_N * CU_HY * CU_HZ;  // 1152
+constexpr int CU_PLANE = 1154;  // voxels per channel-chunk plane (16-byte rows; consecutive planes 8 banks apart)
+constexpr int CU_THREADS = 512;  // 16 warps: (tile, sub-partition, channel half)
+
+__device__ int g_learned_fault = 0;
+
+template <int KP> __host__ __device__ constexpr int cu_halo_bytes() { return (KP / 8) * CU_PLANE * 16; }
+template <int KP, int NP> __host__ __device__ constexpr int cu_w_bytes() { return NET_TAPS * KP * NP * 2; }
+template <int NP> __host__ __device__ constexpr int cu_xch_bytes() { return 16 * 2 * (NP / 2) * 4; }
+template <int KP, int NP> __host__ __device__ constexpr size_t conv_umma_smem() {
+  return 2 * (size_t)cu_halo_bytes<KP>() + cu_w_bytes<KP, NP>() + cu_xch_bytes<NP>() + 64;
+}
+// tensor-memory columns: two accumulator sets of two tiles x 3 NP
+template <int NP> __host__ __device__ constexpr unsigned cu_tmem_cols() { return 2 * 2 * 3 * NP <= 256 ? 256u : 512u; }
+
+__device__ __forceinline__ unsigned cu_smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, no swizzle: start, leading (K direction)
+// and stride (M/N direction, 8-row groups) byte offsets, descriptor version 1.
+__device__ __forceinline__ unsigned long long umma_sdesc(unsigned saddr, unsigned lbo, unsigned sbo) {
+  return (unsigned long long)((saddr >> 4) & 0x3FFF) | ((unsigned long long)((lbo >> 4) & 0x3FFF) << 16) |
+         ((unsigned long long)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr unsigned umma_idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+__device__ __forceinline__ void umma_bf16(unsigned dt, unsigned long long ad, unsigned long long bd, unsigned idesc,
+                                          unsigned acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(unsigned long long* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(cu_smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ bool cu_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(cu_smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// 32 lanes x 32 bit x NC columns of tensor memory into registers (no wait)
+template <int NC>
+__device__ __forceinline__ void tmem_ld_nowait(unsigned taddr, unsigned (&r)[NC]) {
+  static_assert(NC == 8 || NC == 16, "8 or 16 columns");
+  if constexpr (NC == 16) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+  } else {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+  }
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
 template <int KP, int NP, int EPI>
-static void conv_launch(long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* W, const float* bias,
-                        float* pre_out, __nv_bfloat16* act_out, const float* pre_prev, int nout_valid,
-                        cudaStream_t st) {
+__global__ void __launch_bounds__(CU_THREADS, 1)
+conv_umma_kernel(int batch, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
+                 const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
+                 const float* __restrict__ pre_prev, int nout_valid) {
+  constexpr int n = CU_N, KC = KP / 8, NT = 3 * NP, NH = NP / 2;
+  constexpr int HB = cu_halo_bytes<KP>(), WB = cu_w_bytes<KP, NP>();
+  constexpr unsigned TCOLS = cu_tmem_cols<NP>();
+  constexpr unsigned IDESC = umma_idesc_bf16(128, NT);
+  extern __shared__ __align__(1024) unsigned char cu_smem[];
+  unsigned char* const sH = cu_smem;  // two halo buffers
+  unsigned char* const sW = cu_smem + 2 * HB;
+  float* const xch = reinterpret_cast<float*>(cu_smem + 2 * HB + WB);  // [warp][2][NH]
+  unsigned long long* const bar = reinterpret_cast<unsigned long long*>(cu_smem + 2 * HB + WB + cu_xch_bytes<NP>());
+  unsigned* const s_tmem = reinterpret_cast<unsigned*>(bar + 2);
+  int* const s_abort = reinterpret_cast<int*>(s_tmem + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr long long N = (long long)n * n * n;
+  constexpr int RG = n / CU_ROWS;  // row groups per z
+  const long long nblk = (long long)batch * n * RG;
+
+  // weights: tap (dx, dy, dz) = dz 9 + dy 3 + dx -> [dy, dz][chunk][dx NP + co][8]
+  for (int t = tid; t < NET_TAPS * NP * KC; t += CU_THREADS) {
+    const int c = t % KC, row = t / KC, tap = row / NP, co = row - tap * NP;
+    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3, g = dy * 3 + dz;
+    cp_async_16(reinterpret_cast<__nv_bfloat16*>(sW + ((g * KC + c) * NT + dx * NP + co) * 16),
+                Wt + (long long)row * KP + c * 8);
+  }
+  auto load_block = [&](long long b, int buf) {
+    const long long s = b / (n * RG);
+    const int r = (int)(b - s * (n * RG)), z0 = r / RG, y0 = CU_ROWS * (r - (r / RG) * RG);
+    const __nv_bfloat16* ins = in + s * N * KP;
+    unsigned char* const H = sH + buf * HB;
+    for (int t = tid; t < CU_HVOX * KC; t += CU_THREADS) {
+      const int c = t % KC, h = t / KC;
+      const int hz = h / (n * CU_HY), hy = (h / n) % CU_HY, x = h % n;
+      int y = y0 - 1 + hy, z = z0 - 1 + hz;
+      y = y < 0 ? y + n : (y >= n ? y - n : y);
+      z = z < 0 ? z + n : (z >= n ? z - n : z);
+      cp_async_16(reinterpret_cast<__nv_bfloat16*>(H + (c * CU_PLANE + h) * 16),
+                  ins + (((long long)z * n + y) * n + x) * KP + c * 8);
+    }
+  };
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(cu_smem_u32(&bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(cu_smem_u32(&bar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    *s_abort = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(cu_smem_u32(s_tmem)),
+                 "r"(TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  long long b = blockIdx.x;
+  if (b < nblk) load_block(b, 0);
+  cp_async_commit();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = *s_tmem;
+
+  // this warp's share of the epilogue: sub-partition q (lanes 32q..), tile
+  // et (rows 2 et, 2 et + 1), channel half eh; the partner warp (q ^ 1) holds
+  // the other 32 voxels of the same row
+  const int q = warp & 3, et = (warp >> 2) & 1, eh = warp >> 3;
+  const int erow = 2 * et + (q >> 1), x = 32 * (q & 1) + lane, cb = eh * NH;
+  float bb[NH];
+#pragma unroll
+  for (int j = 0; j < NH; ++j) bb[j] = (EPI == 2) ? 0.f : __ldg(bias + cb + j);
+  auto epilogue = [&](long long bp, int set) {
+    const long long s = bp / (n * RG);
+    const int r = (int)(bp - s * (n * RG)), z0 = r / RG, y0 = CU_ROWS * (r - (r / RG) * RG);
+    const unsigned ta = tmem + ((unsigned)(32 * q) << 16) + (unsigned)((set * 2 + et) * NT + cb);
+    unsigned d0[NH], d1[NH], d2[NH];
+    tmem_ld_nowait<NH>(ta, d0);
+    tmem_ld_nowait<NH>(ta + NP, d1);
+    tmem_ld_nowait<NH>(ta + 2 * NP, d2);
+    tmem_wait_ld();
+    // ends of the 32 voxels go to the partner warp
+    float* const mine = xch + warp * 2 * NH;
+    const float* const other = xch + (warp ^ 1) * 2 * NH;
+    if (lane == 31) {
+#pragma unroll
+      for (int j = 0; j < NH; ++j) mine[j] = __uint_as_float(d0[j]);
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < NH; ++j) mine[NH + j] = __uint_as_float(d2[j]);
+    }
+    asm volatile("bar.sync %0, 64;\n" ::"r"(1 + (warp >> 1)) : "memory");
+    float f[NH];
+#pragma unroll
+    for (int j = 0; j < NH; ++j) {
+      // D[x - 1][0] from the lane below, D[x + 1][2] from the lane above
+      float lo = __uint_as_float(__shfl_up_sync(0xffffffffu, d0[j], 1));
+      float hi = __uint_as_float(__shfl_down_sync(0xffffffffu, d2[j], 1));
+      if (lane == 0) lo = other[j];
+      if (lane == 31) hi = other[NH + j];
+      f[j] = lo + __uint_as_float(d1[j]) + hi;
+    }
+    const long long g = s * N + ((long long)z0 * n + (y0 + erow)) * n + x;
+    if (EPI == 0 || EPI == 1) {
+#pragma unroll
+      for (int j = 0; j < NH; j += 4) {
+        float4 v;
+        v.x = f[j] + bb[j];
+        v.y = f[j + 1] + bb[j + 1];
+        v.z = f[j + 2] + bb[j + 2];
+        v.w = f[j + 3] + bb[j + 3];
+        if (EPI == 1) {
+          const int co = cb + j;
+          v.x = co < nout_valid ? v.x : 0.f;
+          v.y = co + 1 < nout_valid ? v.y : 0.f;
+          v.z = co + 2 < nout_valid ? v.z : 0.f;
+          v.w = co + 3 < nout_valid ? v.w : 0.f;
+        }
+        *reinterpret_cast<float4*>(pre_out + g * NP + cb + j) = v;
+        if (EPI == 0) {
+          __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(gelu_f(v.x)), __float2bfloat16(gelu_f(v.y)));
+          __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(gelu_f(v.z)), __float2bfloat16(gelu_f(v.w)));
+          uint2 pk;
+          pk.x = *reinterpret_cast<unsigned*>(&h0);
+          pk.y = *reinterpret_cast<unsigned*>(&h1);
+          *reinterpret_cast<uint2*>(act_out + g * NP + cb + j) = pk;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NH; j += 4) {
+        const float4 pp = *reinterpret_cast<const float4*>(pre_prev + g * NP + cb + j);
+        __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(f[j] * gelu_grad_f(pp.x)),
+                                               __float2bfloat16(f[j + 1] * gelu_grad_f(pp.y)));
+        __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(f[j + 2] * gelu_grad_f(pp.z)),
+                                               __float2bfloat16(f[j + 3] * gelu_grad_f(pp.w)));
+        uint2 pk;
+        pk.x = *reinterpret_cast<unsigned*>(&h0);
+        pk.y = *reinterpret_cast<unsigned*>(&h1);
+        *reinterpret_cast<uint2*>(act_out + g * NP + cb + j) = pk;
+      }
+    }
+  };
+  // bounded wait for the commit of the i-th block (accumulator set i & 1),
+  // warp-uniform: the tensor-memory loads after it are warp collectives
+  auto wait_mma = [&](long long i) -> bool {
+    const unsigned parity = (unsigned)((i >> 1) & 1);
+    bool ok = false;
+    for (int polls = 0; polls < (1 << 20) && !ok; ++polls) ok = cu_try_wait(&bar[i & 1], parity);
+    return __all_sync(0xffffffffu, ok) != 0;
+  };
+
+  long long i = 0;
+  for (; b < nblk; b += gridDim.x, ++i) {
+    const int buf = (int)(i & 1);
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // cp.async data -> tensor-core reads
+    tc_fence_before();
+    __syncthreads();
+    if (*s_abort) break;
+    // one lane issues the block's instructions; the rest of its warp waits
+    // at the warp barrier
+    if (warp == 0) {
+      if (lane == 0) {
+        tc_fence_after();
+        // the start address (/16) is the descriptor's low field: an operand
+        // at a byte offset is the base descriptor plus offset / 16
+        const unsigned long long ad0 = umma_sdesc(cu_smem_u32(sH + buf * HB), CU_PLANE * 16, 128);
+        const unsigned long long bd0 = umma_sdesc(cu_smem_u32(sW), NT * 16, 128);
+#pragma unroll
+        for (int t = 0; t < 2; ++t)
+#pragma unroll
+          for (int g = 0; g < 9; ++g)
+#pragma unroll
+            for (int kk = 0; kk < KP / 16; ++kk) {
+              const int dy = g / 3, dz = g % 3;
+              const unsigned aoff = (unsigned)((dz * CU_HY + 2 * t + dy) * n + kk * 2 * CU_PLANE);
+              const unsigned boff = (unsigned)((g * KC + kk * 2) * NT);
+              umma_bf16(tmem + (unsigned)((buf * 2 + t) * NT), ad0 + aoff, bd0 + boff, IDESC, (g | kk) != 0);
+            }
+        umma_commit(&bar[buf]);
+      }
+      __syncwarp();
+    }
+    const bool ok = i == 0 || wait_mma(i - 1);
+    // the other halo buffer is free once block i-1's MMAs are complete: its
+    // refill flies during the epilogue
+    if (b + gridDim.x < nblk) load_block(b + gridDim.x, buf ^ 1);
+    cp_async_commit();
+    if (!ok) {
+      if (lane == 0) atomicExch(&g_learned_fault, 1);
+      *s_abort = 1;
+    } else if (i > 0) {
+      tc_fence_after();
+      epilogue(b - gridDim.x, buf ^ 1);
+    }
+    tc_fence_before();
+  }
+  __syncthreads();
+  const bool aborted = *s_abort != 0;
+  if (i > 0) {
+    // the last block's MMAs (after an abort: let them finish, bounded)
+    const bool ok = wait_mma(i - 1);
+    if (ok && !aborted) {
+      tc_fence_after();
+      epilogue(b - gridDim.x, (int)((i - 1) & 1));
+    } else if (!ok && lane == 0) {
+      atomicExch(&g_learned_fault, 1);
+    }
+  }
+  cp_async_wait_all();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
+  }
+}
+
+// Engine 0: the tcgen05 kernel on 64^3 grids for 32 input channels (with 16
+// the weight-resident mma.sync kernel measured faster: its epilogue, not the
+// products, bounds both), else the mma.sync forms; engine 1: the mma.sync
+// forms only.
+template <int KP, int NP, int EPI>
+static void conv_launch(int engine, long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* W,
+                        const float* bias, float* pre_out, __nv_bfloat16* act_out, const float* pre_prev,
+                        int nout_valid, cudaStream_t st) {
+  if constexpr (KP == 32) {
+    if (engine == 0 && n == CU_N) {
+      const long long N = (long long)n * n * n;
+      const long long nblk = (V / N) * n * (n / CU_ROWS);
+      const long long ctas = std::min<long long>(nblk, 152);
+      conv_umma_kernel<KP, NP, EPI><<<(unsigned)ctas, CU_THREADS, conv_umma_smem<KP, NP>(), st>>>(
+          (int)(V / N), in, W, bias, pre_out, act_out, pre_prev, nout_valid);
+      return;
+    }
+  }
   if (n % 8 == 0) {
     const long long N = (long long)n * n * n;
     const long long nblk = V / CR_BV;
@@ -866,6 +1201,7 @@ struct exc_net {
   float* adam_v = nullptr;
   __nv_bfloat16* wbf = nullptr;  // Wt1 Wb1 Wt2 Wb2 Wt3 Wb3
   int adam_t = 0;
+  int conv_engine = 0;  // 0: tcgen05 convolutions on 64^3 grids; 1: mma.sync only
   double in_scale = 1.0, out_scale = 1.0;
   long long vcap = 0;  // voxel capacity of the workspace
   int ws_gen = 0;       // bumped whenever the workspace moves (captured graphs must re-capture)
@@ -934,9 +1270,9 @@ static cudaError_t refresh(exc_net* net, cudaStream_t st) {
 
 // forward from the packed input x0; leaves pre1, a1, pre2, a2, out
 static cudaError_t forward_packed(exc_net* net, long long V, int n, cudaStream_t st) {
-  conv_launch<16, 32, 0>(V, n, net->x0, net->Wt(0), net->B(0), net->pre1, net->a1, nullptr, 32, st);
-  conv_launch<32, 32, 0>(V, n, net->a1, net->Wt(1), net->B(1), net->pre2, net->a2, nullptr, 32, st);
-  conv_launch<32, 16, 1>(V, n, net->a2, net->Wt(2), net->B(2), net->out, nullptr, nullptr, 3, st);
+  conv_launch<16, 32, 0>(net->conv_engine, V, n, net->x0, net->Wt(0), net->B(0), net->pre1, net->a1, nullptr, 32, st);
+  conv_launch<32, 32, 0>(net->conv_engine, V, n, net->a1, net->Wt(1), net->B(1), net->pre2, net->a2, nullptr, 32, st);
+  conv_launch<32, 16, 1>(net->conv_engine, V, n, net->a2, net->Wt(2), net->B(2), net->out, nullptr, nullptr, 3, st);
   return cudaGetLastError();
 }
 
@@ -977,9 +1313,9 @@ static cudaError_t backward(exc_net* net, long long V, int n, long long N, const
   sum_kernel<<<1, 256, 0, st>>>(lb, net->lpart, 1.0 / (3.0 * (double)V), net->lpart + 1024);
   cudaError_t e = wgrad<32, 16>(net, 2, V, n, net->a2, net->g3, st);
   // input gradient of layer 3 times GELU'(pre2)
-  conv_launch<16, 32, 2>(V, n, net->g3, net->Wb(2), nullptr, nullptr, net->gp2, net->pre2, 32, st);
+  conv_launch<16, 32, 2>(net->conv_engine, V, n, net->g3, net->Wb(2), nullptr, nullptr, net->gp2, net->pre2, 32, st);
   if (e == cudaSuccess) e = wgrad<32, 32>(net, 1, V, n, net->a1, net->gp2, st);
-  conv_launch<32, 32, 2>(V, n, net->gp2, net->Wb(1), nullptr, nullptr, net->gp1, net->pre1, 32, st);
+  conv_launch<32, 32, 2>(net->conv_engine, V, n, net->gp2, net->Wb(1), nullptr, nullptr, net->gp1, net->pre1, 32, st);
   if (e == cudaSuccess) e = wgrad<16, 32>(net, 0, V, n, net->x0, net->gp1, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;
@@ -1040,6 +1376,11 @@ static cudaError_t conv_res_attr() {
   return cudaFuncSetAttribute(conv_res_kernel<KP, NP, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)conv_res_smem<KP, NP>());
 }
+template <int KP, int NP, int EPI>
+static cudaError_t conv_umma_attr() {
+  return cudaFuncSetAttribute(conv_umma_kernel<KP, NP, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)conv_umma_smem<KP, NP>());
+}
 template <int KP, int NP>
 static cudaError_t wgrad_tile_attr() {
   return cudaFuncSetAttribute(wgrad_tile_kernel<KP, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1063,8 +1404,21 @@ static int configure_learned() {
   if (e == cudaSuccess) e = conv_res_attr<32, 16, 1>();
   if (e == cudaSuccess) e = conv_res_attr<16, 32, 2>();
   if (e == cudaSuccess) e = conv_res_attr<32, 32, 2>();
+  if (e == cudaSuccess) e = conv_umma_attr<32, 32, 0>();
+  if (e == cudaSuccess) e = conv_umma_attr<32, 16, 1>();
+  if (e == cudaSuccess) e = conv_umma_attr<32, 32, 2>();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   done[dev] = true;
+  return EXC_OK;
+}
+
+// Read and clear the flag of a tensor-core wait that gave up.
+int learned_fault_take(int* flag) {
+  int v = 0, zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_learned_fault, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_learned_fault, &zero, sizeof(int));
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  *flag = v;
   return EXC_OK;
 }
 
@@ -1107,6 +1461,12 @@ int exc_net_create(uint64_t seed, exc_net** out) {
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { exc_net_destroy(net); set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   *out = net;
+  return EXC_OK;
+}
+
+int exc_net_set_conv_engine(exc_net* net, int engine) {
+  if (!net || engine < 0 || engine > 1) { set_last_error("invalid network or convolution engine"); return EXC_ERR_ARG; }
+  net->conv_engine = engine;
   return EXC_OK;
 }
 

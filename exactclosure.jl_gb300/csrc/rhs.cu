@@ -765,10 +765,12 @@ template cudaError_t launch_rhs<float>(int, float, float, const float*, float*, 
 
 extern "C" int exc_device_faults(int* flags) {
   if (!flags) { exc::set_last_error("null argument"); return EXC_ERR_ARG; }
-  int v = 0, zero = 0;
+  int v = 0, zero = 0, lf = 0;
   cudaError_t e = cudaMemcpyFromSymbol(&v, exc::g_rhs_tma_fault, sizeof(int));
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(exc::g_rhs_tma_fault, &zero, sizeof(int));
   if (e != cudaSuccess) { exc::set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-  *flags = v;
+  const int rc = exc::learned_fault_take(&lf);
+  if (rc) return rc;
+  *flags = (v ? 1 : 0) | (lf ? 2 : 0);
   return EXC_OK;
 }

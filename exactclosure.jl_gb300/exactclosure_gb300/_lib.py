@@ -115,6 +115,7 @@ SIGNATURES = {
     "exc_net_destroy": [vp],
     "exc_net_param_count": [],
     "exc_net_set_scales": [vp, f64, f64],
+    "exc_net_set_conv_engine": [vp, i32],
     "exc_net_get_params": [vp, C.POINTER(C.c_float), i32],
     "exc_net_set_params": [vp, C.POINTER(C.c_float), i32],
     "exc_net_forward": [vp, i32, i32, i32, vp, vp, vp],

@@ -100,6 +100,11 @@ class Net:
         self.in_scale, self.out_scale = in_scale, out_scale
         call("exc_net_set_scales", self._h, in_scale, out_scale)
 
+    def set_conv_engine(self, engine: int):
+        """0: tcgen05 tensor-core convolutions on 64^3 grids (default);
+        1: mma.sync convolutions everywhere."""
+        call("exc_net_set_conv_engine", self._h, int(engine))
+
     def get_params(self) -> np.ndarray:
         a = np.empty(self.count, dtype=np.float32)
         call("exc_net_get_params", self._h, a.ctypes.data_as(C.POINTER(C.c_float)), self.count)

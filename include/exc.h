@@ -89,8 +89,9 @@ int exc_poisson_create(int precision, int n, double l, exc_poisson** out);
 int exc_poisson_destroy(exc_poisson* ps);
 /* Device faults recorded by kernels since the last call (and cleared): bit 0
  * = a wait for a TMA plane of the FP32 RHS sweep gave up after its poll
- * limit (the copy never completed; that sweep's output is not valid).  0 in
- * normal operation. */
+ * limit (the copy never completed; that sweep's output is not valid); bit 1
+ * = a wait for the tensor-core (tcgen05) convolution of the learned closure
+ * gave up (that convolution's output is not valid).  0 in normal operation. */
 int exc_device_faults(int* flags);
 
 /* FFT engine of a solver (no counterpart in the reference): 0 = register-
@@ -324,6 +325,10 @@ int exc_net_destroy(exc_net* net);
 int exc_net_param_count(void);
 int exc_net_set_scales(exc_net* net, double in_scale, double out_scale);
 int exc_net_get_params(exc_net* net, float* host, int count);
+/* Convolution engine: 0 (default) = tcgen05 tensor-core kernels (tensor
+ * memory accumulators) on 64^3 grids and mma.sync kernels elsewhere; 1 =
+ * mma.sync kernels everywhere.  Both sum the same BF16 products in FP32. */
+int exc_net_set_conv_engine(exc_net* net, int engine);
 /* Also resets the Adam state. */
 int exc_net_set_params(exc_net* net, const float* host, int count);
 /* m = net(u) */

@@ -40,7 +40,7 @@ def conv_backward(x, W, dout):
     dW = np.zeros_like(W)
     for t, (dz, dy, dx_) in enumerate(TAPS):
         xs = shift(x, dz, dy, dx_)
-        dW[t] = np.einsum("bzyxi,bzyxo->io", xs, dout)
+        dW[t] = np.einsum("bzyxi,bzyxo->io", xs, dout, optimize=True)
         dx += shift(dout @ W[t].T, -dz, -dy, -dx_)
     db = dout.sum(axis=(0, 1, 2, 3))
     return dx, dW, db

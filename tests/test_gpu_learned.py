@@ -67,10 +67,14 @@ def setup_net(LN, seed=3):
 
 # n = 8: weight-resident convolutions and per-block weight gradients; 12: the
 # 4^3-tile convolution and per-tap weight gradients; 10: the row-form
-# convolution
-@pytest.mark.parametrize("n,batch", [(8, 2), (12, 1), (10, 1)])
+# convolution; 64: the tcgen05 convolutions (tensor-memory accumulators)
+@pytest.mark.parametrize("n,batch", [(8, 2), (12, 1), (10, 1), (64, 1)])
 def test_forward_and_gradients_match_oracle(LN, n, batch):
     import torch
+
+    from exactclosure_gb300 import navierstokes as NS
+
+    NS.device_faults()
 
     net, params = setup_net(LN)
     rng = np.random.default_rng(n)
@@ -91,6 +95,40 @@ def test_forward_and_gradients_match_oracle(LN, n, batch):
     for l in range(3):
         assert rel(gp[l][0], ref_grads[l][0]) < 2e-3, l
         assert rel(gp[l][1], ref_grads[l][1]) < 2e-3, l
+    assert NS.device_faults() == 0
+    net.close()
+
+
+def test_conv_engines_agree(LN):
+    """On a 64^3 grid the tcgen05 convolutions and the mma.sync ones give the
+    same forward output and gradients up to FP32 summation order (and the BF16
+    roundings of activations it can flip)."""
+    import torch
+
+    from exactclosure_gb300 import navierstokes as NS
+
+    NS.device_faults()
+    net, _ = setup_net(LN, seed=3)
+    n, batch = 64, 2
+    rng = np.random.default_rng(7)
+    u = torch.tensor(rng.normal(0, 1.0, (batch, 3, n, n, n)), device="cuda", dtype=torch.float32)
+    m = torch.tensor(rng.normal(0, 30.0, (batch, 3, n, n, n)), device="cuda", dtype=torch.float32)
+    net.set_scales(1.0, 30.0)
+    res = []
+    for engine in (0, 1):
+        net.set_conv_engine(engine)
+        out = torch.empty_like(u)
+        net.forward(u, out)
+        loss, g = net.gradients(u, m)
+        torch.cuda.synchronize()
+        res.append((out.double().cpu().numpy(), loss, g.astype(np.float64)))
+    (o0, l0, g0), (o1, l1, g1) = res
+    assert rel(o0, o1) < 1e-3
+    assert abs(l0 - l1) < 1e-4 * l1
+    assert rel(g0, g1) < 1e-3
+    assert NS.device_faults() == 0
+    with pytest.raises(Exception):
+        net.set_conv_engine(2)
     net.close()
 
 

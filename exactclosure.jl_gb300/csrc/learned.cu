@@ -13,6 +13,8 @@
 // in shared memory.  Weight gradients are FP32 reductions with fixed-order
 // partials.  Adam keeps FP32 master weights and moments and refreshes the BF16
 // copies.
+#include <cuda.h>  // CUtensorMap
+
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -409,49 +411,64 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
 
 // ---------------------------------------------------------------------------
 // The convolution on the fifth-generation tensor cores (tcgen05), for 64^3
-// grids: tcgen05.mma kind::f16 (BF16 operands in shared memory, FP32
-// accumulators in tensor memory) issued by one thread per CTA.
+// grids with 32 input channels: tcgen05.mma kind::f16 (BF16 operands in
+// shared memory, FP32 accumulators in tensor memory).
 //
 // The x taps ride on the N side of the product.  For the nine (dy, dz) tap
 // pairs, one instruction multiplies M = 128 voxels (two consecutive output
-// rows of 64, the input rows shifted by (dy, dz)) by all three dx taps' weights
-// at once, N = 3 NP columns (dx, co), K = 16 input channels:
+// rows of 64, the input rows shifted by (dy, dz)) by all three dx taps'
+// weights at once, N = 3 NP columns (dx, co), K = 16 input channels:
 //   D[v][dx][co] = sum_{dy, dz, ci} in[v + (dy - 1, dz - 1)][ci] W[dx, dy, dz][co][ci],
 // and the epilogue forms out[x][co] = D[x - 1][0][co] + D[x][1][co] + D[x + 1][2][co]
 // with x periodic along the row.  Input rows therefore need no x halo: a
-// block's halo (4 + 2 rows, 3 planes, 64 voxels each) is stored channel-chunk
-// major, [KP/8][plane][row][x][8 channels], so 128 consecutive voxels (two
-// rows) form the A operand with 8-row groups 128 bytes apart and channel
-// chunks one plane apart (no swizzle).  Weights sit as [dy, dz][KP/8][dx, co][8].
-// A block of 4 rows takes 2 x 9 x KP/16 instructions.
+// block of 4 output rows reads 3 planes x 6 rows of 64 voxels, stored
+// [plane][KP/8][row][x][8 channels], so 128 consecutive voxels (two rows) of
+// one channel chunk form the A operand (8-row groups 128 bytes apart, chunks
+// 6 KB apart, no swizzle).  Weights sit as [dy, dz][KP/8][dx, co][8].  A block
+// takes 2 tiles x 9 (dy, dz) x KP/16 instructions.
 //
-// A persistent CTA of 16 warps keeps the weights resident and walks blocks
-// (sample, z, 4 rows) with two halo buffers and two accumulator sets:
-// thread 0 issues block i's instructions and commits them to an mbarrier;
-// all warps then wait for block i-1's commit, refill the halo buffer it
-// freed with block i+1 (cp.async), and run block i-1's epilogue.  Warp w reads
-// tensor-memory sub-partition w % 4 (M = 128: output voxel m sits in lane m),
-// i.e. 32 voxels of one row, for half of the channels; the x neighbours'
-// D come by shuffles within the warp and, at the ends of its 32 voxels, from
-// the warp holding the other half of the row through shared memory.  Every
-// wait is bounded; a wait that gives up records a fault flag (read by
-// exc_device_faults) and the CTA stops after its copies have landed and frees
-// its tensor memory.
+// A persistent CTA keeps the weights resident and walks blocks (sample, z,
+// 4 rows) with warp-specialised roles and mbarrier hand-offs only:
+//   warp 1 (loads): waits until the halo buffer is free, then fetches the
+//     block's rows by TMA (cp.async.bulk.tensor, one 6-row box per plane and
+//     chunk, single rows where y wraps), completing on the buffer's mbarrier;
+//   warp 0 (products): one lane waits for the halo and for a free accumulator
+//     set, issues the block's instructions and commits them twice (halo
+//     buffer free, accumulators full);
+//   warps 2-17 (epilogue): wait for the accumulators, read them with
+//     tcgen05.ld (warp w reads sub-partition w % 4: output voxel m of an
+//     M = 128 tile sits in lane m), exchange the ends of their 32 voxels with
+//     the warp holding the other half of the row (shared memory, a two-warp
+//     mbarrier), release the set, combine the x taps (shuffles within the
+//     warp), apply bias / GELU / GELU' and store.
+// Two halo buffers and two accumulator sets let loads, products and epilogue
+// of consecutive blocks overlap.  Every wait is bounded; a wait that gives up
+// records a fault flag (read by exc_device_faults), every role stops, the
+// copies and products in flight are waited for (bounded) and the tensor
+// memory is freed.
 // ---------------------------------------------------------------------------
 constexpr int CU_N = 64;    // grid edge this kernel serves (the row is 64 voxels)
 constexpr int CU_ROWS = 4;  // output rows per block: two M = 128 tiles
 constexpr int CU_HY = CU_ROWS + 2, CU_HZ = 3;
-constexpr int CU_HVOX = CU_N * CU_HY * CU_HZ;  // 1152
-constexpr int CU_PLANE = 1154;  // voxels per channel-chunk plane (16-byte rows; consecutive planes 8 banks apart)
-constexpr int CU_THREADS = 512;  // 16 warps: (tile, sub-partition, channel half)
+constexpr int CU_EPI_WARPS = 16;
+constexpr int CU_THREADS = 32 * (2 + CU_EPI_WARPS);
+constexpr int CU_KP = 32, CU_KC = CU_KP / 8;  // input channels (chunks of 8)
+
+// Tensor maps of one input tensor viewed as (8 channels, 64 x, rows) per
+// channel chunk: 6-row and 1-row boxes.
+struct HaloMaps {
+  CUtensorMap rows6[CU_KC];
+  CUtensorMap row1[CU_KC];
+};
 
 __device__ int g_learned_fault = 0;
 
-template <int KP> __host__ __device__ constexpr int cu_halo_bytes() { return (KP / 8) * CU_PLANE * 16; }
-template <int KP, int NP> __host__ __device__ constexpr int cu_w_bytes() { return NET_TAPS * KP * NP * 2; }
-template <int NP> __host__ __device__ constexpr int cu_xch_bytes() { return 16 * 2 * (NP / 2) * 4; }
-template <int KP, int NP> __host__ __device__ constexpr size_t conv_umma_smem() {
-  return 2 * (size_t)cu_halo_bytes<KP>() + cu_w_bytes<KP, NP>() + cu_xch_bytes<NP>() + 64;
+constexpr int cu_row_bytes = CU_N * 16;  // one row of one chunk
+constexpr int cu_halo_bytes = CU_HZ * CU_KC * CU_HY * cu_row_bytes;
+template <int NP> __host__ __device__ constexpr int cu_w_bytes() { return NET_TAPS * CU_KP * NP * 2; }
+template <int NP> __host__ __device__ constexpr int cu_xch_bytes() { return 2 * CU_EPI_WARPS * 2 * (NP / 2) * 4; }
+template <int NP> __host__ __device__ constexpr size_t conv_umma_smem() {
+  return 2 * (size_t)cu_halo_bytes + cu_w_bytes<NP>() + cu_xch_bytes<NP>() + 24 * 8 + 16;
 }
 // tensor-memory columns: two accumulator sets of two tiles x 3 NP
 template <int NP> __host__ __device__ constexpr unsigned cu_tmem_cols() { return 2 * 2 * 3 * NP <= 256 ? 256u : 512u; }
@@ -491,6 +508,27 @@ __device__ __forceinline__ bool cu_try_wait(unsigned long long* bar, unsigned pa
       : "memory");
   return ok != 0;
 }
+// bounded wait for the phase of `parity` to complete
+__device__ __forceinline__ bool cu_wait(unsigned long long* bar, unsigned parity) {
+  for (int polls = 0; polls < (1 << 20); ++polls)
+    if (cu_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void cu_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(cu_smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void cu_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(cu_smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cu_tma_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                          unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+          cu_smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(cu_smem_u32(bar))
+      : "memory");
+}
 // 32 lanes x 32 bit x NC columns of tensor memory into registers (no wait)
 template <int NC>
 __device__ __forceinline__ void tmem_ld_nowait(unsigned taddr, unsigned (&r)[NC]) {
@@ -509,26 +547,43 @@ __device__ __forceinline__ void tmem_ld_nowait(unsigned taddr, unsigned (&r)[NC]
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 
-template <int KP, int NP, int EPI>
+template <int NP, int EPI>
 __global__ void __launch_bounds__(CU_THREADS, 1)
-conv_umma_kernel(int batch, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
+conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bfloat16* __restrict__ Wt,
                  const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
                  const float* __restrict__ pre_prev, int nout_valid) {
-  constexpr int n = CU_N, KC = KP / 8, NT = 3 * NP, NH = NP / 2;
-  constexpr int HB = cu_halo_bytes<KP>(), WB = cu_w_bytes<KP, NP>();
+  constexpr int n = CU_N, KP = CU_KP, KC = CU_KC, NT = 3 * NP, NH = NP / 2;
+  constexpr int HB = cu_halo_bytes, WB = cu_w_bytes<NP>();
   constexpr unsigned TCOLS = cu_tmem_cols<NP>();
   constexpr unsigned IDESC = umma_idesc_bf16(128, NT);
+  constexpr int CHUNK = CU_HY * cu_row_bytes;  // one plane's rows of one chunk (the A operand's K stride)
   extern __shared__ __align__(1024) unsigned char cu_smem[];
   unsigned char* const sH = cu_smem;  // two halo buffers
   unsigned char* const sW = cu_smem + 2 * HB;
-  float* const xch = reinterpret_cast<float*>(cu_smem + 2 * HB + WB);  // [warp][2][NH]
-  unsigned long long* const bar = reinterpret_cast<unsigned long long*>(cu_smem + 2 * HB + WB + cu_xch_bytes<NP>());
-  unsigned* const s_tmem = reinterpret_cast<unsigned*>(bar + 2);
-  int* const s_abort = reinterpret_cast<int*>(s_tmem + 1);
+  float* const xch = reinterpret_cast<float*>(cu_smem + 2 * HB + WB);  // [block parity][warp][2][NH]
+  unsigned long long* const bars = reinterpret_cast<unsigned long long*>(cu_smem + 2 * HB + WB + cu_xch_bytes<NP>());
+  unsigned long long* const hfull = bars;       // [2] halo landed (TMA bytes)
+  unsigned long long* const hempty = bars + 2;  // [2] halo read by the products (commit)
+  unsigned long long* const afull = bars + 4;   // [2] accumulators written (commit)
+  unsigned long long* const aempty = bars + 6;  // [2] accumulators read (16 epilogue warps)
+  unsigned long long* const xbar = bars + 8;    // [8 warp pairs][2] edge exchange (2 warps)
+  unsigned* const s_tmem = reinterpret_cast<unsigned*>(bars + 24);
+  volatile int* const s_abort = reinterpret_cast<volatile int*>(s_tmem + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr long long N = (long long)n * n * n;
   constexpr int RG = n / CU_ROWS;  // row groups per z
   const long long nblk = (long long)batch * n * RG;
+  const int nb = blockIdx.x < nblk ? (int)((nblk - 1 - blockIdx.x) / gridDim.x) + 1 : 0;
+  auto origin = [&](long long b, long long& s, int& z0, int& y0) {
+    s = b / (n * RG);
+    const int r = (int)(b - s * (n * RG));
+    z0 = r / RG;
+    y0 = CU_ROWS * (r - (r / RG) * RG);
+  };
+  auto fault = [&]() {
+    atomicExch(&g_learned_fault, 1);
+    *s_abort = 1;
+  };
 
   // weights: tap (dx, dy, dz) = dz 9 + dy 3 + dx -> [dy, dz][chunk][dx NP + co][8]
   for (int t = tid; t < NET_TAPS * NP * KC; t += CU_THREADS) {
@@ -537,24 +592,12 @@ conv_umma_kernel(int batch, const __nv_bfloat16* __restrict__ in, const __nv_bfl
     cp_async_16(reinterpret_cast<__nv_bfloat16*>(sW + ((g * KC + c) * NT + dx * NP + co) * 16),
                 Wt + (long long)row * KP + c * 8);
   }
-  auto load_block = [&](long long b, int buf) {
-    const long long s = b / (n * RG);
-    const int r = (int)(b - s * (n * RG)), z0 = r / RG, y0 = CU_ROWS * (r - (r / RG) * RG);
-    const __nv_bfloat16* ins = in + s * N * KP;
-    unsigned char* const H = sH + buf * HB;
-    for (int t = tid; t < CU_HVOX * KC; t += CU_THREADS) {
-      const int c = t % KC, h = t / KC;
-      const int hz = h / (n * CU_HY), hy = (h / n) % CU_HY, x = h % n;
-      int y = y0 - 1 + hy, z = z0 - 1 + hz;
-      y = y < 0 ? y + n : (y >= n ? y - n : y);
-      z = z < 0 ? z + n : (z >= n ? z - n : z);
-      cp_async_16(reinterpret_cast<__nv_bfloat16*>(H + (c * CU_PLANE + h) * 16),
-                  ins + (((long long)z * n + y) * n + x) * KP + c * 8);
-    }
-  };
+  cp_async_commit();
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(cu_smem_u32(&bar[0])) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(cu_smem_u32(&bar[1])) : "memory");
+    for (int k = 0; k < 24; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(cu_smem_u32(&bars[k])),
+                   "r"(k < 6 ? 1 : (k < 8 ? CU_EPI_WARPS : 2))
+                   : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     *s_abort = 0;
   }
@@ -564,120 +607,65 @@ conv_umma_kernel(int batch, const __nv_bfloat16* __restrict__ in, const __nv_bfl
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
-  long long b = blockIdx.x;
-  if (b < nblk) load_block(b, 0);
-  cp_async_commit();
+  cp_async_wait_all();
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // weights -> tensor-core reads
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const unsigned tmem = *s_tmem;
 
-  // this warp's share of the epilogue: sub-partition q (lanes 32q..), tile
-  // et (rows 2 et, 2 et + 1), channel half eh; the partner warp (q ^ 1) holds
-  // the other 32 voxels of the same row
-  const int q = warp & 3, et = (warp >> 2) & 1, eh = warp >> 3;
-  const int erow = 2 * et + (q >> 1), x = 32 * (q & 1) + lane, cb = eh * NH;
-  float bb[NH];
-#pragma unroll
-  for (int j = 0; j < NH; ++j) bb[j] = (EPI == 2) ? 0.f : __ldg(bias + cb + j);
-  auto epilogue = [&](long long bp, int set) {
-    const long long s = bp / (n * RG);
-    const int r = (int)(bp - s * (n * RG)), z0 = r / RG, y0 = CU_ROWS * (r - (r / RG) * RG);
-    const unsigned ta = tmem + ((unsigned)(32 * q) << 16) + (unsigned)((set * 2 + et) * NT + cb);
-    unsigned d0[NH], d1[NH], d2[NH];
-    tmem_ld_nowait<NH>(ta, d0);
-    tmem_ld_nowait<NH>(ta + NP, d1);
-    tmem_ld_nowait<NH>(ta + 2 * NP, d2);
-    tmem_wait_ld();
-    // ends of the 32 voxels go to the partner warp
-    float* const mine = xch + warp * 2 * NH;
-    const float* const other = xch + (warp ^ 1) * 2 * NH;
-    if (lane == 31) {
-#pragma unroll
-      for (int j = 0; j < NH; ++j) mine[j] = __uint_as_float(d0[j]);
+  if (warp == 1) {
+    // ---- loads ----
+    int i = 0;
+    for (; i < nb; ++i) {
+      const int buf = i & 1;
+      if (i >= 2 && !__all_sync(0xffffffffu, cu_wait(&hempty[buf], (unsigned)(((i - 2) >> 1) & 1)))) {
+        if (lane == 0) fault();
+        break;
+      }
+      if (*s_abort) break;
+      long long s;
+      int z0, y0;
+      origin(blockIdx.x + (long long)i * gridDim.x, s, z0, y0);
+      if (lane == 0) cu_expect_tx(&hfull[buf], (unsigned)HB);
+      __syncwarp();
+      if (lane < KC * CU_HZ) {
+        const int c = lane / CU_HZ, hz = lane - c * CU_HZ;
+        int zz = z0 - 1 + hz;
+        zz = zz < 0 ? zz + n : (zz >= n ? zz - n : zz);
+        const int rbase = (int)(s * n * n) + zz * n;  // row index of (y = 0, zz, s)
+        unsigned char* const dst = sH + buf * HB + (hz * KC + c) * CHUNK;
+        if (y0 >= 1 && y0 + CU_ROWS < n) {
+          cu_tma_3d(dst, &maps.rows6[c], 0, 0, rbase + y0 - 1, &hfull[buf]);
+        } else {
+          for (int hy = 0; hy < CU_HY; ++hy) {
+            int y = y0 - 1 + hy;
+            y = y < 0 ? y + n : (y >= n ? y - n : y);
+            cu_tma_3d(dst + hy * cu_row_bytes, &maps.row1[c], 0, 0, rbase + y, &hfull[buf]);
+          }
+        }
+      }
     }
+    // copies in flight: the last two issued batches land (bounded)
+    for (int j = i - 2; j < i; ++j)
+      if (j >= 0 && !__all_sync(0xffffffffu, cu_wait(&hfull[j & 1], (unsigned)((j >> 1) & 1))) && lane == 0) fault();
+  } else if (warp == 0) {
+    // ---- products ----
     if (lane == 0) {
-#pragma unroll
-      for (int j = 0; j < NH; ++j) mine[NH + j] = __uint_as_float(d2[j]);
-    }
-    asm volatile("bar.sync %0, 64;\n" ::"r"(1 + (warp >> 1)) : "memory");
-    float f[NH];
-#pragma unroll
-    for (int j = 0; j < NH; ++j) {
-      // D[x - 1][0] from the lane below, D[x + 1][2] from the lane above
-      float lo = __uint_as_float(__shfl_up_sync(0xffffffffu, d0[j], 1));
-      float hi = __uint_as_float(__shfl_down_sync(0xffffffffu, d2[j], 1));
-      if (lane == 0) lo = other[j];
-      if (lane == 31) hi = other[NH + j];
-      f[j] = lo + __uint_as_float(d1[j]) + hi;
-    }
-    const long long g = s * N + ((long long)z0 * n + (y0 + erow)) * n + x;
-    if (EPI == 0 || EPI == 1) {
-#pragma unroll
-      for (int j = 0; j < NH; j += 4) {
-        float4 v;
-        v.x = f[j] + bb[j];
-        v.y = f[j + 1] + bb[j + 1];
-        v.z = f[j + 2] + bb[j + 2];
-        v.w = f[j + 3] + bb[j + 3];
-        if (EPI == 1) {
-          const int co = cb + j;
-          v.x = co < nout_valid ? v.x : 0.f;
-          v.y = co + 1 < nout_valid ? v.y : 0.f;
-          v.z = co + 2 < nout_valid ? v.z : 0.f;
-          v.w = co + 3 < nout_valid ? v.w : 0.f;
+      const unsigned long long bd0 = umma_sdesc(cu_smem_u32(sW), NT * 16, 128);
+      int i = 0;
+      for (; i < nb; ++i) {
+        const int buf = i & 1;
+        if (!cu_wait(&hfull[buf], (unsigned)((i >> 1) & 1)) ||
+            (i >= 2 && !cu_wait(&aempty[buf], (unsigned)(((i - 2) >> 1) & 1)))) {
+          fault();
+          break;
         }
-        *reinterpret_cast<float4*>(pre_out + g * NP + cb + j) = v;
-        if (EPI == 0) {
-          __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(gelu_f(v.x)), __float2bfloat16(gelu_f(v.y)));
-          __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(gelu_f(v.z)), __float2bfloat16(gelu_f(v.w)));
-          uint2 pk;
-          pk.x = *reinterpret_cast<unsigned*>(&h0);
-          pk.y = *reinterpret_cast<unsigned*>(&h1);
-          *reinterpret_cast<uint2*>(act_out + g * NP + cb + j) = pk;
-        }
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < NH; j += 4) {
-        const float4 pp = *reinterpret_cast<const float4*>(pre_prev + g * NP + cb + j);
-        __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(f[j] * gelu_grad_f(pp.x)),
-                                               __float2bfloat16(f[j + 1] * gelu_grad_f(pp.y)));
-        __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(f[j + 2] * gelu_grad_f(pp.z)),
-                                               __float2bfloat16(f[j + 3] * gelu_grad_f(pp.w)));
-        uint2 pk;
-        pk.x = *reinterpret_cast<unsigned*>(&h0);
-        pk.y = *reinterpret_cast<unsigned*>(&h1);
-        *reinterpret_cast<uint2*>(act_out + g * NP + cb + j) = pk;
-      }
-    }
-  };
-  // bounded wait for the commit of the i-th block (accumulator set i & 1),
-  // warp-uniform: the tensor-memory loads after it are warp collectives
-  auto wait_mma = [&](long long i) -> bool {
-    const unsigned parity = (unsigned)((i >> 1) & 1);
-    bool ok = false;
-    for (int polls = 0; polls < (1 << 20) && !ok; ++polls) ok = cu_try_wait(&bar[i & 1], parity);
-    return __all_sync(0xffffffffu, ok) != 0;
-  };
-
-  long long i = 0;
-  for (; b < nblk; b += gridDim.x, ++i) {
-    const int buf = (int)(i & 1);
-    cp_async_wait_all();
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // cp.async data -> tensor-core reads
-    tc_fence_before();
-    __syncthreads();
-    if (*s_abort) break;
-    // one lane issues the block's instructions; the rest of its warp waits
-    // at the warp barrier
-    if (warp == 0) {
-      if (lane == 0) {
+        if (*s_abort) break;
         tc_fence_after();
         // the start address (/16) is the descriptor's low field: an operand
         // at a byte offset is the base descriptor plus offset / 16
-        const unsigned long long ad0 = umma_sdesc(cu_smem_u32(sH + buf * HB), CU_PLANE * 16, 128);
-        const unsigned long long bd0 = umma_sdesc(cu_smem_u32(sW), NT * 16, 128);
+        const unsigned long long ad0 = umma_sdesc(cu_smem_u32(sH + buf * HB), CHUNK, 128);
 #pragma unroll
         for (int t = 0; t < 2; ++t)
 #pragma unroll
@@ -685,47 +673,144 @@ conv_umma_kernel(int batch, const __nv_bfloat16* __restrict__ in, const __nv_bfl
 #pragma unroll
             for (int kk = 0; kk < KP / 16; ++kk) {
               const int dy = g / 3, dz = g % 3;
-              const unsigned aoff = (unsigned)((dz * CU_HY + 2 * t + dy) * n + kk * 2 * CU_PLANE);
+              const unsigned aoff = (unsigned)(((dz * KC + 2 * kk) * CHUNK + (2 * t + dy) * cu_row_bytes) >> 4);
               const unsigned boff = (unsigned)((g * KC + kk * 2) * NT);
               umma_bf16(tmem + (unsigned)((buf * 2 + t) * NT), ad0 + aoff, bd0 + boff, IDESC, (g | kk) != 0);
             }
-        umma_commit(&bar[buf]);
+        umma_commit(&hempty[buf]);
+        umma_commit(&afull[buf]);
+      }
+      // products in flight complete (bounded)
+      if (i > 0 && !cu_wait(&afull[(i - 1) & 1], (unsigned)(((i - 1) >> 1) & 1))) fault();
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue ----
+    // sub-partition q (lanes 32q..), tile et (rows 2 et, 2 et + 1), channel
+    // half eh; the partner warp (w ^ 1, sub-partition q ^ 1) holds the other
+    // 32 voxels of the same row
+    const int q = warp & 3, k = (warp - 2) >> 2, et = k & 1, eh = k >> 1;
+    const int erow = 2 * et + (q >> 1), x = 32 * (q & 1) + lane, cb = eh * NH;
+    float bb[NH];
+#pragma unroll
+    for (int j = 0; j < NH; ++j) bb[j] = (EPI == 2) ? 0.f : __ldg(bias + cb + j);
+    for (int i = 0; i < nb; ++i) {
+      const int set = i & 1;
+      if (!__all_sync(0xffffffffu, cu_wait(&afull[set], (unsigned)((i >> 1) & 1)))) {
+        if (lane == 0) fault();
+        break;
+      }
+      if (*s_abort) break;
+      tc_fence_after();
+      const unsigned ta = tmem + ((unsigned)(32 * q) << 16) + (unsigned)((set * 2 + et) * NT + cb);
+      unsigned d0[NH], d1[NH], d2[NH];
+      tmem_ld_nowait<NH>(ta, d0);
+      tmem_ld_nowait<NH>(ta + NP, d1);
+      tmem_ld_nowait<NH>(ta + 2 * NP, d2);
+      tmem_wait_ld();
+      // ends of the 32 voxels go to the partner warp (buffers alternate with
+      // the block; the pair's mbarrier, two arrivals, orders writes and reads)
+      float* const mine = xch + ((i & 1) * CU_EPI_WARPS + (warp - 2)) * 2 * NH;
+      const float* const other = xch + ((i & 1) * CU_EPI_WARPS + ((warp ^ 1) - 2)) * 2 * NH;
+      if (lane == 31) {
+#pragma unroll
+        for (int j = 0; j < NH; ++j) mine[j] = __uint_as_float(d0[j]);
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NH; ++j) mine[NH + j] = __uint_as_float(d2[j]);
       }
       __syncwarp();
+      unsigned long long* const xb = &xbar[((warp - 2) >> 1) * 2 + (i & 1)];
+      if (lane == 0) cu_arrive(xb);
+      if (!__all_sync(0xffffffffu, cu_wait(xb, (unsigned)((i >> 1) & 1)))) {
+        if (lane == 0) fault();
+        break;
+      }
+      float f[NH];
+#pragma unroll
+      for (int j = 0; j < NH; ++j) {
+        // D[x - 1][0] from the lane below, D[x + 1][2] from the lane above
+        float lo = __uint_as_float(__shfl_up_sync(0xffffffffu, d0[j], 1));
+        float hi = __uint_as_float(__shfl_down_sync(0xffffffffu, d2[j], 1));
+        if (lane == 0) lo = other[j];
+        if (lane == 31) hi = other[NH + j];
+        f[j] = lo + __uint_as_float(d1[j]) + hi;
+      }
+      // the accumulator set and this block's exchange buffer are released:
+      // both are rewritten two blocks later, after every warp's release
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) cu_arrive(&aempty[set]);
+      long long s;
+      int z0, y0;
+      origin(blockIdx.x + (long long)i * gridDim.x, s, z0, y0);
+      const long long g = s * N + ((long long)z0 * n + (y0 + erow)) * n + x;
+      if (EPI == 0 || EPI == 1) {
+#pragma unroll
+        for (int j = 0; j < NH; j += 4) {
+          float4 v;
+          v.x = f[j] + bb[j];
+          v.y = f[j + 1] + bb[j + 1];
+          v.z = f[j + 2] + bb[j + 2];
+          v.w = f[j + 3] + bb[j + 3];
+          if (EPI == 1) {
+            const int co = cb + j;
+            v.x = co < nout_valid ? v.x : 0.f;
+            v.y = co + 1 < nout_valid ? v.y : 0.f;
+            v.z = co + 2 < nout_valid ? v.z : 0.f;
+            v.w = co + 3 < nout_valid ? v.w : 0.f;
+          }
+          *reinterpret_cast<float4*>(pre_out + g * NP + cb + j) = v;
+          if (EPI == 0) {
+            __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(gelu_f(v.x)), __float2bfloat16(gelu_f(v.y)));
+            __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(gelu_f(v.z)), __float2bfloat16(gelu_f(v.w)));
+            uint2 pk;
+            pk.x = *reinterpret_cast<unsigned*>(&h0);
+            pk.y = *reinterpret_cast<unsigned*>(&h1);
+            *reinterpret_cast<uint2*>(act_out + g * NP + cb + j) = pk;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < NH; j += 4) {
+          const float4 pp = *reinterpret_cast<const float4*>(pre_prev + g * NP + cb + j);
+          __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(f[j] * gelu_grad_f(pp.x)),
+                                                 __float2bfloat16(f[j + 1] * gelu_grad_f(pp.y)));
+          __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(f[j + 2] * gelu_grad_f(pp.z)),
+                                                 __float2bfloat16(f[j + 3] * gelu_grad_f(pp.w)));
+          uint2 pk;
+          pk.x = *reinterpret_cast<unsigned*>(&h0);
+          pk.y = *reinterpret_cast<unsigned*>(&h1);
+          *reinterpret_cast<uint2*>(act_out + g * NP + cb + j) = pk;
+        }
+      }
     }
-    const bool ok = i == 0 || wait_mma(i - 1);
-    // the other halo buffer is free once block i-1's MMAs are complete: its
-    // refill flies during the epilogue
-    if (b + gridDim.x < nblk) load_block(b + gridDim.x, buf ^ 1);
-    cp_async_commit();
-    if (!ok) {
-      if (lane == 0) atomicExch(&g_learned_fault, 1);
-      *s_abort = 1;
-    } else if (i > 0) {
-      tc_fence_after();
-      epilogue(b - gridDim.x, buf ^ 1);
-    }
-    tc_fence_before();
   }
-  __syncthreads();
-  const bool aborted = *s_abort != 0;
-  if (i > 0) {
-    // the last block's MMAs (after an abort: let them finish, bounded)
-    const bool ok = wait_mma(i - 1);
-    if (ok && !aborted) {
-      tc_fence_after();
-      epilogue(b - gridDim.x, (int)((i - 1) & 1));
-    } else if (!ok && lane == 0) {
-      atomicExch(&g_learned_fault, 1);
-    }
-  }
-  cp_async_wait_all();
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
   }
+}
+
+// Tiled tensor map encoder (defined with the RHS sweep).
+bool encode_tiled_map(CUtensorMap* map, CUtensorMapDataType dt, unsigned rank, const void* base,
+                      const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box);
+
+// The maps of a [batch][64^3][32] BF16 tensor; false when they cannot be made.
+static bool halo_maps(const __nv_bfloat16* in, int batch, HaloMaps* m) {
+  if ((reinterpret_cast<uintptr_t>(in) & 15) != 0) return false;
+  const cuuint64_t dims[3] = {8, (cuuint64_t)CU_N, (cuuint64_t)batch * CU_N * CU_N};
+  const cuuint64_t strides[2] = {(cuuint64_t)CU_KP * 2, (cuuint64_t)CU_N * CU_KP * 2};
+  const cuuint32_t box6[3] = {8, (cuuint32_t)CU_N, (cuuint32_t)CU_HY}, box1[3] = {8, (cuuint32_t)CU_N, 1};
+  for (int c = 0; c < CU_KC; ++c) {
+    if (!encode_tiled_map(&m->rows6[c], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, in + c * 8, dims, strides, box6) ||
+        !encode_tiled_map(&m->row1[c], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, in + c * 8, dims, strides, box1))
+      return false;
+  }
+  return true;
 }
 
 // Engine 0: the tcgen05 kernel on 64^3 grids for 32 input channels (with 16
@@ -736,14 +821,18 @@ template <int KP, int NP, int EPI>
 static void conv_launch(int engine, long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* W,
                         const float* bias, float* pre_out, __nv_bfloat16* act_out, const float* pre_prev,
                         int nout_valid, cudaStream_t st) {
-  if constexpr (KP == 32) {
+  if constexpr (KP == CU_KP) {
     if (engine == 0 && n == CU_N) {
       const long long N = (long long)n * n * n;
-      const long long nblk = (V / N) * n * (n / CU_ROWS);
-      const long long ctas = std::min<long long>(nblk, 152);
-      conv_umma_kernel<KP, NP, EPI><<<(unsigned)ctas, CU_THREADS, conv_umma_smem<KP, NP>(), st>>>(
-          (int)(V / N), in, W, bias, pre_out, act_out, pre_prev, nout_valid);
-      return;
+      const int batch = (int)(V / N);
+      HaloMaps maps;
+      if (halo_maps(in, batch, &maps)) {
+        const long long nblk = (long long)batch * n * (n / CU_ROWS);
+        const long long ctas = std::min<long long>(nblk, 152);
+        conv_umma_kernel<NP, EPI><<<(unsigned)ctas, CU_THREADS, conv_umma_smem<NP>(), st>>>(
+            batch, maps, W, bias, pre_out, act_out, pre_prev, nout_valid);
+        return;
+      }
     }
   }
   if (n % 8 == 0) {
@@ -1376,10 +1465,10 @@ static cudaError_t conv_res_attr() {
   return cudaFuncSetAttribute(conv_res_kernel<KP, NP, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)conv_res_smem<KP, NP>());
 }
-template <int KP, int NP, int EPI>
+template <int NP, int EPI>
 static cudaError_t conv_umma_attr() {
-  return cudaFuncSetAttribute(conv_umma_kernel<KP, NP, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)conv_umma_smem<KP, NP>());
+  return cudaFuncSetAttribute(conv_umma_kernel<NP, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)conv_umma_smem<NP>());
 }
 template <int KP, int NP>
 static cudaError_t wgrad_tile_attr() {
@@ -1404,9 +1493,9 @@ static int configure_learned() {
   if (e == cudaSuccess) e = conv_res_attr<32, 16, 1>();
   if (e == cudaSuccess) e = conv_res_attr<16, 32, 2>();
   if (e == cudaSuccess) e = conv_res_attr<32, 32, 2>();
-  if (e == cudaSuccess) e = conv_umma_attr<32, 32, 0>();
-  if (e == cudaSuccess) e = conv_umma_attr<32, 16, 1>();
-  if (e == cudaSuccess) e = conv_umma_attr<32, 32, 2>();
+  if (e == cudaSuccess) e = conv_umma_attr<32, 0>();
+  if (e == cudaSuccess) e = conv_umma_attr<16, 1>();
+  if (e == cudaSuccess) e = conv_umma_attr<32, 2>();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   done[dev] = true;
   return EXC_OK;

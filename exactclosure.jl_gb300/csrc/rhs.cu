@@ -665,6 +665,19 @@ static TensorMapEncodeTiled tensor_map_encoder() {
   return fn;
 }
 
+// Tiled tensor map, no interleave or swizzle, 128-byte L2 promotion, zero
+// fill; false when the encoder is unavailable or rejects the arguments.
+bool encode_tiled_map(CUtensorMap* map, CUtensorMapDataType dt, unsigned rank, const void* base,
+                      const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box) {
+  std::memset(map, 0, sizeof(*map));
+  TensorMapEncodeTiled enc = tensor_map_encoder();
+  if (!enc) return false;
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return enc(map, dt, rank, const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Tensor map of the vector fields of nslots solves as one 3-D tensor
 // (x, y, (slot * 3 + component) * n + z) with boxes of bx x by x 1 words;
 // false when it cannot be made (the sweep then copies with cp.async).

@@ -31,7 +31,7 @@ int configure_device() {
 
 static int check_grid(int precision, int n, double l) {
   if (precision != EXC_F64 && precision != EXC_F32) { set_last_error("precision must be EXC_F64 or EXC_F32"); return EXC_ERR_ARG; }
-  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
   if (!(l > 0)) { set_last_error("domain size must be positive"); return EXC_ERR_ARG; }
   return configure_device();
 }

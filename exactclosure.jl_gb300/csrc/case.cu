@@ -734,14 +734,14 @@ extern "C" {
 int exc_case_create(const exc_case_desc* desc, void* stream, exc_case** out) {
   if (!desc || !out) { set_last_error("null argument"); return EXC_ERR_ARG; }
   *out = nullptr;
-  if (!fft_size_ok(desc->n)) { set_last_error("DNS grid size must be 2^a 3^b 5^c, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!fft_size_ok(desc->n)) { set_last_error("DNS grid size must be 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
   if (desc->precision != EXC_F64 && desc->precision != EXC_F32) { set_last_error("bad precision"); return EXC_ERR_ARG; }
   if (!(desc->l > 0) || !(desc->visc > 0) || !(desc->cfl > 0)) { set_last_error("l, visc and cfl must be positive"); return EXC_ERR_ARG; }
   if (desc->nles < 0 || desc->nles > EXC_MAX_LES) { set_last_error("nles out of range"); return EXC_ERR_ARG; }
   for (int i = 0; i < desc->nles; ++i) {
     int c = desc->les[i].ratio;
     if (c < 1 || desc->n % c != 0) { set_last_error("LES ratio must divide n"); return EXC_ERR_RATIO; }
-    if (!fft_size_ok(desc->n / c)) { set_last_error("LES grid size n/ratio must be 2^a 3^b 5^c, a >= 1, >= 4"); return EXC_ERR_RATIO; }
+    if (!fft_size_ok(desc->n / c)) { set_last_error("LES grid size n/ratio must be 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, >= 4"); return EXC_ERR_RATIO; }
     if (desc->les[i].kind != EXC_FILTER_VOLUME && desc->les[i].kind != EXC_FILTER_FACE) { set_last_error("bad filter kind"); return EXC_ERR_ARG; }
   }
   exc_case* cs = new exc_case();

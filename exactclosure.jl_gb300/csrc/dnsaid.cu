@@ -204,7 +204,7 @@ int exc_dnsaid_create(const exc_dnsaid_desc* desc, void* stream, exc_dnsaid** ou
   if (!desc || !out) { set_last_error("null argument"); return EXC_ERR_ARG; }
   *out = nullptr;
   const int n = desc->n, c = desc->ratio;
-  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
   if (c < 1 || n % c || c % 2 == 0) { set_last_error("ratio must be odd and divide n (classic closure)"); return EXC_ERR_RATIO; }
   if (!fft_size_ok(n / c)) { set_last_error("LES grid n/ratio must be an FFT size"); return EXC_ERR_SHAPE; }
   if (!(desc->l > 0) || !(desc->visc > 0)) { set_last_error("l and visc must be positive"); return EXC_ERR_ARG; }

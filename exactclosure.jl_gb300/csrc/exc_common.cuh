@@ -97,13 +97,15 @@ struct SlotBatch {
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-// Grid sizes the FFT supports: n = 2^a 3^b 5^c with a >= 1, 4 <= n <= 1024.
+// Grid sizes the FFT supports: n = 2^a 3^b 5^c 7^d 11^e 13^f 17^g with a >= 1,
+// 4 <= n <= 1024.
 inline bool fft_size_ok(int n) {
   if (n < 4 || n > 1024 || (n & 1)) return false;
   int m = n;
   while (m % 2 == 0) m /= 2;
   while (m % 3 == 0) m /= 3;
-  while (m % 5 == 0) m /= 5;
+  for (int f : {5, 7, 11, 13, 17})
+    while (m % f == 0) m /= f;
   return m == 1;
 }
 

@@ -14,7 +14,7 @@ namespace exc {
 //   X_k = (Z_k + conj Z_{n/2-k})/2 - (i/2) W_n^k (Z_k - conj Z_{n/2-k}).
 // With DIV the input line is d = div(u) (src/N.jl:222-238) computed on the fly.
 // ---------------------------------------------------------------------------
-template <typename T, bool DIV>
+template <typename T, bool DIV, bool EXT = false>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ out, int P,
              const cplx<T>* __restrict__ tw, FftPlan plan, int rows_per_cta, SlotBatch sb) {
@@ -57,7 +57,7 @@ r2c_x_kernel(const T* __restrict__ src, int n, T inv_h, cplx<T>* __restrict__ ou
     s[r * ls + pe(m)] = mk<T>(a, b);
   }
   __syncthreads();
-  fft_lines<false>(s, ls, rows, plan, tw, n);
+  fft_lines<false, EXT>(s, ls, rows, plan, tw, n);
   // untangle and store k = 0..N2
   for (int t = threadIdx.x; t < rows * (N2 + 1); t += blockDim.x) {
     const int r = (int)fast_div((unsigned)t, plan.rL1), k = t - r * (N2 + 1);
@@ -109,7 +109,7 @@ __device__ __forceinline__ ColTiles col_tiles(int n, int nkx, int W, long long o
 // Shared memory: two buffers of W lines of stride n + 1.  A CTA takes the
 // tiles blockIdx.x and blockIdx.x + gridDim.x; the second tile's copies are
 // in flight while the first is transformed.
-template <typename T, bool INV>
+template <typename T, bool INV, bool EXT = false>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_stride,
             long long outer_stride, const cplx<T>* __restrict__ tw, FftPlan plan, SlotBatch sb) {
@@ -130,12 +130,12 @@ cols_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, long long elem_strid
   cp_commit();
   cp_wait<1>();
   __syncthreads();
-  fft_lines<INV>(buf0, ls, ct.lines(a), plan, tw, n);
+  fft_lines<INV, EXT>(buf0, ls, ct.lines(a), plan, tw, n);
   tile_move<false>(buf0, ls, g + ct.offset(a), elem_stride, ct.lines(a), W, ct.wlog, n);
   if (!two) return;
   cp_wait<0>();
   __syncthreads();
-  fft_lines<INV>(buf1, ls, ct.lines(b), plan, tw, n);
+  fft_lines<INV, EXT>(buf1, ls, ct.lines(b), plan, tw, n);
   tile_move<false>(buf1, ls, g + ct.offset(b), elem_stride, ct.lines(b), W, ct.wlog, n);
 }
 
@@ -157,13 +157,13 @@ __device__ __forceinline__ double recip_f64(double d) {
 // divide is computed in float64 for every precision.
 // ---------------------------------------------------------------------------
 // z forward transform, divide and inverse of one tile in shared memory.
-template <typename T>
+template <typename T, bool EXT>
 __device__ __forceinline__ void zsolve_tile(cplx<T>* s, int ls, int lines, int wlog, int n, int nkx, int kx0, int ky,
                                             const cplx<T>* __restrict__ tw, const FftPlan& plan,
                                             const double* __restrict__ sin2, double coef,
                                             const double* __restrict__ invlap) {
   using C = cplx<T>;
-  fft_lines<false>(s, ls, lines, plan, tw, n);
+  fft_lines<false, EXT>(s, ls, lines, plan, tw, n);
   const double sy = sin2[ky];
   const bool pow2 = lines == (1 << wlog);
   for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
@@ -193,11 +193,11 @@ __device__ __forceinline__ void zsolve_tile(cplx<T>* s, int ls, int lines, int w
     s[l * ls + pe(kz)] = v;
   }
   __syncthreads();
-  fft_lines<true>(s, ls, lines, plan, tw, n);
+  fft_lines<true, EXT>(s, ls, lines, plan, tw, n);
 }
 
 // Two tiles per CTA, as in cols_kernel.
-template <typename T>
+template <typename T, bool EXT = false>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<T>* __restrict__ tw,
               FftPlan plan, const double* __restrict__ sin2, double coef, const double* __restrict__ invlap,
@@ -222,14 +222,14 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
   __syncthreads();
   {
     const int ky = a / ct.ntx;
-    zsolve_tile<T>(buf0, ls, ct.lines(a), ct.wlog, n, nkx, (a - ky * ct.ntx) * W, ky, tw, plan, sin2, coef, invlap);
+    zsolve_tile<T, EXT>(buf0, ls, ct.lines(a), ct.wlog, n, nkx, (a - ky * ct.ntx) * W, ky, tw, plan, sin2, coef, invlap);
     tile_move<false>(buf0, ls, g + ct.offset(a), es, ct.lines(a), W, ct.wlog, n);
   }
   if (!two) return;
   cp_wait<0>();
   __syncthreads();
   const int ky = b / ct.ntx;
-  zsolve_tile<T>(buf1, ls, ct.lines(b), ct.wlog, n, nkx, (b - ky * ct.ntx) * W, ky, tw, plan, sin2, coef, invlap);
+  zsolve_tile<T, EXT>(buf1, ls, ct.lines(b), ct.wlog, n, nkx, (b - ky * ct.ntx) * W, ky, tw, plan, sin2, coef, invlap);
   tile_move<false>(buf1, ls, g + ct.offset(b), es, ct.lines(b), W, ct.wlog, n);
 }
 
@@ -238,7 +238,7 @@ zsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int W, int P, const cplx<
 //   Z_k = (X_k + conj X_{N2-k}) + i W_n^-k (X_k - conj X_{N2-k}),
 //   z = IDFT_{N2}(Z) (unnormalised), x_2m = Re z_m, x_2m+1 = Im z_m.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, bool EXT = false>
 __global__ void __launch_bounds__(fft_threads<cplx<T>>(), 3)
 c2r_x_kernel(cplx<T>* __restrict__ g, int n, int P, const cplx<T>* __restrict__ tw, FftPlan plan,
              int rows_per_cta, SlotBatch sb) {
@@ -276,7 +276,7 @@ c2r_x_kernel(cplx<T>* __restrict__ g, int n, int P, const cplx<T>* __restrict__ 
     if (k2 < N2 && k2 != k) s[r * ls + pe(k2)] = zb;
   }
   __syncthreads();
-  fft_lines<true>(s, ls, rows, plan, tw, n);
+  fft_lines<true, EXT>(s, ls, rows, plan, tw, n);
   T* gr = reinterpret_cast<T*>(g);
   for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
     const int r = (int)fast_div((unsigned)t, plan.rL), m = t - r * N2;
@@ -349,12 +349,14 @@ static void geometry(const exc_poisson* ps, int& W, int& rows) {
   if (rows > nn) rows = (int)nn;
 }
 
-template <typename T>
-cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st,
+// Stockham passes with radix 7/11/13/17 are separate kernel instantiations
+// (EXT): their larger butterflies would otherwise cost every size registers.
+static bool plan_ext(const FftPlan& p) { return p.n7 || p.n11 || p.n13 || p.n17; }
+
+template <typename T, bool EXT>
+static cudaError_t stockham_solve(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st,
                                   const SlotBatch& sb, int nslots) {
   using C = cplx<T>;
-  if (ps->engine == 0 && ps->twl_n && ps->twl_h && ps->invlap)
-    return fftreg_solve(ps, src, src_is_vector, st, sb, nslots);
   const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
   C* g = reinterpret_cast<C*>(ps->work);
   const C* tw = reinterpret_cast<const C*>(ps->tw);
@@ -365,28 +367,38 @@ cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vec
   size_t shx = (size_t)rows * padded_len(N2) * sizeof(C);
   dim3 gx((unsigned)((nn + rows - 1) / rows), nslots);
   if (src_is_vector)
-    r2c_x_kernel<T, true><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)(1.0 / ps->h), g, P, tw, ps->plan_h, rows, sb);
+    r2c_x_kernel<T, true, EXT><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)(1.0 / ps->h), g, P, tw, ps->plan_h, rows, sb);
   else
-    r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows, sb);
+    r2c_x_kernel<T, false, EXT><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows, sb);
   // y forward
   const long long ntiles = (long long)((nkx + W - 1) / W) * n;
   size_t shc = 2 * (size_t)W * padded_len(n) * sizeof(C);
   dim3 gc(column_ctas(ntiles), 1, nslots);
-  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, sb);
+  cols_kernel<T, false, EXT><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, sb);
   // z forward + divide + inverse; coef = 1/(lambda N) numerator: -h^2/(4 N)
   double coef = -ps->h * ps->h / (4.0 * (double)n * (double)n * (double)n);
-  zsolve_kernel<T><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef, ps->invlap, sb);
+  zsolve_kernel<T, EXT><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, tw, ps->plan_n, ps->sin2, coef, ps->invlap, sb);
   // y inverse
-  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, sb);
+  cols_kernel<T, true, EXT><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, sb);
   // x inverse (in place)
-  c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows, sb);
+  c2r_x_kernel<T, EXT><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows, sb);
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st,
+                                  const SlotBatch& sb, int nslots) {
+  if (ps->engine == 0 && ps->twl_n && ps->twl_h && ps->invlap)
+    return fftreg_solve(ps, src, src_is_vector, st, sb, nslots);
+  if (plan_ext(ps->plan_n) || plan_ext(ps->plan_h))
+    return stockham_solve<T, true>(ps, src, src_is_vector, st, sb, nslots);
+  return stockham_solve<T, false>(ps, src, src_is_vector, st, sb, nslots);
 }
 
 // Plain 3-D real transforms on the work array (no divide): forward leaves the
 // half spectrum [n][n][P]; inverse (unnormalised) leaves reals at pitch 2P.
-template <typename T>
-cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st) {
+template <typename T, bool EXT>
+static cudaError_t fft3d_forward_t(exc_poisson* ps, const T* src, cudaStream_t st) {
   using C = cplx<T>;
   const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
   C* g = reinterpret_cast<C*>(ps->work);
@@ -397,34 +409,46 @@ cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st) {
   const SlotBatch one;
   size_t shx = (size_t)rows * padded_len(N2) * sizeof(C);
   int gx = (int)((nn + rows - 1) / rows);
-  r2c_x_kernel<T, false><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows, one);
+  r2c_x_kernel<T, false, EXT><<<gx, fft_threads<C>(), shx, st>>>(src, n, (T)1, g, P, tw, ps->plan_h, rows, one);
   const long long ntiles = (long long)((nkx + W - 1) / W) * n;
   size_t shc = 2 * (size_t)W * padded_len(n) * sizeof(C);
   dim3 gc(column_ctas(ntiles));
-  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, one);
-  cols_kernel<T, false><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n, one);
+  cols_kernel<T, false, EXT><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, one);
+  cols_kernel<T, false, EXT><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n, one);
+  return cudaGetLastError();
+}
+
+template <typename T, bool EXT>
+static cudaError_t fft3d_inverse_t(exc_poisson* ps, cudaStream_t st) {
+  using C = cplx<T>;
+  const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
+  C* g = reinterpret_cast<C*>(ps->work);
+  const C* tw = reinterpret_cast<const C*>(ps->tw);
+  const long long nn = (long long)n * n;
+  int W, rows;
+  geometry<C>(ps, W, rows);
+  const SlotBatch one;
+  const long long ntiles = (long long)((nkx + W - 1) / W) * n;
+  size_t shc = 2 * (size_t)W * padded_len(n) * sizeof(C);
+  dim3 gc(column_ctas(ntiles));
+  cols_kernel<T, true, EXT><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n, one);
+  cols_kernel<T, true, EXT><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, one);
+  size_t shx = (size_t)rows * padded_len(N2) * sizeof(C);
+  int gx = (int)((nn + rows - 1) / rows);
+  c2r_x_kernel<T, EXT><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows, one);
   return cudaGetLastError();
 }
 
 template <typename T>
+cudaError_t fft3d_forward(exc_poisson* ps, const T* src, cudaStream_t st) {
+  return plan_ext(ps->plan_n) || plan_ext(ps->plan_h) ? fft3d_forward_t<T, true>(ps, src, st)
+                                                      : fft3d_forward_t<T, false>(ps, src, st);
+}
+
+template <typename T>
 cudaError_t fft3d_inverse(exc_poisson* ps, cudaStream_t st) {
-  using C = cplx<T>;
-  const int n = ps->n, P = ps->P, N2 = n / 2, nkx = N2 + 1;
-  C* g = reinterpret_cast<C*>(ps->work);
-  const C* tw = reinterpret_cast<const C*>(ps->tw);
-  const long long nn = (long long)n * n;
-  int W, rows;
-  geometry<C>(ps, W, rows);
-  const SlotBatch one;
-  const long long ntiles = (long long)((nkx + W - 1) / W) * n;
-  size_t shc = 2 * (size_t)W * padded_len(n) * sizeof(C);
-  dim3 gc(column_ctas(ntiles));
-  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, (long long)n * P, P, tw, ps->plan_n, one);
-  cols_kernel<T, true><<<gc, fft_threads<C>(), shc, st>>>(g, n, nkx, W, P, (long long)n * P, tw, ps->plan_n, one);
-  size_t shx = (size_t)rows * padded_len(N2) * sizeof(C);
-  int gx = (int)((nn + rows - 1) / rows);
-  c2r_x_kernel<T><<<gx, fft_threads<C>(), shx, st>>>(g, n, P, tw, ps->plan_h, rows, one);
-  return cudaGetLastError();
+  return plan_ext(ps->plan_n) || plan_ext(ps->plan_h) ? fft3d_inverse_t<T, true>(ps, st)
+                                                      : fft3d_inverse_t<T, false>(ps, st);
 }
 
 template cudaError_t fft3d_forward<double>(exc_poisson*, const double*, cudaStream_t);
@@ -447,24 +471,26 @@ template cudaError_t poisson_solve_inplace<float>(exc_poisson*, const float*, bo
 template cudaError_t copy_pressure<double>(const exc_poisson*, double*, cudaStream_t);
 template cudaError_t copy_pressure<float>(const exc_poisson*, float*, cudaStream_t);
 
-template <typename T>
+template <typename T, bool EXT>
 static cudaError_t configure_fft_t() {
   using C = cplx<T>;
   // a tile of fft_tile elements in padded lines: at most 9/8 of it plus a slot per line
   int maxsh = (int)(fft_tile<C>() * 9 / 8 + 1024) * (int)sizeof(C);
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(cols_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(cols_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(zsolve_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(c2r_x_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, true, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(r2c_x_kernel<T, false, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(cols_kernel<T, false, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(cols_kernel<T, true, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(zsolve_kernel<T, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * maxsh)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(c2r_x_kernel<T, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsh)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 
 cudaError_t configure_fft() {
-  cudaError_t e = configure_fft_t<double>();
-  if (e == cudaSuccess) e = configure_fft_t<float>();
+  cudaError_t e = configure_fft_t<double, false>();
+  if (e == cudaSuccess) e = configure_fft_t<float, false>();
+  if (e == cudaSuccess) e = configure_fft_t<double, true>();
+  if (e == cudaSuccess) e = configure_fft_t<float, true>();
   if (e == cudaSuccess) e = configure_fftreg_f64();
   if (e == cudaSuccess) e = configure_fftreg_f32();
   return e;
@@ -504,7 +530,7 @@ static int alloc_level_tables(exc_poisson* ps) {
 }
 
 int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
-  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
   if (!(l > 0)) { set_last_error("domain size must be positive"); return EXC_ERR_ARG; }
   if (precision != EXC_F64 && precision != EXC_F32) { set_last_error("bad precision"); return EXC_ERR_ARG; }
   ps->precision = precision;

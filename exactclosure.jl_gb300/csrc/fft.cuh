@@ -1,4 +1,5 @@
-// Batched radix-2/3/4/8 Stockham FFTs over lines held in shared memory.
+// Batched radix-2/3/4/5/8 (and prime radix 7/11/13/17) Stockham FFTs over lines
+// held in shared memory.
 //
 // Replaces the CUFFT/FFTW real-to-complex plan of the reference's Poisson
 // solver (`poissonsolver`/`project!`, src/N.jl:202-307).  A CTA holds
@@ -23,8 +24,8 @@ template <typename C> constexpr int fft_tile() { return 32768 / (int)sizeof(C); 
 __host__ __device__ __forceinline__ int pe(int e) { return e + (e >> 3); }
 __host__ __device__ __forceinline__ int padded_len(int L) { return L + (L >> 3) + 1; }
 // Pass sequence of a length-L transform: n8 radix-8 passes, then at most one
-// radix-4 or radix-2 pass, then n3 radix-3 and n5 radix-5 passes
-// (L = 8^n8 4^n4 2^n2 3^n3 5^n5).
+// radix-4 or radix-2 pass, then the radix-3, 5, 7, 11, 13 and 17 passes
+// (L = 8^n8 4^n4 2^n2 3^n3 5^n5 7^n7 11^n11 13^n13 17^n17).
 // The pass index math divides by nb = L/R and by Ns (the product of the
 // earlier radices); both divisions use multiply-high reciprocals
 // ceil(2^32/d), exact for every quotient here (dividends < 2^17, d <= 2^11;
@@ -32,7 +33,7 @@ __host__ __device__ __forceinline__ int padded_len(int L) { return L + (L >> 3) 
 constexpr int FFT_MAX_PASSES = 12;
 struct FftPlan {
   int L;
-  int n8, n4, n2, n3, n5;
+  int n8, n4, n2, n3, n5, n7, n11, n13, n17;
   unsigned rnb[FFT_MAX_PASSES], rns[FFT_MAX_PASSES];
   unsigned rL, rL1, rhalf, r2L;  // reciprocals of L, L + 1, L/2 + 1, 2L (row splits of the x passes)
 };
@@ -43,21 +44,33 @@ __device__ __forceinline__ unsigned fast_div(unsigned x, unsigned r) { return r 
 inline FftPlan make_plan(int L) {
   FftPlan p{};
   p.L = L;
-  int m = L, a = 0, b = 0, c5 = 0;
+  int m = L, a = 0, b = 0, c5 = 0, c7 = 0, c11 = 0, c13 = 0, c17 = 0;
   while (m % 2 == 0) { m /= 2; ++a; }
   while (m % 3 == 0) { m /= 3; ++b; }
   while (m % 5 == 0) { m /= 5; ++c5; }
+  while (m % 7 == 0) { m /= 7; ++c7; }
+  while (m % 11 == 0) { m /= 11; ++c11; }
+  while (m % 13 == 0) { m /= 13; ++c13; }
+  while (m % 17 == 0) { m /= 17; ++c17; }
   p.n8 = a / 3;
   p.n4 = (a % 3) == 2;
   p.n2 = (a % 3) == 1;
   p.n3 = b;
   p.n5 = c5;
+  p.n7 = c7;
+  p.n11 = c11;
+  p.n13 = c13;
+  p.n17 = c17;
   int radix[FFT_MAX_PASSES], np = 0;
   for (int q = 0; q < p.n8; ++q) radix[np++] = 8;
   if (p.n4) radix[np++] = 4;
   if (p.n2) radix[np++] = 2;
   for (int q = 0; q < p.n3; ++q) radix[np++] = 3;
   for (int q = 0; q < p.n5; ++q) radix[np++] = 5;
+  for (int q = 0; q < p.n7; ++q) radix[np++] = 7;
+  for (int q = 0; q < p.n11; ++q) radix[np++] = 11;
+  for (int q = 0; q < p.n13; ++q) radix[np++] = 13;
+  for (int q = 0; q < p.n17; ++q) radix[np++] = 17;
   int Ns = 1;
   for (int q = 0; q < np; ++q) {
     p.rnb[q] = fast_recip((unsigned)(L / radix[q]));
@@ -69,6 +82,67 @@ inline FftPlan make_plan(int L) {
   p.rhalf = fast_recip((unsigned)(L / 2 + 1));
   p.r2L = fast_recip((unsigned)(2 * L));
   return p;
+}
+
+// ---------------------------------------------------------------------------
+// Compile-time roots of unity: cos and sin of 2 pi j / R by octant reduction
+// and Taylor series on [0, pi/4] (terms to x^23: below 1e-17 there).
+// ---------------------------------------------------------------------------
+constexpr double kPiD = 3.14159265358979323846;
+constexpr double taylor_sin(double x) {
+  double x2 = x * x, term = x, sum = x;
+  for (int k = 1; k < 12; ++k) {
+    term *= -x2 / (double)((2 * k) * (2 * k + 1));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double taylor_cos(double x) {
+  double x2 = x * x, term = 1.0, sum = 1.0;
+  for (int k = 1; k < 12; ++k) {
+    term *= -x2 / (double)((2 * k - 1) * (2 * k));
+    sum += term;
+  }
+  return sum;
+}
+struct CosSin { double c, s; };
+// angle 2 pi j / R = q pi/4 + theta, q the octant
+constexpr CosSin cos_sin_2pi(int j, int R) {
+  j %= R;
+  if (j < 0) j += R;
+  const int q = (8 * j) / R, r = 8 * j - q * R;
+  if (q % 2 == 0) {
+    const double t = kPiD * r / (4.0 * R);
+    const double c = taylor_cos(t), s = taylor_sin(t);
+    switch ((q / 2) & 3) {
+      case 0: return {c, s};
+      case 1: return {-s, c};
+      case 2: return {-c, -s};
+      default: return {s, -c};
+    }
+  }
+  // odd octant: angle = p pi/2 - phi, p = (q + 1)/2, phi = pi/4 - theta
+  const double f = kPiD * (R - r) / (4.0 * R);
+  const double c = taylor_cos(f), s = taylor_sin(f);
+  switch (((q + 1) / 2) & 3) {
+    case 0: return {c, -s};
+    case 1: return {s, c};
+    case 2: return {-c, s};
+    default: return {-s, -c};
+  }
+}
+
+// cos and sin of 2 pi m / R for m < R, for indexing with unrolled loop
+// counters (folded to immediates).
+template <int R> struct RootTable { double c[R], s[R]; };
+template <int R> constexpr RootTable<R> root_table() {
+  RootTable<R> t{};
+  for (int m = 0; m < R; ++m) {
+    const CosSin w = cos_sin_2pi(m, R);
+    t.c[m] = w.c;
+    t.s[m] = w.s;
+  }
+  return t;
 }
 
 // In-register DFT of size R (forward: exp(-2 pi i qr/R); INV: conjugate).
@@ -135,6 +209,40 @@ template <int R, bool INV, typename C> __device__ __forceinline__ void dft_small
     dft_small<4, INV, C>(b);
 #pragma unroll
     for (int k = 0; k < 4; ++k) { v[2 * k] = a[k]; v[2 * k + 1] = b[k]; }
+  } else {
+    // odd prime R >= 7 by pairs (j, R - j): with t_j = v_j + v_{R-j} and
+    // d_j = v_j - v_{R-j}, X_k = a_k - i b_k and X_{R-k} = a_k + i b_k
+    // (forward), a_k = v_0 + sum_j cos(2 pi jk/R) t_j, b_k = sum_j sin(2 pi jk/R) d_j
+    static_assert(R % 2 == 1 && R >= 7, "radix");
+    constexpr int H = (R - 1) / 2;
+    constexpr RootTable<R> rt = root_table<R>();
+    C t[H], d[H];
+    C x0 = v[0];
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+      t[j - 1] = cadd(v[j], v[R - j]);
+      d[j - 1] = csub(v[j], v[R - j]);
+      x0 = cadd(x0, t[j - 1]);
+    }
+    const C v0 = v[0];
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+      C a = v0, b;
+      b.x = (T)0;
+      b.y = (T)0;
+#pragma unroll
+      for (int j = 1; j <= H; ++j) {
+        const T c = (T)rt.c[(j * k) % R], sn = (T)rt.s[(j * k) % R];
+        a.x = fma(c, t[j - 1].x, a.x);
+        a.y = fma(c, t[j - 1].y, a.y);
+        b.x = fma(sn, d[j - 1].x, b.x);
+        b.y = fma(sn, d[j - 1].y, b.y);
+      }
+      const C ib = mul_mi<INV>(b);
+      v[k] = cadd(a, ib);
+      v[R - k] = csub(a, ib);
+    }
+    v[0] = x0;
   }
 }
 
@@ -264,7 +372,7 @@ __device__ __forceinline__ void tile_load_async(C* s, int ls, const C* base, lon
 
 // Full transform of every line in the tile (natural-order in and out).  One
 // loop per radix keeps each pass body's registers separate.
-template <bool INV, typename C>
+template <bool INV, bool EXT, typename C>
 __device__ void fft_lines(C* s, int ls, int nlines, const FftPlan& plan,
                           const C* __restrict__ tw, int n) {
   int Ns = 1, p = 0;
@@ -274,6 +382,11 @@ __device__ void fft_lines(C* s, int ls, int nlines, const FftPlan& plan,
   if (plan.n2) { fft_pass<2, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 2; ++p; }
   for (int q = 0; q < plan.n3; ++q, ++p) { fft_pass<3, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 3; }
   for (int q = 0; q < plan.n5; ++q, ++p) { fft_pass<5, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 5; }
+  if constexpr (!EXT) return;
+  for (int q = 0; q < plan.n7; ++q, ++p) { fft_pass<7, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 7; }
+  for (int q = 0; q < plan.n11; ++q, ++p) { fft_pass<11, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 11; }
+  for (int q = 0; q < plan.n13; ++q, ++p) { fft_pass<13, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 13; }
+  for (int q = 0; q < plan.n17; ++q, ++p) { fft_pass<17, INV>(s, ls, nlines, L, Ns, plan.rnb[p], plan.rns[p], tw, n); Ns *= 17; }
 }
 
 }  // namespace exc

@@ -24,54 +24,6 @@
 
 namespace exc {
 
-// ---------------------------------------------------------------------------
-// Compile-time roots of unity: cos and sin of 2 pi j / R by octant reduction
-// and Taylor series on [0, pi/4] (terms to x^23: below 1e-17 there).
-// ---------------------------------------------------------------------------
-constexpr double kPiD = 3.14159265358979323846;
-constexpr double taylor_sin(double x) {
-  double x2 = x * x, term = x, sum = x;
-  for (int k = 1; k < 12; ++k) {
-    term *= -x2 / (double)((2 * k) * (2 * k + 1));
-    sum += term;
-  }
-  return sum;
-}
-constexpr double taylor_cos(double x) {
-  double x2 = x * x, term = 1.0, sum = 1.0;
-  for (int k = 1; k < 12; ++k) {
-    term *= -x2 / (double)((2 * k - 1) * (2 * k));
-    sum += term;
-  }
-  return sum;
-}
-struct CosSin { double c, s; };
-// angle 2 pi j / R = q pi/4 + theta, q the octant
-constexpr CosSin cos_sin_2pi(int j, int R) {
-  j %= R;
-  if (j < 0) j += R;
-  const int q = (8 * j) / R, r = 8 * j - q * R;
-  if (q % 2 == 0) {
-    const double t = kPiD * r / (4.0 * R);
-    const double c = taylor_cos(t), s = taylor_sin(t);
-    switch ((q / 2) & 3) {
-      case 0: return {c, s};
-      case 1: return {-s, c};
-      case 2: return {-c, -s};
-      default: return {s, -c};
-    }
-  }
-  // odd octant: angle = p pi/2 - phi, p = (q + 1)/2, phi = pi/4 - theta
-  const double f = kPiD * (R - r) / (4.0 * R);
-  const double c = taylor_cos(f), s = taylor_sin(f);
-  switch (((q + 1) / 2) & 3) {
-    case 0: return {c, -s};
-    case 1: return {s, c};
-    case 2: return {-c, s};
-    default: return {-s, -c};
-  }
-}
-
 // u * W_R^J (forward W_R = exp(-2 pi i / R); INV: conjugate root).
 template <int R, int J, bool INV, typename C>
 __device__ __forceinline__ C mul_root(C u) {

@@ -99,7 +99,7 @@ using namespace exc;
 
 extern "C" int exc_project_noalloc(int precision, int n, double l, void* u, void* p_out, void* stream) {
   if (precision != EXC_F64 && precision != EXC_F32) { set_last_error("precision must be EXC_F64 or EXC_F32"); return EXC_ERR_ARG; }
-  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
   if (!(l > 0) || !u) { set_last_error("bad argument"); return EXC_ERR_ARG; }
   const size_t csz = precision == EXC_F64 ? sizeof(double2) : sizeof(float2);
   if (noalloc_bytes(n, csz) > NOALLOC_SCRATCH_BYTES) {

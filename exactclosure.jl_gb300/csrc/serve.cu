@@ -583,7 +583,7 @@ int exc_server_destroy(exc_server* sv) {
 
 int exc_server_submit(exc_server* sv, const exc_solve_req* req, int64_t* id) {
   if (!sv || !req) { set_last_error("null argument"); return EXC_ERR_ARG; }
-  if (!fft_size_ok(req->n)) { set_last_error("grid size must be 2^a 3^b 5^c, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
+  if (!fft_size_ok(req->n)) { set_last_error("grid size must be 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
   if (!(req->l > 0) || !(req->visc > 0) || !(req->cfl > 0) || !(req->kpeak > 0) || !(req->energy > 0) ||
       req->nsteps < 1) {
     set_last_error("bad request parameters");

@@ -20,7 +20,7 @@
  *     (s11, s22, s33, s12, s23, s31; src/N.jl:94-104) or 9 non-symmetric
  *     ones in the order (s11, s21, s31, s12, s22, s32, s13, s23, s33)
  *     (src/N.jl:181), each an n^3 (or n_les^3) array.
- *   - Grid sizes: n = 2^a 3^b 5^c, a >= 1, 4 <= n <= 1024; an LES ratio c must
+ *   - Grid sizes: n = 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, 4 <= n <= 1024; an LES ratio c must
  *     divide n and n/c must itself be a supported size for LES projection.
  *   - Case-level host pointers are borrowed for the duration of the call.
  *   - A handle is not re-entrant; distinct handles may be used from

@@ -41,7 +41,7 @@ def test_argument_validation_without_gpu(built_lib):
     from exactclosure_gb300 import _lib
 
     d = _lib.CaseDesc()
-    d.n, d.l, d.visc, d.cfl, d.precision, d.nles = 98, 1.0, 1e-3, 0.3, 0, 0  # 98 = 2 7^2
+    d.n, d.l, d.visc, d.cfl, d.precision, d.nles = 38, 1.0, 1e-3, 0.3, 0, 0  # 38 = 2 19
     h = C.c_void_p()
     assert built_lib.exc_case_create(C.byref(d), None, C.byref(h)) == 2  # EXC_ERR_SHAPE
     d.n, d.nles = 64, 1

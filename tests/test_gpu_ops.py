@@ -82,6 +82,49 @@ def test_project_f64(NS, n):
     assert rel(host(p), pref) < TOL64
 
 
+# sizes with the prime radices 7, 11, 13 and 17: the reference's mediumcase
+# (DNS n = 510 = 2 3 5 17, LES 102 and 170)
+@pytest.mark.parametrize("n", [14, 22, 26, 34, 42, 102, 170])
+def test_project_prime_radices(NS, n):
+    import torch
+
+    l = 1.0
+    rng = np.random.default_rng(n)
+    u = rng.standard_normal((3, n, n, n))
+    ref, pref = ns.project(u, l / n, return_p=True)
+    ps = NS.poissonsolver(NS.Grid(l, n))
+    ut = dev(u)
+    p = torch.empty((n, n, n), dtype=torch.float64, device="cuda")
+    ps.project(ut, p)
+    assert rel(host(ut), ref) < TOL64
+    assert rel(host(p), pref) < TOL64
+    ps32 = NS.poissonsolver(NS.Grid(l, n), precision=1)
+    u32 = dev(u, "float32")
+    ps32.project(u32)
+    assert rel(host(u32), ref) < TOL32
+
+
+def test_project_mediumcase_grid(NS):
+    """n = 510 (radix 17 among 2, 3, 5), too large for the oracle: the FP32
+    projection leaves a field whose grid divergence vanishes and that a second
+    projection leaves unchanged."""
+    import torch
+
+    n = 510
+    g = NS.Grid(1.0, n)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    u = torch.randn((3, n, n, n), generator=gen, device="cuda", dtype=torch.float32)
+    ps = NS.poissonsolver(g, precision=1)
+    ps.project(u)
+    d = torch.empty((n, n, n), dtype=torch.float32, device="cuda")
+    NS.divergence(d, u, g)
+    scale = float(torch.linalg.vector_norm(u.double())) * n
+    assert float(torch.linalg.vector_norm(d.double())) < 2e-5 * scale
+    v = u.clone()
+    ps.project(v)
+    assert float(torch.linalg.vector_norm((v - u).double()) / torch.linalg.vector_norm(u.double())) < 1e-5
+
+
 @pytest.mark.parametrize("n", [8, 12, 30, 32, 96, 100])
 def test_poisson_solve_and_divergence(NS, n):
     import torch
@@ -227,4 +270,4 @@ def test_errors_are_reported(NS):
     from exactclosure_gb300 import ExcError
 
     with pytest.raises(ExcError):
-        NS.poissonsolver(NS.Grid(1.0, 98))  # 2 7^2: no radix-7 pass
+        NS.poissonsolver(NS.Grid(1.0, 38))  # 2 19: no radix-19 pass

@@ -2,6 +2,9 @@
 // on the GPU: a forward-Euler warm-up of the DNS, then the DNS and five LES
 // -- no model, classic, classic+flux, classic+flux+div (the exact closure)
 // and its symmetrised form -- stepped in lockstep with the DNS time step.
+// A second mode runs the paper's volume-average driver `dns_aid_volavg`
+// (src/NavierStokes.jl:141-304) with four LES: no model, classic (volume-
+// filtered flux), swap (face-filtered flux) and its symmetric part.
 //
 // Every operator is a libexc kernel (stress/divergence, FFT projection,
 // filtered fluxes); this file holds the driver, two pointwise tensor kernels
@@ -37,9 +40,13 @@ struct exc_dnsaid {
   double* scal = nullptr;  // device scalars
   double* part = nullptr;  // reduction partials
   double* spec = nullptr;  // init scratch: 3 spectral arrays
+  double* pl = nullptr;    // LES pressure M (paper mode)
+  double* dsig = nullptr;  // closure divergence 3M (paper mode)
   double t = 0;
   int steps = 0;
   bool started = false;
+  bool paper = false;      // dns_aid_volavg instead of dnsaid_project
+  bool doproject = true;   // its `doproject`
 };
 
 namespace exc {
@@ -65,6 +72,26 @@ __global__ void symmetrize_kernel(long long M, const double* __restrict__ r9, do
     s6[4 * M + i] = (r9[5 * M + i] + r9[7 * M + i]) / 2;
     s6[5 * M + i] = (r9[2 * M + i] + r9[6 * M + i]) / 2;
   }
+}
+
+// s6 diagonal += p: r = sigma + p I on the LES grid.
+__global__ void add_diag_kernel(long long M, double* __restrict__ s6, const double* __restrict__ p) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    const double q = p[i];
+    s6[i] += q;
+    s6[M + i] += q;
+    s6[2 * M + i] += q;
+  }
+}
+
+// r9 -= s6 with the symmetric s6 (s11, s22, s33, s12, s23, s31) expanded to
+// the 9-component order (s11, s21, s31, s12, s22, s32, s13, s23, s33).
+__global__ void sub_sym_kernel(long long M, double* __restrict__ r9, const double* __restrict__ s6) {
+  // 9-component slot -> symmetric slot
+  const int map[9] = {0, 3, 5, 3, 1, 4, 5, 4, 2};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) r9[k * M + i] -= s6[map[k] * M + i];
 }
 
 int gridsz(long long cnt) {
@@ -182,6 +209,63 @@ int lockstep(exc_dnsaid* d, double dt) {
   return cuda_rc(launch_axpy<double>(N3, d->u, d->du, dt, st));
 }
 
+// `fu` of dns_aid_volavg (src/NavierStokes.jl:169-170, 290-291): the volume
+// filter of the DNS, projected when `doproject`.
+int paper_target(exc_dnsaid* d, double* out) {
+  int rc = filter_vector<double>(d->n, d->c, EXC_FILTER_VOLUME, fd(d), nfd(d), d->u, out, d->st);
+  if (rc || !d->doproject) return rc;
+  return cuda_rc(project(&d->psl, out, d->st));
+}
+
+// One step of dns_aid_volavg (src/NavierStokes.jl:186-288).
+int lockstep_paper(exc_dnsaid* d, double dt) {
+  const int n = d->n, m = d->m, c = d->c;
+  const long long N3 = 3LL * n * n * n, M = (long long)m * m * m;
+  cudaStream_t st = d->st;
+  // DNS right-hand side, projected; its pressure enters r = sigma + p I
+  cudaError_t e = launch_rhs<double>(n, d->h, d->visc, d->u, d->du, false, st);
+  if (e == cudaSuccess) e = project(&d->psd, d->du, st);
+  if (e == cudaSuccess) e = copy_pressure<double>(&d->psd, d->p, st);
+  if (e != cudaSuccess) return cuda_rc(e);
+  // fru: volume-filtered r (sdh); firu: face-filtered r (r9)
+  int rc = filtered_stress<double>(n, c, d->l, d->visc, fd(d), nfd(d), d->u, d->sdh, st, d->p);
+  if (!rc) rc = closure_flux<double>(n, c, d->l, d->visc, fd(d), nfd(d), d->u, d->p, d->r9, st);
+  // fu and rfu = sigma_H(fu) + p_H I, p_H from the LES right-hand side of fu
+  if (!rc) rc = paper_target(d, d->ub);
+  if (rc) return rc;
+  e = launch_stress<double>(m, d->H, d->visc, d->ub, d->sl, st);
+  if (e == cudaSuccess) e = launch_tensordiv<double>(m, d->H, 6, d->sl, d->dul, false, st);
+  if (e == cudaSuccess) e = poisson_solve_inplace<double>(&d->psl, d->dul, true, st);
+  if (e == cudaSuccess) e = copy_pressure<double>(&d->psl, d->pl, st);
+  if (e == cudaSuccess) { add_diag_kernel<<<gridsz(M), 256, 0, st>>>(M, d->sl, d->pl); e = cudaGetLastError(); }
+  // closures: classic fru - rfu (sc), swap firu - rfu (r9), its symmetric part (sdh)
+  if (e == cudaSuccess) { combine6_kernel<<<gridsz(6 * M), 256, 0, st>>>(6 * M, d->sdh, nullptr, d->sl, d->sc); e = cudaGetLastError(); }
+  if (e == cudaSuccess) { sub_sym_kernel<<<gridsz(M), 256, 0, st>>>(M, d->r9, d->sl); e = cudaGetLastError(); }
+  if (e == cudaSuccess) { symmetrize_kernel<<<gridsz(M), 256, 0, st>>>(M, d->r9, d->sdh); e = cudaGetLastError(); }
+  // DNS step
+  if (e == cudaSuccess) e = launch_axpy<double>(N3, d->u, d->du, dt, st);
+  if (e != cudaSuccess) return cuda_rc(e);
+  // no model: v += dt P(RHS_H(v))
+  e = launch_stress<double>(m, d->H, d->visc, d->les[0], d->sl, st);
+  if (e != cudaSuccess) return cuda_rc(e);
+  rc = les_update(d, d->les[0], d->sl, nullptr, nullptr, dt);
+  // classic, swap, swap-symmetric: v += dt P(RHS_H(v)); v += dt dsigma; project
+  const double* sig[3] = {d->sc, d->r9, d->sdh};
+  const int ncomp[3] = {6, 9, 6};
+  for (int k = 0; k < 3 && !rc; ++k) {
+    double* v = d->les[k + 1];
+    e = launch_stress<double>(m, d->H, d->visc, v, d->sl, st);
+    if (e != cudaSuccess) return cuda_rc(e);
+    rc = les_update(d, v, d->sl, nullptr, nullptr, dt);
+    if (rc) return rc;
+    e = launch_tensordiv<double>(m, d->H, ncomp[k], sig[k], d->dsig, false, st);
+    if (e == cudaSuccess) e = launch_axpy<double>(3 * M, v, d->dsig, dt, st);
+    if (e == cudaSuccess && d->doproject) e = project(&d->psl, v, st);
+    if (e != cudaSuccess) return cuda_rc(e);
+  }
+  return rc;
+}
+
 template <typename P>
 int dalloc(P** p, size_t count) {
   if (cudaMalloc(p, count * sizeof(P)) != cudaSuccess) {
@@ -230,6 +314,7 @@ int exc_dnsaid_create(const exc_dnsaid_desc* desc, void* stream, exc_dnsaid** ou
                 dalloc(&d->sl, 6 * M) || dalloc(&d->sc, 6 * M) || dalloc(&d->zero, M) || dalloc(&d->scal, 16) ||
                 dalloc(&d->part, (size_t)SHELL_BLOCKS * 1024 + 2048 + RED_PARTS) || dalloc(&d->spec, spec);
   for (int k = 0; k < 5 && !rc; ++k) rc = dalloc(&d->les[k], 3 * M);
+  if (!rc) rc = dalloc(&d->pl, M) || dalloc(&d->dsig, 3 * M);
   if (rc) { exc_dnsaid_destroy(d); return rc; }
   cudaMemsetAsync(d->zero, 0, M * sizeof(double), d->st);
   cudaMemsetAsync(d->u, 0, 3 * N * sizeof(double), d->st);
@@ -245,7 +330,7 @@ int exc_dnsaid_destroy(exc_dnsaid* d) {
   poisson_free(&d->psd);
   poisson_free(&d->psl);
   double* bufs[] = {d->u, d->du, d->p, d->ub, d->dul, d->sdh, d->s2, d->r9, d->sl, d->sc, d->zero, d->scal,
-                    d->part, d->spec};
+                    d->part, d->spec, d->pl, d->dsig};
   for (double* b : bufs) cudaFree(b);
   for (double* b : d->les) cudaFree(b);
   delete d;
@@ -305,9 +390,17 @@ int exc_dnsaid_warmup(exc_dnsaid* d, double twarm, double cfl, int max_steps, in
   return cuda_rc(cudaStreamSynchronize(d->st));
 }
 
+int exc_dnsaid_set_paper(exc_dnsaid* d, int doproject) {
+  if (!d) { set_last_error("null handle"); return EXC_ERR_ARG; }
+  if (d->started) { set_last_error("the driver is chosen before exc_dnsaid_start"); return EXC_ERR_STATE; }
+  d->paper = true;
+  d->doproject = doproject != 0;
+  return EXC_OK;
+}
+
 int exc_dnsaid_start(exc_dnsaid* d) {
   if (!d) { set_last_error("null handle"); return EXC_ERR_ARG; }
-  int rc = apply_dhpi(d, d->ub);
+  int rc = d->paper ? paper_target(d, d->ub) : apply_dhpi(d, d->ub);
   if (rc) return rc;
   const size_t M3 = 3ull * d->m * d->m * d->m;
   for (int k = 0; k < 5; ++k) {
@@ -331,7 +424,7 @@ int exc_dnsaid_step(exc_dnsaid* d, double tstop, double cfl, int max_steps, int*
     dt = dt < tstop - d->t ? dt : tstop - d->t;
     d->t += dt;
     ++it;
-    rc = lockstep(d, dt);
+    rc = d->paper ? lockstep_paper(d, dt) : lockstep(d, dt);
     if (rc) return rc;
   }
   d->steps += it;
@@ -352,7 +445,7 @@ int exc_dnsaid_get(exc_dnsaid* d, int which, double* host) {
   const size_t M3 = 3ull * d->m * d->m * d->m;
   const double* src;
   if (which == 0) {
-    int rc = apply_dhpi(d, d->ub);
+    int rc = d->paper ? paper_target(d, d->ub) : apply_dhpi(d, d->ub);
     if (rc) return rc;
     src = d->ub;
   } else {
@@ -367,8 +460,10 @@ int exc_dnsaid_get(exc_dnsaid* d, int which, double* host) {
 int exc_dnsaid_errors(exc_dnsaid* d, double out[5]) {
   if (!d || !out) { set_last_error("null argument"); return EXC_ERR_ARG; }
   if (!d->started) { set_last_error("call exc_dnsaid_start first"); return EXC_ERR_STATE; }
-  int rc = apply_dhpi(d, d->ub);
+  int rc = d->paper ? paper_target(d, d->ub) : apply_dhpi(d, d->ub);
   if (rc) return rc;
+  const int nles = d->paper ? 4 : 5;
+  if (d->paper) out[4] = 0;
   const long long M = (long long)d->m * d->m * d->m;
   double* part = d->part + SHELL_BLOCKS * 1024 + 2048;
   // scal[0..2]: sum b_i^2; scal[3 + 3k + i]: sum (a_ki - b_i)^2
@@ -376,7 +471,7 @@ int exc_dnsaid_errors(exc_dnsaid* d, double out[5]) {
   for (int i = 0; i < 3 && e == cudaSuccess; ++i) e = launch_sqdiff<double>(M, d->ub + i * M, d->zero, part, d->scal + i, d->st);
   double hs[3];
   if (e == cudaSuccess) e = cudaMemcpyAsync(hs, d->scal, sizeof(hs), cudaMemcpyDeviceToHost, d->st);
-  for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+  for (int k = 0; k < nles && e == cudaSuccess; ++k) {
     double ha[3];
     for (int i = 0; i < 3 && e == cudaSuccess; ++i)
       e = launch_sqdiff<double>(M, d->les[k] + i * M, d->ub + i * M, part, d->scal + 3 + i, d->st);

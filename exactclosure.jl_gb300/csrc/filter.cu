@@ -259,10 +259,12 @@ int closure_flux(int n, int c, double l, double visc, const double* fdelta, int 
 }
 
 // sigmaDH (src/N.jl:1088-1115): volume filter GDH of each stress component,
-// sampled at LES centres/edges; order s11,s22,s33,s12,s23,s31.
+// sampled at LES centres/edges; order s11,s22,s33,s12,s23,s31.  With p the
+// total flux r = sigma + p I is filtered (the paper driver's volume-filtered
+// flux, src/NavierStokes.jl:199).
 template <typename T>
 int filtered_stress(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, T* s6,
-                    cudaStream_t st) {
+                    cudaStream_t st, const T* p) {
   const int m = n / c;
   const long long M = (long long)m * m * m;
   const int comps[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {2, 0}};
@@ -273,7 +275,7 @@ int filtered_stress(int n, int c, double l, double visc, const double* fdelta, i
     Taps3 taps;
     int rc = make_taps3(c, stag, point, fdelta, nfd, &taps);
     if (rc) return rc;
-    launch_flux_filter_rt<T>(i, j, u, (const T*)nullptr, n, (T)(1.0 / (l / n)), (T)visc, c, taps, s6 + (long long)k * M,
+    launch_flux_filter_rt<T>(i, j, u, p, n, (T)(1.0 / (l / n)), (T)visc, c, taps, s6 + (long long)k * M,
                              M, st);
   }
   cudaError_t e = cudaGetLastError();
@@ -524,7 +526,7 @@ int classic_stress(int n, int c, double l, double visc, const double* fdelta, in
   template int filter_vector<T>(int, int, int, const double*, int, const T*, T*, cudaStream_t);          \
   template int closure_flux<T>(int, int, double, double, const double*, int, const T*, const T*, T*,     \
                                cudaStream_t);                                                            \
-  template int filtered_stress<T>(int, int, double, double, const double*, int, const T*, T*, cudaStream_t);
+  template int filtered_stress<T>(int, int, double, double, const double*, int, const T*, T*, cudaStream_t, const T*);
 INST(double)
 INST(float)
 #undef INST

@@ -40,6 +40,7 @@ int classic_stress(int n, int c, double l, double visc, const double* fdelta, in
                    cudaStream_t st);
 template <typename T>
 int filtered_stress(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, T* s6,
-                    cudaStream_t st);
+                    cudaStream_t st,
+                    const T* p = nullptr);
 
 }  // namespace exc

@@ -136,6 +136,7 @@ SIGNATURES = {
     "exc_dnsaid_get_velocity": [vp, dp],
     "exc_dnsaid_warmup": [vp, f64, f64, i32, C.POINTER(i32)],
     "exc_dnsaid_start": [vp],
+    "exc_dnsaid_set_paper": [vp, i32],
     "exc_dnsaid_step": [vp, f64, f64, i32, C.POINTER(i32)],
     "exc_dnsaid_time": [vp, dp, C.POINTER(i32)],
     "exc_dnsaid_get": [vp, i32, dp],

@@ -316,6 +316,8 @@ class Case:
 # The reference's driver `dnsaid_project` (src/N.jl:1239-1332)
 # ---------------------------------------------------------------------------
 DNSAID_FIELDS = ("u_les", "u_nomo", "u_c", "u_cf", "u_cfd", "u_cfd_symm")
+# the paper's dns_aid_volavg (src/NavierStokes.jl:141-304): target fu, four LES
+PAPER_FIELDS = ("fu", "nomodel", "classic", "swapfil", "swapfil_symm")
 
 
 def gaussian(h: float, delta: float, nsigma: float) -> np.ndarray:
@@ -346,6 +348,14 @@ class DnsAid:
         h = C.c_void_p()
         call("exc_dnsaid_create", C.byref(desc), stream, C.byref(h))
         self._h = h
+        self.fields = DNSAID_FIELDS
+
+    def set_paper(self, doproject: bool = True):
+        """Run the paper's volume-average driver ``dns_aid_volavg``
+        (src/NavierStokes.jl:141-304) instead of ``dnsaid_project``; call
+        before ``start``.  Fields: ``PAPER_FIELDS``."""
+        call("exc_dnsaid_set_paper", self._h, 1 if doproject else 0)
+        self.fields = PAPER_FIELDS
 
     def init_random(self, profile: str = "power", param: float = -5 / 3, energy: float = 1.0, seed: int = 0):
         call("exc_dnsaid_init_random", self._h, {"peak": 0, "power": 1}[profile], param, energy, seed)
@@ -379,13 +389,13 @@ class DnsAid:
 
     def get(self, which: str) -> np.ndarray:
         out = np.empty((3, self.m, self.m, self.m))
-        call("exc_dnsaid_get", self._h, DNSAID_FIELDS.index(which), out.ctypes.data_as(C.POINTER(C.c_double)))
+        call("exc_dnsaid_get", self._h, self.fields.index(which), out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
     def errors(self) -> dict:
         e = np.empty(5)
         call("exc_dnsaid_errors", self._h, e.ctypes.data_as(C.POINTER(C.c_double)))
-        return dict(zip(DNSAID_FIELDS[1:], e.tolist()))
+        return dict(zip(self.fields[1:], e.tolist()))
 
     def close(self):
         if getattr(self, "_h", None):

@@ -382,16 +382,28 @@ int exc_dnsaid_get_velocity(exc_dnsaid* d, double* host);
 /* The warm-up loop (src/N.jl:1264-1276): step_forwardeuler! until t reaches
  * twarm (at most max_steps steps when > 0). */
 int exc_dnsaid_warmup(exc_dnsaid* d, double twarm, double cfl, int max_steps, int* steps);
-/* LES initial states: all five = apply_ΔHπ(u) (src/N.jl:1278-1287); t = 0. */
+/* Switch the handle (before exc_dnsaid_start) to the paper's volume-average
+ * driver `dns_aid_volavg` (src/NavierStokes.jl:141-304): four LES -- no
+ * model, classic (divergence of the volume-filtered flux minus
+ * sigma_H(fu) + p_H I), swap (the face-filtered flux instead) and the swap
+ * flux's symmetric part -- each stepped v += dt P(RHS_H(v)) + dt dsigma, then
+ * projected when doproject != 0; the target fu is the volume-filtered DNS,
+ * projected when doproject.  The paper module's Turbulox filters are the
+ * reference's own GDH (volume) and GDHi (face) filters of src/N.jl. */
+int exc_dnsaid_set_paper(exc_dnsaid* d, int doproject);
+/* LES initial states: all five = apply_ΔHπ(u) (src/N.jl:1278-1287), or the
+ * four paper LES = fu; t = 0. */
 int exc_dnsaid_start(exc_dnsaid* d);
 /* The lockstep loop (src/N.jl:1289-1323) until t reaches tstop (at most
  * max_steps steps when > 0). */
 int exc_dnsaid_step(exc_dnsaid* d, double tstop, double cfl, int max_steps, int* steps);
 int exc_dnsaid_time(exc_dnsaid* d, double* t, int* steps);
 /* host (3 n_les^3): 0 = apply_ΔHπ of the current DNS (`u_les`), 1 u_nomo,
- * 2 u_c, 3 u_cf, 4 u_cfd, 5 u_cfd_symm. */
+ * 2 u_c, 3 u_cf, 4 u_cfd, 5 u_cfd_symm; paper driver: 0 = fu, 1 nomodel,
+ * 2 classic, 3 swapfil, 4 swapfil_symm. */
 int exc_dnsaid_get(exc_dnsaid* d, int which, double* host);
-/* `compute_errors` (src/N.jl:1334-1349) of the five LES against u_les. */
+/* `compute_errors` (src/N.jl:1334-1349) of the five LES against u_les (the
+ * paper driver: of its four LES against fu, out[4] = 0). */
 int exc_dnsaid_errors(exc_dnsaid* d, double out[5]);
 
 /* ======================================================================

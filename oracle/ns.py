@@ -756,3 +756,62 @@ def dnsaid_project_steps(u, les, visc, l, c, tstop, cfl, fdelta=None, max_steps=
         les["u_cfd_symm"] = step_classic_flux_div(les["u_cfd_symm"], ub, u, p, visc, l, c, dt, fdelta, symm=True)
         u = u + dt * du
     return u, les, t, it
+
+
+# --------------------------------------------------------------------------
+# The paper's volume-average driver `dns_aid_volavg` (src/NavierStokes.jl:141-304)
+# --------------------------------------------------------------------------
+# The paper module calls Turbulox.jl (not vendored, no pinned version) for its
+# filters; they are restated with the reference's own filters of src/N.jl:
+# `volumefilter!` as the c^3 top-hat GDH sampled at the LES positions
+# (`lazyfilter` + `lazycoarsegrain`, src/N.jl:639-698) and the flux's
+# `surfacefilter!(., false)` as GDHi (`get_rΔHi`, src/N.jl:1038-1073).  Parity
+# of this path is against this restatement only (no reference vectors).
+PAPER_NAMES = ("nomodel", "classic", "swapfil", "swapfil_symm")
+
+
+def paper_volavg_target(u, l, c, doproject, fdelta=None):
+    """``fu``: the volume-filtered DNS, projected when ``doproject``
+    (src/NavierStokes.jl:169-170, 290-291)."""
+    fu = volume_filter(u, c, fdelta)
+    return project(fu, l / fu.shape[1]) if doproject else fu
+
+
+def dns_aid_volavg_steps(u, les, visc, l, c, tstop, cfl, doproject, fdelta=None, max_steps=None, t0=0.0):
+    """Steps of the loop of ``dns_aid_volavg`` (src/NavierStokes.jl:186-288):
+    with ``r = sigma(u) + p I`` of the projected DNS right-hand side and
+    ``rfu = sigma_H(fu) + p_H I`` (``p_H`` the pressure of the LES
+    right-hand side of ``fu``), the closures are the divergences of
+    ``fru - rfu`` (classic, volume-filtered flux), ``firu - rfu`` (swap, the
+    face-filtered flux) and its symmetric part; each LES takes
+    ``v += dt P(RHS_H(v))``, ``v += dt dsigma``, then a projection when
+    ``doproject``.  Returns (u, les, t, steps)."""
+    n = u.shape[1]
+    h = l / n
+    m = n // c
+    H = l / m
+    les = {k: v.copy() for k, v in les.items()}
+    t, it = t0, 0
+    while t < tstop and (max_steps is None or it < max_steps):
+        dt = min(propose_timestep(u, visc, cfl, h), tstop - t)
+        t += dt
+        it += 1
+        du, p = project(rhs(u, visc, h), h, return_p=True)
+        r = get_r(stresstensor(u, visc, h), p)
+        fru = get_sigmaDH(r, c, fdelta)
+        firu = get_rDHi(r, c, fdelta)
+        fu = paper_volavg_target(u, l, c, doproject, fdelta)
+        sfu = stresstensor(fu, visc, H)
+        p_les = poisson_solve(divergence(tensordivergence(sfu, H), H), H)
+        rfu = get_r(sfu, p_les)
+        s_classic = {k: fru[k] - rfu[k] for k in fru}
+        s_swap = {k: firu[k] - rfu[k] for k in firu}
+        dsig = {"classic": tensordivergence(s_classic, H), "swapfil": tensordivergence(s_swap, H),
+                "swapfil_symm": tensordivergence(symmetrize(s_swap), H)}
+        u = u + dt * du
+        les["nomodel"] = les["nomodel"] + dt * project(rhs(les["nomodel"], visc, H), H)
+        for k in ("classic", "swapfil", "swapfil_symm"):
+            v = les[k] + dt * project(rhs(les[k], visc, H), H)
+            v = v + dt * dsig[k]
+            les[k] = project(v, H) if doproject else v
+    return u, les, t, it

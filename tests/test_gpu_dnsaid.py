@@ -59,6 +59,34 @@ def test_warmup_start_and_lockstep_per_step(NS, n, c, use_fdelta):
     assert rel(d.get("u_les"), ns.apply_DHpi(u, c, l, fdelta)) < 1e-12
 
 
+@pytest.mark.parametrize("doproject", [True, False])
+def test_paper_volavg_driver_per_step(NS, doproject):
+    """The paper's dns_aid_volavg (src/NavierStokes.jl:141-304): start and
+    three lockstep steps against the oracle (1e-12); the swap closure (face-
+    filtered flux) keeps its LES on the filtered DNS to round-off."""
+    n, c, l, visc, cfl = 30, 3, 1.0, 1e-3, 0.4
+    u = ns.randomfield(n, l, -5 / 3, 2, 1.0, profile="power")
+    d = NS.DnsAid(n, l, visc, c)
+    d.set_velocity(u)
+    d.set_paper(doproject)
+    d.start()
+    fu = ns.paper_volavg_target(u, l, c, doproject)
+    les = {k: fu.copy() for k in ns.PAPER_NAMES}
+    assert rel(d.get("fu"), fu) < 1e-12
+    t = 0.0
+    for k in range(3):
+        d.step(0.05, cfl, max_steps=1)
+        u, les, t, _ = ns.dns_aid_volavg_steps(u, les, visc, l, c, 0.05, cfl, doproject, max_steps=1, t0=t)
+        assert rel(d.velocity(), u) < 1e-12, k
+        for key in ns.PAPER_NAMES:
+            assert rel(d.get(key), les[key]) < 1e-12, (k, key)
+    e = d.errors()
+    assert e["swapfil"] < 1e-13
+    for key in ("nomodel", "classic", "swapfil_symm"):
+        assert e[key] > 1e-4, key
+    d.close()
+
+
 def test_exact_closure_invariant_and_errors(NS):
     setup = NS.getsetup(n_dns=72, n_les=24, twarm=0.02, tstop=0.02, visc=1e-3)
     out = NS.dnsaid_project(setup)

@@ -217,3 +217,21 @@ def test_counter_normal_statistics():
     x = ns.counter_normal(0, 200000)
     assert abs(x.mean()) < 0.01 and abs(x.std() - 1) < 0.01
     assert np.array_equal(ns.counter_normal(5, 10, offset=3), ns.counter_normal(5, 13)[3:])
+
+
+@pytest.mark.parametrize("doproject", [True, False])
+def test_paper_volavg_swap_closure_is_exact(doproject):
+    """The paper driver dns_aid_volavg (src/NavierStokes.jl:141-304), restated
+    with the reference's own filters: its swap closure (face-filtered flux)
+    keeps the LES on the volume-filtered DNS to round-off, with and without
+    the projections; the other LES drift."""
+    n, c, l, visc = 24, 3, 1.0, 1e-3
+    u = ns.randomfield(n, l, -5 / 3, 1, 1.0, profile="power")
+    fu = ns.paper_volavg_target(u, l, c, doproject)
+    les = {k: fu.copy() for k in ns.PAPER_NAMES}
+    u2, les2, _, it = ns.dns_aid_volavg_steps(u, les, visc, l, c, 0.05, 0.4, doproject, max_steps=3)
+    assert it == 3
+    ref = ns.paper_volavg_target(u2, l, c, doproject)
+    assert ns.rel_l2(les2["swapfil"], ref) < 1e-13
+    for k in ("nomodel", "classic", "swapfil_symm"):
+        assert ns.rel_l2(les2[k], ref) > 1e-4, k

@@ -826,6 +826,7 @@ static void conv_launch(int engine, long long V, int n, const __nv_bfloat16* in,
       const long long N = (long long)n * n * n;
       const int batch = (int)(V / N);
       HaloMaps maps;
+      if (batch == 0) return;
       if (halo_maps(in, batch, &maps)) {
         const long long nblk = (long long)batch * n * (n / CU_ROWS);
         const long long ctas = std::min<long long>(nblk, 152);

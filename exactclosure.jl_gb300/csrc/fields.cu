@@ -418,6 +418,10 @@ __device__ __forceinline__ unsigned long long splitmix(unsigned long long x) {
   x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
   return x ^ (x >> 31);
 }
+// The FP32 form draws the same counters with 24-bit uniforms and FP32
+// Box-Muller (the FP64 pipe is the slow one on this part): each normal
+// differs from the FP64 draw by about 1e-7 relative, below the form's own
+// rounding; the FP64 path keeps the oracle's formula exactly.
 template <typename T>
 __global__ void normal_kernel(long long count, unsigned long long seed, T* __restrict__ out) {
   const unsigned long long base = seed * 0x9E3779B97F4A7C15ull;
@@ -425,9 +429,15 @@ __global__ void normal_kernel(long long count, unsigned long long seed, T* __res
     unsigned long long m = (unsigned long long)i;
     unsigned long long z1 = splitmix(base + 2ull * m);
     unsigned long long z2 = splitmix(base + 2ull * m + 1ull);
-    double u1 = ((double)(z1 >> 11) + 0.5) * 0x1.0p-53;
-    double u2 = ((double)(z2 >> 11) + 0.5) * 0x1.0p-53;
-    out[i] = (T)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+    if constexpr (sizeof(T) == 4) {
+      const float u1 = ((float)(unsigned)(z1 >> 40) + 0.5f) * 0x1.0p-24f;
+      const float u2 = ((float)(unsigned)(z2 >> 40) + 0.5f) * 0x1.0p-24f;
+      out[i] = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+    } else {
+      double u1 = ((double)(z1 >> 11) + 0.5) * 0x1.0p-53;
+      double u2 = ((double)(z2 >> 11) + 0.5) * 0x1.0p-53;
+      out[i] = (T)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+    }
   }
 }
 template <typename T>
@@ -645,22 +655,29 @@ __device__ __forceinline__ double shell_profile(int profile, double param, int k
   return (double)k * k * (double)k * k * exp(-2.0 * q * q);
 }
 
+// One CTA: the profiles in parallel, their total in shell order by one thread.
 __global__ void shell_factor_kernel(int nshell, int profile, double param, double energy,
                                     const double* __restrict__ eshell, double* __restrict__ factor) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
+  extern __shared__ double sprof[];  // nshell profiles, then the total
+  for (int k = threadIdx.x; k < nshell; k += blockDim.x) sprof[k] = shell_profile(profile, param, k);
+  __syncthreads();
+  if (threadIdx.x == 0) {
     double tot = 0.0;
-    for (int k = 0; k < nshell; ++k) tot += shell_profile(profile, param, k);
-    for (int k = 0; k < nshell; ++k) {
-      double prof = shell_profile(profile, param, k);
-      double e0 = energy * prof / tot;
-      double es = eshell[k];
-      factor[k] = es > 0 ? sqrt(e0 / es) : 1.0;
-    }
+    for (int k = 0; k < nshell; ++k) tot += sprof[k];
+    sprof[nshell] = tot;
+  }
+  __syncthreads();
+  const double tot = sprof[nshell];
+  for (int k = threadIdx.x; k < nshell; k += blockDim.x) {
+    const double e0 = energy * sprof[k] / tot;
+    const double es = eshell[k];
+    factor[k] = es > 0 ? sqrt(e0 / es) : 1.0;
   }
 }
 cudaError_t launch_shell_factor(int nshell, int profile, double param, double energy, const double* eshell,
                                 double* factor, cudaStream_t st) {
-  shell_factor_kernel<<<1, 32, 0, st>>>(nshell, profile, param, energy, eshell, factor);
+  shell_factor_kernel<<<1, 256, (size_t)(nshell + 1) * sizeof(double), st>>>(nshell, profile, param, energy, eshell,
+                                                                             factor);
   return cudaGetLastError();
 }
 

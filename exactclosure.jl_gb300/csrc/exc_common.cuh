@@ -119,4 +119,20 @@ inline bool fft_size_ok(int n) {
 
 namespace exc {
 void set_last_error(const char* msg);
+
+// |x| as its magnitude bits: for non-negative IEEE values the unsigned
+// integer order is the numeric order, and NaN patterns sort above infinity,
+// so maxima of magnitudes run exactly on the integer pipe.
+template <typename T> struct MagBits;
+template <> struct MagBits<double> { using type = unsigned long long; using vec = double2; };
+template <> struct MagBits<float> { using type = unsigned; using vec = float4; };
+__device__ __forceinline__ unsigned long long mag_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ unsigned mag_bits(float x) { return __float_as_uint(x) & 0x7FFFFFFFu; }
+template <typename T> __device__ __forceinline__ T from_mag_bits(typename MagBits<T>::type b);
+template <> __device__ __forceinline__ double from_mag_bits<double>(unsigned long long b) {
+  return __longlong_as_double((long long)b);
+}
+template <> __device__ __forceinline__ float from_mag_bits<float>(unsigned b) { return __uint_as_float(b); }
 }

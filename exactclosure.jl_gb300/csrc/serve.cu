@@ -33,31 +33,36 @@ namespace exc {
 // ---------------------------------------------------------------------------
 // Batched kernels of the serving step
 // ---------------------------------------------------------------------------
-constexpr int SRV_RED = 64;  // partial blocks per slot for max |u|
+constexpr int SRV_RED = 256;  // partial blocks per slot for max |u|
 
 template <typename T>
 __global__ void slot_maxabs_partial(long long count, const T* __restrict__ u, long long stride,
                                     const int* __restrict__ active, double* __restrict__ part) {
   const int slot = blockIdx.y;
   if (!active[slot]) return;
-  const T* x = u + slot * stride;
-  // maximum in the field's word type (exact; no FP64-pipe work for FP32)
-  T m = (T)0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
-    T v = fabs(x[i]);
-    m = (v > m || v != v) ? v : m;
+  // maximum of the magnitude bits (exact, integer pipe, NaN propagates); the
+  // slot strides keep 16-byte alignment and count is a multiple of 4
+  using B = typename MagBits<T>::type;
+  using V = typename MagBits<T>::vec;
+  constexpr int E = 16 / (int)sizeof(T);
+  const V* x = reinterpret_cast<const V*>(u + slot * stride);
+  B m = 0;
+  const long long nv = count / E;
+#pragma unroll 4
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
+    const V v = x[i];
+    const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+    for (int k = 0; k < E; ++k) m = max(m, mag_bits(e[k]));
   }
-  __shared__ T red[8];
-  for (int o = 16; o > 0; o >>= 1) {
-    T w = __shfl_xor_sync(0xffffffffu, m, o);
-    m = (w > m || w != w) ? w : m;
-  }
+  __shared__ B red[8];
+  for (int o = 16; o > 0; o >>= 1) m = max(m, (B)__shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    T r = (T)0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = (red[w] > r || red[w] != red[w]) ? red[w] : r;
-    part[slot * SRV_RED + blockIdx.x] = (double)r;
+    B r = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = max(r, red[w]);
+    part[slot * SRV_RED + blockIdx.x] = (double)from_mag_bits<T>(r);
   }
 }
 

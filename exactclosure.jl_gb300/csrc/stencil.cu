@@ -143,27 +143,37 @@ cudaError_t launch_gradient(int n, T h, T* u, const T* p, int ppitch, cudaStream
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void maxabs_partial_kernel(size_t count, const T* __restrict__ x, double* __restrict__ partial) {
-  // the maximum is taken in the field's own word type (exact), so an FP32
-  // field costs no FP64-pipe work
-  __shared__ T red[32];
-  T m = (T)0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
-    T v = fabs(x[i]);
-    m = (v > m || v != v) ? v : m;  // NaN propagates
+  // the maximum of |x| is taken on the magnitude bits (unsigned integer order
+  // equals the order of non-negative IEEE values, and NaN patterns sort above
+  // infinity, so a NaN propagates): exact, on the integer pipe, and with
+  // 16-byte loads when the array allows them
+  using B = typename MagBits<T>::type;
+  __shared__ B red[32];
+  B m = 0;
+  constexpr int E = 16 / (int)sizeof(T);
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
+  size_t done = 0;
+  if ((reinterpret_cast<uintptr_t>(x) & 15) == 0) {
+    using V = typename MagBits<T>::vec;
+    const V* xv = reinterpret_cast<const V*>(x);
+    const size_t nv = count / E;
+#pragma unroll 4
+    for (size_t i = tid; i < nv; i += nth) {
+      const V v = xv[i];
+      const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+      for (int k = 0; k < E; ++k) m = max(m, mag_bits(e[k]));
+    }
+    done = nv * E;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    T w = __shfl_xor_sync(0xffffffffu, m, o);
-    m = (w > m || w != w) ? w : m;
-  }
+  for (size_t i = done + tid; i < count; i += nth) m = max(m, mag_bits(x[i]));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, (B)__shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x < 32) {
-    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : (T)0;
-    for (int o = 16; o > 0; o >>= 1) {
-      T w = __shfl_xor_sync(0xffffffffu, m, o);
-      m = (w > m || w != w) ? w : m;
-    }
-    if (threadIdx.x == 0) partial[blockIdx.x] = (double)m;
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : (B)0;
+    for (int o = 16; o > 0; o >>= 1) m = max(m, (B)__shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) partial[blockIdx.x] = (double)from_mag_bits<T>(m);
   }
 }
 

@@ -9,7 +9,7 @@ condition with k0 = 6 normalised to unit kinetic energy.  Metric:
 cell-updates/s = 512^3 DNS cells x RK4 steps / second.
 
 ``--impl reference`` times the CPU restatement of the same path on the host
-cores (the reference is Julia, which is not installed; see DESIGN.md).
+cores (the reference is Julia, which is not installed).
 Multi-GPU runs are independent replicas (each rank its own solve; no
 collective on the data path): ``value`` sums all ranks' cell updates over the
 slowest rank's time.

@@ -471,7 +471,9 @@ struct FineFilteredStressSrc {
   __device__ __forceinline__ double operator()(int x, int y, int z) const {
     constexpr int off = (I != J);
     const double uir = uf_at<J>(I, x, y, z, off), uil = uf_at<J>(I, x, y, z, off - 1);
-    const double ujr = uf_at<I>(J, x, y, z, off), ujl = uf_at<I>(J, x, y, z, off - 1);
+    // on the diagonal the two pairs are the same filtered values
+    const double ujr = I == J ? uir : uf_at<I>(J, x, y, z, off);
+    const double ujl = I == J ? uil : uf_at<I>(J, x, y, z, off - 1);
     const double etaj_ui = (uir + uil) / 2, etai_uj = (ujr + ujl) / 2;
     const double dj_ui = (uir - uil) * (double)inv_h, di_uj = (ujr - ujl) * (double)inv_h;
     return etaj_ui * etai_uj - (double)visc * (dj_ui + di_uj);

@@ -10,8 +10,7 @@
 // six warps evaluate the halo stresses lane-parallel (one task per warp), and
 // the divergence is formed from shared memory and registers.  Every stress
 // value is computed once (plus the x/y halo), copy offsets are computed once
-// per thread, and global loads and stores are row-contiguous.  Stresses are
-// kept divided by h.
+// per thread, and global loads and stores are row-contiguous.
 #include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's driver entry point)
 
 #include <cstring>
@@ -89,39 +88,39 @@ constexpr size_t plane_smem_bytes() {
 
 // sigma_ii at box (bx, by) of plane buffer b (uses u_i at the cell and at -e_i)
 template <typename T, int I, typename U>
-__device__ __forceinline__ T sdiag(const U& u, int bx, int by, T kd, T kv2) {
+__device__ __forceinline__ T sdiag(const U& u, int bx, int by, T rv2) {
   bx += SH<T>;
   const T a = u[I][by][bx];
   const T b = I == 0 ? u[0][by][bx - 1] : u[1][by - 1][bx];
   const T s = a + b, d = a - b;
-  return s * s * kd - kv2 * d;
+  return s * s - rv2 * d;
 }
 // sigma_12 at box (bx, by): u1, u1(+y), u2, u2(+x)
 template <typename T, typename U>
-__device__ __forceinline__ T s12(const U& u, int bx, int by, T kd, T kv) {
+__device__ __forceinline__ T s12(const U& u, int bx, int by, T rv) {
   bx += SH<T>;
   const T a = u[0][by][bx], b = u[0][by + 1][bx], c = u[1][by][bx], d = u[1][by][bx + 1];
-  return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
+  return (a + b) * (c + d) - rv * ((b - a) + (d - c));
 }
 // sigma_13 at box (bx, by): u1, u1(+z) [next plane], u3, u3(+x)
 template <typename T, typename U>
-__device__ __forceinline__ T s13(const U& uc, const U& un, int bx, int by, T kd, T kv) {
+__device__ __forceinline__ T s13(const U& uc, const U& un, int bx, int by, T rv) {
   bx += SH<T>;
   const T a = uc[0][by][bx], b = un[0][by][bx], c = uc[2][by][bx], d = uc[2][by][bx + 1];
-  return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
+  return (a + b) * (c + d) - rv * ((b - a) + (d - c));
 }
 // sigma_23 at box (bx, by): u2, u2(+z) [next plane], u3, u3(+y)
 template <typename T, typename U>
-__device__ __forceinline__ T s23(const U& uc, const U& un, int bx, int by, T kd, T kv) {
+__device__ __forceinline__ T s23(const U& uc, const U& un, int bx, int by, T rv) {
   bx += SH<T>;
   const T a = uc[1][by][bx], b = un[1][by][bx], c = uc[2][by][bx], d = uc[2][by + 1][bx];
-  return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
+  return (a + b) * (c + d) - rv * ((b - a) + (d - c));
 }
 // sigma_33 between planes: u3 of the upper plane and of the lower plane
 template <typename T>
-__device__ __forceinline__ T s33(T up, T lo, T kd, T kv2) {
+__device__ __forceinline__ T s33(T up, T lo, T rv2) {
   const T s = up + lo, d = up - lo;
-  return s * s * kd - kv2 * d;
+  return s * s - rv2 * d;
 }
 
 template <typename T, int NC, bool DOADD>
@@ -144,9 +143,10 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int lane = tx, warp = ty;
   const int x0 = blockIdx.x * PTX, y0 = blockIdx.y * PTY, z0 = zb * ptz;
+  // stresses are kept as 4 sigma (rv = 4 visc / h), the divergence takes 1/(4h)
   const T kd = (T)0.25 * inv_h;
-  const T kv = visc * inv_h * inv_h;
-  const T kv2 = (T)2 * kv;
+  const T rv = (T)4 * visc * inv_h;
+  const T rv2 = (T)2 * rv;
   auto wrap = [n](int g) { return g < 0 ? g + n : (g >= n ? g - n : g); };
   auto wrapm = [n](int g) { return ((g % n) + n) % n; };
   const bool big = n >= PBX;
@@ -259,9 +259,9 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
 #pragma unroll
   for (int i = 0; i < NC; ++i) {
     const int by = NC * ty + 1 + i;
-    s13_prev[i] = s13<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
-    s23_prev[i] = s23<T>(sm.u[0], sm.u[1], bx, by, kd, kv);
-    s33_cur[i] = s33<T>(sm.u[1][2][by][bx + SH<T>], sm.u[0][2][by][bx + SH<T>], kd, kv2);
+    s13_prev[i] = s13<T>(sm.u[0], sm.u[1], bx, by, rv);
+    s23_prev[i] = s23<T>(sm.u[0], sm.u[1], bx, by, rv);
+    s33_cur[i] = s33<T>(sm.u[1][2][by][bx + SH<T>], sm.u[0][2][by][bx + SH<T>], rv2);
   }
   __syncthreads();  // buffer 0 is refilled by the first prefetch
   // buffers: cur = plane z, nxt = plane z + 1, pre = the free one
@@ -283,12 +283,12 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
 #pragma unroll
     for (int i = 0; i < NC; ++i) {
       const int by = NC * ty + 1 + i;
-      v11[i] = sdiag<T, 0>(uc, bx, by, kd, kv2);
-      v22[i] = sdiag<T, 1>(uc, bx, by, kd, kv2);
-      v12[i] = s12<T>(uc, bx, by, kd, kv);
-      v13[i] = s13<T>(uc, un, bx, by, kd, kv);
-      v23[i] = s23<T>(uc, un, bx, by, kd, kv);
-      v33n[i] = s33<T>(un[2][by][bx + SH<T>], uc[2][by][bx + SH<T>], kd, kv2);
+      v11[i] = sdiag<T, 0>(uc, bx, by, rv2);
+      v22[i] = sdiag<T, 1>(uc, bx, by, rv2);
+      v12[i] = s12<T>(uc, bx, by, rv);
+      v13[i] = s13<T>(uc, un, bx, by, rv);
+      v23[i] = s23<T>(uc, un, bx, by, rv);
+      v33n[i] = s33<T>(un[2][by][bx + SH<T>], uc[2][by][bx + SH<T>], rv2);
       // s22 is read from the row above and s23 from the row below: inside a
       // thread's rows they stay in registers
       sm.s[0][by][bx] = v11[i];
@@ -301,17 +301,17 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     // on the upper halo row, s12 and s13 on the left halo column, s11 on the
     // right halo column
     if (warp == 0) {
-      sm.s[2][0][lane + 1] = s12<T>(uc, lane + 1, 0, kd, kv);
+      sm.s[2][0][lane + 1] = s12<T>(uc, lane + 1, 0, rv);
     } else if (warp == 1) {
-      sm.s[4][0][lane + 1] = s23<T>(uc, un, lane + 1, 0, kd, kv);
+      sm.s[4][0][lane + 1] = s23<T>(uc, un, lane + 1, 0, rv);
     } else if (warp == 2) {
-      sm.s[1][PTY + 1][lane + 1] = sdiag<T, 1>(uc, lane + 1, PTY + 1, kd, kv2);
+      sm.s[1][PTY + 1][lane + 1] = sdiag<T, 1>(uc, lane + 1, PTY + 1, rv2);
     } else if (warp == 3) {
-      for (int r = lane; r <= PTY; r += 32) sm.s[2][r][0] = s12<T>(uc, 0, r, kd, kv);
+      for (int r = lane; r <= PTY; r += 32) sm.s[2][r][0] = s12<T>(uc, 0, r, rv);
     } else if (warp == 4) {
-      for (int r = lane + 1; r <= PTY; r += 32) sm.s[3][r][0] = s13<T>(uc, un, 0, r, kd, kv);
+      for (int r = lane + 1; r <= PTY; r += 32) sm.s[3][r][0] = s13<T>(uc, un, 0, r, rv);
     } else if (warp == 5) {
-      for (int r = lane + 1; r <= PTY; r += 32) sm.s[0][r][PTX + 1] = sdiag<T, 0>(uc, PTX + 1, r, kd, kv2);
+      for (int r = lane + 1; r <= PTY; r += 32) sm.s[0][r][PTX + 1] = sdiag<T, 0>(uc, PTX + 1, r, rv2);
     }
     __syncthreads();
     if (gx < n) {
@@ -331,13 +331,13 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
           const T d3 = (v13[i] - S[3][by][bx - 1]) + (v23[i] - s23_below) + (v33n[i] - s33_cur[i]);
           const long long g = ((long long)z * n + gy) * n + gx;
           if (DOADD) {
-            du1[g] -= d1;
-            du2[g] -= d2;
-            du3[g] -= d3;
+            du1[g] -= kd * d1;
+            du2[g] -= kd * d2;
+            du3[g] -= kd * d3;
           } else {
-            du1[g] = -d1;
-            du2[g] = -d2;
-            du3[g] = -d3;
+            du1[g] = -kd * d1;
+            du2[g] = -kd * d2;
+            du3[g] = -kd * d3;
           }
         }
         s13_prev[i] = v13[i];
@@ -382,12 +382,12 @@ constexpr size_t QUAD_SMEM = sizeof(QuadSmem) + 128;
 
 
 
-__device__ __forceinline__ float qdiag(float a, float b, float kd, float kv2) {
+__device__ __forceinline__ float qdiag(float a, float b, float rv2) {
   const float s = a + b, d = a - b;
-  return s * s * kd - kv2 * d;
+  return s * s - rv2 * d;
 }
-__device__ __forceinline__ float qoff(float a, float b, float c, float d, float kd, float kv) {
-  return (a + b) * (c + d) * kd - kv * ((b - a) + (d - c));
+__device__ __forceinline__ float qoff(float a, float b, float c, float d, float rv) {
+  return (a + b) * (c + d) - rv * ((b - a) + (d - c));
 }
 
 template <bool DOADD>
@@ -405,7 +405,7 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
   if (sb.visc) visc = reinterpret_cast<const float*>(sb.visc)[slot];
   const int tx = threadIdx.x, ty = threadIdx.y, lane = tx, warp = ty;
   const int x0 = blockIdx.x * QX, y0 = blockIdx.y * QY, z0 = zb * ptz;
-  const float kd = 0.25f * inv_h, kv = visc * inv_h * inv_h, kv2 = 2.0f * kv;
+  const float kd = 0.25f * inv_h, rv = 4.0f * visc * inv_h, rv2 = 2.0f * rv;  // 4 sigma kept, as above
   auto wrap = [n](int g) { return g < 0 ? g + n : (g >= n ? g - n : g); };
   // 16-byte copy pieces of a plane: 18 pieces per box row (left, 16 interior,
   // right), offsets computed once
@@ -497,12 +497,12 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
     const float a3r = ua[2].r[r][sc + 2];
     const float2 a3u = f2(ua[2].r[r + 1]);
     const float2 b3 = f2(ub[2].r[r]);
-    p13[j][0] = qoff(a1.x, b1.x, a3.x, a3.y, kd, kv);
-    p13[j][1] = qoff(a1.y, b1.y, a3.y, a3r, kd, kv);
-    p23[j][0] = qoff(a2.x, b2.x, a3.x, a3u.x, kd, kv);
-    p23[j][1] = qoff(a2.y, b2.y, a3.y, a3u.y, kd, kv);
-    p33[j][0] = qdiag(b3.x, a3.x, kd, kv2);
-    p33[j][1] = qdiag(b3.y, a3.y, kd, kv2);
+    p13[j][0] = qoff(a1.x, b1.x, a3.x, a3.y, rv);
+    p13[j][1] = qoff(a1.y, b1.y, a3.y, a3r, rv);
+    p23[j][0] = qoff(a2.x, b2.x, a3.x, a3u.x, rv);
+    p23[j][1] = qoff(a2.y, b2.y, a3.y, a3u.y, rv);
+    p33[j][0] = qdiag(b3.x, a3.x, rv2);
+    p33[j][1] = qdiag(b3.y, a3.y, rv2);
   }
   __syncthreads();  // buffer 0 is refilled by the first prefetch
   int cur = 1, nxt = 2, pre = 0;
@@ -542,18 +542,18 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
       const float2 a1 = u1r[j], a1u = u1r[j + 1];
       const float2 a2 = u2r[j + 1], a2d = u2r[j];
       const float2 a3 = u3r[j], a3u = u3r[j + 1];
-      v11[j][0] = qdiag(a1.x, u1l[j], kd, kv2);
-      v11[j][1] = qdiag(a1.y, a1.x, kd, kv2);
-      v22[j][0] = qdiag(a2.x, a2d.x, kd, kv2);
-      v22[j][1] = qdiag(a2.y, a2d.y, kd, kv2);
-      v12[j][0] = qoff(a1.x, a1u.x, a2.x, a2.y, kd, kv);
-      v12[j][1] = qoff(a1.y, a1u.y, a2.y, u2r2[j], kd, kv);
-      v13[j][0] = qoff(a1.x, u1n[j].x, a3.x, a3.y, kd, kv);
-      v13[j][1] = qoff(a1.y, u1n[j].y, a3.y, u3r2[j], kd, kv);
-      v23[j][0] = qoff(a2.x, u2n[j].x, a3.x, a3u.x, kd, kv);
-      v23[j][1] = qoff(a2.y, u2n[j].y, a3.y, a3u.y, kd, kv);
-      v33[j][0] = qdiag(u3n[j].x, a3.x, kd, kv2);
-      v33[j][1] = qdiag(u3n[j].y, a3.y, kd, kv2);
+      v11[j][0] = qdiag(a1.x, u1l[j], rv2);
+      v11[j][1] = qdiag(a1.y, a1.x, rv2);
+      v22[j][0] = qdiag(a2.x, a2d.x, rv2);
+      v22[j][1] = qdiag(a2.y, a2d.y, rv2);
+      v12[j][0] = qoff(a1.x, a1u.x, a2.x, a2.y, rv);
+      v12[j][1] = qoff(a1.y, a1u.y, a2.y, u2r2[j], rv);
+      v13[j][0] = qoff(a1.x, u1n[j].x, a3.x, a3.y, rv);
+      v13[j][1] = qoff(a1.y, u1n[j].y, a3.y, u3r2[j], rv);
+      v23[j][0] = qoff(a2.x, u2n[j].x, a3.x, a3u.x, rv);
+      v23[j][1] = qoff(a2.y, u2n[j].y, a3.y, a3u.y, rv);
+      v33[j][0] = qdiag(u3n[j].x, a3.x, rv2);
+      v33[j][1] = qdiag(u3n[j].y, a3.y, rv2);
     }
     // stresses other threads read: s11 of column c0 (left neighbour), s12 of
     // column c0+1 and of row r0+1 (right neighbour, row above), s13 of column
@@ -574,24 +574,24 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
     // column QX+1)
     if (warp == 0) {
       for (int c = lane + 1; c <= QX; c += 32)
-        sm.s[2][0][c] = qoff(uc[0].r[0][c + 3], uc[0].r[1][c + 3], uc[1].r[0][c + 3], uc[1].r[0][c + 4], kd, kv);
+        sm.s[2][0][c] = qoff(uc[0].r[0][c + 3], uc[0].r[1][c + 3], uc[1].r[0][c + 3], uc[1].r[0][c + 4], rv);
     } else if (warp == 1) {
       for (int c = lane + 1; c <= QX; c += 32)
-        sm.s[4][0][c] = qoff(uc[1].r[0][c + 3], un[1].r[0][c + 3], uc[2].r[0][c + 3], uc[2].r[1][c + 3], kd, kv);
+        sm.s[4][0][c] = qoff(uc[1].r[0][c + 3], un[1].r[0][c + 3], uc[2].r[0][c + 3], uc[2].r[1][c + 3], rv);
     } else if (warp == 2) {
       for (int c = lane + 1; c <= QX; c += 32)
-        sm.s[1][QY + 1][c] = qdiag(uc[1].r[QY + 1][c + 3], uc[1].r[QY][c + 3], kd, kv2);
+        sm.s[1][QY + 1][c] = qdiag(uc[1].r[QY + 1][c + 3], uc[1].r[QY][c + 3], rv2);
     } else if (warp == 3) {
-      if (lane <= QY) sm.s[2][lane][0] = qoff(uc[0].r[lane][3], uc[0].r[lane + 1][3], uc[1].r[lane][3], uc[1].r[lane][4], kd, kv);
+      if (lane <= QY) sm.s[2][lane][0] = qoff(uc[0].r[lane][3], uc[0].r[lane + 1][3], uc[1].r[lane][3], uc[1].r[lane][4], rv);
     } else if (warp == 4) {
       if (lane < QY) {
         const int r = lane + 1;
-        sm.s[3][r][0] = qoff(uc[0].r[r][3], un[0].r[r][3], uc[2].r[r][3], uc[2].r[r][4], kd, kv);
+        sm.s[3][r][0] = qoff(uc[0].r[r][3], un[0].r[r][3], uc[2].r[r][3], uc[2].r[r][4], rv);
       }
     } else if (warp == 5) {
       if (lane < QY) {
         const int r = lane + 1;
-        sm.s[0][r][QX + 1] = qdiag(uc[0].r[r][QX + 4], uc[0].r[r][QX + 3], kd, kv2);
+        sm.s[0][r][QX + 1] = qdiag(uc[0].r[r][QX + 4], uc[0].r[r][QX + 3], rv2);
       }
     }
     __syncthreads();
@@ -622,14 +622,14 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
       float2* o3 = reinterpret_cast<float2*>(du3 + g);
       if (DOADD) {
         float2 a = *o1, b = *o2, c = *o3;
-        a.x -= d1[0]; a.y -= d1[1];
-        b.x -= d2[0]; b.y -= d2[1];
-        c.x -= d3[0]; c.y -= d3[1];
+        a.x -= kd * d1[0]; a.y -= kd * d1[1];
+        b.x -= kd * d2[0]; b.y -= kd * d2[1];
+        c.x -= kd * d3[0]; c.y -= kd * d3[1];
         *o1 = a; *o2 = b; *o3 = c;
       } else {
-        *o1 = make_float2(-d1[0], -d1[1]);
-        *o2 = make_float2(-d2[0], -d2[1]);
-        *o3 = make_float2(-d3[0], -d3[1]);
+        *o1 = make_float2(-kd * d1[0], -kd * d1[1]);
+        *o2 = make_float2(-kd * d2[0], -kd * d2[1]);
+        *o3 = make_float2(-kd * d3[0], -kd * d3[1]);
       }
     }
     if (kz + 1 < ptz && z + 1 < n) wait_plane(pre);

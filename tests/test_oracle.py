@@ -235,3 +235,24 @@ def test_paper_volavg_swap_closure_is_exact(doproject):
     assert ns.rel_l2(les2["swapfil"], ref) < 1e-13
     for k in ("nomodel", "classic", "swapfil_symm"):
         assert ns.rel_l2(les2[k], ref) > 1e-4, k
+
+
+@pytest.mark.parametrize("dtype,ui,mask", [(np.float64, np.uint64, 0x7FFFFFFFFFFFFFFF), (np.float32, np.uint32, 0x7FFFFFFF)])
+def test_magnitude_bit_maximum(dtype, ui, mask):
+    """The time step's max |u| is taken on the magnitude bits of the words:
+    for non-negative IEEE values the unsigned integer order is the numeric
+    order and NaN patterns sort above infinity, so the integer maximum is the
+    exact max |u| and a NaN propagates."""
+    rng = np.random.default_rng(0)
+    x = (rng.standard_normal(10000) * np.exp(rng.uniform(-30, 30, 10000))).astype(dtype)
+    x[:5] = [0.0, -0.0, np.finfo(dtype).tiny / 4, -np.finfo(dtype).max, np.finfo(dtype).tiny]
+
+    def bitmax(a):
+        return np.array([np.max(a.view(ui) & ui(mask))], dtype=ui).view(dtype)[0]
+
+    assert bitmax(x) == np.max(np.abs(x))
+    y = x.copy()
+    y[17] = -np.inf
+    assert bitmax(y) == np.inf
+    y[99] = np.nan
+    assert np.isnan(bitmax(y))

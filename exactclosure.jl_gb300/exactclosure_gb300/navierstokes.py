@@ -410,9 +410,11 @@ class DnsAid:
 
 
 def getsetup(**kw) -> dict:
-    """``getsetup`` (``src/N.jl:712-723``) with grid sizes the FFT of this
-    library supports (n = 2^a 3^b); keywords override."""
-    s = dict(l=1.0, n_dns=192, n_les=64, visc=2.0e-4, Δ_ratio=2, nσ=2, twarm=0.1, tstop=0.1, cfl=0.4,
+    """``getsetup`` (``src/N.jl:712-723``): the reference's defaults (DNS
+    500^3, LES 100^3, visc 2e-4, Gaussian width 2H with 2 sigmas), plus the
+    driver's warm-up/stop times, CFL and initial spectrum (``src/N.jl:1239-1262``);
+    keywords override."""
+    s = dict(l=1.0, n_dns=500, n_les=100, visc=2.0e-4, Δ_ratio=2, nσ=2, twarm=0.1, tstop=0.1, cfl=0.4,
              profile=("power", -5 / 3), seed=0)
     s.update(kw)
     return s
@@ -436,6 +438,39 @@ def dnsaid_project(setup: dict, stream=None) -> dict:
     out["errors"] = d.errors()
     d.close()
     return out
+
+
+def dns_aid_volavg(ustart: np.ndarray, n_les: int, viscosity: float, doproject: bool, tstop: float, cfl: float,
+                   l: float = 1.0, stream=None):
+    """``dns_aid_volavg`` (``src/NavierStokes.jl:141-304``) on the GPU: the
+    DNS from ``ustart`` and the four LES (no model, classic, swap,
+    swap-symmetric) in lockstep until ``tstop``.  Returns ``(u, relerr)`` like
+    the reference: ``u`` with ``dns_ref``, ``dns_fil`` and the four LES fields,
+    ``relerr`` with ``time`` and each LES's ``|v - fu| / |fu|`` recorded at
+    t = 0 and after every step."""
+    n = ustart.shape[1]
+    d = DnsAid(n, l, viscosity, n // n_les, None, stream)
+    d.set_velocity(ustart)
+    d.set_paper(doproject)
+    d.start()
+    names = PAPER_FIELDS[1:]
+    relerr = {k: [] for k in ("time",) + names}
+    t = 0.0
+    while True:
+        fu = d.get("fu")
+        nf = np.linalg.norm(fu.ravel())
+        relerr["time"].append(t)
+        for k in names:
+            relerr[k].append(float(np.linalg.norm((d.get(k) - fu).ravel()) / nf))
+        if t >= tstop:
+            break
+        d.step(tstop, cfl, max_steps=1)
+        t = d.time()[0]
+    u = {"dns_ref": d.velocity(), "dns_fil": d.get("fu")}
+    for k in names:
+        u[k] = d.get(k)
+    d.close()
+    return u, {k: np.asarray(v) for k, v in relerr.items()}
 
 
 def compute_errors(uaid: dict) -> dict:

@@ -87,6 +87,26 @@ def test_paper_volavg_driver_per_step(NS, doproject):
     d.close()
 
 
+def test_paper_volavg_host_driver(NS):
+    """The reference-shaped driver ``dns_aid_volavg(...) -> (u, relerr)``:
+    relative errors at t = 0 and after each step against the oracle's LES,
+    the swap closure on the filtered DNS to round-off."""
+    n, m, l, visc, cfl, tstop = 30, 10, 1.0, 1e-3, 0.4, 0.004
+    u0 = ns.randomfield(n, l, -5 / 3, 3, 1.0, profile="power")
+    u, rel_err = NS.dns_aid_volavg(u0, m, visc, True, tstop, cfl, l)
+    fu = ns.paper_volavg_target(u0, l, 3, True)
+    les = {k: fu.copy() for k in ns.PAPER_NAMES}
+    uo, les, t, it = ns.dns_aid_volavg_steps(u0, les, visc, l, 3, tstop, cfl, True)
+    assert len(rel_err["time"]) == it + 1 and abs(rel_err["time"][-1] - t) <= 1e-15
+    assert rel(u["dns_ref"], uo) < 1e-12
+    ref = ns.paper_volavg_target(uo, l, 3, True)
+    for k in ns.PAPER_NAMES:
+        assert rel(u[k], les[k]) < 1e-12, k
+        assert abs(rel_err[k][-1] - rel(les[k], ref)) <= 1e-10 * max(rel(les[k], ref), 1e-30) + 1e-14, k
+    assert rel_err["swapfil"].max() < 1e-13
+    assert rel_err["nomodel"][0] == 0.0 and rel_err["nomodel"][-1] > 1e-6
+
+
 def test_exact_closure_invariant_and_errors(NS):
     setup = NS.getsetup(n_dns=72, n_les=24, twarm=0.02, tstop=0.02, visc=1e-3)
     out = NS.dnsaid_project(setup)

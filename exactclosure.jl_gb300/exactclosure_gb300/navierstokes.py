@@ -440,6 +440,41 @@ def dnsaid_project(setup: dict, stream=None) -> dict:
     return out
 
 
+def testcase(n_dns: int, viscosity: float, seed: int = 123, l: float = 1.0, kpeak: float = 5.0,
+             compression=(5, 3), totalenergy: float = 0.5) -> dict:
+    """``testcase`` (``src/NavierStokes.jl:14-35``): a DNS grid with one LES
+    grid per compression ratio (each must divide ``n_dns``), the peak profile
+    with ``kpeak`` and ``totalenergy`` of the initial field, and its seed."""
+    if any(n_dns % c for c in compression):
+        raise ValueError("every compression must divide n_dns")
+    return dict(l=l, n_dns=n_dns, n_les=[n_dns // c for c in compression], compression=list(compression),
+                viscosity=viscosity, seed=seed, kpeak=kpeak, totalenergy=totalenergy)
+
+
+def smallcase() -> dict:
+    """``smallcase`` (``src/NavierStokes.jl:37-42``): DNS 90^3, LES 18^3 and 30^3."""
+    return testcase(n_dns=90, viscosity=5e-4)
+
+
+def mediumcase() -> dict:
+    """``mediumcase`` (``src/NavierStokes.jl:44-49``): DNS 510^3, LES 102^3 and 170^3."""
+    return testcase(n_dns=510, viscosity=5e-5)
+
+
+def largecase() -> dict:
+    """``largecase`` (``src/NavierStokes.jl:51-57``): DNS 810^3, LES 162^3 and 270^3."""
+    return testcase(n_dns=810, viscosity=2.5e-5)
+
+
+def case_for(tc: dict, cfl: float = 0.3, kind: str = "volume", precision: int = EXC_F64, stream=None) -> "Case":
+    """A device case for a ``testcase``: the DNS with its LES grids (filter
+    ``kind``) and the seeded peak-profile initial field."""
+    cs = Case(tc["n_dns"], tc["l"], tc["viscosity"], cfl, precision=precision,
+              les=[(c, kind) for c in tc["compression"]], stream=stream)
+    cs.init_random(tc["kpeak"], tc["totalenergy"], tc["seed"])
+    return cs
+
+
 def dns_aid_volavg(ustart: np.ndarray, n_les: int, viscosity: float, doproject: bool, tstop: float, cfl: float,
                    l: float = 1.0, stream=None):
     """``dns_aid_volavg`` (``src/NavierStokes.jl:141-304``) on the GPU: the

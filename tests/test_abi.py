@@ -52,3 +52,29 @@ def test_argument_validation_without_gpu(built_lib):
     assert built_lib.exc_case_create(C.byref(d), None, C.byref(h)) == 1  # EXC_ERR_ARG
     assert built_lib.exc_case_create(None, None, C.byref(h)) == 1
 
+
+
+def test_reference_test_cases():
+    """``smallcase`` / ``mediumcase`` / ``largecase`` (src/NavierStokes.jl:37-57):
+    DNS 90, 510, 810 with compression 5 and 3; every grid is an FFT size of
+    the library (radix 2, 3, 5 and 17 among them)."""
+    from exactclosure_gb300 import navierstokes as NS
+
+    cases = {"small": NS.smallcase(), "medium": NS.mediumcase(), "large": NS.largecase()}
+    assert [c["n_dns"] for c in cases.values()] == [90, 510, 810]
+    assert cases["medium"]["n_les"] == [102, 170] and cases["medium"]["viscosity"] == 5e-5
+    assert cases["large"]["n_les"] == [162, 270] and cases["small"]["n_les"] == [18, 30]
+
+    def fft_ok(n):
+        m = n
+        for f in (2, 3, 5, 7, 11, 13, 17):
+            while m % f == 0:
+                m //= f
+        return m == 1 and n % 2 == 0 and 4 <= n <= 1024
+
+    for c in cases.values():
+        assert all(fft_ok(n) for n in [c["n_dns"]] + c["n_les"])
+    import pytest
+
+    with pytest.raises(ValueError):
+        NS.testcase(n_dns=100, viscosity=1e-3, compression=(3,))

@@ -47,10 +47,13 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--serve-only", action="store_true")
+    ap.add_argument("--serve-steps", type=int, default=200, help="RK4 steps per solve of the serving stream")
+    ap.add_argument("--no-fp64-stream", action="store_true")
     ap.add_argument("--no-burgers", action="store_true")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
-    ap.add_argument("--only", default="", choices=["", "burgers", "large", "learned"],
+    ap.add_argument("--no-c1", action="store_true")
+    ap.add_argument("--only", default="", choices=["", "burgers", "large", "learned", "c1", "rhs"],
                     help="run one side workload alone and print its JSON object")
     ap.add_argument("--burgers-samples", type=int, default=1000)
     ap.add_argument("--burgers-tstop", type=float, default=0.1)
@@ -210,6 +213,81 @@ def forms_errors(n, les, kpeak, visc, nsteps, stream):
     ca.close()
     cb.close()
     return out
+
+
+def c1_section(nsteps=100, cpu=True):
+    """The plain-method configuration: DNS 128^3 FP64, nu = 1/2000, seeded
+    peak spectrum k0 = 4 with unit energy, RK4 at CFL 0.3 for 100 steps with
+    the exact closure every stage for a 32^3 volume-average LES (ratio 4).
+    All 100 steps are timed with CUDA events on the case's stream (inputs fit
+    in L2 at this size: 50 MB per vector field)."""
+    import torch
+
+    from exactclosure_gb300 import navierstokes as NS
+
+    n, les = 128, [(4, "volume")]
+    stream = torch.cuda.Stream()
+    cs = NS.Case(n, 1.0, 1 / 2000, 0.3, precision=0, les=les, stream=stream.cuda_stream)
+    cs.init_random(4.0, 1.0, seed=0)
+    cs.step(3)  # warm-up: graph capture
+    cs.sync()
+    cs.init_random(4.0, 1.0, seed=0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    cs.step(nsteps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cs.sync()
+    e_exact, e_nomo = cs.errors(0)
+    out = {"metric": "cell-updates/s", "value": n ** 3 * nsteps / (ms / 1e3), "unit": "cell-updates/s",
+           "dtype": "f64", "steps": nsteps, "ms_per_step": ms / nsteps, "t_end": cs.time()[0],
+           "config": {"workload": "DNS 128^3 FP64 RK4 CFL 0.3, nu 1/2000, k0 4, exact closure every stage for "
+                                  "LES 32^3 volume ratio 4", "timing": "CUDA events around all steps",
+                      "l2": "fields fit in L2 at this size"},
+           "les_errors_vs_filtered_dns": {"exact": e_exact, "nomodel": e_nomo}}
+    cs.close()
+    if cpu:
+        try:
+            from oracle import cpu_ref
+
+            r = cpu_ref.time_stages(n, les, 4.0, 1 / 2000, budget_s=6.0, max_stages=40)
+            out["cpu_baseline"] = {"value": r["cell_updates_per_s"], "unit": "cell-updates/s", "cores": r["threads"],
+                                   "kind": "port", "sample": r["sample"]}
+        except Exception as ex:
+            out["cpu_baseline"] = {"value": None, "sample": f"failed: {ex}"}
+    return out
+
+
+def rhs_section(args, launches=4):
+    """The RHS sweep alone on the workload's seeded field (no stepping):
+    `launches` launches timed with CUDA events; a small command for profiling
+    one launch of the sweep at full size."""
+    import torch
+
+    from exactclosure_gb300 import navierstokes as NS
+    from exactclosure_gb300._lib import call
+    import ctypes as C
+
+    prec = 0 if args.precision == "f64" else 1
+    n = args.n
+    dtype = torch.float64 if prec == 0 else torch.float32
+    stream = torch.cuda.Stream()
+    cs = NS.Case(n, 1.0, args.visc, 0.3, precision=prec, stream=stream.cuda_stream)
+    cs.init_random(args.kpeak, 1.0, seed=0)
+    cs.sync()
+    du = torch.empty((3, n, n, n), dtype=dtype, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(launches):
+        call("exc_tensordivergence", prec, n, 1.0, args.visc, C.c_void_p(cs.device_ptr()), C.c_void_p(du.data_ptr()),
+             0, C.c_void_p(stream.cuda_stream))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    cs.close()
+    return {"n": n, "precision": args.precision, "launches": launches, "ms_per_launch": e0.elapsed_time(e1) / launches}
 
 
 def large_section(n=1024, nsteps=30, every=10):
@@ -373,15 +451,26 @@ def serve_requests(nreq=96, rate=20.0, seed=0, nsteps=200):
     return [dict(t=float(t[i]), n=int(n[i]), visc=float(v[i]), seed=1000 + i, nsteps=nsteps) for i in range(nreq)]
 
 
-def serve_stream(precision=1, nreq=96, rate=20.0, nsteps=200):
-    """Replay the stream in real time through the serving form; returns
-    aggregate cell-updates/s and solve-latency percentiles."""
+def _latency_summary(res, nreq):
     import numpy as np
 
+    lat = np.array([r["t_finish"] - r["t_submit"] for r in res])
+    t_first = min(r["t_submit"] for r in res)
+    t_last = max(r["t_finish"] for r in res)
+    cells = sum(r["n"] ** 3 * r["nsteps"] for r in res)
+    return {"value": cells / (t_last - t_first), "unit": "cell-updates/s", "solves": len(res),
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "makespan_s": t_last - t_first}
+
+
+def serve_stream(precision=1, nreq=96, rate=20.0, nsteps=200, max_active_per_size=0):
+    """Replay the stream in real time through the serving form; returns
+    aggregate cell-updates/s and solve-latency percentiles (latency = finish
+    on the GPU clock minus arrival)."""
     from exactclosure_gb300 import serving
 
     reqs = serve_requests(nreq, rate, nsteps=nsteps)
-    sv = serving.Server(precision=precision, mem_fraction=0.6)
+    sv = serving.Server(precision=precision, mem_fraction=0.6, max_active_per_size=max_active_per_size)
     # warm the per-size batches (allocation, autotuning, graph capture) untimed
     for n in SERVE_SIZES:
         sv.submit(n, 1 / 1000, 1, seed=1)
@@ -404,50 +493,70 @@ def serve_stream(precision=1, nreq=96, rate=20.0, nsteps=200):
                 done[r["id"]] = r
         if active == 0 and queued == 0 and i < nreq:
             time.sleep(max(0.0, min(0.01, reqs[i]["t"] - (time.perf_counter() - t0))))
-    res = list(done.values())
-    lat = np.array([r["t_finish"] - r["t_submit"] for r in res])
-    t_first = min(r["t_submit"] for r in res)
-    t_last = max(r["t_finish"] for r in res)
-    cells = sum(r["n"] ** 3 * r["nsteps"] for r in res)
     st = sv.stats()
     sv.close()
-    return {"value": cells / (t_last - t_first), "unit": "cell-updates/s", "solves": len(res),
-            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-            "makespan_s": t_last - t_first, "ticks": st["ticks"], "chunks": st["chunks"],
-            "dtype": "f32 (FP64 spectral divide and diagnostics)" if precision == 1 else "f64",
-            "stream": f"{nreq} solves, Poisson arrivals {rate}/s (seed 0), n in {list(SERVE_SIZES)}, "
-                      f"visc in {{1/1000, 1/2000, 1/4000}}, {nsteps} RK4 steps each"}
+    out = _latency_summary(list(done.values()), nreq)
+    out.update({"ticks": st["ticks"], "chunks": st["chunks"],
+                "admission": f"at most {max_active_per_size} active solves per grid size" if max_active_per_size
+                else "every request admitted as memory and slots allow",
+                "dtype": "f32 (FP64 spectral divide and diagnostics)" if precision == 1 else "f64",
+                "stream": f"{nreq} solves, Poisson arrivals {rate}/s (seed 0), n in {list(SERVE_SIZES)}, "
+                          f"visc in {{1/1000, 1/2000, 1/4000}}, {nsteps} RK4 steps each"})
+    return out
 
 
-def plain_fp64_stream_sample(nsteps=8):
-    """The plain FP64 path on the same stream: each grid size of the stream
-    timed alone through the case API (one solve at a time, no batching), then
-    the stream's own mix weighted in -- total cell-updates over the sum of
-    each request's cell-updates divided by its size's rate (arrival gaps not
-    counted, which favours the plain path)."""
+def plain_fp64_stream(nreq=96, rate=20.0, nsteps=200):
+    """The same stream through the plain FP64 path: one solve at a time
+    through the case API (no batching, no overlap), in arrival order, each
+    started when it has arrived and the previous solve has finished (seeded
+    initial field on the GPU, 200 RK4 steps, device synchronised).  Cases are
+    created and their step graphs captured per (size, viscosity) before the
+    stream starts.  Latency = finish minus arrival."""
     import torch
 
     from exactclosure_gb300 import navierstokes as NS
 
-    reqs = serve_requests()
-    rate = {}
-    for n in SERVE_SIZES:
-        q = next(r for r in reqs if r["n"] == n)
-        cs = NS.Case(n, 1.0, q["visc"], 0.3, precision=0)
+    reqs = serve_requests(nreq, rate, nsteps=nsteps)
+    stream = torch.cuda.Stream()
+    cases = {}
+    for q in reqs:
+        key = (q["n"], q["visc"])
+        if key not in cases:
+            cs = NS.Case(q["n"], 1.0, q["visc"], 0.3, precision=0, stream=stream.cuda_stream)
+            cs.init_random(4.0, 1.0, 1)
+            cs.step(1)
+            cs.sync()
+            cases[key] = cs
+    res = []
+    t0 = time.perf_counter()
+    for q in reqs:
+        now = time.perf_counter() - t0
+        if now < q["t"]:
+            time.sleep(q["t"] - now)
+        cs = cases[(q["n"], q["visc"])]
         cs.init_random(4.0, 1.0, q["seed"])
-        cs.step(1)
+        cs.step(q["nsteps"])
         cs.sync()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        cs.step(nsteps)
-        cs.sync()
-        rate[n] = n ** 3 * nsteps / (time.perf_counter() - t0)
+        res.append({"t_submit": q["t"], "t_finish": time.perf_counter() - t0, "n": q["n"], "nsteps": q["nsteps"]})
+    for cs in cases.values():
         cs.close()
-    cells = sum(r["n"] ** 3 * r["nsteps"] for r in reqs)
-    seconds = sum(r["n"] ** 3 * r["nsteps"] / rate[r["n"]] for r in reqs)
-    return {"value": cells / seconds, "unit": "cell-updates/s", "per_size": {str(k): v for k, v in rate.items()},
-            "sample": f"each stream size alone ({nsteps} RK4 steps, FP64), weighted by the stream's "
-                      f"{len(reqs)} requests x {reqs[0]['nsteps']} steps"}
+    torch.cuda.empty_cache()
+    out = _latency_summary(res, nreq)
+    out.update({"dtype": "f64", "path": "case API (exc_case_*), one solve at a time in arrival order",
+                "stream": f"{nreq} solves, Poisson arrivals {rate}/s (seed 0), n in {list(SERVE_SIZES)}, "
+                          f"visc in {{1/1000, 1/2000, 1/4000}}, {nsteps} RK4 steps each"})
+    return out
+
+
+def workload_config(args, world=1):
+    """The workload's `config` object, identical on both arms."""
+    les = les_list(args.les)
+    n = args.n
+    return {"workload": f"DNS {n}^3 RK4 (4 FFT projections/step) + exact closure at every stage "
+                        f"for LES {', '.join(f'{n // c}^3 {k} ratio {c}' for c, k in les)}",
+            "n": n, "visc": args.visc, "kpeak": args.kpeak, "cfl": 0.3, "les": args.les,
+            "l2": "inputs larger than L2 (each field >= 0.5 GB)",
+            "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args):
@@ -460,7 +569,7 @@ def run_reference(args):
     if cpu_ref.available():
         # one "step" of the reference arm = one RK4 stage of the full workload
         # (a quarter of an RK4 step) on all host threads
-        cs = cpu_ref.timing_case(args.n, les, args.visc)
+        cs = cpu_ref.timing_case(args.n, les, args.visc, args.kpeak)
         for s in range(args.warmup):
             cs.stage(1 + s % 3)
         t0 = time.perf_counter()
@@ -484,8 +593,7 @@ def run_reference(args):
         "impl": "reference", "metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded spectral initial condition)",
-        "config": {"workload": f"DNS {args.n}^3 RK4 + exact closure LES {args.les}", "n": args.n,
-                   "les": args.les, "kpeak": args.kpeak, "visc": args.visc},
+        "config": workload_config(args, int(os.environ.get("WORLD_SIZE", "1"))),
         "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": info["cores"], "kind": info["kind"],
                          "sample": info["sample"]},
         "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -521,11 +629,19 @@ def main():
         pk = measured_peaks()
         fn = {"burgers": lambda: burgers_section(args.burgers_samples, cpu=not args.no_cpu, tstop=args.burgers_tstop),
               "large": lambda: large_section(nsteps=args.large_steps),
-              "learned": lambda: learned_section(args.learned_steps, peaks_json=pk)}[args.only]
+              "learned": lambda: learned_section(args.learned_steps, peaks_json=pk),
+              "c1": lambda: c1_section(cpu=not args.no_cpu),
+              "rhs": lambda: rhs_section(args)}[args.only]
         print(json.dumps({args.only: fn()}))
         return
     if args.serve_only:
-        served = serve_stream(precision=0 if args.precision == "f64" else 1, nsteps=args.steps)
+        served = serve_stream(precision=1, nsteps=args.serve_steps)
+        served["bounded_admission"] = serve_stream(precision=1, nsteps=args.serve_steps, max_active_per_size=2)
+        if not args.no_fp64_stream:
+            plain = plain_fp64_stream(nsteps=args.serve_steps)
+            served["plain_fp64_same_stream"] = plain
+            served["served_over_plain_fp64"] = served["value"] / plain["value"]
+            served["p99_plain_over_served"] = plain["p99_latency_s"] / served["p99_latency_s"]
         print(json.dumps({"serving": served}))
         return
     prec = 0 if args.precision == "f64" else 1
@@ -626,14 +742,21 @@ def main():
         if not args.no_serve:
             try:
                 served = serve_stream(precision=1)
-                plain = plain_fp64_stream_sample()
+                served["bounded_admission"] = serve_stream(precision=1, max_active_per_size=2)
+                plain = plain_fp64_stream()
                 served["plain_fp64_same_stream"] = plain
                 served["served_over_plain_fp64"] = served["value"] / plain["value"]
+                served["p99_plain_over_served"] = plain["p99_latency_s"] / served["p99_latency_s"]
                 serving_line = served
             except Exception as ex:
                 serving_line = {"error": str(ex)}
 
-    large = learned = None
+    large = learned = c1 = None
+    if rank == 0 and world == 1 and not args.no_c1:
+        try:
+            c1 = c1_section(cpu=not args.no_cpu)
+        except Exception as ex:
+            c1 = {"error": str(ex)}
     if rank == 0 and world == 1 and not args.no_large:
         try:
             large = large_section(nsteps=args.large_steps)
@@ -665,17 +788,14 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
             "data": "synthetic (seeded spectral initial condition, E(k) ~ k^4 exp(-2(k/k0)^2), unit energy)",
-            "config": {"workload": f"DNS {n}^3 RK4 (4 FFT projections/step) + exact closure at every stage "
-                                   f"for LES {', '.join(f'{n // c}^3 {k} ratio {c}' for c, k in les)}",
-                       "n": n, "visc": args.visc, "kpeak": args.kpeak, "cfl": 0.3, "les": args.les,
-                       "l2": "inputs larger than L2 (each field >= 0.5 GB)",
-                       "parallelism": f"replicas x{world}"},
+            "config": workload_config(args, world),
             "gpu_launches": launches * args.steps,
             "clocks": clk.summary(),
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "forms": forms,
+            "c1": c1,
             "serving": serving_line,
             "burgers": burgers,
             "large": large,
@@ -686,9 +806,46 @@ def main():
         dist.destroy_process_group()
 
 
+# Algorithmic FP64 operations per cell of one RHS sweep (stresstensor +
+# tensordivergence, src/N.jl:94-160), an FMA counted as two: each of the
+# three off-diagonal stresses 1/4 (u_i + u_i')(u_j + u_j') - (nu/h)(du_i + du_j)
+# takes 9 (two sums, the product, three differences and sums, a multiply and
+# an FMA), each diagonal stress 6; the divergence of each of the three
+# components takes three differences, two sums and the 1/h scaling (6).
+RHS_FLOPS_PER_CELL = 3 * 9 + 3 * 6 + 3 * 6
+
+
+def dgemm_peak(reps=5, size=8192):
+    """The FP64 ceiling of this GPU, measured: cuBLAS DGEMM size^3, best of
+    `reps` launches (CUDA events), with the SM clock sampled meanwhile."""
+    import torch
+
+    a = torch.randn(size, size, dtype=torch.float64, device="cuda")
+    b = torch.randn(size, size, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = None
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(reps):
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record()
+            torch.matmul(a, b)
+            f1.record()
+            torch.cuda.synchronize()
+            t = f0.elapsed_time(f1) / 1e3
+            best = t if best is None else min(best, t)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2 * size ** 3 / best / 1e12, clk.summary(), f"cuBLAS DGEMM {size}^3, best of {reps} (CUDA events), this run"
+
+
 def roofline(cs, NS, n, prec, args, stream):
-    """Time the RHS sweep (stresstensor + tensordivergence) alone with CUDA
-    events on its stream, on the case's own device velocity."""
+    """The dominant kernel of the step, the RHS sweep (stresstensor +
+    tensordivergence), timed alone with CUDA events on its own stream, on the
+    case's device velocity.  In FP64 it is bound by the FP64 pipe: achieved
+    = algorithmic FP64 operations per launch / launch time, against the DGEMM
+    rate measured in the same run; its HBM figures sit beside.  In FP32 it
+    is bound by HBM: achieved = algorithmic bytes / launch time."""
     import torch
 
     hbm, src = peaks()
@@ -715,32 +872,10 @@ def roofline(cs, NS, n, prec, args, stream):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
+    del du
     alg_bytes = 6 * N * w  # read u (3 words), write du (3 words) per cell
-    achieved = alg_bytes / (ms / 1e3) / 1e9
-    # 6 stresses (45 flops) + their share of halo stresses (~4) + divergence
-    # and store (18): about 67 flops per cell, FMA counted as 2
-    flops = 67 * N
-    fp64 = None
-    if prec == 0:
-        # FP64 ceiling of this GB300, measured: cuBLAS DGEMM 4096^3, best of 3
-        a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
-        b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
-        torch.matmul(a, b)
-        best = None
-        for _ in range(3):
-            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            f0.record()
-            torch.matmul(a, b)
-            f1.record()
-            torch.cuda.synchronize()
-            t = f0.elapsed_time(f1) / 1e3
-            best = t if best is None else min(best, t)
-        dgemm = 2 * 4096 ** 3 / best / 1e12
-        ach = flops / (ms / 1e3) / 1e12
-        fp64 = {"achieved_tflops": ach, "peak_tflops": dgemm, "frac": ach / dgemm,
-                "peak_source": "measured here: cuBLAS DGEMM 4096^3",
-                "note": "the FP64 form is bound by the FP64 pipe, not by HBM (see frac above)"}
-        del a, b
+    gbs = alg_bytes / (ms / 1e3) / 1e9
+    flops = RHS_FLOPS_PER_CELL * N
     traffic = None
     tp = ROOT / "profiles" / "rhs_traffic.json"
     if tp.exists():
@@ -748,9 +883,20 @@ def roofline(cs, NS, n, prec, args, stream):
         key = f"{'f64' if prec == 0 else 'f32'}_{n}"
         if key in d:
             traffic = d[key]
-    return {"kernel": "rhs_kernel (stress + divergence sweep)", "bound": "hbm", "achieved": achieved,
-            "peak": hbm, "peak_source": src, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-            "ms_per_launch": ms, "algorithmic_bytes_per_launch": alg_bytes, "fp64": fp64}
+    hbm_part = {"achieved": gbs, "peak": hbm, "peak_source": src, "unit": "GB/s", "frac": gbs / hbm,
+                "algorithmic_bytes_per_launch": alg_bytes}
+    common = {"kernel": "rhs_kernel (stress + divergence sweep)", "ms_per_launch": ms, "traffic": traffic,
+              "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one launch at this size (ncu), "
+                              "bytes per launch"}
+    if prec == 0:
+        dgemm, dclk, dsrc = dgemm_peak()
+        ach = flops / (ms / 1e3) / 1e12
+        return {**common, "bound": "fp64", "achieved": ach, "peak": dgemm, "peak_source": dsrc,
+                "peak_clocks": dclk, "unit": "TFLOP/s", "frac": ach / dgemm,
+                "algorithmic_flops_per_launch": flops, "flops_per_cell": RHS_FLOPS_PER_CELL,
+                "hbm": hbm_part}
+    return {**common, "bound": "hbm", **hbm_part,
+            "fp32": {"achieved_tflops": flops / (ms / 1e3) / 1e12, "flops_per_cell": RHS_FLOPS_PER_CELL}}
 
 
 if __name__ == "__main__":

@@ -132,7 +132,10 @@ int exc_poisson_destroy(exc_poisson* ps) {
 
 int exc_poisson_set_engine(exc_poisson* ps, int engine) {
   if (!ps) { set_last_error("null solver"); return EXC_ERR_ARG; }
-  if (engine != 0 && engine != 1) { set_last_error("engine must be 0 (register passes where planned) or 1 (Stockham)"); return EXC_ERR_ARG; }
+  if (engine < 0 || engine > 2) {
+    set_last_error("engine must be 0 (default), 1 (Stockham passes) or 2 (register passes, no mixed precision)");
+    return EXC_ERR_ARG;
+  }
   ps->engine = engine;
   return EXC_OK;
 }

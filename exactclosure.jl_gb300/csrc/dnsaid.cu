@@ -4,7 +4,10 @@
 // and its symmetrised form -- stepped in lockstep with the DNS time step.
 // A second mode runs the paper's volume-average driver `dns_aid_volavg`
 // (src/NavierStokes.jl:141-304) with four LES: no model, classic (volume-
-// filtered flux), swap (face-filtered flux) and its symmetric part.
+// filtered flux), swap (face-filtered flux) and its symmetric part; a third
+// its surface-average driver `dns_aid_surface` (src/NavierStokes.jl:306-468):
+// the same four LES on the face-filtered DNS, classic with the surface-
+// filtered flux, swap with the line-filtered flux off the diagonal.
 //
 // Every operator is a libexc kernel (stress/divergence, FFT projection,
 // filtered fluxes); this file holds the driver, two pointwise tensor kernels
@@ -42,11 +45,13 @@ struct exc_dnsaid {
   double* spec = nullptr;  // init scratch: 3 spectral arrays
   double* pl = nullptr;    // LES pressure M (paper mode)
   double* dsig = nullptr;  // closure divergence 3M (paper mode)
+  double* rc9 = nullptr;   // surface-filtered flux 9M (surface mode)
   double t = 0;
   int steps = 0;
   bool started = false;
   bool paper = false;      // dns_aid_volavg instead of dnsaid_project
   bool doproject = true;   // its `doproject`
+  bool surface = false;    // dns_aid_surface instead of dns_aid_volavg
 };
 
 namespace exc {
@@ -210,14 +215,18 @@ int lockstep(exc_dnsaid* d, double dt) {
 }
 
 // `fu` of dns_aid_volavg (src/NavierStokes.jl:169-170, 290-291): the volume
-// filter of the DNS, projected when `doproject`.
+// filter of the DNS, projected when `doproject`; `fiu` of dns_aid_surface
+// (src/NavierStokes.jl:333, 449): the face filter, divergence free on the
+// LES grid and never projected.
 int paper_target(exc_dnsaid* d, double* out) {
-  int rc = filter_vector<double>(d->n, d->c, EXC_FILTER_VOLUME, fd(d), nfd(d), d->u, out, d->st);
-  if (rc || !d->doproject) return rc;
+  int rc = filter_vector<double>(d->n, d->c, d->surface ? EXC_FILTER_FACE : EXC_FILTER_VOLUME, fd(d), nfd(d), d->u,
+                                 out, d->st);
+  if (rc || !d->doproject || d->surface) return rc;
   return cuda_rc(project(&d->psl, out, d->st));
 }
 
-// One step of dns_aid_volavg (src/NavierStokes.jl:186-288).
+// One step of dns_aid_volavg (src/NavierStokes.jl:186-288) or of
+// dns_aid_surface (src/NavierStokes.jl:350-452).
 int lockstep_paper(exc_dnsaid* d, double dt) {
   const int n = d->n, m = d->m, c = d->c;
   const long long N3 = 3LL * n * n * n, M = (long long)m * m * m;
@@ -227,9 +236,17 @@ int lockstep_paper(exc_dnsaid* d, double dt) {
   if (e == cudaSuccess) e = project(&d->psd, d->du, st);
   if (e == cudaSuccess) e = copy_pressure<double>(&d->psd, d->p, st);
   if (e != cudaSuccess) return cuda_rc(e);
-  // fru: volume-filtered r (sdh); firu: face-filtered r (r9)
-  int rc = filtered_stress<double>(n, c, d->l, d->visc, fd(d), nfd(d), d->u, d->sdh, st, d->p);
-  if (!rc) rc = closure_flux<double>(n, c, d->l, d->visc, fd(d), nfd(d), d->u, d->p, d->r9, st);
+  // volume: fru = volume-filtered r (sdh), firu = face-filtered r (r9);
+  // surface: firu = surface-filtered r (rc9), swap flux = firu on the
+  // diagonal, line-filtered r off it (r9)
+  int rc;
+  if (d->surface) {
+    rc = surface_flux<double>(n, c, d->l, d->visc, fd(d), nfd(d), d->u, d->p, d->rc9, false, st);
+    if (!rc) rc = surface_flux<double>(n, c, d->l, d->visc, fd(d), nfd(d), d->u, d->p, d->r9, true, st);
+  } else {
+    rc = filtered_stress<double>(n, c, d->l, d->visc, fd(d), nfd(d), d->u, d->sdh, st, d->p);
+    if (!rc) rc = closure_flux<double>(n, c, d->l, d->visc, fd(d), nfd(d), d->u, d->p, d->r9, st);
+  }
   // fu and rfu = sigma_H(fu) + p_H I, p_H from the LES right-hand side of fu
   if (!rc) rc = paper_target(d, d->ub);
   if (rc) return rc;
@@ -238,8 +255,10 @@ int lockstep_paper(exc_dnsaid* d, double dt) {
   if (e == cudaSuccess) e = poisson_solve_inplace<double>(&d->psl, d->dul, true, st);
   if (e == cudaSuccess) e = copy_pressure<double>(&d->psl, d->pl, st);
   if (e == cudaSuccess) { add_diag_kernel<<<gridsz(M), 256, 0, st>>>(M, d->sl, d->pl); e = cudaGetLastError(); }
-  // closures: classic fru - rfu (sc), swap firu - rfu (r9), its symmetric part (sdh)
-  if (e == cudaSuccess) { combine6_kernel<<<gridsz(6 * M), 256, 0, st>>>(6 * M, d->sdh, nullptr, d->sl, d->sc); e = cudaGetLastError(); }
+  // closures: classic fru - rfu (sc; surface: firu - rfiu in rc9), swap
+  // firu - rfu (r9), its symmetric part (sdh)
+  if (e == cudaSuccess && !d->surface) { combine6_kernel<<<gridsz(6 * M), 256, 0, st>>>(6 * M, d->sdh, nullptr, d->sl, d->sc); e = cudaGetLastError(); }
+  if (e == cudaSuccess && d->surface) { sub_sym_kernel<<<gridsz(M), 256, 0, st>>>(M, d->rc9, d->sl); e = cudaGetLastError(); }
   if (e == cudaSuccess) { sub_sym_kernel<<<gridsz(M), 256, 0, st>>>(M, d->r9, d->sl); e = cudaGetLastError(); }
   if (e == cudaSuccess) { symmetrize_kernel<<<gridsz(M), 256, 0, st>>>(M, d->r9, d->sdh); e = cudaGetLastError(); }
   // DNS step
@@ -250,8 +269,8 @@ int lockstep_paper(exc_dnsaid* d, double dt) {
   if (e != cudaSuccess) return cuda_rc(e);
   rc = les_update(d, d->les[0], d->sl, nullptr, nullptr, dt);
   // classic, swap, swap-symmetric: v += dt P(RHS_H(v)); v += dt dsigma; project
-  const double* sig[3] = {d->sc, d->r9, d->sdh};
-  const int ncomp[3] = {6, 9, 6};
+  const double* sig[3] = {d->surface ? d->rc9 : d->sc, d->r9, d->sdh};
+  const int ncomp[3] = {d->surface ? 9 : 6, 9, 6};
   for (int k = 0; k < 3 && !rc; ++k) {
     double* v = d->les[k + 1];
     e = launch_stress<double>(m, d->H, d->visc, v, d->sl, st);
@@ -289,7 +308,7 @@ int exc_dnsaid_create(const exc_dnsaid_desc* desc, void* stream, exc_dnsaid** ou
   *out = nullptr;
   const int n = desc->n, c = desc->ratio;
   if (!fft_size_ok(n)) { set_last_error("grid size must be 2^a 3^b 5^c 7^d 11^e 13^f 17^g, a >= 1, 4 <= n <= 1024"); return EXC_ERR_SHAPE; }
-  if (c < 1 || n % c || c % 2 == 0) { set_last_error("ratio must be odd and divide n (classic closure)"); return EXC_ERR_RATIO; }
+  if (c < 1 || n % c) { set_last_error("ratio must divide n"); return EXC_ERR_RATIO; }
   if (!fft_size_ok(n / c)) { set_last_error("LES grid n/ratio must be an FFT size"); return EXC_ERR_SHAPE; }
   if (!(desc->l > 0) || !(desc->visc > 0)) { set_last_error("l and visc must be positive"); return EXC_ERR_ARG; }
   if (desc->nfdelta > 1 && (!desc->fdelta || desc->nfdelta % 2 == 0)) { set_last_error("fdelta must have odd length"); return EXC_ERR_ARG; }
@@ -330,7 +349,7 @@ int exc_dnsaid_destroy(exc_dnsaid* d) {
   poisson_free(&d->psd);
   poisson_free(&d->psl);
   double* bufs[] = {d->u, d->du, d->p, d->ub, d->dul, d->sdh, d->s2, d->r9, d->sl, d->sc, d->zero, d->scal,
-                    d->part, d->spec, d->pl, d->dsig};
+                    d->part, d->spec, d->pl, d->dsig, d->rc9};
   for (double* b : bufs) cudaFree(b);
   for (double* b : d->les) cudaFree(b);
   delete d;
@@ -394,12 +413,30 @@ int exc_dnsaid_set_paper(exc_dnsaid* d, int doproject) {
   if (!d) { set_last_error("null handle"); return EXC_ERR_ARG; }
   if (d->started) { set_last_error("the driver is chosen before exc_dnsaid_start"); return EXC_ERR_STATE; }
   d->paper = true;
+  d->surface = false;
+  d->doproject = doproject != 0;
+  return EXC_OK;
+}
+
+int exc_dnsaid_set_surface(exc_dnsaid* d, int doproject) {
+  if (!d) { set_last_error("null handle"); return EXC_ERR_ARG; }
+  if (d->started) { set_last_error("the driver is chosen before exc_dnsaid_start"); return EXC_ERR_STATE; }
+  if (!d->rc9) {
+    int rc = dalloc(&d->rc9, 9ull * d->m * d->m * d->m);
+    if (rc) return rc;
+  }
+  d->paper = true;
+  d->surface = true;
   d->doproject = doproject != 0;
   return EXC_OK;
 }
 
 int exc_dnsaid_start(exc_dnsaid* d) {
   if (!d) { set_last_error("null handle"); return EXC_ERR_ARG; }
+  if (!d->paper && d->c % 2 == 0) {
+    set_last_error("dnsaid_project's classic closure needs an odd ratio (its fine-grid filter is odd-only)");
+    return EXC_ERR_RATIO;
+  }
   int rc = d->paper ? paper_target(d, d->ub) : apply_dhpi(d, d->ub);
   if (rc) return rc;
   const size_t M3 = 3ull * d->m * d->m * d->m;
@@ -480,6 +517,25 @@ int exc_dnsaid_errors(exc_dnsaid* d, double out[5]) {
     // `compute_errors` (src/N.jl:1334-1349): sqrt(mean_i |a_i - b_i|^2 / |b_i|^2)
     if (e == cudaSuccess) out[k] = std::sqrt((ha[0] / hs[0] + ha[1] / hs[1] + ha[2] / hs[2]) / 3);
   }
+  return cuda_rc(e);
+}
+
+int exc_dnsaid_relerr(exc_dnsaid* d, double out[4]) {
+  if (!d || !out) { set_last_error("null argument"); return EXC_ERR_ARG; }
+  if (!d->started || !d->paper) { set_last_error("call exc_dnsaid_set_paper/set_surface and exc_dnsaid_start first"); return EXC_ERR_STATE; }
+  int rc = paper_target(d, d->ub);
+  if (rc) return rc;
+  const long long M = (long long)d->m * d->m * d->m;
+  double* part = d->part + SHELL_BLOCKS * 1024 + 2048;
+  // scal[0]: |fu|^2; scal[1 + k]: |v_k - fu|^2, each over the 3 M words
+  cudaError_t e = launch_sqdiff<double>(3 * M, d->ub, nullptr, part, d->scal, d->st);
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+    e = launch_sqdiff<double>(3 * M, d->les[k], d->ub, part, d->scal + 1 + k, d->st);
+  double hs[5];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hs, d->scal, sizeof(hs), cudaMemcpyDeviceToHost, d->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+  if (e == cudaSuccess)
+    for (int k = 0; k < 4; ++k) out[k] = std::sqrt(hs[1 + k] / hs[0]);
   return cuda_rc(e);
 }
 

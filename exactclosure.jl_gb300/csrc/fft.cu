@@ -388,7 +388,11 @@ static cudaError_t stockham_solve(exc_poisson* ps, const T* src, bool src_is_vec
 template <typename T>
 cudaError_t poisson_solve_inplace(exc_poisson* ps, const T* src, bool src_is_vector, cudaStream_t st,
                                   const SlotBatch& sb, int nslots) {
-  if (ps->engine == 0 && ps->twl_n && ps->twl_h && ps->invlap)
+  if constexpr (sizeof(T) == 8) {
+    if (ps->engine == 0 && ps->mix && nslots == 1 && !sb.active)
+      return fftmix_solve(ps, reinterpret_cast<const double*>(src), src_is_vector, st);
+  }
+  if (ps->engine != 1 && ps->twl_n && ps->twl_h && ps->invlap)
     return fftreg_solve(ps, src, src_is_vector, st, sb, nslots);
   if (plan_ext(ps->plan_n) || plan_ext(ps->plan_h))
     return stockham_solve<T, true>(ps, src, src_is_vector, st, sb, nslots);
@@ -493,6 +497,7 @@ cudaError_t configure_fft() {
   if (e == cudaSuccess) e = configure_fft_t<float, true>();
   if (e == cudaSuccess) e = configure_fftreg_f64();
   if (e == cudaSuccess) e = configure_fftreg_f32();
+  if (e == cudaSuccess) e = configure_fftmix();
   return e;
 }
 
@@ -583,6 +588,24 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
     const int rc = precision == EXC_F64 ? alloc_level_tables<double2>(ps) : alloc_level_tables<float2>(ps);
     if (rc) { poisson_free(ps); return rc; }
   }
+  if (precision == EXC_F64 && !work && fftmix_supported(n)) {
+    // the mixed-precision solve's FP32 inner solver, with the factor 1/h of
+    // the unscaled FP64 divergence folded into its divide table
+    ps->mix = new exc_poisson;
+    int rc = poisson_init(ps->mix, EXC_F32, n, l, nullptr);
+    if (rc) { poisson_free(ps); return rc; }
+    const long long tot = (long long)(n / 2 + 1) * (n / 2 + 1) * (n / 2 + 1);
+    const double coef_mix = -ps->h / (4.0 * (double)n * (double)n * (double)n);
+    const int blocks = (int)std::min<long long>((tot + 255) / 256, 152LL * 32);
+    invlap_kernel<<<blocks, 256>>>(n, ps->mix->sin2, coef_mix, ps->mix->invlap);
+    invlap_split_kernel<<<blocks, 256>>>(tot, ps->mix->invlap);
+    if (cudaMalloc(&ps->mix_d, (size_t)n * n * n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&ps->mix_part, (size_t)fftmix_part_words(n) * sizeof(double)) != cudaSuccess) {
+      set_last_error("out of device memory (mixed-precision poisson buffers)");
+      poisson_free(ps);
+      return EXC_ERR_OOM;
+    }
+  }
   size_t wbytes = (size_t)n * n * ps->P * csz;
   if (work) {
     ps->work = work;
@@ -601,6 +624,14 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
 }
 
 void poisson_free(exc_poisson* ps) {
+  if (ps->mix) {
+    poisson_free(ps->mix);
+    delete ps->mix;
+    ps->mix = nullptr;
+  }
+  if (ps->mix_d) cudaFree(ps->mix_d);
+  if (ps->mix_part) cudaFree(ps->mix_part);
+  ps->mix_d = ps->mix_part = nullptr;
   if (ps->tw) cudaFree(ps->tw);
   if (ps->sin2) cudaFree(ps->sin2);
   if (ps->invlap) cudaFree(ps->invlap);

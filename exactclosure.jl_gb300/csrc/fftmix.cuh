@@ -1,0 +1,375 @@
+// FP64 Poisson solve by mixed-precision iterative refinement.
+//
+// The FP64 pressure solve of `project!` (src/N.jl:256-307) computes p with
+// L_h p = d, d = div(u), on the GPU's FP64 pipe, which on GB300 retires about
+// two operations per clock per SM: the FFT passes of a 512^3 solve are bound
+// by it.  This solve instead runs the FFTs in FP32 (register-resident passes
+// of fftreg.cuh, bound by HBM) and recovers FP64 accuracy by refinement with
+// residuals formed in FP64:
+//
+//   p  = S32(d)
+//   p += S32(d - L_h p)          (twice)
+//
+// where S32 is the FP32 spectral solve (relative error about 1e-7) and L_h
+// the 7-point staggered Laplacian, (sum of the 6 neighbours - 6 p) / h^2,
+// whose eigenvalues are the spectral solver's -4/h^2 sum sin^2(pi k/n).  Each
+// correction shrinks the error by about the FP32 solve's relative error, so
+// after two corrections p agrees with the FP64 FFT solve to FP64 rounding
+// (about 1e-15 relative for smooth and for white-noise right-hand sides).
+// The divergence is formed once in FP64 and kept (unscaled by 1/h: the FP32
+// solves carry the factor 1/h in their 1/(lambda N) table); the pressure's
+// mean (the solution's free constant, which the FP32 solves leave at their
+// rounding level) is measured during the last residual pass and removed in
+// the last accumulation, so p has zero mean like the reference's.
+//
+// Included by fftreg_f32.cu only: the FP32 column kernels it launches must be
+// the instantiations of that translation unit, whose shared-memory opt-ins
+// RegSolve<float, N>::configure sets.
+#pragma once
+#include "fftreg.cuh"
+
+namespace exc {
+
+enum { MIX_DIV = 0, MIX_SCAL = 1, MIX_RES = 2, MIX_RES_MEAN = 3 };
+enum { MIX_SET = 0, MIX_ADD = 1, MIX_ADD_MEAN = 2 };
+
+template <typename C>
+__device__ __forceinline__ C to_f32c(double a, double b) {
+  C r;
+  r.x = (float)a;
+  r.y = (float)b;
+  return r;
+}
+
+// x pass, FP64 input -> FP32 half spectrum (the rr2c_kernel transform):
+//   MIX_DIV:  d' = h div(u) from the FP64 vector u, stored, transformed;
+//   MIX_SCAL: d' = h (d - mean d) from a scalar FP64 right-hand side (its
+//             mean, the part no pressure can balance, is removed first so the
+//             FP32 residual solves do not carry it), stored, transformed;
+//   MIX_RES:  r' = d' - (sum of neighbours of p - 6 p) / h, transformed
+//             (p: FP64 real view of the FP64 work array, row pitch 2P);
+//   MIX_RES_MEAN: as MIX_RES, and the CTA's sum of p goes to part[blockIdx.x].
+template <int N1, int N2, int MODE>
+__global__ void __launch_bounds__(XGeom<float, N1, N2>::NT)
+mr2c_kernel(const double* __restrict__ src, double h, double* __restrict__ d, const double* __restrict__ p, int P,
+            double inv_h, cplx<float>* __restrict__ out, const cplx<float>* __restrict__ tw,
+            const cplx<float>* __restrict__ tl, double* __restrict__ part) {
+  using C = cplx<float>;
+  using G = XGeom<float, N1, N2>;
+  constexpr int L = N1 * N2, n = 2 * L, RW = G::RW, XS = G::XS;
+  extern __shared__ unsigned char smem_raw[];
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  constexpr long long nn = (long long)n * n, N = nn * n;
+  const long long row0 = (long long)blockIdx.x * RW;
+  const int tid = threadIdx.x;
+  const int line = tid / N2, m2 = tid - line * N2;
+  double psum = 0.0;
+  C v[N1];
+  if (tid < RW * N2) {
+    const long long row = row0 + line;
+    if (row < nn) {
+      const int z = (int)(row / n), y = (int)(row - (long long)z * n);
+      const long long base = row * n;
+      if constexpr (MODE == MIX_DIV) {
+        const long long rowy = (long long)z * n + wrap_dn(y, n);
+        const long long rowz = (long long)wrap_dn(z, n) * n + y;
+        const double* ux = src;
+        const double2* ux2 = reinterpret_cast<const double2*>(src + base);
+        const double2* uy2 = reinterpret_cast<const double2*>(src + N + base);
+        const double2* uyd = reinterpret_cast<const double2*>(src + N + rowy * n);
+        const double2* uz2 = reinterpret_cast<const double2*>(src + 2 * N + base);
+        const double2* uzd = reinterpret_cast<const double2*>(src + 2 * N + rowz * n);
+        double2* d2 = reinterpret_cast<double2*>(d + base);
+#pragma unroll
+        for (int m1 = 0; m1 < N1; ++m1) {
+          const int m = m2 + N2 * m1;
+          const int xm = (m == 0) ? n - 1 : 2 * m - 1;
+          const double2 a0 = ux2[m], b0 = uy2[m], b1 = uyd[m], c0 = uz2[m], c1 = uzd[m];
+          const double uxm = ux[base + xm];
+          double2 dv;
+          dv.x = (a0.x - uxm) + (b0.x - b1.x) + (c0.x - c1.x);
+          dv.y = (a0.y - a0.x) + (b0.y - b1.y) + (c0.y - c1.y);
+          d2[m] = dv;
+          v[m1] = to_f32c<C>(dv.x, dv.y);
+        }
+      } else if constexpr (MODE == MIX_SCAL) {
+        const double2* s2 = reinterpret_cast<const double2*>(src + base);
+        double2* d2 = reinterpret_cast<double2*>(d + base);
+        const double dm = part[0];
+#pragma unroll
+        for (int m1 = 0; m1 < N1; ++m1) {
+          const int m = m2 + N2 * m1;
+          double2 dv = s2[m];
+          dv.x = (dv.x - dm) * h;
+          dv.y = (dv.y - dm) * h;
+          d2[m] = dv;
+          v[m1] = to_f32c<C>(dv.x, dv.y);
+        }
+      } else {
+        const long long pp = 2LL * P;
+        const double* pr = p + row * pp;
+        const double2* pc2 = reinterpret_cast<const double2*>(pr);
+        const double2* pym = reinterpret_cast<const double2*>(p + ((long long)z * n + wrap_dn(y, n)) * pp);
+        const double2* pyp = reinterpret_cast<const double2*>(p + ((long long)z * n + wrap_up(y, n)) * pp);
+        const double2* pzm = reinterpret_cast<const double2*>(p + ((long long)wrap_dn(z, n) * n + y) * pp);
+        const double2* pzp = reinterpret_cast<const double2*>(p + ((long long)wrap_up(z, n) * n + y) * pp);
+        const double2* d2 = reinterpret_cast<const double2*>(d + base);
+#pragma unroll
+        for (int m1 = 0; m1 < N1; ++m1) {
+          const int m = m2 + N2 * m1;
+          const double2 pc = pc2[m];
+          const double pxm = pr[m == 0 ? n - 1 : 2 * m - 1];
+          const double pxp = pr[m == L - 1 ? 0 : 2 * m + 2];
+          const double2 a = pym[m], b = pyp[m], c = pzm[m], e = pzp[m];
+          const double2 dv = d2[m];
+          // neighbours of x = 2m: pxm and 2m + 1; of x = 2m + 1: 2m and pxp
+          const double sx = ((pxm + pc.y) + (a.x + b.x)) + (c.x + e.x);
+          const double sy = ((pc.x + pxp) + (a.y + b.y)) + (c.y + e.y);
+          const double rx = fma(-inv_h, fma(-6.0, pc.x, sx), dv.x);
+          const double ry = fma(-inv_h, fma(-6.0, pc.y, sy), dv.y);
+          if constexpr (MODE == MIX_RES_MEAN) psum += pc.x + pc.y;
+          v[m1] = to_f32c<C>(rx, ry);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int m1 = 0; m1 < N1; ++m1) v[m1] = mk<float>(0, 0);
+    }
+    dft_reg<N1, false>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], __ldg(&tl[k1 * N2 + m2]));
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) xs[line * XS + k1 * (N2 + 1) + m2] = v[k1];
+  }
+  __syncthreads();
+  const int lb = tid / N1, k1 = tid - lb * N1;
+  const bool actb = tid < RW * N1;
+  C zz[N2];
+  if (actb) {
+#pragma unroll
+    for (int q = 0; q < N2; ++q) zz[q] = xs[lb * XS + k1 * (N2 + 1) + q];
+    dft_reg<N2, false>(zz);
+  }
+  __syncthreads();
+  if (actb) {
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) xs[lb * XS + k1 + N1 * k2] = zz[k2];
+  }
+  __syncthreads();
+  const long long row = row0 + lb;
+  if (actb && row < nn) {
+    C* o = out + row * P;
+    const C* zr = xs + lb * XS;
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+      const int k = k1 + N1 * k2;
+      const C zk = zz[k2];
+      const C zc = cconj(zr[k == 0 ? 0 : L - k]);
+      const C e = cadd(zk, zc), dd = csub(zk, zc);
+      const C wo = cmul(dd, __ldg(&tw[k]));
+      C X;
+      X.x = 0.5f * (e.x + wo.y);
+      X.y = 0.5f * (e.y - wo.x);
+      o[k] = X;
+    }
+    if (k1 == 0) {
+      const C zk = zz[0], zc = cconj(zz[0]);
+      const C e = cadd(zk, zc), dd = csub(zk, zc);
+      const C wo = cmul(dd, __ldg(&tw[L]));
+      C X;
+      X.x = 0.5f * (e.x + wo.y);
+      X.y = 0.5f * (e.y - wo.x);
+      o[L] = X;
+    }
+  }
+  if constexpr (MODE == MIX_RES_MEAN) {
+    // fixed-order block sum of p (deterministic for a fixed launch shape)
+    __shared__ double red[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) psum += __shfl_down_sync(0xffffffffu, psum, o);
+    const int warp = tid >> 5, lane = tid & 31;
+    if (lane == 0) red[warp] = psum;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+      part[blockIdx.x] = s;
+    }
+  }
+}
+
+// x pass, FP32 half spectrum -> reals (the rc2r_kernel transform), written
+// to the FP64 pressure p (row pitch 2P): MIX_SET p = c; MIX_ADD p += c;
+// MIX_ADD_MEAN p += c - mean.
+template <int N1, int N2, int MODE>
+__global__ void __launch_bounds__(XGeom<float, N1, N2>::NT)
+mc2r_kernel(const cplx<float>* __restrict__ g, int P, const cplx<float>* __restrict__ tw,
+            const cplx<float>* __restrict__ tl, double* __restrict__ p, const double* __restrict__ mean) {
+  using C = cplx<float>;
+  using G = XGeom<float, N1, N2>;
+  constexpr int L = N1 * N2, n = 2 * L, RW = G::RW, XS = G::XS;
+  extern __shared__ unsigned char smem_raw[];
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  constexpr long long nn = (long long)n * n;
+  const long long row0 = (long long)blockIdx.x * RW;
+  const int tid = threadIdx.x;
+  if (tid < RW * N2) {
+    const int line = tid / N2, m2 = tid - line * N2;
+    const long long row = row0 + line;
+    C v[N1];
+    if (row < nn) {
+      const C* x = g + row * P;
+#pragma unroll
+      for (int m1 = 0; m1 < N1; ++m1) {
+        const int k = m2 + N2 * m1;
+        const C xa = x[k], xb = x[L - k];
+        const C e = cadd(xa, cconj(xb));
+        const C o = cmulc(csub(xa, cconj(xb)), __ldg(&tw[k]));
+        v[m1].x = e.x - o.y;
+        v[m1].y = e.y + o.x;
+      }
+    } else {
+#pragma unroll
+      for (int m1 = 0; m1 < N1; ++m1) v[m1] = mk<float>(0, 0);
+    }
+    dft_reg<N1, true>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmulc(v[k1], __ldg(&tl[k1 * N2 + m2]));
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) xs[line * XS + k1 * (N2 + 1) + m2] = v[k1];
+  }
+  __syncthreads();
+  const int lb = tid / N1, k1 = tid - lb * N1;
+  const long long row = row0 + lb;
+  if (tid < RW * N1 && row < nn) {
+    C zz[N2];
+#pragma unroll
+    for (int q = 0; q < N2; ++q) zz[q] = xs[lb * XS + k1 * (N2 + 1) + q];
+    dft_reg<N2, true>(zz);
+    double2* r = reinterpret_cast<double2*>(p + row * 2LL * P);
+    double mu = 0.0;
+    if constexpr (MODE == MIX_ADD_MEAN) mu = *mean;
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+      const int m = k1 + N1 * k2;
+      double2 o;
+      if constexpr (MODE == MIX_SET) {
+        o.x = (double)zz[k2].x;
+        o.y = (double)zz[k2].y;
+      } else {
+        const double2 a = r[m];
+        if constexpr (MODE == MIX_ADD) {
+          o.x = a.x + (double)zz[k2].x;
+          o.y = a.y + (double)zz[k2].y;
+        } else {
+          o.x = (a.x - mu) + (double)zz[k2].x;
+          o.y = (a.y - mu) + (double)zz[k2].y;
+        }
+      }
+      r[m] = o;
+    }
+  }
+}
+
+// Per-CTA sums of a dense field (the scalar right-hand side's mean), fixed order.
+__global__ void mix_sum_kernel(const double* __restrict__ src, long long count, double* __restrict__ part) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < count; i += 256LL * gridDim.x) s += src[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// Mean of p from the per-CTA sums, in a fixed order.
+__global__ void mix_mean_kernel(const double* __restrict__ part, int nparts, double invN, double* __restrict__ mean) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += 256) s += part[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *mean = red[0] * invN;
+}
+
+template <int NN>
+struct MixSolve {
+  using RS = RegSolve<float, NN>;
+  static constexpr int A1 = RS::A1, A2 = RS::A2, B1 = RS::B1, B2 = RS::B2;
+  using CG = typename RS::CG;
+  using XG = typename RS::XG;
+  static constexpr long long NPARTS = ((long long)NN * NN + XG::RW - 1) / XG::RW;
+  static constexpr int SUM_CTAS = 1024;  // mix_sum_kernel grid
+  // doubles of `part`: the CTA sums of the last residual pass (NPARTS) and
+  // the mean of p after them, or the scalar right-hand side's mean and its
+  // SUM_CTAS partial sums
+  static constexpr long long PART_WORDS = (NPARTS > SUM_CTAS ? NPARTS : SUM_CTAS) + 2;
+
+  static cudaError_t configure() {
+    cudaError_t e = cudaSuccess;
+    auto set = [&](const void* f, size_t sh) {
+      if (e == cudaSuccess && sh > 48 * 1024)
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+    };
+    set((const void*)mr2c_kernel<B1, B2, MIX_DIV>, XG::SMEM);
+    set((const void*)mr2c_kernel<B1, B2, MIX_SCAL>, XG::SMEM);
+    set((const void*)mr2c_kernel<B1, B2, MIX_RES>, XG::SMEM);
+    set((const void*)mr2c_kernel<B1, B2, MIX_RES_MEAN>, XG::SMEM);
+    set((const void*)mc2r_kernel<B1, B2, MIX_SET>, XG::SMEM);
+    set((const void*)mc2r_kernel<B1, B2, MIX_ADD>, XG::SMEM);
+    set((const void*)mc2r_kernel<B1, B2, MIX_ADD_MEAN>, XG::SMEM);
+    return e;
+  }
+
+  static cudaError_t solve(exc_poisson* ps, const double* src, bool vec, cudaStream_t st) {
+    using C = cplx<float>;
+    constexpr int n = NN;
+    exc_poisson* sp = ps->mix;
+    const int P = ps->P, nkx = n / 2 + 1;
+    C* g = reinterpret_cast<C*>(sp->work);
+    const C* tw = reinterpret_cast<const C*>(sp->tw);
+    const C* tln = reinterpret_cast<const C*>(sp->twl_n);
+    const C* tlh = reinterpret_cast<const C*>(sp->twl_h);
+    double* p = reinterpret_cast<double*>(ps->work);
+    double* d = ps->mix_d;
+    double* part = ps->mix_part;
+    double* mean = part + NPARTS;
+    const double h = ps->h, inv_h = 1.0 / ps->h;
+    const unsigned gx = (unsigned)NPARTS;
+    const int ntx = (nkx + CG::W - 1) / CG::W;
+    const dim3 gc((unsigned)(ntx * n), 1, 1);
+    const SlotBatch one;
+    auto columns = [&]() {
+      rcols_kernel<float, A1, A2, false><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, one);
+      rzsolve_kernel<float, A1, A2><<<gc, CG::NT, CG::SMEM_Z, st>>>(g, n, nkx, ntx, P, tln, sp->invlap, one);
+      rcols_kernel<float, A1, A2, true><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, one);
+    };
+    if (vec) {
+      mr2c_kernel<B1, B2, MIX_DIV><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+    } else {
+      // mean of d into part[0] (partials in part[1 .. SUM_CTAS])
+      mix_sum_kernel<<<SUM_CTAS, 256, 0, st>>>(src, (long long)n * n * n, part + 1);
+      mix_mean_kernel<<<1, 256, 0, st>>>(part + 1, SUM_CTAS, 1.0 / ((double)n * n * n), part);
+      mr2c_kernel<B1, B2, MIX_SCAL><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+    }
+    columns();
+    mc2r_kernel<B1, B2, MIX_SET><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+    mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+    columns();
+    mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+    mr2c_kernel<B1, B2, MIX_RES_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+    mix_mean_kernel<<<1, 256, 0, st>>>(part, (int)NPARTS, 1.0 / ((double)n * n * n), mean);
+    columns();
+    mc2r_kernel<B1, B2, MIX_ADD_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+    return cudaGetLastError();
+  }
+};
+
+}  // namespace exc

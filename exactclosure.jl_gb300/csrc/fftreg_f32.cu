@@ -1,4 +1,6 @@
-// Register-resident FFT Poisson solve, FP32 instantiations (grids 32..1024).
+// Register-resident FFT Poisson solve, FP32 instantiations (grids 32..1024),
+// and the mixed-precision FP64 solve built on them (fftmix.cuh).
+#include "fftmix.cuh"
 #include "fftreg.cuh"
 
 namespace exc {
@@ -52,6 +54,49 @@ cudaError_t configure_fftreg_f32() {
 #define EXC_CONF(N) \
   if (e == cudaSuccess) e = RegSolve<float, N>::configure();
   EXC_REG_SIZES_F32(EXC_CONF)
+#undef EXC_CONF
+  return e;
+}
+
+// ---- mixed-precision FP64 solve (fftmix.cuh) ----
+#define EXC_MIX_SIZES(X) X(128) X(192) X(256) X(384) X(512) X(1024)
+
+bool fftmix_supported(int n) {
+  switch (n) {
+#define EXC_CASE(N) case N:
+    EXC_MIX_SIZES(EXC_CASE)
+#undef EXC_CASE
+    return true;
+    default: return false;
+  }
+}
+
+// Doubles of per-CTA partial sums (plus the mean) the solve of grid n uses.
+long long fftmix_part_words(int n) {
+  switch (n) {
+#define EXC_CASE(N) \
+  case N: return MixSolve<N>::PART_WORDS;
+    EXC_MIX_SIZES(EXC_CASE)
+#undef EXC_CASE
+    default: return 0;
+  }
+}
+
+cudaError_t fftmix_solve(exc_poisson* ps, const double* src, bool vec, cudaStream_t st) {
+  switch (ps->n) {
+#define EXC_CASE(N) \
+  case N: return MixSolve<N>::solve(ps, src, vec, st);
+    EXC_MIX_SIZES(EXC_CASE)
+#undef EXC_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t configure_fftmix() {
+  cudaError_t e = cudaSuccess;
+#define EXC_CONF(N) \
+  if (e == cudaSuccess) e = MixSolve<N>::configure();
+  EXC_MIX_SIZES(EXC_CONF)
 #undef EXC_CONF
   return e;
 }

@@ -258,6 +258,36 @@ int closure_flux(int n, int c, double l, double visc, const double* fdelta, int 
   return EXC_OK;
 }
 
+// Surface-filtered flux of the paper's face-average driver (dns_aid_surface,
+// src/NavierStokes.jl:368-369): component (i, j) = r_ij point-sampled along i
+// (the face of the velocity u_i it updates) and boxed along the other two
+// axes (Turbulox's surfacefilter!(firu, ru, c, true)); with `line`, the
+// off-diagonal components are point-sampled along j too and boxed along the
+// third axis only (linefilter!), the diagonal unchanged.  Sampled at the LES
+// centre (i == j) or edge (i, j); order s11,s21,s31,s12,... like rDHi.
+template <typename T>
+int surface_flux(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, const T* p,
+                 T* r9, bool line, cudaStream_t st) {
+  const int m = n / c;
+  const long long M = (long long)m * m * m;
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i) {
+      bool stag[3], point[3];
+      for (int d = 0; d < 3; ++d) {
+        stag[d] = (i != j) && (d == i || d == j);
+        point[d] = (d == i) || (line && d == j);
+      }
+      Taps3 taps;
+      int rc = make_taps3(c, stag, point, fdelta, nfd, &taps);
+      if (rc) return rc;
+      launch_flux_filter_rt<T>(i, j, u, p, n, (T)(1.0 / (l / n)), (T)visc, c, taps, r9 + (long long)(3 * j + i) * M, M,
+                               st);
+    }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
 // sigmaDH (src/N.jl:1088-1115): volume filter GDH of each stress component,
 // sampled at LES centres/edges; order s11,s22,s33,s12,s23,s31.  With p the
 // total flux r = sigma + p I is filtered (the paper driver's volume-filtered
@@ -526,6 +556,8 @@ int classic_stress(int n, int c, double l, double visc, const double* fdelta, in
   template cudaError_t box_tb_coarsen<T>(int, int, int, const T*, T*, cudaStream_t);                     \
   template cudaError_t box_oa<T>(int, int, int, const T*, T*, cudaStream_t);                             \
   template int filter_vector<T>(int, int, int, const double*, int, const T*, T*, cudaStream_t);          \
+  template int surface_flux<T>(int, int, double, double, const double*, int, const T*, const T*, T*, bool, \
+                               cudaStream_t);                                                             \
   template int closure_flux<T>(int, int, double, double, const double*, int, const T*, const T*, T*,     \
                                cudaStream_t);                                                            \
   template int filtered_stress<T>(int, int, double, double, const double*, int, const T*, T*, cudaStream_t, const T*);

@@ -36,6 +36,9 @@ template <typename T>
 int closure_flux(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, const T* p,
                  T* r9, cudaStream_t st);
 template <typename T>
+int surface_flux(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, const T* p,
+                 T* r9, bool line, cudaStream_t st);
+template <typename T>
 int classic_stress(int n, int c, double l, double visc, const double* fdelta, int nfd, const T* u, T* s6,
                    cudaStream_t st);
 template <typename T>

@@ -23,7 +23,17 @@ struct exc_poisson {
   // shared-memory passes
   void* twl_n = nullptr;
   void* twl_h = nullptr;
+  // engine 0: the mixed-precision solve where built (FP64 grids with an FP32
+  // register plan, fftmix.cu), else the register passes, else Stockham;
+  // 1: the FP64 shared-memory Stockham passes; 2: the FP64 register passes
+  // where planned, else Stockham (no mixed precision)
   int engine = 0;
+  // mixed-precision FP64 solve (fftmix.cu): the FP32 inner solver (its own
+  // work array and tables, 1/(lambda N h) divide table), the FP64 divergence
+  // (n^3, unscaled by 1/h) and per-CTA partial sums of p with the mean last
+  exc_poisson* mix = nullptr;
+  double* mix_d = nullptr;
+  double* mix_part = nullptr;
 };
 
 namespace exc {
@@ -57,6 +67,13 @@ cudaError_t fftreg_solve(exc_poisson* ps, const float* src, bool src_is_vector, 
                          int nslots);
 cudaError_t fftreg_solve(exc_poisson* ps, const double* src, bool src_is_vector, cudaStream_t st, const SlotBatch& sb,
                          int nslots);
+// The mixed-precision FP64 solve (fftmix.cu): grids it is built for, the
+// doubles of partial sums it needs, the solve (pressure into the FP64 real
+// view of ps->work, like poisson_solve_inplace) and its shared-memory opt-ins.
+bool fftmix_supported(int n);
+long long fftmix_part_words(int n);
+cudaError_t fftmix_solve(exc_poisson* ps, const double* src, bool src_is_vector, cudaStream_t st);
+cudaError_t configure_fftmix();
 // Lines per column tile and rows per x-pass CTA of a grid's register plan.
 void fftreg_geometry(int n, int precision, int* col_w, int* x_rows);
 // Read and clear the learned closure's tensor-core wait fault flag.

@@ -221,6 +221,7 @@ struct exc_server {
   std::vector<std::unique_ptr<exc::ChunkBase>> chunks;
   std::vector<exc::FinishRec> finishing;
   int64_t next_id = 1;
+  int max_active_per_size = 0;  // admission bound per grid size (0: none)
   // init scratch (largest grid seen so far)
   void* spec3 = nullptr;
   size_t spec3_bytes = 0;
@@ -498,13 +499,27 @@ static int tick_chunk(exc_server* sv, Chunk<T>* ck) {
   return EXC_OK;
 }
 
+// Solves of grid size n in the chunks (admitted and not yet retired).
+static int active_of_size(const exc_server* sv, int n) {
+  int c = 0;
+  for (auto& cb : sv->chunks)
+    if (cb->n == n) c += cb->active_count();
+  return c;
+}
+
 template <typename T>
 static int server_tick(exc_server* sv, int* active, int* queued) {
-  // admission (continuous batching): any queued request that fits; when a
-  // request waits for memory, idle chunks (no active slot) are released once
+  // admission (continuous batching): any queued request that fits, in
+  // arrival order; with an admission bound a request also waits while its
+  // grid size has max_active_per_size solves running.  When a request waits
+  // for memory, idle chunks (no active slot) are released once
   for (int pass = 0; pass < 2; ++pass) {
     bool blocked = false;
     for (size_t i = 0; i < sv->pending.size();) {
+      if (sv->max_active_per_size > 0 && active_of_size(sv, sv->pending[i].req.n) >= sv->max_active_per_size) {
+        ++i;
+        continue;
+      }
       bool ok = false;
       int rc = admit<T>(sv, sv->pending[i], &ok);
       if (rc) return rc;
@@ -583,6 +598,12 @@ int exc_server_destroy(exc_server* sv) {
   if (sv->ev0) cudaEventDestroy(sv->ev0);
   if (sv->admit_stream) cudaStreamDestroy(sv->admit_stream);
   delete sv;
+  return EXC_OK;
+}
+
+int exc_server_set_admission(exc_server* sv, int max_active_per_size) {
+  if (!sv || max_active_per_size < 0) { set_last_error("null server or negative bound"); return EXC_ERR_ARG; }
+  sv->max_active_per_size = max_active_per_size;
   return EXC_OK;
 }
 

@@ -123,6 +123,7 @@ SIGNATURES = {
     "exc_net_train_step": [vp, i32, i32, i32, vp, vp, f64, dp, vp],
     "exc_server_create": [C.POINTER(ServerDesc), C.POINTER(vp)],
     "exc_server_destroy": [vp],
+    "exc_server_set_admission": [vp, i32],
     "exc_server_submit": [vp, C.POINTER(SolveReq), C.POINTER(C.c_int64)],
     "exc_server_tick": [vp, C.POINTER(i32), C.POINTER(i32)],
     "exc_server_poll": [vp, C.POINTER(SolveResult), i32, C.POINTER(i32)],
@@ -137,6 +138,8 @@ SIGNATURES = {
     "exc_dnsaid_warmup": [vp, f64, f64, i32, C.POINTER(i32)],
     "exc_dnsaid_start": [vp],
     "exc_dnsaid_set_paper": [vp, i32],
+    "exc_dnsaid_set_surface": [vp, i32],
+    "exc_dnsaid_relerr": [vp, dp],
     "exc_dnsaid_step": [vp, f64, f64, i32, C.POINTER(i32)],
     "exc_dnsaid_time": [vp, dp, C.POINTER(i32)],
     "exc_dnsaid_get": [vp, i32, dp],

@@ -350,11 +350,16 @@ class DnsAid:
         self._h = h
         self.fields = DNSAID_FIELDS
 
-    def set_paper(self, doproject: bool = True):
+    def set_paper(self, doproject: bool = True, filter: str = "volume"):
         """Run the paper's volume-average driver ``dns_aid_volavg``
-        (src/NavierStokes.jl:141-304) instead of ``dnsaid_project``; call
-        before ``start``.  Fields: ``PAPER_FIELDS``."""
-        call("exc_dnsaid_set_paper", self._h, 1 if doproject else 0)
+        (src/NavierStokes.jl:141-304), or with ``filter="surface"`` its
+        surface-average driver ``dns_aid_surface`` (src/NavierStokes.jl:306-468),
+        instead of ``dnsaid_project``; call before ``start``.  Fields:
+        ``PAPER_FIELDS``."""
+        if filter not in ("volume", "surface"):
+            raise ValueError("filter must be 'volume' or 'surface'")
+        call("exc_dnsaid_set_paper" if filter == "volume" else "exc_dnsaid_set_surface", self._h,
+             1 if doproject else 0)
         self.fields = PAPER_FIELDS
 
     def init_random(self, profile: str = "power", param: float = -5 / 3, energy: float = 1.0, seed: int = 0):
@@ -391,6 +396,12 @@ class DnsAid:
         out = np.empty((3, self.m, self.m, self.m))
         call("exc_dnsaid_get", self._h, self.fields.index(which), out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
+
+    def relerr(self) -> dict:
+        """The paper drivers' ``|v - fu| / |fu|`` of the four LES, on the device."""
+        e = np.empty(4)
+        call("exc_dnsaid_relerr", self._h, e.ctypes.data_as(C.POINTER(C.c_double)))
+        return dict(zip(self.fields[1:], e.tolist()))
 
     def errors(self) -> dict:
         e = np.empty(5)
@@ -475,6 +486,39 @@ def case_for(tc: dict, cfl: float = 0.3, kind: str = "volume", precision: int = 
     return cs
 
 
+def _paper_driver(ustart: np.ndarray, n_les: int, viscosity: float, doproject: bool, tstop: float, cfl: float,
+                  l: float, stream, filter: str):
+    ustart = np.asarray(ustart)
+    if ustart.ndim != 4 or ustart.shape[0] != 3 or not (ustart.shape[1] == ustart.shape[2] == ustart.shape[3]):
+        raise ValueError("ustart must have shape (3, n, n, n)")
+    n = ustart.shape[1]
+    if n_les < 1 or n % n_les:
+        raise ValueError(f"n_les = {n_les} must divide the DNS size n = {n}")
+    d = DnsAid(n, l, viscosity, n // n_les, None, stream)
+    d.set_velocity(ustart)
+    d.set_paper(doproject, filter)
+    d.start()
+    names = PAPER_FIELDS[1:]
+    relerr = {k: [] for k in ("time",) + names}
+    t, i = 0.0, 0
+    # the reference's loop: errors of the initial state in the first pass,
+    # then one step per pass while t < tstop
+    while t < tstop:
+        if i > 0:
+            d.step(tstop, cfl, max_steps=1)
+            t = d.time()[0]
+        e = d.relerr()
+        relerr["time"].append(t)
+        for k in names:
+            relerr[k].append(e[k])
+        i += 1
+    u = {"dns_ref": d.velocity(), "dns_fil": d.get("fu")}
+    for k in names:
+        u[k] = d.get(k)
+    d.close()
+    return u, {k: np.asarray(v, dtype=np.float64) for k, v in relerr.items()}
+
+
 def dns_aid_volavg(ustart: np.ndarray, n_les: int, viscosity: float, doproject: bool, tstop: float, cfl: float,
                    l: float = 1.0, stream=None):
     """``dns_aid_volavg`` (``src/NavierStokes.jl:141-304``) on the GPU: the
@@ -482,30 +526,18 @@ def dns_aid_volavg(ustart: np.ndarray, n_les: int, viscosity: float, doproject: 
     swap-symmetric) in lockstep until ``tstop``.  Returns ``(u, relerr)`` like
     the reference: ``u`` with ``dns_ref``, ``dns_fil`` and the four LES fields,
     ``relerr`` with ``time`` and each LES's ``|v - fu| / |fu|`` recorded at
-    t = 0 and after every step."""
-    n = ustart.shape[1]
-    d = DnsAid(n, l, viscosity, n // n_les, None, stream)
-    d.set_velocity(ustart)
-    d.set_paper(doproject)
-    d.start()
-    names = PAPER_FIELDS[1:]
-    relerr = {k: [] for k in ("time",) + names}
-    t = 0.0
-    while True:
-        fu = d.get("fu")
-        nf = np.linalg.norm(fu.ravel())
-        relerr["time"].append(t)
-        for k in names:
-            relerr[k].append(float(np.linalg.norm((d.get(k) - fu).ravel()) / nf))
-        if t >= tstop:
-            break
-        d.step(tstop, cfl, max_steps=1)
-        t = d.time()[0]
-    u = {"dns_ref": d.velocity(), "dns_fil": d.get("fu")}
-    for k in names:
-        u[k] = d.get(k)
-    d.close()
-    return u, {k: np.asarray(v) for k, v in relerr.items()}
+    t = 0 and after every step (empty when ``tstop <= 0``)."""
+    return _paper_driver(ustart, n_les, viscosity, doproject, tstop, cfl, l, stream, "volume")
+
+
+def dns_aid_surface(ustart: np.ndarray, n_les: int, viscosity: float, doproject: bool, tstop: float, cfl: float,
+                    l: float = 1.0, stream=None):
+    """``dns_aid_surface`` (``src/NavierStokes.jl:306-468``) on the GPU: the
+    DNS and four LES on the face-averaged (surface-filtered) DNS ``fiu``;
+    classic with the surface-filtered flux, swap with the line-filtered flux
+    off the diagonal, its symmetric part.  Returns ``(u, relerr)`` like
+    ``dns_aid_volavg``."""
+    return _paper_driver(ustart, n_les, viscosity, doproject, tstop, cfl, l, stream, "surface")
 
 
 def compute_errors(uaid: dict) -> dict:

@@ -17,7 +17,7 @@ from ._lib import EXC_F32, ServerDesc, ServerInfo, SolveReq, SolveResult, call, 
 
 class Server:
     def __init__(self, precision: int = EXC_F32, mem_fraction: float = 0.5, slots_per_chunk: int = 0,
-                 autotune: bool = True, max_bytes: float = 0.0):
+                 autotune: bool = True, max_bytes: float = 0.0, max_active_per_size: int = 0):
         d = ServerDesc()
         d.precision, d.mem_fraction, d.slots_per_chunk, d.autotune = precision, mem_fraction, slots_per_chunk, \
             int(autotune)
@@ -27,6 +27,13 @@ class Server:
         self._h = h
         self.precision = precision
         self._keep = {}
+        if max_active_per_size:
+            self.set_admission(max_active_per_size)
+
+    def set_admission(self, max_active_per_size: int):
+        """Admit a request only while fewer than ``max_active_per_size`` solves
+        of its grid size run (0: no bound)."""
+        call("exc_server_set_admission", self._h, max_active_per_size)
 
     def submit(self, n: int, visc: float, nsteps: int, seed: int = 0, kpeak: float = 4.0, energy: float = 1.0,
                l: float = 1.0, cfl: float = 0.3, keep_field: bool = False) -> int:

@@ -94,11 +94,16 @@ int exc_poisson_destroy(exc_poisson* ps);
  * gave up (that convolution's output is not valid).  0 in normal operation. */
 int exc_device_faults(int* flags);
 
-/* FFT engine of a solver (no counterpart in the reference): 0 = register-
- * resident two-level passes where the grid has a plan (n = 32, 48, 64, 96,
- * 128, 192, 256 and, in FP32, 384, 512, 1024), shared-memory Stockham passes
- * otherwise (the default); 1 = Stockham passes for every grid.  Results agree
- * to round-off; the autotuner of the serving form picks per grid. */
+/* FFT engine of a solver (no counterpart in the reference).  0 (the
+ * default): in FP64 on grids n = 128, 192, 256, 384, 512, 1024 a
+ * mixed-precision solve (three FP32 register-pass solves refined by residuals
+ * formed in FP64: the pressure agrees with the FP64 FFT solve to FP64
+ * rounding); otherwise register-resident two-level passes where the grid has
+ * a plan (n = 32, 48, 64, 96, 128, 192, 256 and, in FP32, 384, 512, 1024),
+ * shared-memory Stockham passes for the rest.  1 = FP64/FP32 Stockham passes
+ * for every grid.  2 = register passes where planned, else Stockham, in the
+ * solver's own precision throughout.  Results agree to round-off; the
+ * autotuner of the serving form picks per grid. */
 int exc_poisson_set_engine(exc_poisson* ps, int engine);
 /* p with L_h p = d, mean(p) = 0 (src/N.jl:262-301).  d and p may alias. */
 int exc_poisson_solve(exc_poisson* ps, const void* d, void* p, void* stream);
@@ -291,6 +296,11 @@ typedef struct {
 int exc_server_create(const exc_server_desc* desc, exc_server** out);
 int exc_server_destroy(exc_server* sv);
 /* Queue a solve; *id identifies its result. */
+/* Admission bound (no counterpart in the reference): a queued request is
+ * admitted only while fewer than max_active_per_size solves of its grid size
+ * run (0 = no bound, the default); requests are taken in arrival order among
+ * those eligible.  Trades aggregate throughput for lower median latency. */
+int exc_server_set_admission(exc_server* sv, int max_active_per_size);
 int exc_server_submit(exc_server* sv, const exc_solve_req* req, int64_t* id);
 /* Admit, advance every active solve one RK4 step, retire finished solves
  * (asynchronous: at most two ticks in flight per batch). */
@@ -391,6 +401,18 @@ int exc_dnsaid_warmup(exc_dnsaid* d, double twarm, double cfl, int max_steps, in
  * projected when doproject.  The paper module's Turbulox filters are the
  * reference's own GDH (volume) and GDHi (face) filters of src/N.jl. */
 int exc_dnsaid_set_paper(exc_dnsaid* d, int doproject);
+/* Switch the handle (before exc_dnsaid_start) to the paper's surface-average
+ * driver `dns_aid_surface` (src/NavierStokes.jl:306-468): the target fiu is
+ * the face-filtered DNS (`surfacefilter!(fiu, u, c)`, never projected); four
+ * LES -- no model, classic (divergence of the surface-filtered flux r_ij,
+ * point-sampled along i and boxed along the other axes, minus
+ * sigma_H(fiu) + p_H I), swap (the surface-filtered flux on the diagonal and
+ * the line-filtered flux, point-sampled along i and j, off it) and the swap
+ * flux's symmetric part -- each stepped like the volume driver's.  The
+ * Turbulox filters are restated from their finite-volume meaning; the swap
+ * closure is exact off the diagonal only (the normal flux term of a face
+ * average is a fine-grid difference across the face). */
+int exc_dnsaid_set_surface(exc_dnsaid* d, int doproject);
 /* LES initial states: all five = apply_ΔHπ(u) (src/N.jl:1278-1287), or the
  * four paper LES = fu; t = 0. */
 int exc_dnsaid_start(exc_dnsaid* d);
@@ -405,6 +427,10 @@ int exc_dnsaid_get(exc_dnsaid* d, int which, double* host);
 /* `compute_errors` (src/N.jl:1334-1349) of the five LES against u_les (the
  * paper driver: of its four LES against fu, out[4] = 0). */
 int exc_dnsaid_errors(exc_dnsaid* d, double out[5]);
+/* The paper drivers' relerr (src/NavierStokes.jl:292-296, 456-460): out[k] =
+ * |v_k - fu| / |fu| over all three components for the four LES (nomodel,
+ * classic, swapfil, swapfil_symm), reduced on the device in FP64. */
+int exc_dnsaid_relerr(exc_dnsaid* d, double out[4]);
 
 /* ======================================================================
  * 1-D Burgers, batched over samples (module `Burgers`, src/Burgers.jl)

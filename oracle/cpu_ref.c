@@ -616,3 +616,24 @@ int cref_stage(cref* cs, int s) {
   do_stage(cs, s);
   return 0;
 }
+
+/* ------------------------------------------------ standalone operators -- */
+/* project!(u, poisson) (src/N.jl:256-307) on a caller-owned 3 x n^3 field,
+ * in place; the pressure goes to p (n^3) when it is not NULL. */
+int cref_project(int n, double l, double* u, double* p) {
+  poisson ps;
+  poisson_init(&ps, n, l);
+  double* scr = p ? p : malloc(sizeof(double) * (size_t)n * n * n);
+  if (!scr) { poisson_free(&ps); return 1; }
+  project(&ps, u, scr);
+  if (!p) free(scr);
+  poisson_free(&ps);
+  return 0;
+}
+
+/* du = tensordivergence(stresstensor(u, visc)) (src/N.jl:94-160) on caller
+ * buffers (3 x n^3 each). */
+int cref_rhs(int n, double l, double visc, const double* u, double* du) {
+  rhs(n, l / n, visc, u, du);
+  return 0;
+}

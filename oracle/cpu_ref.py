@@ -36,8 +36,10 @@ def lib():
         L.cref_init_analytic.argtypes = [C.c_void_p]
         L.cref_init_analytic.restype = C.c_int
         L.cref_time.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.cref_project.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.cref_rhs.argtypes = [C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         for f in ("cref_init_random", "cref_set_velocity", "cref_get_velocity", "cref_get_les", "cref_step",
-                  "cref_stage", "cref_time"):
+                  "cref_stage", "cref_time", "cref_project", "cref_rhs"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -98,11 +100,39 @@ class CpuCase:
             pass
 
 
-def timing_case(n, les, visc):
-    """A full-size CPU case with a smooth analytic field (values do not change
-    the work of a stage) for timing samples."""
+def project(u, l=1.0):
+    """``project!`` of a float64 ``(3, n, n, n)`` field (a new array) and its
+    pressure, by the C restatement on all host threads."""
+    import numpy as np
+
+    a = np.array(u, dtype=np.float64, order="C", copy=True)
+    n = a.shape[1]
+    p = np.empty((n, n, n))
+    dp = C.POINTER(C.c_double)
+    assert lib().cref_project(n, l, a.ctypes.data_as(dp), p.ctypes.data_as(dp)) == 0
+    return a, p
+
+
+def rhs(u, visc, l=1.0):
+    """``tensordivergence(stresstensor(u, visc))`` by the C restatement."""
+    import numpy as np
+
+    a = np.ascontiguousarray(u, dtype=np.float64)
+    du = np.empty_like(a)
+    dp = C.POINTER(C.c_double)
+    assert lib().cref_rhs(a.shape[1], l, visc, a.ctypes.data_as(dp), du.ctypes.data_as(dp)) == 0
+    return du
+
+
+def timing_case(n, les, visc, kpeak=None):
+    """A full-size CPU case for timing samples: the seeded peak-spectrum
+    field of the workload (``kpeak``), or a smooth analytic field when
+    ``kpeak`` is None (values do not change the work of a stage)."""
     cs = CpuCase(n, 1.0, visc, 0.3, les)
-    assert lib().cref_init_analytic(cs._h) == 0
+    if kpeak is None:
+        assert lib().cref_init_analytic(cs._h) == 0
+    else:
+        cs.init_random(kpeak, 1.0, 0)
     cs.stage(0)  # warm-up (page faults, dt)
     return cs
 
@@ -111,7 +141,7 @@ def time_stages(n, les, kpeak, visc, budget_s=20.0, cs=None, max_stages=8):
     """Time whole RK4 stages of the full-size workload on all host threads."""
     own = cs is None
     if own:
-        cs = timing_case(n, les, visc)
+        cs = timing_case(n, les, visc, kpeak)
     t0 = time.perf_counter()
     k = 0
     while True:

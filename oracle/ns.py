@@ -815,3 +815,92 @@ def dns_aid_volavg_steps(u, les, visc, l, c, tstop, cfl, doproject, fdelta=None,
             v = v + dt * dsig[k]
             les[k] = project(v, H) if doproject else v
     return u, les, t, it
+
+
+# --------------------------------------------------------------------------
+# The paper's surface-average driver `dns_aid_surface` (src/NavierStokes.jl:306-468)
+# --------------------------------------------------------------------------
+# Its filters come from Turbulox.jl (not vendored, no pinned version); they are
+# restated from their finite-volume meaning with the separable stencils above:
+#   `surfacefilter!(fiu, u, c)`     the face average: the c x c transverse box
+#                                   of fine faces inside each coarse face of
+#                                   u_i (point sample along i) = face_filter;
+#   `surfacefilter!(firu, ru, c, true)`  the flux r_ij (used in du_i, derivative
+#                                   along j) filtered like the velocity it
+#                                   updates: point sample along i, box along the
+#                                   two other axes, at the LES centre (i == j)
+#                                   or edge (i, j);
+#   `linefilter!(fijru, ru, c)`     r_ij (i != j) point-sampled along i and j,
+#                                   averaged along the third axis only.
+# Why these: the face average of the fine flux divergence sum_j delta_j r_ij
+# over the coarse face of u_i telescopes along each transverse axis j != i
+# into a coarse difference of the line average of r_ij (exactly), while the
+# normal term delta_i r_ii is a fine-grid difference across the face that no
+# coarse difference of a local field reproduces; the swap closure keeps the
+# face average of r_ii at the coarse centre for it.  So the swap LES on the
+# face filter is exact off the diagonal only (surface_offdiag_identity),
+# unlike the volume filter's, whose every term telescopes.
+def surface_flux(r: dict, c: int, line: bool, fdelta=None) -> dict:
+    """``surfacefilter!(firu, ru, c, true)`` (``line`` False) or the swap flux
+    of ``dns_aid_surface`` (``line`` True: ``linefilter!`` off the diagonal,
+    the same surface filter on it), 9 components keyed ``(i, j)``
+    (src/NavierStokes.jl:368-369, 386-394)."""
+    out = {}
+    for i in range(3):
+        for j in range(3):
+            modes = tuple(POINT if (d == i or (line and d == j)) else VOLUME for d in range(3))
+            out[(i, j)] = filter_coarse(r[(i, j)], c, positions_sigma(i, j), modes, fdelta)
+    return out
+
+
+def surface_offdiag_identity(u, p, visc, l, c):
+    """Both sides of the identity the line filter rests on: the face average
+    of the fine off-diagonal flux divergence, and the coarse divergence of the
+    line-filtered flux (diagonal terms left out on both sides)."""
+    n = u.shape[1]
+    h, H = l / n, l / (n // c)
+    r = get_r(stresstensor(u, visc, h), p)
+    off = {k: (v if k[0] != k[1] else np.zeros_like(v)) for k, v in r.items()}
+    fine = tensordivergence(off, h)
+    lhs = face_filter(fine, c)
+    rl = surface_flux(r, c, True)
+    roff = {k: (v if k[0] != k[1] else np.zeros_like(v)) for k, v in rl.items()}
+    return lhs, tensordivergence(roff, H)
+
+
+def dns_aid_surface_steps(u, les, visc, l, c, tstop, cfl, doproject, fdelta=None, max_steps=None, t0=0.0):
+    """Steps of the loop of ``dns_aid_surface`` (src/NavierStokes.jl:350-452):
+    ``fiu`` the face-filtered DNS (divergence free on the LES grid, never
+    projected), ``rfiu = sigma_H(fiu) + p_H I``; closures: the divergences of
+    ``firu - rfiu`` (classic), of the swap flux ``diag(firu) + offdiag(fijru) -
+    rfiu`` and of its symmetric part; each LES takes ``v += dt P(RHS_H(v))``,
+    ``v += dt dsigma`` and a projection when ``doproject``.  Returns
+    (u, les, t, steps)."""
+    n = u.shape[1]
+    h = l / n
+    H = l / (n // c)
+    les = {k: v.copy() for k, v in les.items()}
+    t, it = t0, 0
+    while t < tstop and (max_steps is None or it < max_steps):
+        dt = min(propose_timestep(u, visc, cfl, h), tstop - t)
+        t += dt
+        it += 1
+        du, p = project(rhs(u, visc, h), h, return_p=True)
+        r = get_r(stresstensor(u, visc, h), p)
+        firu = surface_flux(r, c, False, fdelta)
+        fswap = surface_flux(r, c, True, fdelta)
+        fiu = face_filter(u, c, fdelta)
+        sfiu = stresstensor(fiu, visc, H)
+        p_les = poisson_solve(divergence(tensordivergence(sfiu, H), H), H)
+        rfiu = get_r(sfiu, p_les)
+        s_classic = {k: firu[k] - rfiu[k] for k in firu}
+        s_swap = {k: fswap[k] - rfiu[k] for k in fswap}
+        dsig = {"classic": tensordivergence(s_classic, H), "swapfil": tensordivergence(s_swap, H),
+                "swapfil_symm": tensordivergence(symmetrize(s_swap), H)}
+        u = u + dt * du
+        les["nomodel"] = les["nomodel"] + dt * project(rhs(les["nomodel"], visc, H), H)
+        for k in ("classic", "swapfil", "swapfil_symm"):
+            v = les[k] + dt * project(rhs(les[k], visc, H), H)
+            v = v + dt * dsig[k]
+            les[k] = project(v, H) if doproject else v
+    return u, les, t, it

@@ -120,11 +120,71 @@ def test_exact_closure_invariant_and_errors(NS):
 
 
 def test_even_ratio_rejected(NS):
+    """dnsaid_project's classic closure filters on the fine grid with an odd
+    top-hat only: an even ratio is refused at start (the paper drivers take
+    it)."""
     from exactclosure_gb300 import ExcError
 
+    d = NS.DnsAid(48, 1.0, 1e-3, 4)
+    d.set_velocity(ns.randomfield(48, 1.0, 3, 0))
     with pytest.raises(ExcError) as ei:
-        NS.DnsAid(48, 1.0, 1e-3, 4)
+        d.start()
     assert ei.value.code == 3
+    d.close()
+
+
+@pytest.mark.parametrize("c,doproject", [(3, True), (3, False), (4, True)])
+def test_paper_surface_driver_per_step(NS, c, doproject):
+    """The paper's dns_aid_surface (src/NavierStokes.jl:306-468): the face-
+    filtered target, start and three lockstep steps of the DNS and the four
+    LES against the oracle (1e-12 relative L2 per step); the device relerr
+    equals the oracle's |v - fiu| / |fiu|."""
+    n, l, visc, cfl = 24, 1.0, 1e-3, 0.4
+    u = ns.randomfield(n, l, -5 / 3, 2, 1.0, profile="power")
+    d = NS.DnsAid(n, l, visc, c)
+    d.set_velocity(u)
+    d.set_paper(doproject, "surface")
+    d.start()
+    fiu = ns.face_filter(u, c)
+    les = {k: fiu.copy() for k in ns.PAPER_NAMES}
+    assert rel(d.get("fu"), fiu) < 1e-12
+    t = 0.0
+    for k in range(3):
+        d.step(0.05, cfl, max_steps=1)
+        u, les, t, _ = ns.dns_aid_surface_steps(u, les, visc, l, c, 0.05, cfl, doproject, max_steps=1, t0=t)
+        assert rel(d.velocity(), u) < 1e-12, k
+        for key in ns.PAPER_NAMES:
+            assert rel(d.get(key), les[key]) < 1e-12, (k, key)
+    ref = ns.face_filter(u, c)
+    e = d.relerr()
+    for key in ns.PAPER_NAMES:
+        assert abs(e[key] - rel(les[key], ref)) <= 1e-10 * rel(les[key], ref), key
+    d.close()
+
+
+def test_paper_surface_host_driver(NS):
+    """The reference-shaped ``dns_aid_surface(...) -> (u, relerr)``: relerr
+    at t = 0 and after every step against the oracle, and an empty relerr
+    when tstop <= 0 (the reference's `while t < tstop` loop)."""
+    n, m, l, visc, cfl, tstop = 24, 8, 1.0, 1e-3, 0.4, 0.004
+    u0 = ns.randomfield(n, l, -5 / 3, 3, 1.0, profile="power")
+    u, rel_err = NS.dns_aid_surface(u0, m, visc, True, tstop, cfl, l)
+    fiu = ns.face_filter(u0, 3)
+    les = {k: fiu.copy() for k in ns.PAPER_NAMES}
+    uo, les, t, it = ns.dns_aid_surface_steps(u0, les, visc, l, 3, tstop, cfl, True)
+    assert len(rel_err["time"]) == it + 1 and abs(rel_err["time"][-1] - t) <= 1e-15
+    assert rel(u["dns_ref"], uo) < 1e-12
+    assert rel(u["dns_fil"], ns.face_filter(uo, 3)) < 1e-12
+    ref = ns.face_filter(uo, 3)
+    for k in ns.PAPER_NAMES:
+        assert rel(u[k], les[k]) < 1e-12, k
+        assert abs(rel_err[k][-1] - rel(les[k], ref)) <= 1e-10 * rel(les[k], ref), k
+    assert rel_err["nomodel"][0] == 0.0
+    u_empty, r_empty = NS.dns_aid_surface(u0, m, visc, True, 0.0, cfl, l)
+    assert all(len(v) == 0 for v in r_empty.values())
+    assert rel(u_empty["dns_fil"], fiu) < 1e-12
+    with pytest.raises(ValueError):
+        NS.dns_aid_surface(u0, 7, visc, True, tstop, cfl, l)
 
 
 def test_reference_ratio_5_grid(NS):

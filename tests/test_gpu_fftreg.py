@@ -1,7 +1,9 @@
-"""GPU parity of the register-resident FFT passes (engine 0) of the Poisson
-solver: projection and pressure solve against the oracle (float64: 1e-12
-relative; float32 form: 2e-5), and, at grids too large for the oracle, against
-the shared-memory Stockham passes (engine 1) of the same library."""
+"""GPU parity of the Poisson solver's FFT engines: the register-resident
+passes (engine 2, and engine 0 where no mixed-precision solve is built), the
+mixed-precision FP64 solve (engine 0 on FP64 grids of 128 and more) and the
+shared-memory Stockham passes (engine 1).  Projection and pressure solve
+against the oracle (float64: 1e-12 relative; float32 form: 2e-5), and, at grids
+too large for the oracle, against each other."""
 import numpy as np
 import pytest
 
@@ -36,13 +38,13 @@ def rel(a, b):
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
 
 
-@pytest.mark.parametrize("n", [32, 48, 64, 96, 128])
-def test_register_projection_f64(NS, n):
+@pytest.mark.parametrize("n,engine", [(32, 0), (48, 0), (64, 0), (96, 0), (128, 2), (128, 0), (192, 0)])
+def test_register_projection_f64(NS, n, engine):
     import torch
 
     l = 2.0
     u = np.random.default_rng(n).standard_normal((3, n, n, n))
-    ps = NS.poissonsolver(NS.Grid(l, n), engine=0)
+    ps = NS.poissonsolver(NS.Grid(l, n), engine=engine)
     ut = dev(u)
     p = torch.empty((n, n, n), dtype=torch.float64, device="cuda")
     ps.project(ut, p)
@@ -66,7 +68,7 @@ def test_register_projection_f32(NS, n):
     assert rel(host(ut), ns.project(u, l / n)) < TOL32
 
 
-def engines_agree(NS, n, precision, tol, seed=0):
+def engines_agree(NS, n, precision, tol, seed=0, engines=(0, 1)):
     import torch
 
     dt = "float64" if precision == 0 else "float32"
@@ -74,7 +76,7 @@ def engines_agree(NS, n, precision, tol, seed=0):
     gen = torch.Generator(device="cuda").manual_seed(seed)
     u = torch.randn((3, n, n, n), generator=gen, device="cuda", dtype=getattr(torch, dt))
     out = []
-    for engine in (0, 1):
+    for engine in engines:
         ps = NS.poissonsolver(g, precision=precision, engine=engine)
         ut = u.clone()
         p = torch.empty((n, n, n), dtype=u.dtype, device="cuda")
@@ -82,7 +84,7 @@ def engines_agree(NS, n, precision, tol, seed=0):
         torch.cuda.synchronize()
         out.append((ut, p))
         ps.close()
-    (ua, pa), (ub, pb) = out
+    (ua, pa), (ub, pb) = out[0], out[-1]
     eu = float(torch.linalg.vector_norm((ua - ub).double()) / torch.linalg.vector_norm(ub.double()))
     ep = float(torch.linalg.vector_norm((pa - pb).double()) / torch.linalg.vector_norm(pb.double()))
     assert eu < tol and ep < tol, (n, eu, ep)
@@ -95,7 +97,15 @@ def engines_agree(NS, n, precision, tol, seed=0):
 
 @pytest.mark.parametrize("n", [192, 256])
 def test_register_engine_matches_stockham_f64(NS, n):
-    engines_agree(NS, n, 0, TOL64)
+    engines_agree(NS, n, 0, TOL64, engines=(2, 1))
+
+
+@pytest.mark.parametrize("n", [192, 256, 384, 1024])
+def test_mixed_precision_engine_matches_stockham_f64(NS, n):
+    """The mixed-precision FP64 solve (FP32 FFT solves refined by FP64
+    residuals) against the FP64 Stockham passes, on a white-noise field (the
+    hardest right-hand side for the refinement: no decay in the spectrum)."""
+    engines_agree(NS, n, 0, TOL64, engines=(0, 1))
 
 
 @pytest.mark.parametrize("n", [256, 384, 512, 1024])
@@ -107,4 +117,4 @@ def test_engine_argument_checked(NS):
     from exactclosure_gb300 import ExcError
 
     with pytest.raises(ExcError):
-        NS.poissonsolver(NS.Grid(1.0, 32), engine=2)
+        NS.poissonsolver(NS.Grid(1.0, 32), engine=3)

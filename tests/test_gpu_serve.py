@@ -87,7 +87,12 @@ def test_large_grid_batch_equals_alone_and_case(SV, prec, built_lib):
     cs = NS.Case(n, 1.0, visc, 0.3, precision=prec)
     cs.init_random(4.0, 1.0, seed)
     cs.step(nsteps)
-    assert np.array_equal(alone["field"], cs.velocity())
+    if prec == 1:
+        assert np.array_equal(alone["field"], cs.velocity())
+    else:
+        # the FP64 case path solves the pressure by mixed-precision refinement
+        # at this size, the served batch by the FP64 register passes
+        assert ns.rel_l2(alone["field"], cs.velocity()) < 1e-12
     cs.close()
     assert NS.device_faults() == 0
 
@@ -127,4 +132,36 @@ def test_autotuner_records_a_choice(SV):
     sv.drain()
     e, w, r = SV.Server.tuning(1, 32, 2)
     assert e in (0, 1) and w >= 1 and r >= 1
+    sv.close()
+
+
+def test_admission_bound_per_size(SV):
+    """With at most two active solves per grid size, a burst of five 32^3
+    requests runs two at a time (arrival order) next to a 24^3 solve; every
+    result is the same as without the bound."""
+    kw = [dict(n=32, visc=1 / 1000, nsteps=4 + k, seed=20 + k) for k in range(5)] + \
+         [dict(n=24, visc=1 / 2000, nsteps=6, seed=30)]
+    ref = {}
+    sv = SV.Server(precision=1)
+    for q in kw:
+        ref[q["seed"]] = sv.submit(q["n"], q["visc"], q["nsteps"], seed=q["seed"], keep_field=True)
+    sv.drain()
+    free = {r["id"]: r for r in sv.poll()}
+    sv.close()
+    sv = SV.Server(precision=1, max_active_per_size=2)
+    ids = {q["seed"]: sv.submit(q["n"], q["visc"], q["nsteps"], seed=q["seed"], keep_field=True) for q in kw}
+    done = {}
+    while len(done) < len(kw):
+        active, queued = sv.tick()
+        assert active <= 3  # two 32^3 solves and the 24^3 one
+        for r in sv.poll():
+            done[r["id"]] = r
+        if active == 0 and queued == 0:
+            sv.drain()
+    for seed, rid in ids.items():
+        assert np.array_equal(done[rid]["field"], free[ref[seed]]["field"]), seed
+    # the 32^3 requests are admitted in arrival order, two at first
+    t32 = sorted((done[ids[q["seed"]]]["t_admit"], q["seed"]) for q in kw if q["n"] == 32)
+    assert [s for _, s in t32] == [20, 21, 22, 23, 24]
+    assert done[ids[22]]["t_admit"] > done[ids[21]]["t_admit"]
     sv.close()

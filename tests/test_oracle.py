@@ -237,6 +237,42 @@ def test_paper_volavg_swap_closure_is_exact(doproject):
         assert ns.rel_l2(les2[k], ref) > 1e-4, k
 
 
+@pytest.mark.parametrize("n,c", [(24, 3), (24, 4), (30, 5), (16, 2)])
+def test_surface_line_filter_telescopes(n, c):
+    """The face average of the fine off-diagonal flux divergence over a
+    coarse face equals the coarse divergence of the line-filtered flux (the
+    `linefilter!` of dns_aid_surface, src/NavierStokes.jl:369), for odd and
+    even ratios, to round-off."""
+    l, visc = 1.0, 1 / 500
+    u = ns.randomfield(n, l, 3, 1)
+    _, p = ns.project(ns.rhs(u, visc, l / n), l / n, return_p=True)
+    a, b = ns.surface_offdiag_identity(u, p, visc, l, c)
+    assert ns.rel_l2(b, a) < 1e-13
+
+
+@pytest.mark.parametrize("c,doproject", [(3, True), (4, False)])
+def test_paper_surface_driver_properties(c, doproject):
+    """dns_aid_surface (src/NavierStokes.jl:306-468) as restated: the target
+    fiu (the face average) is divergence free on the LES grid; the swap flux
+    (line filter off the diagonal) is symmetric, so the swap and swap-
+    symmetric LES coincide; the swap LES stays closer to fiu than the no-model
+    LES; no LES is exact (the normal flux term of a face average is a fine
+    difference across the face)."""
+    n, l, visc = 24, 1.0, 1e-3
+    u = ns.randomfield(n, l, -5 / 3, 1, 1.0, profile="power")
+    fiu = ns.face_filter(u, c)
+    H = l / (n // c)
+    assert np.linalg.norm(ns.divergence(fiu, H)) < 1e-12 * np.linalg.norm(fiu) / H
+    les = {k: fiu.copy() for k in ns.PAPER_NAMES}
+    u2, les2, _, it = ns.dns_aid_surface_steps(u, les, visc, l, c, 0.05, 0.4, doproject, max_steps=3)
+    assert it == 3
+    ref = ns.face_filter(u2, c)
+    assert ns.rel_l2(les2["swapfil"], les2["swapfil_symm"]) < 1e-14
+    e = {k: ns.rel_l2(les2[k], ref) for k in ns.PAPER_NAMES}
+    assert e["swapfil"] < e["nomodel"]
+    assert min(e.values()) > 1e-6
+
+
 @pytest.mark.parametrize("dtype,ui,mask", [(np.float64, np.uint64, 0x7FFFFFFFFFFFFFFF), (np.float32, np.uint32, 0x7FFFFFFF)])
 def test_magnitude_bit_maximum(dtype, ui, mask):
     """The time step's max |u| is taken on the magnitude bits of the words:

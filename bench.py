@@ -57,8 +57,11 @@ def parse():
                     help="run one side workload alone and print its JSON object")
     ap.add_argument("--burgers-samples", type=int, default=1000)
     ap.add_argument("--burgers-tstop", type=float, default=0.1)
-    ap.add_argument("--large-steps", type=int, default=30)
-    ap.add_argument("--learned-steps", type=int, default=300)
+    ap.add_argument("--large-steps", type=int, default=300,
+                    help="steps of the 1024^3 run (pairs every 10 steps; the learned closure trains on them)")
+    ap.add_argument("--learned-steps", type=int, default=300, help="Adam steps of the learned closure")
+    ap.add_argument("--learned-les-steps", type=int, default=200,
+                    help="steps of the learned-closure LES in lockstep with the 1024^3 DNS")
     ap.add_argument("--forms-steps", type=int, default=200,
                     help="steps of the FP32-vs-FP64 error comparison (0: skip)")
     return ap.parse_args()
@@ -290,16 +293,30 @@ def rhs_section(args, launches=4):
     return {"n": n, "precision": args.precision, "launches": launches, "ms_per_launch": e0.elapsed_time(e1) / launches}
 
 
-def large_section(n=1024, nsteps=30, every=10):
-    """DNS-aided LES at 1024^3 in FP32 (FP64 spectral divide), nu = 1/8000,
-    k0 = 8, exact closure at every RK4 stage for 64^3 and 128^3 LES grids with
-    both the volume and the face filter, filtered-velocity/closure pairs of
-    the 64^3 volume LES written every `every` steps (raw binary + JSON header).
-    A bounded sample of the 500-step run: `nsteps` steps."""
+def large_and_learned_sections(n=1024, nsteps=300, every=10, do_large=True, do_learned=True, train_steps=300,
+                               les_steps=200, peaks_json=None):
+    """The large DNS-aided LES and the learned closure trained on its data.
+
+    Large: DNS at 1024^3 in FP32 (FP64 spectral divide), nu = 1/8000, k0 = 8,
+    exact closure at every RK4 stage for 64^3 and 128^3 LES grids with both
+    the volume and the face filter; (filtered velocity, exact closure) pairs
+    of the 64^3 volume LES written every `every` steps (raw binary + JSON
+    header).  A bounded sample of the 500-step run: `nsteps` steps.
+
+    Learned: 3 BF16 conv layers 3->32->32->3, 3^3 periodic, GELU, FP32
+    accumulation, Adam lr 1e-3, batch 8 snapshots of 64^3 x 3, trained on the
+    pairs the large run wrote (read back from its files): the first 80% of
+    the run for training, the last 20% held out (a later part of the run).
+    Then the net drives a 64^3 LES in lockstep with the same DNS from its
+    filtered state for `les_steps` steps (a sample of the 2000 steps), with
+    the no-model fallback armed; errors against the filtered DNS beside the
+    no-model and exact-closure LES."""
     import tempfile
 
+    import numpy as np
     import torch
 
+    from exactclosure_gb300 import learned as LN
     from exactclosure_gb300 import navierstokes as NS
     from exactclosure_gb300 import snapshots
 
@@ -309,80 +326,90 @@ def large_section(n=1024, nsteps=30, every=10):
     cs.init_random(8.0, 1.0, seed=0)
     cs.step(1)
     cs.sync()
+    large = learned = None
+    nsnap = max(1, nsteps // every)
     with tempfile.TemporaryDirectory() as td:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        hp = snapshots.write_pairs(cs, 0, td, nsnap=max(1, nsteps // every), every=every, stem="large")
+        hp = snapshots.write_pairs(cs, 0, td, nsnap=nsnap, every=every, stem="large")
         cs.sync()
         el = time.perf_counter() - t0
         nbytes = sum(f.stat().st_size for f in Path(td).iterdir())
         nfiles = len(list(Path(td).glob("large_*.bin")))
-    steps = max(1, nsteps // every) * every
-    errs = {f"{n // c}^3 {k}": cs.errors(i)[0] for i, (c, k) in enumerate(les)}
-    out = {"metric": "cell-updates/s", "value": n ** 3 * steps / el, "unit": "cell-updates/s", "dtype": "f32",
-           "steps": steps, "seconds": el,
-           "config": {"workload": f"DNS {n}^3 FP32 (FP64 spectral divide), nu 1/8000, k0 8, exact closure every "
-                                  f"RK4 stage for LES 64^3 and 128^3 x volume/face, pairs every {every} steps",
-                      "sample": f"{steps} of the 500 steps"},
-           "snapshots": {"files": nfiles, "bytes": nbytes, "header": Path(hp).name},
-           "exact_closure_error_vs_filtered_dns": errs,
-           "timing": "wall clock around the stepping and the snapshot writes (host copies included)"}
+        if do_learned:
+            U_np, M_np, header = snapshots.read_pairs(hp)
+    steps = nsnap * every
+    if do_large:
+        errs = {f"{n // c}^3 {k}": cs.errors(i)[0] for i, (c, k) in enumerate(les)}
+        large = {"metric": "cell-updates/s", "value": n ** 3 * steps / el, "unit": "cell-updates/s", "dtype": "f32",
+                 "steps": steps, "seconds": el,
+                 "config": {"workload": f"DNS {n}^3 FP32 (FP64 spectral divide), nu 1/8000, k0 8, exact closure every "
+                                        f"RK4 stage for LES 64^3 and 128^3 x volume/face, pairs every {every} steps",
+                            "sample": f"{steps} of the 500 steps"},
+                 "snapshots": {"files": nfiles, "bytes": nbytes, "header": Path(hp).name},
+                 "exact_closure_error_vs_filtered_dns": errs,
+                 "timing": "wall clock around the stepping and the snapshot writes (host copies included)"}
+    if do_learned:
+        S = U_np.shape[0]
+        ntr = max(1, int(round(0.8 * S)))
+        U = torch.tensor(U_np, dtype=torch.float32, device="cuda")
+        M = torch.tensor(M_np, dtype=torch.float32, device="cuda")
+        del U_np, M_np
+        net = LN.Net(seed=1)
+        LN.train(net, U[:ntr], M[:ntr], steps=3)  # warm-up (also fixes the scales)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        losses = LN.train(net, U[:ntr], M[:ntr], steps=train_steps, batch=8, lr=1e-3)
+        torch.cuda.synchronize()
+        tel = time.perf_counter() - t0
+        m = n // les[0][0]
+        flop_fwd = 2 * 27 * (3 * 32 + 32 * 32 + 32 * 3) * m ** 3  # per sample, useful channels
+        flops = 3 * flop_fwd * 8 * train_steps  # forward + input and weight gradients
+        pred = torch.empty_like(U[ntr:])
+        net.forward(U[ntr:].contiguous(), pred)
+        torch.cuda.synchronize()
+        e_closure = float((pred - M[ntr:]).double().norm() / M[ntr:].double().norm())
+        pred_tr = torch.empty_like(U[:ntr])
+        net.forward(U[:ntr].contiguous(), pred_tr)
+        torch.cuda.synchronize()
+        e_closure_train = float((pred_tr - M[:ntr]).double().norm() / M[:ntr].double().norm())
+        del pred, pred_tr
+        # a posteriori: the learned LES in lockstep with the DNS, fallback armed
+        cs.reset_les()
+        cs.attach_net(0, net)
+        e0 = 0.5 * float(U[-1].double().pow(2).sum()) / m ** 3
+        cs.set_fallback(0, 0.0, 4.0 * e0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cs.step(les_steps)
+        cs.sync()
+        les_el = time.perf_counter() - t0
+        achieved = flops / tel / 1e12
+        peak = (peaks_json or {}).get("bf16_tflops")
+        times = header["times_after_step"]
+        learned = {
+            "metric": "training samples/s", "value": 8 * train_steps / tel, "unit": "samples/s",
+            "dtype": "bf16 (fp32 accumulate)",
+            "config": {"workload": f"conv 3->32->32->3 on {m}^3 x 3, batch 8, Adam lr 1e-3, {train_steps} steps; "
+                                   f"trained on the {n}^3 run's pairs (files), {ntr} of {S} snapshots "
+                                   f"(t <= {times[ntr - 1]:.4f}), held out the last {S - ntr} (t >= {times[ntr]:.4f})"
+                       if S > ntr else f"{S} snapshots"},
+            "tensor": {"achieved_tflops": achieved, "peak_tflops": peak, "frac": (achieved / peak) if peak else None,
+                       "note": "useful-channel flops (3->32->32->3) of forward + both gradients; BF16 on tcgen05 "
+                               "(32-channel-input convolutions, tensor-memory accumulators) and mma.sync (the rest)"},
+            "loss_first_last": [losses[0], losses[-1]],
+            "closure_error_vs_exact": {"held_out_later_snapshots": e_closure, "training_snapshots": e_closure_train,
+                                       "no_model": 1.0},
+            "les_in_lockstep": {"steps": les_steps, "sample": f"{les_steps} of the 2000 steps", "seconds": les_el,
+                                "error_vs_filtered_dns": {"learned": cs.les_error(0, "learned"),
+                                                          "nomodel": cs.les_error(0, "nomodel"),
+                                                          "exact": cs.les_error(0, "exact")},
+                                "fallback_band": [0.0, 4.0 * e0], "fallback_engaged": cs.fallback_engaged(0)}}
+        net.close()
+        del U, M
     cs.close()
     torch.cuda.empty_cache()
-    return out
-
-
-def learned_section(train_steps=300, les_steps=100, peaks_json=None):
-    """Learned closure: 3 BF16 conv layers 3->32->32->3, 3^3 periodic, GELU,
-    FP32 accumulation, Adam lr 1e-3, batch 8 snapshots of 64^3 x 3, trained on
-    (filtered velocity, exact closure) pairs of a GPU DNS-aided run (256^3
-    FP32 DNS, 64^3 volume LES), then run inside the LES; errors against the
-    exact closure and the no-model LES."""
-    import torch
-
-    from exactclosure_gb300 import learned as LN
-    from exactclosure_gb300 import navierstokes as NS
-
-    n, c = 256, 4
-    cs = NS.Case(n, 1.0, 1 / 2000, 0.3, precision=1, les=[(c, "volume")])
-    cs.init_random(4.0, 1.0, 0)
-    cs.step(10)
-    U, M = LN.collect_pairs(cs, 0, nsnap=64, every=1)
-    net = LN.Net(seed=1)
-    LN.train(net, U[:8], M[:8], steps=3)  # warm-up (also fixes the scales)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    losses = LN.train(net, U[:56], M[:56], steps=train_steps, batch=8, lr=1e-3)
-    torch.cuda.synchronize()
-    el = time.perf_counter() - t0
-    m = n // c
-    flop_fwd = 2 * 27 * (3 * 32 + 32 * 32 + 32 * 3) * m ** 3  # per sample, useful channels
-    flops = 3 * flop_fwd * 8 * train_steps  # forward + input and weight gradients
-    pred = torch.empty_like(U[56:])
-    net.forward(U[56:].contiguous(), pred)
-    torch.cuda.synchronize()
-    e_closure = float((pred - M[56:]).double().norm() / M[56:].double().norm())
-    cs.reset_les()
-    cs.attach_net(0, net)
-    cs.step(les_steps)
-    cs.sync()
-    achieved = flops / el / 1e12
-    peak = (peaks_json or {}).get("bf16_tflops")
-    out = {"metric": "training samples/s", "value": 8 * train_steps / el, "unit": "samples/s",
-           "dtype": "bf16 (fp32 accumulate)",
-           "config": {"workload": f"conv 3->32->32->3 on {m}^3 x 3, batch 8, Adam lr 1e-3, {train_steps} steps; "
-                                  f"pairs from a {n}^3 FP32 DNS-aided run"},
-           "tensor": {"achieved_tflops": achieved, "peak_tflops": peak,
-                      "frac": (achieved / peak) if peak else None,
-                      "note": "useful-channel flops (3->32->32->3) of forward + both gradients; BF16 on tcgen05 (32-channel-input convolutions, tensor-memory accumulators) and mma.sync (the rest)"},
-           "loss_first_last": [losses[0], losses[-1]],
-           "held_out_closure_error": e_closure,
-           "les_error_after_steps": {"steps": les_steps, "learned": cs.les_error(0, "learned"),
-                                     "nomodel": cs.les_error(0, "nomodel"), "exact": cs.les_error(0, "exact")}}
-    net.close()
-    cs.close()
-    torch.cuda.empty_cache()
-    return out
+    return large, learned
 
 
 def burgers_section(nsample=1000, grids=(300, 900, 2700), cpu=True, tstop=0.1):
@@ -628,8 +655,10 @@ def main():
     if args.only:
         pk = measured_peaks()
         fn = {"burgers": lambda: burgers_section(args.burgers_samples, cpu=not args.no_cpu, tstop=args.burgers_tstop),
-              "large": lambda: large_section(nsteps=args.large_steps),
-              "learned": lambda: learned_section(args.learned_steps, peaks_json=pk),
+              "large": lambda: large_and_learned_sections(nsteps=args.large_steps, do_learned=False)[0],
+              "learned": lambda: large_and_learned_sections(nsteps=args.large_steps, do_large=False,
+                                                            train_steps=args.learned_steps,
+                                                            les_steps=args.learned_les_steps, peaks_json=pk)[1],
               "c1": lambda: c1_section(cpu=not args.no_cpu),
               "rhs": lambda: rhs_section(args)}[args.only]
         print(json.dumps({args.only: fn()}))
@@ -757,16 +786,15 @@ def main():
             c1 = c1_section(cpu=not args.no_cpu)
         except Exception as ex:
             c1 = {"error": str(ex)}
-    if rank == 0 and world == 1 and not args.no_large:
+    if rank == 0 and world == 1 and not (args.no_large and args.no_learned):
         try:
-            large = large_section(nsteps=args.large_steps)
+            large, learned = large_and_learned_sections(nsteps=args.large_steps, do_large=not args.no_large,
+                                                        do_learned=not args.no_learned,
+                                                        train_steps=args.learned_steps,
+                                                        les_steps=args.learned_les_steps,
+                                                        peaks_json=measured_peaks())
         except Exception as ex:
-            large = {"error": str(ex)}
-    if rank == 0 and world == 1 and not args.no_learned:
-        try:
-            learned = learned_section(args.learned_steps, peaks_json=measured_peaks())
-        except Exception as ex:
-            learned = {"error": str(ex)}
+            large = learned = {"error": str(ex)}
     burgers = None
     if rank == 0 and world == 1 and not args.no_burgers:
         try:

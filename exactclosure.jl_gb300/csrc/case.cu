@@ -42,6 +42,11 @@ struct LesState {
   T *vn[2], *vns, *kn;  // no-model LES
   T* ublast;            // target at stage 0 of the last step (pairs with mlast)
   T *vl[2], *vls, *kl, *nn;  // LES driven by the learned closure (when a net is attached)
+  T* vgood;                  // its last state inside the energy band (fallback)
+  // fallback of the learned LES (device, 8 doubles): [0] engaged (0/1), [1]
+  // lower and [2] upper bound of its kinetic energy, [3] sum of squares of
+  // the state ([4] the reduction's second word)
+  double* fb = nullptr;
   exc_net* net = nullptr;
 };
 
@@ -80,6 +85,38 @@ struct CaseImpl {
   long long net_gen = 0;  // workspace generations of attached nets at capture
   int kernels_per_step = 0;  // kernel nodes in the captured step graph
 };
+
+// No-model fallback of a learned-closure LES, checked before every step on
+// the device: with E = 1/2 sum v^2 / M of the current state, a state whose E
+// is not finite or leaves [fb[1], fb[2]] is replaced by the last state inside
+// the band and the fallback is engaged for good (fb[0] = 1); a state inside
+// the band becomes the last good one.  Every thread decides from the same
+// fb[3] (written by the preceding reduction), so the grid agrees.
+template <typename T>
+__global__ void learned_guard_kernel(long long count, T* __restrict__ v, T* __restrict__ good,
+                                     double* __restrict__ fb, double inv_m) {
+  const double e = 0.5 * fb[3] * inv_m;
+  const bool bad = !(e >= fb[1] && e <= fb[2]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    if (bad) v[i] = good[i];
+    else good[i] = v[i];
+  }
+  if (bad && blockIdx.x == 0 && threadIdx.x == 0) fb[0] = 1.0;
+}
+
+// y += x unless the fallback is engaged (the net's closure term).
+template <typename T>
+__global__ void add_unless_kernel(long long count, T* __restrict__ y, const T* __restrict__ x,
+                                  const double* __restrict__ fb) {
+  if (fb[0] != 0.0) return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    y[i] += x[i];
+}
+
+static int grid_for_count(long long cnt) {
+  long long b = (cnt + 255) / 256;
+  return (int)(b < 152LL * 8 ? b : 152LL * 8);
+}
 
 template <typename T>
 static int project_vec(exc_poisson* ps, T* u, cudaStream_t st) {
@@ -185,6 +222,18 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
   if (e == cudaSuccess)
     e = launch_set_dt(ci->dscal + 2, ci->h, cs->desc.visc, cs->desc.cfl, dt_fixed, dt, ci->dscal + 1, ci->dflag, st);
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  // no-model fallback of the learned-closure LES (energy band, finiteness)
+  for (int li = 0; li < ci->nles; ++li) {
+    LesState<T>& L = ci->les[li];
+    if (!L.net) continue;
+    e = launch_sqdiff<T>(3 * L.M, L.vl[cur], nullptr, ci->part, L.fb + 3, st);
+    if (e == cudaSuccess) {
+      learned_guard_kernel<T><<<grid_for_count(3 * L.M), 256, 0, st>>>(3 * L.M, L.vl[cur], L.vgood, L.fb,
+                                                                        1.0 / (double)L.M);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  }
   const bool fused = ci->fuse_root >= 0;
   T* const root_k = fused ? ci->les[ci->fuse_root].tb : nullptr;   // sums of k_s
   T* const root_s = fused ? ci->les[ci->fuse_root].tb2 : nullptr;  // sums of the stage state
@@ -277,7 +326,8 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
         if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
         rc = exc_net_forward(L.net, cs->precision, 1, m, vsrc, L.nn, st);
         if (rc) return rc;
-        e = launch_axpy<T>(3 * L.M, L.kl, L.nn, (T)1, st);
+        add_unless_kernel<T><<<grid_for_count(3 * L.M), 256, 0, st>>>(3 * L.M, L.kl, L.nn, L.fb);
+        e = cudaGetLastError();
         if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
         rc = project_vec<T>(&L.ps, L.kl, st);
         if (rc) return rc;
@@ -367,6 +417,7 @@ static void case_destroy(exc_case* cs) {
     if (ci->les[li].buf) cudaFree(ci->les[li].buf);
     if (ci->les[li].tb) cudaFree(ci->les[li].tb);
     if (ci->les[li].tb2) cudaFree(ci->les[li].tb2);
+    if (ci->les[li].fb) cudaFree(ci->les[li].fb);
   }
   delete ci;
   cs->impl = nullptr;
@@ -384,6 +435,9 @@ static int case_create(exc_case* cs) {
   ci->h = d.l / d.n;
   int rc = poisson_init(&ci->ps, cs->precision, d.n, d.l, nullptr);
   if (rc) return rc;
+  // the DNS pressure enters only through its gradient (RK stage): its
+  // additive constant need not be removed
+  ci->ps.mix_zero_mean = false;
   size_t vb = 3 * ci->N * sizeof(T);
   void* big = nullptr;
   if (cudaMalloc(&big, 4 * vb) != cudaSuccess) { set_last_error("out of device memory (DNS fields)"); return EXC_ERR_OOM; }
@@ -408,7 +462,7 @@ static int case_create(exc_case* cs) {
     L.M = (long long)L.m * L.m * L.m;
     rc = poisson_init(&L.ps, cs->precision, L.m, d.l, nullptr);
     if (rc) return rc;
-    size_t nb = 20 * 3 * L.M * sizeof(T);
+    size_t nb = 21 * 3 * L.M * sizeof(T);
     if (cudaMalloc(&L.buf, nb) != cudaSuccess) { set_last_error("out of device memory (LES fields)"); return EXC_ERR_OOM; }
     cudaMemset(L.buf, 0, nb);
     size_t tbb = 3 * (size_t)d.n * L.m * L.m * sizeof(T);
@@ -420,6 +474,11 @@ static int case_create(exc_case* cs) {
     L.vn[0] = take(); L.vn[1] = take(); L.vns = take(); L.kn = take();
     L.ublast = take();
     L.vl[0] = take(); L.vl[1] = take(); L.vls = take(); L.kl = take(); L.nn = take();
+    L.vgood = take();
+    // 8 doubles: fb[3..4] receive the two-word result of the sum of squares
+    if (cudaMalloc(&L.fb, 8 * sizeof(double)) != cudaSuccess) { set_last_error("out of device memory (LES fallback)"); return EXC_ERR_OOM; }
+    const double fb0[8] = {0.0, 0.0, INFINITY, 0.0, 0.0, 0.0, 0.0, 0.0};
+    cudaMemcpy(L.fb, fb0, sizeof(fb0), cudaMemcpyHostToDevice);
   }
   // sources of the transverse box sums: an earlier LES of the same ratio, else
   // the LES with the largest ratio that divides this one, else the fine field
@@ -478,6 +537,8 @@ static int reset_les(exc_case* cs) {
     cudaMemcpyAsync(L.ve[ci->cur], L.ub, b, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(L.vn[ci->cur], L.ub, b, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(L.vl[ci->cur], L.ub, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(L.vgood, L.ub, b, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(L.fb, 0, sizeof(double), st);  // fallback disengaged
     cudaMemcpyAsync(L.ublast, L.ub, b, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(L.mlast, 0, b, st);
   }
@@ -612,6 +673,29 @@ static int attach_net(exc_case* cs, int li, exc_net* net) {
   ci->net_gen = net_generation(ci);
   size_t b = 3 * L.M * sizeof(T);
   cudaMemcpyAsync(L.vl[ci->cur], L.ve[ci->cur], b, cudaMemcpyDeviceToDevice, cs->stream);
+  cudaMemcpyAsync(L.vgood, L.ve[ci->cur], b, cudaMemcpyDeviceToDevice, cs->stream);
+  cudaMemsetAsync(L.fb, 0, sizeof(double), cs->stream);
+  return EXC_OK;
+}
+
+template <typename T>
+static int set_fallback(exc_case* cs, int li, double e_lo, double e_hi) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  const double band[2] = {e_lo, e_hi};
+  cudaError_t e = cudaMemcpyAsync(ci->les[li].fb + 1, band, sizeof(band), cudaMemcpyHostToDevice, cs->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs->stream);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
+template <typename T>
+static int fallback_state(exc_case* cs, int li, int* engaged) {
+  CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
+  double v = 0.0;
+  cudaError_t e = cudaMemcpyAsync(&v, ci->les[li].fb, sizeof(double), cudaMemcpyDeviceToHost, cs->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs->stream);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  *engaged = v != 0.0;
   return EXC_OK;
 }
 
@@ -822,6 +906,16 @@ int exc_case_snapshot(exc_case* cs, int li, void* dev_u, void* dev_m) {
 int exc_case_attach_net(exc_case* cs, int li, exc_net* net) {
   if (!cs || li < 0 || li >= cs->desc.nles) { set_last_error("bad argument"); return EXC_ERR_ARG; }
   return DISPATCH(cs, attach_net, cs, li, net);
+}
+
+int exc_case_set_fallback(exc_case* cs, int li, double e_lo, double e_hi) {
+  if (!cs || li < 0 || li >= cs->desc.nles || !(e_lo <= e_hi)) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, set_fallback, cs, li, e_lo, e_hi);
+}
+
+int exc_case_fallback(exc_case* cs, int li, int* engaged) {
+  if (!cs || !engaged || li < 0 || li >= cs->desc.nles) { set_last_error("bad argument"); return EXC_ERR_ARG; }
+  return DISPATCH(cs, fallback_state, cs, li, engaged);
 }
 
 int exc_case_step(exc_case* cs, int nsteps, double dt_fixed) {

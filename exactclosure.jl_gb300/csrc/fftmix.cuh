@@ -20,7 +20,9 @@
 // solves carry the factor 1/h in their 1/(lambda N) table); the pressure's
 // mean (the solution's free constant, which the FP32 solves leave at their
 // rounding level) is measured during the last residual pass and removed in
-// the last accumulation, so p has zero mean like the reference's.
+// the last accumulation, so p has zero mean like the reference's -- unless
+// the owner reads p only through its gradient (mix_zero_mean false: the case
+// stepper), where the constant changes nothing.
 //
 // Included by fftreg_f32.cu only: the FP32 column kernels it launches must be
 // the instantiations of that translation unit, whose shared-memory opt-ins
@@ -33,11 +35,41 @@ namespace exc {
 enum { MIX_DIV = 0, MIX_SCAL = 1, MIX_RES = 2, MIX_RES_MEAN = 3 };
 enum { MIX_SET = 0, MIX_ADD = 1, MIX_ADD_MEAN = 2 };
 
+// Conversions between the FP64 fields and the FP32 transforms on the integer
+// pipe (the FP64 pipe, about two operations per clock per SM on GB300, is the
+// solve's bottleneck), by moving the IEEE 754 binary64/binary32 fields:
+// exponent rebiased by 1023 - 127 = 896, mantissa shifted by 29 bits.
+//
+// FP64 -> FP32 truncates the mantissa (the refinement needs about seven
+// digits from each FP32 solve, not a rounded input); magnitudes below the
+// smallest normal float become a signed zero, above the largest float an
+// infinity, NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32_trunc(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned a = hi & 0x7FFFFFFFu, sign = hi & 0x80000000u;
+  const unsigned t = a - 0x38000000u;  // exponent field minus 896 (in bits 30..20)
+  unsigned f = (__funnelshift_l(lo, t, 3) & 0x7FFFFFFFu) | sign;
+  if (a < 0x38100000u) f = sign;  // below 2^-126 (and zero)
+  if (a >= 0x47F00000u) f = sign | 0x7F800000u | ((a > 0x7FF00000u || (a == 0x7FF00000u && lo)) ? 0x400000u : 0u);
+  return __uint_as_float(f);
+}
+
+// FP32 -> FP64, exact for normal numbers, zeros, infinities and NaN (float
+// subnormals, below 1.2e-38, become a signed zero).
+__device__ __forceinline__ double f32_to_f64(float v) {
+  const unsigned b = __float_as_uint(v);
+  const unsigned a = b & 0x7FFFFFFFu, sign = b & 0x80000000u;
+  unsigned hi = ((a >> 3) + (a >= 0x7F800000u ? 0x70000000u : 0x38000000u)) | sign;
+  unsigned lo = b << 29;
+  if (a < 0x00800000u) { hi = sign; lo = 0u; }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
 template <typename C>
 __device__ __forceinline__ C to_f32c(double a, double b) {
   C r;
-  r.x = (float)a;
-  r.y = (float)b;
+  r.x = f64_to_f32_trunc(a);
+  r.y = f64_to_f32_trunc(b);
   return r;
 }
 
@@ -253,17 +285,18 @@ mc2r_kernel(const cplx<float>* __restrict__ g, int P, const cplx<float>* __restr
     for (int k2 = 0; k2 < N2; ++k2) {
       const int m = k1 + N1 * k2;
       double2 o;
+      const double cx = f32_to_f64(zz[k2].x), cy = f32_to_f64(zz[k2].y);
       if constexpr (MODE == MIX_SET) {
-        o.x = (double)zz[k2].x;
-        o.y = (double)zz[k2].y;
+        o.x = cx;
+        o.y = cy;
       } else {
         const double2 a = r[m];
         if constexpr (MODE == MIX_ADD) {
-          o.x = a.x + (double)zz[k2].x;
-          o.y = a.y + (double)zz[k2].y;
+          o.x = a.x + cx;
+          o.y = a.y + cy;
         } else {
-          o.x = (a.x - mu) + (double)zz[k2].x;
-          o.y = (a.y - mu) + (double)zz[k2].y;
+          o.x = (a.x - mu) + cx;
+          o.y = (a.y - mu) + cy;
         }
       }
       r[m] = o;
@@ -364,10 +397,16 @@ struct MixSolve {
     mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
     columns();
     mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
-    mr2c_kernel<B1, B2, MIX_RES_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
-    mix_mean_kernel<<<1, 256, 0, st>>>(part, (int)NPARTS, 1.0 / ((double)n * n * n), mean);
-    columns();
-    mc2r_kernel<B1, B2, MIX_ADD_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+    if (ps->mix_zero_mean) {
+      mr2c_kernel<B1, B2, MIX_RES_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+      mix_mean_kernel<<<1, 256, 0, st>>>(part, (int)NPARTS, 1.0 / ((double)n * n * n), mean);
+      columns();
+      mc2r_kernel<B1, B2, MIX_ADD_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+    } else {
+      mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+      columns();
+      mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+    }
     return cudaGetLastError();
   }
 };

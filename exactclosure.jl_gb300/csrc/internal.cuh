@@ -34,6 +34,9 @@ struct exc_poisson {
   exc_poisson* mix = nullptr;
   double* mix_d = nullptr;
   double* mix_part = nullptr;
+  // remove the pressure's mean (its free constant) in the mixed solve; false
+  // where p is only used through its gradient
+  bool mix_zero_mean = true;
 };
 
 namespace exc {
@@ -78,6 +81,8 @@ cudaError_t configure_fftmix();
 void fftreg_geometry(int n, int precision, int* col_w, int* x_rows);
 // Read and clear the learned closure's tensor-core wait fault flag.
 int learned_fault_take(int* flag);
+// Set the tensor-core convolution's wait drill (exc_debug_wait_drill bit 1).
+int learned_set_drill(int on);
 cudaError_t configure_fftreg_f32();
 cudaError_t configure_fftreg_f64();
 

@@ -462,6 +462,11 @@ struct HaloMaps {
 };
 
 __device__ int g_learned_fault = 0;
+// Wait drill (exc_debug_wait_drill bit 1): the load warp issues no copy at
+// all, so the products and the epilogue wait for data that never comes; every
+// wait then gives up after CU_DRILL_POLLS polls with nothing in flight.
+__device__ int g_learned_drill = 0;
+constexpr int CU_POLLS = 1 << 20, CU_DRILL_POLLS = 64;
 
 constexpr int cu_row_bytes = CU_N * 16;  // one row of one chunk
 constexpr int cu_halo_bytes = CU_HZ * CU_KC * CU_HY * cu_row_bytes;
@@ -509,8 +514,8 @@ __device__ __forceinline__ bool cu_try_wait(unsigned long long* bar, unsigned pa
   return ok != 0;
 }
 // bounded wait for the phase of `parity` to complete
-__device__ __forceinline__ bool cu_wait(unsigned long long* bar, unsigned parity) {
-  for (int polls = 0; polls < (1 << 20); ++polls)
+__device__ __forceinline__ bool cu_wait(unsigned long long* bar, unsigned parity, int limit = CU_POLLS) {
+  for (int polls = 0; polls < limit; ++polls)
     if (cu_try_wait(bar, parity)) return true;
   return false;
 }
@@ -584,6 +589,8 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
     atomicExch(&g_learned_fault, 1);
     *s_abort = 1;
   };
+  const bool drill = g_learned_drill != 0;
+  const int polls = drill ? CU_DRILL_POLLS : CU_POLLS;
 
   // weights: tap (dx, dy, dz) = dz 9 + dy 3 + dx -> [dy, dz][chunk][dx NP + co][8]
   for (int t = tid; t < NET_TAPS * NP * KC; t += CU_THREADS) {
@@ -617,9 +624,9 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
   if (warp == 1) {
     // ---- loads ----
     int i = 0;
-    for (; i < nb; ++i) {
+    for (; i < nb && !drill; ++i) {
       const int buf = i & 1;
-      if (i >= 2 && !__all_sync(0xffffffffu, cu_wait(&hempty[buf], (unsigned)(((i - 2) >> 1) & 1)))) {
+      if (i >= 2 && !__all_sync(0xffffffffu, cu_wait(&hempty[buf], (unsigned)(((i - 2) >> 1) & 1), polls))) {
         if (lane == 0) fault();
         break;
       }
@@ -648,7 +655,7 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
     }
     // copies in flight: the last two issued batches land (bounded)
     for (int j = i - 2; j < i; ++j)
-      if (j >= 0 && !__all_sync(0xffffffffu, cu_wait(&hfull[j & 1], (unsigned)((j >> 1) & 1))) && lane == 0) fault();
+      if (j >= 0 && !__all_sync(0xffffffffu, cu_wait(&hfull[j & 1], (unsigned)((j >> 1) & 1), polls)) && lane == 0) fault();
   } else if (warp == 0) {
     // ---- products ----
     if (lane == 0) {
@@ -656,8 +663,8 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
       int i = 0;
       for (; i < nb; ++i) {
         const int buf = i & 1;
-        if (!cu_wait(&hfull[buf], (unsigned)((i >> 1) & 1)) ||
-            (i >= 2 && !cu_wait(&aempty[buf], (unsigned)(((i - 2) >> 1) & 1)))) {
+        if (!cu_wait(&hfull[buf], (unsigned)((i >> 1) & 1), polls) ||
+            (i >= 2 && !cu_wait(&aempty[buf], (unsigned)(((i - 2) >> 1) & 1), polls))) {
           fault();
           break;
         }
@@ -681,7 +688,7 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
         umma_commit(&afull[buf]);
       }
       // products in flight complete (bounded)
-      if (i > 0 && !cu_wait(&afull[(i - 1) & 1], (unsigned)(((i - 1) >> 1) & 1))) fault();
+      if (i > 0 && !cu_wait(&afull[(i - 1) & 1], (unsigned)(((i - 1) >> 1) & 1), polls)) fault();
     }
     __syncwarp();
   } else {
@@ -696,7 +703,7 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
     for (int j = 0; j < NH; ++j) bb[j] = (EPI == 2) ? 0.f : __ldg(bias + cb + j);
     for (int i = 0; i < nb; ++i) {
       const int set = i & 1;
-      if (!__all_sync(0xffffffffu, cu_wait(&afull[set], (unsigned)((i >> 1) & 1)))) {
+      if (!__all_sync(0xffffffffu, cu_wait(&afull[set], (unsigned)((i >> 1) & 1), polls))) {
         if (lane == 0) fault();
         break;
       }
@@ -723,7 +730,7 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
       __syncwarp();
       unsigned long long* const xb = &xbar[((warp - 2) >> 1) * 2 + (i & 1)];
       if (lane == 0) cu_arrive(xb);
-      if (!__all_sync(0xffffffffu, cu_wait(xb, (unsigned)((i >> 1) & 1)))) {
+      if (!__all_sync(0xffffffffu, cu_wait(xb, (unsigned)((i >> 1) & 1), polls))) {
         if (lane == 0) fault();
         break;
       }
@@ -1503,6 +1510,12 @@ static int configure_learned() {
 }
 
 // Read and clear the flag of a tensor-core wait that gave up.
+int learned_set_drill(int on) {
+  cudaError_t e = cudaMemcpyToSymbol(g_learned_drill, &on, sizeof(int));
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return EXC_OK;
+}
+
 int learned_fault_take(int* flag) {
   int v = 0, zero = 0;
   cudaError_t e = cudaMemcpyFromSymbol(&v, g_learned_fault, sizeof(int));

@@ -12,8 +12,6 @@
 // GPU race.  Each call writes every scratch word it reads (tables first, then
 // the spectrum) before reading it, so the previous call's contents need no
 // clearing.
-#include <mutex>
-
 #include "internal.cuh"
 
 namespace exc {
@@ -21,27 +19,19 @@ namespace exc {
 constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(4) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-// Device address of the scratch array, looked up once per device with that
-// device current (a host-side reference to the symbol is not a device address).
+// Device address of the scratch array in the current context, looked up on
+// every call (a host-side reference to the symbol is not a device address).
+// The lookup is a cheap host call; not caching it keeps the address right
+// after a device reset or a new primary context, which reload the module and
+// may place the array elsewhere.
 static int noalloc_scratch_address(void** out) {
-  static std::mutex mu;
-  static void* addr[64];
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-    set_last_error("no usable CUDA device");
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    set_last_error(e != cudaSuccess ? cudaGetErrorString(e) : "cudaGetSymbolAddress returned null");
     return EXC_ERR_CUDA;
   }
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      set_last_error(e != cudaSuccess ? cudaGetErrorString(e) : "cudaGetSymbolAddress returned null");
-      return EXC_ERR_CUDA;
-    }
-    addr[dev] = p;
-  }
-  *out = addr[dev];
+  *out = p;
   return EXC_OK;
 }
 

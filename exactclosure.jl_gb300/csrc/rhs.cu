@@ -23,6 +23,12 @@ namespace exc {
 // Set when a wait for a TMA plane gave up (the copy never completed): the
 // sweep then ran on incomplete data; read and cleared by exc_device_faults.
 __device__ int g_rhs_tma_fault = 0;
+// Wait drill (exc_debug_wait_drill bit 0): tiles that would take their planes
+// by TMA issue no copy at all, so their plane waits give up after
+// RHS_DRILL_POLLS polls with nothing in flight (the sweep's output is then
+// not valid); 0 in normal operation.
+__device__ int g_rhs_drill = 0;
+constexpr int RHS_POLLS = 1 << 20, RHS_DRILL_POLLS = 64;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
@@ -189,6 +195,8 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   // on the buffer's mbarrier; the others use the cp.async pieces
   const bool tma = vec && have_map && x0 >= VE && x0 - VE + UROW<T> <= n && y0 >= 1 && y0 + PTY + 1 <= n;
   unsigned parity = 0;  // bit b: phase of buffer b's mbarrier to wait for
+  const bool drill = tma && g_rhs_drill != 0;
+  const int poll_limit = drill ? RHS_DRILL_POLLS : RHS_POLLS;
   if (tma) {
     if (tid == 0) {
 #pragma unroll
@@ -199,7 +207,7 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   }
   auto load_plane = [&](int buf, int gz) {
     if (tma) {
-      if (tid == 0) {
+      if (tid == 0 && !drill) {
         mbar_expect_tx(&sm.bar[buf], 3u * CompPlane<T, NC>::WORDS * sizeof(T));
 #pragma unroll
         for (int c = 0; c < 3; ++c)
@@ -232,8 +240,8 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   // prologue: planes z0-1 (buffer 0) and z0 (buffer 1) give s13, s23 of plane
   // z0-1 and s33 of plane z0 for this thread's cells
   // completion of the loads of buffer buf (its mbarrier phase, or every
-  // cp.async of this thread); a TMA wait gives up after about 2^20 polls,
-  // records the fault and goes on
+  // cp.async of this thread); a TMA wait gives up after about 2^20 polls
+  // (RHS_DRILL_POLLS in the wait drill), records the fault and goes on
   auto wait_plane = [&](int buf) {
     if (!tma) {
       cp_async_wait_all();
@@ -241,7 +249,7 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     }
     int polls = 0;
     while (!mbar_try_wait(&sm.bar[buf], (parity >> buf) & 1u)) {
-      if (++polls > (1 << 20)) {
+      if (++polls > poll_limit) {
         if (tid == 0) atomicExch(&g_rhs_tma_fault, 1);
         break;
       }
@@ -434,6 +442,8 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
   // boundary) use the cp.async pieces
   const bool tma = have_map && x0 >= 4 && x0 + QX + 4 <= n && y0 >= 1 && y0 + QY + 1 <= n;
   unsigned parity = 0;  // bit b: phase of buffer b's mbarrier to wait for
+  const bool drill = tma && g_rhs_drill != 0;
+  const int poll_limit = drill ? RHS_DRILL_POLLS : RHS_POLLS;
   if (tma) {
     if (tid == 0) {
 #pragma unroll
@@ -444,7 +454,7 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
   }
   auto load_plane = [&](int buf, int gz) {
     if (tma) {
-      if (tid == 0) {
+      if (tid == 0 && !drill) {
         mbar_expect_tx(&sm.bar[buf], 3u * QPLANE * sizeof(float));
 #pragma unroll
         for (int c = 0; c < 3; ++c)
@@ -460,8 +470,8 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
     cp_async_commit();
   };
   // completion of the loads of buffer buf (its mbarrier phase, or every
-  // cp.async of this thread); a TMA wait gives up after about 2^20 polls,
-  // records the fault and goes on
+  // cp.async of this thread); a TMA wait gives up after about 2^20 polls
+  // (RHS_DRILL_POLLS in the wait drill), records the fault and goes on
   auto wait_plane = [&](int buf) {
     if (!tma) {
       cp_async_wait_all();
@@ -469,7 +479,7 @@ rhs_quad_kernel(int n, float inv_h, float visc, const float* __restrict__ u, flo
     }
     int polls = 0;
     while (!mbar_try_wait(&sm.bar[buf], (parity >> buf) & 1u)) {
-      if (++polls > (1 << 20)) {
+      if (++polls > poll_limit) {
         if (tid == 0) atomicExch(&g_rhs_tma_fault, 1);
         break;
       }
@@ -775,6 +785,32 @@ template cudaError_t launch_rhs<float>(int, float, float, const float*, float*, 
                                        int);
 
 }  // namespace exc
+
+extern "C" int exc_debug_wait_drill(int flags) {
+  if (flags < 0 || flags > 3) { exc::set_last_error("drill flags must be 0..3"); return EXC_ERR_ARG; }
+  int rc = exc::configure_device();
+  if (rc) return rc;
+  const int rhs = flags & 1;
+  cudaError_t e = cudaMemcpyToSymbol(exc::g_rhs_drill, &rhs, sizeof(int));
+  if (e != cudaSuccess) { exc::set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return exc::learned_set_drill((flags >> 1) & 1);
+}
+
+extern "C" int exc_device_sync(void* stream, int* flags) {
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) { exc::set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  int f = 0;
+  int rc = exc_device_faults(&f);
+  if (rc) return rc;
+  if (flags) *flags = f;
+  if (f) {
+    exc::set_last_error(f & 1 ? (f & 2 ? "device waits gave up (RHS sweep TMA plane, tensor-core convolution)"
+                                       : "a device wait gave up (RHS sweep TMA plane)")
+                              : "a device wait gave up (tensor-core convolution)");
+    return EXC_ERR_TIMEOUT;
+  }
+  return EXC_OK;
+}
 
 extern "C" int exc_device_faults(int* flags) {
   if (!flags) { exc::set_last_error("null argument"); return EXC_ERR_ARG; }

@@ -84,6 +84,8 @@ SIGNATURES = {
     "exc_poisson_destroy": [vp],
     "exc_poisson_set_engine": [vp, i32],
     "exc_device_faults": [C.POINTER(i32)],
+    "exc_device_sync": [vp, C.POINTER(i32)],
+    "exc_debug_wait_drill": [i32],
     "exc_poisson_solve": [vp, vp, vp, vp],
     "exc_project": [vp, vp, vp, vp],
     "exc_project_noalloc": [i32, i32, f64, vp, vp, vp],
@@ -110,6 +112,8 @@ SIGNATURES = {
     "exc_case_les_error": [vp, i32, i32, dp],
     "exc_case_snapshot": [vp, i32, vp, vp],
     "exc_case_attach_net": [vp, i32, vp],
+    "exc_case_set_fallback": [vp, i32, f64, f64],
+    "exc_case_fallback": [vp, i32, C.POINTER(i32)],
     "exc_case_sync": [vp],
     "exc_net_create": [u64, C.POINTER(vp)],
     "exc_net_destroy": [vp],

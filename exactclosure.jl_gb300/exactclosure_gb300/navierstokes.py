@@ -138,6 +138,23 @@ def device_faults() -> int:
     return v.value
 
 
+def device_sync(stream=None) -> int:
+    """Synchronise the stream (default: torch's current stream) and check the
+    device fault flags: raises ExcError (EXC_ERR_TIMEOUT) when a bounded
+    device wait gave up, else returns 0."""
+    v = C.c_int()
+    st = C.c_void_p(stream) if stream is not None else _stream()
+    call("exc_device_sync", st, C.byref(v))
+    return v.value
+
+
+def debug_wait_drill(flags: int):
+    """Test hook of the bounded device waits (0: normal operation).  Bit 0:
+    the RHS sweep's TMA tiles issue no copy; bit 1: the tensor-core
+    convolution issues no copy; their waits give up after 64 polls."""
+    call("exc_debug_wait_drill", int(flags))
+
+
 def poissonsolver(grid: Grid, precision: int = EXC_F64, engine: int = 0) -> PoissonSolver:
     return PoissonSolver(grid, precision, engine)
 
@@ -266,6 +283,17 @@ class Case:
         """Drive a learned-closure LES on LES grid ``index`` (None detaches)."""
         call("exc_case_attach_net", self._h, index, net.handle if net is not None else None)
         self._net = net
+
+    def set_fallback(self, index: int, e_lo: float = 0.0, e_hi: float = float("inf")):
+        """No-model fallback of the learned LES on grid ``index``: when its
+        kinetic energy is not finite or leaves [e_lo, e_hi], it goes back to
+        its last state inside the band and continues without the net."""
+        call("exc_case_set_fallback", self._h, index, e_lo, e_hi)
+
+    def fallback_engaged(self, index: int) -> bool:
+        v = C.c_int()
+        call("exc_case_fallback", self._h, index, C.byref(v))
+        return bool(v.value)
 
     def step(self, nsteps: int = 1, dt: float = 0.0):
         call("exc_case_step", self._h, nsteps, dt)

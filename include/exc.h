@@ -93,6 +93,21 @@ int exc_poisson_destroy(exc_poisson* ps);
  * = a wait for the tensor-core (tcgen05) convolution of the learned closure
  * gave up (that convolution's output is not valid).  0 in normal operation. */
 int exc_device_faults(int* flags);
+/* Synchronise `stream` (null: the legacy default stream), then read and
+ * clear the device fault flags like exc_device_faults; returns
+ * EXC_ERR_TIMEOUT when any is set (a bounded device wait gave up: the output
+ * of that kernel is not valid), EXC_OK otherwise.  No counterpart in the
+ * reference. */
+int exc_device_sync(void* stream, int* flags);
+/* Wait drill, for testing the give-up path of the bounded device waits (no
+ * counterpart in the reference; 0, the default, is normal operation).  Bit 0:
+ * the RHS sweep's tiles that take their planes by TMA issue no copy; bit 1:
+ * the tensor-core convolution of the learned closure issues no copy.  The
+ * waits for those copies then give up after 64 polls with nothing in flight,
+ * set their fault bit and the kernels finish (their outputs are not valid);
+ * the context stays usable.  Process-wide; launches made while it is set are
+ * affected. */
+int exc_debug_wait_drill(int flags);
 
 /* FFT engine of a solver (no counterpart in the reference).  0 (the
  * default): in FP64 on grids n = 128, 192, 256, 384, 512, 1024 a
@@ -117,10 +132,12 @@ int exc_project(exc_poisson* ps, void* u, void* p_out, void* stream);
  * code that cannot afford the synchronisation cudaFree implies).  Its work
  * array lives in one static 4 MiB device array that every GPU loading the
  * library holds until exit, so grids are limited to n <= 72 (EXC_F64) and
- * n <= 96 (EXC_F32); larger n returns EXC_ERR_SHAPE.  The first call on a
- * device looks the array up (cudaGetSymbolAddress) and should come before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race. */
+ * n <= 96 (EXC_F32); larger n returns EXC_ERR_SHAPE.  Every call looks the
+ * array's device address up in the current context (cudaGetSymbolAddress, a
+ * host call), so a device reset or a new primary context is handled; the
+ * first call on a device also sets the library's kernel attributes and should
+ * come before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race. */
 int exc_project_noalloc(int precision, int n, double l, void* u, void* p_out, void* stream);
 
 /* max_i |x_i| over `count` words, written as a double to *out_dev (device). */
@@ -356,6 +373,16 @@ int exc_net_train_step(exc_net* net, int precision, int batch, int n, const void
  * k = P_H(RHS_H(v) + net(v)), starting from the exact-closure state (NULL
  * detaches).  exc_case_get_les(which = 4) reads it. */
 int exc_case_attach_net(exc_case* cs, int les_index, exc_net* net);
+/* No-model fallback of the learned-closure LES of `les_index` (no
+ * counterpart in the reference): before every step the state's kinetic
+ * energy E = 1/2 sum v^2 / (n/ratio)^3 is checked on the device; when it is
+ * not finite or leaves [e_lo, e_hi] the state goes back to the last one
+ * inside the band and the LES continues without the net's term (no model)
+ * from then on.  Default band [0, inf): non-finite states only.  Attaching a
+ * net or exc_case_reset_les disengages it. */
+int exc_case_set_fallback(exc_case* cs, int les_index, double e_lo, double e_hi);
+/* Whether that fallback has engaged (1) or not (0). */
+int exc_case_fallback(exc_case* cs, int les_index, int* engaged);
 
 /* ======================================================================
  * The reference's driver `dnsaid_project` (src/N.jl:1239-1332): a forward

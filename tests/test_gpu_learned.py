@@ -206,3 +206,49 @@ def test_training_lowers_the_loss(LN):
     assert all(np.isfinite(losses))
     teacher.close()
     student.close()
+
+
+def test_learned_les_fallback_to_no_model(LN):
+    """The no-model fallback of the learned-closure LES.  A net whose output
+    is zero leaves the learned LES equal to the no-model LES bit for bit and
+    the fallback idle; a net scaled to blow the LES up trips the energy band:
+    the state goes back to the last one inside the band and the LES runs on
+    without the net, finite and inside the band; a reset disengages it."""
+    from exactclosure_gb300 import navierstokes as NS
+
+    n, c = 64, 4
+    cs = NS.Case(n, 1.0, 1 / 2000, 0.3, precision=1, les=[(c, "volume")])
+    cs.init_random(4.0, 1.0, 0)
+    net = LN.Net(seed=2)
+    net.set_params(np.zeros(net.count, dtype=np.float32))
+    cs.reset_les()
+    cs.attach_net(0, net)
+    cs.step(5)
+    cs.sync()
+    assert np.array_equal(cs.les(0, "learned"), cs.les(0, "nomodel"))
+    assert not cs.fallback_engaged(0)
+    # a net whose closure term is about 1e6 times the velocity
+    bad = LN.Net(seed=3)
+    bad.set_scales(1.0, 1e6)
+    e0 = 0.5 * float(np.mean(cs.les(0, "nomodel") ** 2)) * 3
+    cs.reset_les()
+    cs.attach_net(0, bad)
+    cs.set_fallback(0, 0.0, 4.0 * e0)
+    cs.step(3)
+    cs.sync()
+    assert cs.fallback_engaged(0)
+    v = cs.les(0, "learned")
+    assert np.all(np.isfinite(v))
+    assert 0.5 * float(np.mean(v ** 2)) * 3 <= 4.0 * e0
+    # without the net's term it runs on like a no-model LES: finite, in the band
+    cs.step(2)
+    cs.sync()
+    assert cs.fallback_engaged(0)
+    v = cs.les(0, "learned")
+    assert np.all(np.isfinite(v)) and 0.5 * float(np.mean(v ** 2)) * 3 <= 4.0 * e0
+    # a reset disengages it
+    cs.reset_les()
+    assert not cs.fallback_engaged(0)
+    net.close()
+    bad.close()
+    cs.close()

@@ -27,8 +27,9 @@ def test_noalloc_projection_matches_exc_project_on_consecutive_calls(built_lib):
     L = 1.0
     st = torch.cuda.Stream()
     # two calls in a row on different grids and inputs: the second call
-    # overwrites the first call's tables and spectrum in the shared array
-    for n, seed in ((32, 1), (48, 2), (32, 3)):
+    # overwrites the first call's tables and spectrum in the shared array;
+    # 72 is the largest FP64 grid the 4 MiB array holds
+    for n, seed in ((32, 1), (48, 2), (32, 3), (72, 4), (72, 5)):
         rng = np.random.default_rng(seed)
         u0 = torch.tensor(rng.standard_normal((3, n, n, n)), dtype=torch.float64, device="cuda")
         ua, ub = u0.clone(), u0.clone()
@@ -56,20 +57,23 @@ def test_noalloc_float32_and_size_limit(built_lib):
 
     from exactclosure_gb300._lib import ExcError, call
 
-    n = 24
-    rng = np.random.default_rng(5)
-    u0 = torch.tensor(rng.standard_normal((3, n, n, n)), dtype=torch.float32, device="cuda")
-    ua, ub = u0.clone(), u0.clone()
-    ps = C.c_void_p()
-    call("exc_poisson_create", 1, n, 1.0, C.byref(ps))
-    try:
-        call("exc_project", ps, C.c_void_p(ua.data_ptr()), None, None)
-        call("exc_project_noalloc", 1, n, 1.0, C.c_void_p(ub.data_ptr()), None, None)
-        torch.cuda.synchronize()
-    finally:
-        built_lib.exc_poisson_destroy(ps)
-    assert rel(ub.cpu().double().numpy(), ua.cpu().double().numpy()) < 2e-5
-    # beyond the static scratch: rejected on the host with a clear error
-    with pytest.raises(ExcError) as ei:
-        call("exc_project_noalloc", 0, 96, 1.0, C.c_void_p(ub.data_ptr()), None, None)
-    assert ei.value.code == 2 and "4 MiB" in str(ei.value)
+    # 96 is the largest FP32 grid the 4 MiB array holds
+    for n in (24, 96):
+        rng = np.random.default_rng(5)
+        u0 = torch.tensor(rng.standard_normal((3, n, n, n)), dtype=torch.float32, device="cuda")
+        ua, ub = u0.clone(), u0.clone()
+        ps = C.c_void_p()
+        call("exc_poisson_create", 1, n, 1.0, C.byref(ps))
+        try:
+            call("exc_project", ps, C.c_void_p(ua.data_ptr()), None, None)
+            call("exc_project_noalloc", 1, n, 1.0, C.c_void_p(ub.data_ptr()), None, None)
+            torch.cuda.synchronize()
+        finally:
+            built_lib.exc_poisson_destroy(ps)
+        assert rel(ub.cpu().double().numpy(), ua.cpu().double().numpy()) < 2e-5, n
+    # beyond the static scratch (the next FFT sizes above the limits: 80 in
+    # FP64, 100 in FP32): rejected on the host with a clear error
+    for prec, n in ((0, 80), (0, 96), (1, 100)):
+        with pytest.raises(ExcError) as ei:
+            call("exc_project_noalloc", prec, n, 1.0, C.c_void_p(ub.data_ptr()), None, None)
+        assert ei.value.code == 2 and "4 MiB" in str(ei.value), (prec, n)

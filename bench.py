@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--burgers-tstop", type=float, default=0.1)
     ap.add_argument("--large-steps", type=int, default=300,
                     help="steps of the 1024^3 run (pairs every 10 steps; the learned closure trains on them)")
-    ap.add_argument("--learned-steps", type=int, default=300, help="Adam steps of the learned closure")
+    ap.add_argument("--learned-steps", type=int, default=1000, help="Adam steps of the learned closure")
     ap.add_argument("--learned-les-steps", type=int, default=200,
                     help="steps of the learned-closure LES in lockstep with the 1024^3 DNS")
     ap.add_argument("--forms-steps", type=int, default=200,

@@ -2,26 +2,35 @@
 // mixed grid sizes on one GPU (no counterpart in the reference, whose driver
 // runs one solve at a time, src/N.jl:1239-1332).
 //
-// Requests queue on the host.  Every tick admits what fits -- a free slot of
-// a chunk for the request's grid size, or a new chunk if the memory budget
-// (a share of the free HBM taken at creation) allows -- then advances every
-// active solve by one RK4 step and retires the solves that reached their step
-// count.  A chunk holds S same-size solves slot after slot in device memory
-// (velocity ping-pong, stage state, RHS, spectral work array; nothing moves
-// between steps) and replays one captured CUDA graph per step whose kernels
-// cover all S slots at once (the slot is a grid dimension; inactive slots
-// return at once, so admission never re-captures).  Each solve keeps its own
+// Requests queue on the host.  A chunk holds S same-size solves slot after
+// slot in device memory (velocity ping-pong, stage state, RHS, spectral work
+// array; nothing moves between steps).  Its stepping runs on the device: one
+// captured graph whose conditional WHILE node repeats a body of two RK4 steps
+// while any slot has steps left (at most kpairs times per launch).  The body's
+// kernels cover all S slots at once (the slot is a grid dimension; inactive
+// slots return at once, so admission never re-captures), and after each step
+// a control kernel counts down every slot's steps, retires the slots that
+// reached their count (GPU timestamp, final clock, buffer of the final state)
+// and sets the loop condition; after the loop the energies of the retired
+// slots are reduced and the control block is copied to pinned host memory.
+// The host never waits on a chunk: a tick collects the chunks whose loop has
+// ended (event query), reports their retired solves, admits what fits -- a
+// free slot of an idle chunk of the request's grid size, or a new chunk if the
+// memory budget (a share of the free HBM taken at creation) allows -- and
+// relaunches every idle chunk that has work.  Each solve keeps its own
 // viscosity, CFL time step and clock.  Chunks of different sizes run on their
-// own streams and overlap on the device; the host runs at most two ticks ahead
-// of each chunk.  The FFT tile shapes of each grid size are chosen by timing
-// candidates on the chunk's own batched work (autotuner) before capture.
+// own streams and overlap on the device.  The FFT tile shapes of each grid
+// size are chosen by timing candidates on the chunk's own batched work
+// (autotuner) before capture.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -90,13 +99,107 @@ __global__ void set_active_kernel(int S, unsigned long long mask, int* __restric
   if (s < S) active[s] = (int)((mask >> s) & 1ull);
 }
 
+// Device-side lifecycle of a chunk's slots; copied to pinned host memory at
+// the end of every loop launch.
+constexpr int SRV_MAXS = 64;
+struct SlotCtl {
+  int steps_left[SRV_MAXS];
+  int fin[SRV_MAXS];         // 1 once the slot has taken its last step
+  int fin_parity[SRV_MAXS];  // velocity buffer holding its final state
+  int edone[SRV_MAXS];       // its energy has been reduced
+  int iter;                  // body iterations (two steps each) of the current launch
+  int pad[3];
+  unsigned long long fin_time[SRV_MAXS];  // GPU global timer (ns) at its last step
+  double fin_clock[SRV_MAXS];             // its simulated time
+  double energy[SRV_MAXS];                // sum of u^2 of its final state
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__global__ void global_ns_kernel(unsigned long long* out) { *out = global_ns(); }
+
 template <typename T>
-__global__ void set_slot_kernel(int s, double visc, T* __restrict__ vdev, double* __restrict__ vd,
-                                double* __restrict__ clock, int* __restrict__ flag) {
+__global__ void set_slot_kernel(int s, double visc, int nsteps, T* __restrict__ vdev, double* __restrict__ vd,
+                                double* __restrict__ clock, int* __restrict__ flag, SlotCtl* __restrict__ ctl) {
   vdev[s] = (T)visc;
   vd[s] = visc;
   clock[s] = 0.0;
   flag[s] = 0;
+  ctl->steps_left[s] = nsteps;
+  ctl->fin[s] = 0;
+  ctl->edone[s] = 0;
+}
+
+// start of a loop launch: the slots with steps left are active
+__global__ void loop_begin_kernel(int S, SlotCtl* __restrict__ ctl, int* __restrict__ active) {
+  const int s = threadIdx.x;
+  if (s < S) active[s] = ctl->steps_left[s] > 0;
+  if (s == 0) ctl->iter = 0;
+}
+
+// after one step: count down, retire the slots that took their last step,
+// activity of the next step; after the body's second step, the loop
+// condition (any slot active and fewer than kpairs iterations)
+__global__ void slot_ctl_kernel(int S, int parity_after, int last, int kpairs, SlotCtl* __restrict__ ctl,
+                                int* __restrict__ active, const double* __restrict__ clock,
+                                cudaGraphConditionalHandle loop) {
+  const int s = threadIdx.x;
+  int act = 0;
+  if (s < S) {
+    if (active[s]) {
+      const int left = ctl->steps_left[s] - 1;
+      ctl->steps_left[s] = left;
+      if (left == 0) {
+        ctl->fin[s] = 1;
+        ctl->fin_parity[s] = parity_after;
+        ctl->fin_time[s] = global_ns();
+        ctl->fin_clock[s] = clock[s];
+      }
+    }
+    act = ctl->steps_left[s] > 0;
+    active[s] = act;
+  }
+  const int any = __syncthreads_or(act);
+  if (last && s == 0) {
+    const int it = ctl->iter + 1;
+    ctl->iter = it;
+    cudaGraphSetConditional(loop, (any && it < kpairs) ? 1u : 0u);
+  }
+}
+
+// sum of u^2 of every slot retired and not yet reduced (fixed order per slot)
+template <typename T>
+__global__ void slot_energy_partial(long long count, const T* __restrict__ u0, const T* __restrict__ u1,
+                                    long long stride, const SlotCtl* __restrict__ ctl, double* __restrict__ part) {
+  const int s = blockIdx.y;
+  if (!ctl->fin[s] || ctl->edone[s]) return;
+  const T* u = (ctl->fin_parity[s] ? u1 : u0) + s * stride;
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    const double v = (double)u[i];
+    acc = fma(v, v, acc);
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[s * SRV_RED + blockIdx.x] = red[0];
+}
+
+__global__ void slot_energy_fold(int S, SlotCtl* __restrict__ ctl, const double* __restrict__ part) {
+  const int s = threadIdx.x;
+  if (s >= S || !ctl->fin[s] || ctl->edone[s]) return;
+  double e = 0.0;
+  for (int b = 0; b < SRV_RED; ++b) e += part[s * SRV_RED + b];
+  ctl->energy[s] = e;
+  ctl->edone[s] = 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -110,8 +213,7 @@ struct PendingReq {
 
 struct FinishRec {
   exc_solve_result res;
-  cudaEvent_t ev = nullptr;
-  double* pinned = nullptr;  // [0] sum u^2, [1] unused, [2] clock
+  cudaEvent_t ev = nullptr;  // completion of the final-field copy, if one was asked for
 };
 
 class ChunkBase {
@@ -122,12 +224,14 @@ class ChunkBase {
   size_t bytes = 0;
   cudaStream_t stream = nullptr;
   std::vector<int64_t> slot_id;
-  std::vector<int> steps_left, nsteps;
+  std::vector<int> nsteps;
   std::vector<double> t_submit, t_admit;
   std::vector<double*> result_host;
-  cudaEvent_t tick_ev[2] = {nullptr, nullptr};
-  int tick_parity = 0;
-  long long ticks = 0;
+  cudaEvent_t done_ev = nullptr;  // end of the last loop launch
+  bool in_flight = false;         // a loop launch has not been collected yet
+  SlotCtl* mirror = nullptr;      // pinned copy of the control block (valid after done_ev)
+  int kpairs = 1;                 // body iterations (two steps each) per launch at most
+  long long ticks = 0;            // loop launches
   int free_slot() const {
     for (int s = 0; s < S; ++s)
       if (slot_id[s] < 0) return s;
@@ -153,22 +257,23 @@ class Chunk : public ChunkBase {
   T* visc = nullptr;
   double *dt = nullptr, *clock = nullptr, *part = nullptr, *red = nullptr, *viscd = nullptr;
   int *active = nullptr, *flag = nullptr;
-  int cur = 0;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  SlotCtl* ctl = nullptr;  // device control block
+  int cur = 0;             // 0: every active slot's state is in u[0] between launches
+  cudaGraphExec_t loop = nullptr;
   int kernels_per_step = 0;
 
   ~Chunk() override {
     if (stream) cudaStreamSynchronize(stream);
-    for (auto& g : graph)
-      if (g) cudaGraphExecDestroy(g);
+    if (loop) cudaGraphExecDestroy(loop);
+    if (ctl) cudaFree(ctl);
+    if (mirror) cudaFreeHost(mirror);
+    if (done_ev) cudaEventDestroy(done_ev);
     poisson_free(&ps);
     if (work) cudaFree(work);
     if (big) cudaFree(big);
     if (visc) cudaFree(visc);
     if (dt) cudaFree(dt);
     if (active) cudaFree(active);
-    for (auto& e : tick_ev)
-      if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -200,6 +305,55 @@ class Chunk : public ChunkBase {
     }
     return e;
   }
+
+  // The device-side loop: WHILE (condition set by slot_ctl_kernel) { step
+  // from u[0]; control; step from u[1]; control }, then the energies of the
+  // retired slots and the copy of the control block to the pinned mirror.
+  cudaError_t build_loop() {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    cudaGraphConditionalHandle h;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNode_t wnode = nullptr;
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &cp);
+    if (e == cudaSuccess) {
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      e = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e2 = enqueue_step(0);
+        slot_ctl_kernel<<<1, SRV_MAXS, 0, stream>>>(S, 1, 0, kpairs, ctl, active, clock, h);
+        if (e2 == cudaSuccess) e2 = enqueue_step(1);
+        slot_ctl_kernel<<<1, SRV_MAXS, 0, stream>>>(S, 0, 1, kpairs, ctl, active, clock, h);
+        if (e2 == cudaSuccess) e2 = cudaGetLastError();
+        e = cudaStreamEndCapture(stream, &body);
+        if (e2 != cudaSuccess) e = e2;
+      }
+      if (e == cudaSuccess) {
+        size_t num = 0;
+        cudaGraphGetNodes(body, nullptr, &num);
+        kernels_per_step = (int)num / 2;
+      }
+    }
+    if (e == cudaSuccess)
+      e = cudaStreamBeginCaptureToGraph(stream, g, &wnode, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      slot_energy_partial<T><<<dim3(SRV_RED, S), 256, 0, stream>>>(3 * N, u[0], u[1], 3 * N, ctl, part);
+      slot_energy_fold<<<1, SRV_MAXS, 0, stream>>>(S, ctl, part);
+      cudaError_t e2 = cudaMemcpyAsync(mirror, ctl, sizeof(SlotCtl), cudaMemcpyDeviceToHost, stream);
+      if (e2 == cudaSuccess) e2 = cudaGetLastError();
+      cudaGraph_t g2 = g;
+      e = cudaStreamEndCapture(stream, &g2);
+      if (e2 != cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&loop, g, 0);
+    if (g) cudaGraphDestroy(g);
+    return e;
+  }
 };
 
 // autotuned FFT engine and Stockham tile shape per (n, precision, S)
@@ -222,6 +376,7 @@ struct exc_server {
   std::vector<exc::FinishRec> finishing;
   int64_t next_id = 1;
   int max_active_per_size = 0;  // admission bound per grid size (0: none)
+  unsigned long long gt0 = 0;   // GPU global timer (ns) at the server's time origin
   // init scratch (largest grid seen so far)
   void* spec3 = nullptr;
   size_t spec3_bytes = 0;
@@ -299,6 +454,15 @@ static size_t chunk_bytes(int n, int S, size_t w) {
   return S * (12 * N * w + (size_t)n * n * P * 2 * w) + (size_t)n * n * (n / 2 + 1) * 8 + S * 128 + S * SRV_RED * 8;
 }
 
+// body iterations (two RK4 steps each) per loop launch at most: a few
+// milliseconds of work per launch
+static int kpairs_for(int n) {
+  if (n <= 64) return 16;
+  if (n <= 128) return 8;
+  if (n <= 192) return 4;
+  return 2;
+}
+
 static int slots_for(const exc_server* sv, int n) {
   if (sv->desc.slots_per_chunk > 0) return std::min(sv->desc.slots_per_chunk, 64);
   if (n <= 64) return 16;
@@ -319,13 +483,20 @@ static int make_chunk(exc_server* sv, int n, double l, double cfl, ChunkBase** o
   ck->cfl = cfl;
   ck->N = (long long)n * n * n;
   ck->slot_id.assign(S, -1);
-  ck->steps_left.assign(S, 0);
   ck->nsteps.assign(S, 0);
   ck->t_submit.assign(S, 0);
   ck->t_admit.assign(S, 0);
   ck->result_host.assign(S, nullptr);
   if (cudaStreamCreateWithFlags(&ck->stream, cudaStreamNonBlocking) != cudaSuccess) { set_last_error("stream"); return EXC_ERR_CUDA; }
-  for (auto& e : ck->tick_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&ck->done_ev, cudaEventDisableTiming);
+  ck->kpairs = kpairs_for(n);
+  if (cudaMalloc(&ck->ctl, sizeof(SlotCtl)) != cudaSuccess ||
+      cudaHostAlloc(&ck->mirror, sizeof(SlotCtl), cudaHostAllocDefault) != cudaSuccess) {
+    set_last_error("out of memory (chunk control block)");
+    return EXC_ERR_OOM;
+  }
+  cudaMemsetAsync(ck->ctl, 0, sizeof(SlotCtl), ck->stream);
+  std::memset(ck->mirror, 0, sizeof(SlotCtl));
   using C = cplx<T>;
   const long long wst = (long long)n * n * spec_pitch(n);
   if (cudaMalloc(&ck->work, S * wst * sizeof(C)) != cudaSuccess) { set_last_error("out of device memory (chunk work)"); return EXC_ERR_OOM; }
@@ -357,22 +528,9 @@ static int make_chunk(exc_server* sv, int n, double l, double cfl, ChunkBase** o
     rc = tune_chunk<T>(sv, ck.get());
     if (rc) return rc;
   }
-  // capture the step graphs (one per velocity parity)
-  for (int c = 0; c < 2; ++c) {
-    cudaGraph_t g;
-    cudaError_t e = cudaStreamBeginCapture(ck->stream, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-      cudaError_t e2 = ck->enqueue_step(c);
-      e = cudaStreamEndCapture(ck->stream, &g);
-      if (e2 != cudaSuccess) e = e2;
-    }
-    if (e == cudaSuccess) {
-      size_t num = 0;
-      cudaGraphGetNodes(g, nullptr, &num);
-      ck->kernels_per_step = (int)num;
-      e = cudaGraphInstantiate(&ck->graph[c], g, 0);
-      cudaGraphDestroy(g);
-    }
+  // capture the device-side step loop
+  {
+    cudaError_t e = ck->build_loop();
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   }
   ck->bytes = need;
@@ -395,16 +553,26 @@ static int ensure_init_scratch(exc_server* sv, int n) {
 
 // Put request `pr` into a free slot (new chunk if needed and affordable).
 template <typename T>
-static int admit(exc_server* sv, const PendingReq& pr, bool* admitted) {
+static int admit(exc_server* sv, const PendingReq& pr, bool* admitted, bool* waiting) {
   *admitted = false;
+  *waiting = false;
   const exc_solve_req& q = pr.req;
   Chunk<T>* ck = nullptr;
   int slot = -1;
+  bool busy_slot = false;
   for (auto& cb : sv->chunks) {
     if (cb->n != q.n || cb->l != q.l || cb->cfl != q.cfl) continue;
     int s = cb->free_slot();
-    if (s >= 0) { ck = static_cast<Chunk<T>*>(cb.get()); slot = s; break; }
+    if (s < 0) continue;
+    // a chunk whose loop runs takes new solves only after it is collected
+    // (its launch holds a few milliseconds of work): wait for it rather than
+    // open another chunk
+    if (cb->in_flight) { busy_slot = true; continue; }
+    ck = static_cast<Chunk<T>*>(cb.get());
+    slot = s;
+    break;
   }
+  if (!ck && busy_slot) { *waiting = true; return EXC_OK; }
   if (!ck) {
     ChunkBase* nb = nullptr;
     int rc = make_chunk<T>(sv, q.n, q.l, q.cfl, &nb);
@@ -423,7 +591,8 @@ static int admit(exc_server* sv, const PendingReq& pr, bool* admitted) {
   exc_poisson view = ck->ps;
   view.work = reinterpret_cast<cplx<T>*>(ck->work) + slot * (long long)q.n * q.n * ck->ps.P;
   T* u = ck->u[ck->cur] + slot * 3 * ck->N;
-  set_slot_kernel<T><<<1, 1, 0, sv->admit_stream>>>(slot, q.visc, ck->visc, ck->viscd, ck->clock, ck->flag);
+  set_slot_kernel<T><<<1, 1, 0, sv->admit_stream>>>(slot, q.visc, q.nsteps, ck->visc, ck->viscd, ck->clock, ck->flag,
+                                                      ck->ctl);
   rc = init_random_field<T>(&view, u, reinterpret_cast<cplx<T>*>(sv->spec3), sv->init_part, q.kpeak, q.energy, q.seed,
                             sv->admit_stream);
   cudaEventRecord(ready, sv->admit_stream);
@@ -431,7 +600,6 @@ static int admit(exc_server* sv, const PendingReq& pr, bool* admitted) {
   cudaEventDestroy(ready);
   if (rc) return rc;
   ck->slot_id[slot] = pr.id;
-  ck->steps_left[slot] = q.nsteps;
   ck->nsteps[slot] = q.nsteps;
   ck->t_submit[slot] = pr.t_submit;
   ck->t_admit[slot] = sv->now();
@@ -440,33 +608,33 @@ static int admit(exc_server* sv, const PendingReq& pr, bool* admitted) {
   return EXC_OK;
 }
 
+// A chunk whose loop launch has ended: report its retired solves (times and
+// energies from the control block's pinned mirror; the optional final-field
+// copy is queued on the chunk stream) and free their slots.
 template <typename T>
-static int tick_chunk(exc_server* sv, Chunk<T>* ck) {
-  unsigned long long mask = 0;
-  for (int s = 0; s < ck->S; ++s)
-    if (ck->slot_id[s] >= 0 && ck->steps_left[s] > 0) mask |= 1ull << s;
-  if (!mask) return EXC_OK;
-  // at most two ticks in flight per chunk
-  cudaEventSynchronize(ck->tick_ev[ck->tick_parity]);
-  set_active_kernel<<<1, 64, 0, ck->stream>>>(ck->S, mask, ck->active);
-  cudaError_t e = cudaGraphLaunch(ck->graph[ck->cur], ck->stream);
-  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-  ck->cur ^= 1;
-  ck->ticks++;
+static int collect_chunk(exc_server* sv, Chunk<T>* ck) {
+  if (!ck->in_flight) return EXC_OK;
+  cudaError_t q = cudaEventQuery(ck->done_ev);
+  if (q == cudaErrorNotReady) return EXC_OK;
+  if (q != cudaSuccess) { set_last_error(cudaGetErrorString(q)); return EXC_ERR_CUDA; }
+  ck->in_flight = false;
+  const SlotCtl* m = ck->mirror;
   for (int s = 0; s < ck->S; ++s) {
-    if (!((mask >> s) & 1ull)) continue;
-    if (--ck->steps_left[s] > 0) continue;
-    // finished: FP64 energy and clock into pinned host memory, optional field copy
+    if (ck->slot_id[s] < 0 || !m->fin[s]) continue;
     FinishRec rec;
-    cudaHostAlloc(&rec.pinned, 4 * sizeof(double), cudaHostAllocDefault);
-    T* uf = ck->u[ck->cur] + s * 3 * ck->N;
-    e = launch_sqdiff<T>(3 * ck->N, uf, nullptr, ck->part, ck->red, ck->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(rec.pinned, ck->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, ck->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(rec.pinned + 2, ck->clock + s, sizeof(double), cudaMemcpyDeviceToHost, ck->stream);
-    if (e == cudaSuccess && ck->result_host[s]) {
+    rec.res.id = ck->slot_id[s];
+    rec.res.n = ck->n;
+    rec.res.nsteps = ck->nsteps[s];
+    rec.res.t_submit = ck->t_submit[s];
+    rec.res.t_admit = ck->t_admit[s];
+    rec.res.t_finish = (double)(long long)(m->fin_time[s] - sv->gt0) * 1e-9;
+    rec.res.energy = m->energy[s] / 2.0 / (double)ck->N;
+    rec.res.sim_time = m->fin_clock[s];
+    if (ck->result_host[s]) {
       // float64 copy of the final velocity through the slot's RHS buffer
+      const T* uf = ck->u[m->fin_parity[s]] + s * 3 * ck->N;
       double* stage = reinterpret_cast<double*>(ck->rhs + s * 3 * ck->N);
+      cudaError_t e = cudaSuccess;
       if (sizeof(T) == sizeof(double)) {
         e = cudaMemcpyAsync(ck->result_host[s], uf, 3 * ck->N * sizeof(double), cudaMemcpyDeviceToHost, ck->stream);
       } else {
@@ -478,24 +646,29 @@ static int tick_chunk(exc_server* sv, Chunk<T>* ck) {
                                 ck->stream);
         }
       }
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&rec.ev, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(rec.ev, ck->stream);
+      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
     }
-    if (e != cudaSuccess) { cudaFreeHost(rec.pinned); set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-    cudaEventCreate(&rec.ev);
-    cudaEventRecord(rec.ev, ck->stream);
-    rec.res.id = ck->slot_id[s];
-    rec.res.n = ck->n;
-    rec.res.nsteps = ck->nsteps[s];
-    rec.res.t_submit = ck->t_submit[s];
-    rec.res.t_admit = ck->t_admit[s];
-    rec.res.t_finish = -1;
-    rec.res.energy = 0;
-    rec.res.sim_time = 0;
     sv->finishing.push_back(rec);
     ck->slot_id[s] = -1;
     ck->result_host[s] = nullptr;
   }
-  cudaEventRecord(ck->tick_ev[ck->tick_parity], ck->stream);
-  ck->tick_parity ^= 1;
+  return EXC_OK;
+}
+
+// An idle chunk with solves that have steps left: one loop launch.
+template <typename T>
+static int launch_chunk(exc_server* sv, Chunk<T>* ck) {
+  (void)sv;
+  if (ck->in_flight || ck->active_count() == 0) return EXC_OK;
+  loop_begin_kernel<<<1, SRV_MAXS, 0, ck->stream>>>(ck->S, ck->ctl, ck->active);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaGraphLaunch(ck->loop, ck->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(ck->done_ev, ck->stream);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  ck->in_flight = true;
+  ck->ticks++;
   return EXC_OK;
 }
 
@@ -509,6 +682,11 @@ static int active_of_size(const exc_server* sv, int n) {
 
 template <typename T>
 static int server_tick(exc_server* sv, int* active, int* queued) {
+  // chunks whose loop launch has ended: report and free their retired solves
+  for (auto& cb : sv->chunks) {
+    int rc = collect_chunk<T>(sv, static_cast<Chunk<T>*>(cb.get()));
+    if (rc) return rc;
+  }
   // admission (continuous batching): any queued request that fits, in
   // arrival order; with an admission bound a request also waits while its
   // grid size has max_active_per_size solves running.  When a request waits
@@ -520,10 +698,11 @@ static int server_tick(exc_server* sv, int* active, int* queued) {
         ++i;
         continue;
       }
-      bool ok = false;
-      int rc = admit<T>(sv, sv->pending[i], &ok);
+      bool ok = false, waiting = false;
+      int rc = admit<T>(sv, sv->pending[i], &ok, &waiting);
       if (rc) return rc;
       if (ok) sv->pending.erase(sv->pending.begin() + i);
+      else if (waiting) ++i;  // a slot frees when a running chunk is collected
       else { blocked = true; ++i; }
     }
     if (!blocked || pass == 1) break;
@@ -539,9 +718,10 @@ static int server_tick(exc_server* sv, int* active, int* queued) {
     }
     if (!freed) break;
   }
+  // every idle chunk with work runs its device-side loop
   int act = 0;
   for (auto& cb : sv->chunks) {
-    int rc = tick_chunk<T>(sv, static_cast<Chunk<T>*>(cb.get()));
+    int rc = launch_chunk<T>(sv, static_cast<Chunk<T>*>(cb.get()));
     if (rc) return rc;
     act += cb->active_count();
   }
@@ -578,8 +758,18 @@ int exc_server_create(const exc_server_desc* desc, exc_server** out) {
     set_last_error("cannot create server resources");
     return EXC_ERR_CUDA;
   }
-  cudaEventRecord(sv->ev0, sv->admit_stream);
-  cudaEventSynchronize(sv->ev0);
+  // time origin: the GPU global timer read by a kernel, then the host clock
+  // (finish times come from the global timer, submit/admit times from the host)
+  unsigned long long* gt = reinterpret_cast<unsigned long long*>(sv->init_part);
+  global_ns_kernel<<<1, 1, 0, sv->admit_stream>>>(gt);
+  cudaError_t e = cudaMemcpyAsync(&sv->gt0, gt, sizeof(sv->gt0), cudaMemcpyDeviceToHost, sv->admit_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(sv->ev0, sv->admit_stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(sv->ev0);
+  if (e != cudaSuccess) {
+    exc_server_destroy(sv);
+    set_last_error(cudaGetErrorString(e));
+    return EXC_ERR_CUDA;
+  }
   sv->t0 = std::chrono::steady_clock::now();
   *out = sv;
   return EXC_OK;
@@ -589,10 +779,8 @@ int exc_server_destroy(exc_server* sv) {
   if (!sv) return EXC_OK;
   cudaDeviceSynchronize();
   sv->chunks.clear();
-  for (auto& r : sv->finishing) {
+  for (auto& r : sv->finishing)
     if (r.ev) cudaEventDestroy(r.ev);
-    if (r.pinned) cudaFreeHost(r.pinned);
-  }
   if (sv->spec3) cudaFree(sv->spec3);
   if (sv->init_part) cudaFree(sv->init_part);
   if (sv->ev0) cudaEventDestroy(sv->ev0);
@@ -634,18 +822,14 @@ int exc_server_poll(exc_server* sv, exc_solve_result* out, int max, int* count) 
   int c = 0;
   for (size_t i = 0; i < sv->finishing.size() && c < max;) {
     FinishRec& r = sv->finishing[i];
-    cudaError_t q = cudaEventQuery(r.ev);
-    if (q == cudaErrorNotReady) { ++i; continue; }
-    if (q != cudaSuccess) { set_last_error(cudaGetErrorString(q)); return EXC_ERR_CUDA; }
-    float ms = 0;
-    cudaEventElapsedTime(&ms, sv->ev0, r.ev);
-    r.res.t_finish = ms * 1e-3;
-    const int n = r.res.n;
-    r.res.energy = r.pinned[0] / 2.0 / ((double)n * n * n);
-    r.res.sim_time = r.pinned[2];
+    if (r.ev) {
+      // the final field is still on its way to the caller's buffer
+      cudaError_t q = cudaEventQuery(r.ev);
+      if (q == cudaErrorNotReady) { ++i; continue; }
+      if (q != cudaSuccess) { set_last_error(cudaGetErrorString(q)); return EXC_ERR_CUDA; }
+      cudaEventDestroy(r.ev);
+    }
     out[c++] = r.res;
-    cudaEventDestroy(r.ev);
-    cudaFreeHost(r.pinned);
     sv->finishing.erase(sv->finishing.begin() + i);
   }
   *count = c;
@@ -661,8 +845,9 @@ int exc_server_drain(exc_server* sv) {
     if (rc) return rc;
     if (act == 0 && q == 0) break;
     // solves retired in this tick free their slots for the next one; only a
-    // second tick without any active solve means the queue cannot be served
+    // second tick without any admitted solve means the queue cannot be served
     idle_ticks = act == 0 ? idle_ticks + 1 : 0;
+    if (act > 0) std::this_thread::yield();  // loops run on the device meanwhile
     if (idle_ticks >= 2) { set_last_error("queued requests cannot be admitted (memory budget)"); return EXC_ERR_OOM; }
   }
   cudaError_t e = cudaDeviceSynchronize();

@@ -312,15 +312,22 @@ typedef struct {
 
 int exc_server_create(const exc_server_desc* desc, exc_server** out);
 int exc_server_destroy(exc_server* sv);
-/* Queue a solve; *id identifies its result. */
 /* Admission bound (no counterpart in the reference): a queued request is
  * admitted only while fewer than max_active_per_size solves of its grid size
  * run (0 = no bound, the default); requests are taken in arrival order among
  * those eligible.  Trades aggregate throughput for lower median latency. */
 int exc_server_set_admission(exc_server* sv, int max_active_per_size);
+/* Queue a solve; *id identifies its result. */
 int exc_server_submit(exc_server* sv, const exc_solve_req* req, int64_t* id);
-/* Admit, advance every active solve one RK4 step, retire finished solves
- * (asynchronous: at most two ticks in flight per batch). */
+/* One non-blocking pass of the host side: collect every batch whose device
+ * loop has ended (its retired solves become results), admit queued requests
+ * into free slots of idle batches or new batches, and relaunch every idle
+ * batch that has work.  A batch's stepping runs on the device: a captured
+ * graph whose WHILE node repeats two RK4 steps of all its slots while any has
+ * steps left (a few milliseconds of work per launch at most); the device
+ * counts each solve's steps, retires it at its own step count and records its
+ * finish time, energy and simulated time.  *active: admitted, unreported
+ * solves; *queued: waiting requests. */
 int exc_server_tick(exc_server* sv, int* active, int* queued);
 /* Up to `max` results of finished solves whose device work has completed. */
 int exc_server_poll(exc_server* sv, exc_solve_result* out, int max, int* count);

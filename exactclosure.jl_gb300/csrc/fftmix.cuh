@@ -376,14 +376,8 @@ struct MixSolve {
     double* mean = part + NPARTS;
     const double h = ps->h, inv_h = 1.0 / ps->h;
     const unsigned gx = (unsigned)NPARTS;
-    const int ntx = (nkx + CG::W - 1) / CG::W;
-    const dim3 gc((unsigned)(ntx * n), 1, 1);
     const SlotBatch one;
-    auto columns = [&]() {
-      rcols_kernel<float, A1, A2, false><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, one);
-      rzsolve_kernel<float, A1, A2><<<gc, CG::NT, CG::SMEM_Z, st>>>(g, n, nkx, ntx, P, tln, sp->invlap, one);
-      rcols_kernel<float, A1, A2, true><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, one);
-    };
+    auto columns = [&]() { RS::columns(g, nkx, P, tln, sp->invlap, st, one, 1); };
     if (vec) {
       mr2c_kernel<B1, B2, MIX_DIV><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
     } else {

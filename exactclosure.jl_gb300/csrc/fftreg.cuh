@@ -329,6 +329,216 @@ rzsolve_kernel(cplx<T>* __restrict__ g, int n, int nkx, int ntx, int P, const cp
 }
 
 // ---------------------------------------------------------------------------
+// Pipelined column passes (FP32 grids whose tile and divide table fit twice
+// in shared memory).  Persistent CTAs walk the tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ...; a tile's W lines arrive in a staging buffer by
+// 16-byte cp.async copies issued while the previous tile is transformed, so
+// the HBM reads overlap the DFTs instead of alternating with them (two CTAs
+// per SM).  Same arithmetic as rcols_kernel / rzsolve_kernel, term for term.
+// ---------------------------------------------------------------------------
+template <typename T, int N1, int N2>
+struct PipeGeom {
+  using CG = ColGeom<T, N1, N2>;
+  static constexpr int L = N1 * N2, W = CG::W;
+  static constexpr int CPL = 16 / (int)(2 * sizeof(T));  // complex words per 16-byte piece
+  static constexpr int PW = W / CPL;                      // pieces per line row
+  // exchange rows padded by 64 bytes when a tile row is 64 bytes wide: a
+  // warp's four row groups then alternate between the two halves of the
+  // banks (two wavefronts) instead of sharing the same 16 banks
+  // (the y passes; measured slower in the z pass, which keeps the dense rows)
+  static constexpr int PADC = (W * 2 * (int)sizeof(T) == 64) ? 64 / (2 * (int)sizeof(T)) : 0;
+  static constexpr int RS1 = N2 * W + PADC;  // y pass exchange: row k1 of [m2][line]
+  static constexpr int XSC = N1 * RS1;       // y pass exchange size, complex words
+  static constexpr size_t SMEM_COLS = ((size_t)XSC + (size_t)W * L) * 2 * sizeof(T);
+  static constexpr size_t SMEM_Z = 2 * (size_t)W * L * 2 * sizeof(T) + (size_t)W * L * 8;
+  static constexpr bool OK = sizeof(T) == 4 && CG::TABS && SMEM_Z <= 110 * 1024;
+};
+
+// Stage the W lines of tile (outer, kx0) -- rows r = 0..L-1 at base + r es --
+// into stg[r][line]; pieces past the padded row (column >= P) are skipped.
+template <typename T, int N1, int N2>
+__device__ __forceinline__ void stage_tile(cplx<T>* stg, const cplx<T>* base, long long es, int kx0, int P, int tid,
+                                           int nthreads) {
+  using Gp = PipeGeom<T, N1, N2>;
+  constexpr int W = Gp::W, CPL = Gp::CPL, PW = Gp::PW, L = Gp::L;
+  for (int q = tid; q < L * PW; q += nthreads) {
+    const int r = q / PW, j = q - r * PW;
+    if (kx0 + j * CPL < P) cp_async_16(stg + r * W + j * CPL, base + r * es + j * CPL);
+  }
+}
+
+template <typename T, int N1, int N2, bool INV>
+__global__ void __launch_bounds__(ColGeom<T, N1, N2>::NT, 3)
+rcols_pipe_kernel(cplx<T>* __restrict__ g, int nkx, int ntx, int ntiles, int P, long long es, long long outer_stride,
+                  const cplx<T>* __restrict__ tl, SlotBatch sb) {
+  using C = cplx<T>;
+  using G = ColGeom<T, N1, N2>;
+  using Gp = PipeGeom<T, N1, N2>;
+  constexpr int W = G::W, RS1 = Gp::RS1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  C* stg = xs + Gp::XSC;
+  if (sb.active && !sb.active[blockIdx.z]) return;
+  g += blockIdx.z * sb.wstride;
+  const int tid = threadIdx.x, line = tid % W;
+  auto prefetch = [&](int t) {
+    const int outer = t / ntx, kx0 = (t - outer * ntx) * W;
+    stage_tile<T, N1, N2>(stg, g + outer * outer_stride + kx0, es, kx0, P, tid, G::NT);
+    cp_async_commit();
+  };
+  int t = blockIdx.x;
+  if (t < ntiles) prefetch(t);
+  for (; t < ntiles; t += gridDim.x) {
+    const int outer = t / ntx, kx0 = (t - outer * ntx) * W;
+    const int lines = min(W, nkx - kx0);
+    const bool lv = line < lines;
+    cp_async_wait_all();
+    __syncthreads();  // the tile is staged; the previous tile's xs reads are done
+    if (tid < W * N2) {
+      const int m2 = tid / W;
+      C v[N1];
+#pragma unroll
+      for (int m1 = 0; m1 < N1; ++m1) v[m1] = stg[(N2 * m1 + m2) * W + line];
+      dft_reg<N1, INV>(v);
+#pragma unroll
+      for (int k1 = 1; k1 < N1; ++k1) {
+        const C w = __ldg(&tl[k1 * N2 + m2]);
+        v[k1] = INV ? cmulc(v[k1], w) : cmul(v[k1], w);
+      }
+#pragma unroll
+      for (int k1 = 0; k1 < N1; ++k1) xs[k1 * RS1 + m2 * W + line] = v[k1];
+    }
+    __syncthreads();  // stg consumed, xs complete
+    if (t + (int)gridDim.x < ntiles) prefetch(t + gridDim.x);
+    if (tid < W * N1) {
+      const int k1 = tid / W;
+      C v[N2];
+#pragma unroll
+      for (int m2 = 0; m2 < N2; ++m2) v[m2] = xs[k1 * RS1 + m2 * W + line];
+      dft_reg<N2, INV>(v);
+      if (lv) {
+        C* q = g + outer * outer_stride + kx0 + k1 * es + line;
+        const long long step = N1 * es;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) q[k2 * step] = v[k2];
+      }
+    }
+  }
+}
+
+template <typename T, int N1, int N2>
+__global__ void __launch_bounds__(ColGeom<T, N1, N2>::NT, 2)
+rzsolve_pipe_kernel(cplx<T>* __restrict__ g, int n, int nkx, int ntx, int ntiles, int P,
+                    const cplx<T>* __restrict__ tl, const double* __restrict__ invlap, SlotBatch sb) {
+  using C = cplx<T>;
+  using G = ColGeom<T, N1, N2>;
+  using Gp = PipeGeom<T, N1, N2>;
+  constexpr int W = G::W, L = N1 * N2, RS1 = N2 * W, RS2 = N1 * W;
+  static_assert(G::TABS, "the pipelined z pass stages the divide table");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  C* stg = xs + W * L;
+  double* tab = reinterpret_cast<double*>(stg + W * L);  // [kz][line]
+  if (sb.active && !sb.active[blockIdx.z]) return;
+  g += blockIdx.z * sb.wstride;
+  const long long es = (long long)n * P;
+  const int tid = threadIdx.x, line = tid % W;
+  auto prefetch_cols = [&](int t) {
+    const int ky = t / ntx, kx0 = (t - ky * ntx) * W;
+    stage_tile<T, N1, N2>(stg, g + (long long)ky * P + kx0, es, kx0, P, tid, G::NT);
+    cp_async_commit();
+  };
+  auto prefetch_tab = [&](int t) {
+    const int ky = t / ntx, kx0 = (t - ky * ntx) * W;
+    const int lines = min(W, nkx - kx0);
+    for (int q = tid; q < L * W; q += G::NT) {
+      const int kz = q / W, l = q - kz * W;
+      if (l < lines) cp_async_word(&tab[q], invlap + invlap_index(n, kz, ky, kx0 + l));
+    }
+    cp_async_commit();
+  };
+  int t = blockIdx.x;
+  if (t < ntiles) {
+    prefetch_cols(t);
+    prefetch_tab(t);
+  }
+  for (; t < ntiles; t += gridDim.x) {
+    const int ky = t / ntx, kx0 = (t - ky * ntx) * W;
+    const int lines = min(W, nkx - kx0);
+    const bool lv = line < lines;
+    C* const base = g + (long long)ky * P + kx0;
+    cp_async_wait_all();
+    __syncthreads();  // tile and table staged; the previous tile's xs reads are done
+    if (tid < W * N2) {
+      const int m2 = tid / W;
+      C v[N1];
+#pragma unroll
+      for (int m1 = 0; m1 < N1; ++m1) v[m1] = stg[(N2 * m1 + m2) * W + line];
+      dft_reg<N1, false>(v);
+#pragma unroll
+      for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], __ldg(&tl[k1 * N2 + m2]));
+#pragma unroll
+      for (int k1 = 0; k1 < N1; ++k1) xs[k1 * RS1 + m2 * W + line] = v[k1];
+    }
+    __syncthreads();  // stg consumed, xs complete
+    if (t + (int)gridDim.x < ntiles) prefetch_cols(t + gridDim.x);
+    C v[N2];
+    const int k1 = tid / W;
+    const bool actb = tid < W * N1;
+    if (actb) {
+#pragma unroll
+      for (int m2 = 0; m2 < N2; ++m2) v[m2] = xs[k1 * RS1 + m2 * W + line];
+      dft_reg<N2, false>(v);
+      if (lv) {
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) {
+          const int kz = k1 + N1 * k2;
+          if constexpr (sizeof(T) == 4) {
+            const float2 f = reinterpret_cast<const float2*>(tab)[kz * W + line];
+            v[k2].x = fmaf(v[k2].x, f.x, v[k2].x * f.y);
+            v[k2].y = fmaf(v[k2].y, f.x, v[k2].y * f.y);
+          } else {
+            const double f = tab[kz * W + line];
+            v[k2].x = (T)((double)v[k2].x * f);
+            v[k2].y = (T)((double)v[k2].y * f);
+          }
+        }
+      }
+      dft_reg<N2, true>(v);
+#pragma unroll
+      for (int j1 = 1; j1 < N2; ++j1) v[j1] = cmulc(v[j1], __ldg(&tl[k1 * N2 + j1]));
+    }
+    __syncthreads();  // level-B reads of xs and of the table are complete
+    if (t + (int)gridDim.x < ntiles) prefetch_tab(t + gridDim.x);
+    if (actb) {
+#pragma unroll
+      for (int j1 = 0; j1 < N2; ++j1) xs[j1 * RS2 + k1 * W + line] = v[j1];
+    }
+    __syncthreads();
+    if (tid < W * N2) {
+      const int j1 = tid / W;
+      C y[N1];
+#pragma unroll
+      for (int k = 0; k < N1; ++k) y[k] = xs[j1 * RS2 + k * W + line];
+      dft_reg<N1, true>(y);
+      if (lv) {
+        C* q = base + j1 * es + line;
+        const long long step = N2 * es;
+#pragma unroll
+        for (int j2 = 0; j2 < N1; ++j2) q[j2 * step] = y[j2];
+      }
+    }
+  }
+}
+
+// Persistent CTAs per slot of a pipelined column pass: the CTAs resident at
+// once (per_sm on each of the 152 SMs) shared among the slots.
+inline int pipe_ctas(int ntiles, int nslots, int per_sm) {
+  const int per = (per_sm * 152 + nslots - 1) / nslots;
+  return ntiles < per ? ntiles : per;
+}
+
+// ---------------------------------------------------------------------------
 // x pass, real -> half complex (L = n/2 complex points z_m = x_2m + i x_2m+1
 // per row, then X_k = (Z_k + conj Z_{L-k})/2 - (i/2) W_n^k (Z_k - conj Z_{L-k}),
 // k = 0..L).  With DIV the row is d = div(u) (src/N.jl:222-238) computed on
@@ -552,6 +762,7 @@ struct RegSolve {
   static constexpr int B1 = reg_split(H), B2 = H / (B1 ? B1 : 1);
   using CG = ColGeom<T, A1, A2>;
   using XG = XGeom<T, B1, B2>;
+  using C_t = cplx<T>;
 
   static cudaError_t configure() {
     cudaError_t e = cudaSuccess;
@@ -566,7 +777,34 @@ struct RegSolve {
     if constexpr (XG::STAGE) set((const void*)rr2c_kernel<T, B1, B2, true, true>, XG::SMEM_DIV);
     set((const void*)rr2c_kernel<T, B1, B2, false>, XG::SMEM);
     set((const void*)rc2r_kernel<T, B1, B2>, XG::SMEM);
+    if constexpr (PipeGeom<T, A1, A2>::OK) {
+      set((const void*)rcols_pipe_kernel<T, A1, A2, false>, PipeGeom<T, A1, A2>::SMEM_COLS);
+      set((const void*)rcols_pipe_kernel<T, A1, A2, true>, PipeGeom<T, A1, A2>::SMEM_COLS);
+      set((const void*)rzsolve_pipe_kernel<T, A1, A2>, PipeGeom<T, A1, A2>::SMEM_Z);
+    }
     return e;
+  }
+
+  // y forward, z solve, y inverse on the spectral array g (pitch P)
+  static void columns(C_t* g, int nkx, int P, const C_t* tln, const double* invlap, cudaStream_t st,
+                      const SlotBatch& sb, int ns) {
+    constexpr int n = NN;
+    const int ntx = (nkx + CG::W - 1) / CG::W;
+    const int ntiles = ntx * n;
+    if constexpr (PipeGeom<T, A1, A2>::OK) {
+      using Gp = PipeGeom<T, A1, A2>;
+      const dim3 gy((unsigned)pipe_ctas(ntiles, ns, 3), 1, ns), gz((unsigned)pipe_ctas(ntiles, ns, 4), 1, ns);
+      rcols_pipe_kernel<T, A1, A2, false><<<gy, CG::NT, Gp::SMEM_COLS, st>>>(g, nkx, ntx, ntiles, P, P,
+                                                                             (long long)n * P, tln, sb);
+      rzsolve_pipe_kernel<T, A1, A2><<<gz, CG::NT, Gp::SMEM_Z, st>>>(g, n, nkx, ntx, ntiles, P, tln, invlap, sb);
+      rcols_pipe_kernel<T, A1, A2, true><<<gy, CG::NT, Gp::SMEM_COLS, st>>>(g, nkx, ntx, ntiles, P, P,
+                                                                            (long long)n * P, tln, sb);
+    } else {
+      const dim3 gc((unsigned)ntiles, 1, ns);
+      rcols_kernel<T, A1, A2, false><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, sb);
+      rzsolve_kernel<T, A1, A2><<<gc, CG::NT, CG::SMEM_Z, st>>>(g, n, nkx, ntx, P, tln, invlap, sb);
+      rcols_kernel<T, A1, A2, true><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, sb);
+    }
   }
 
   static cudaError_t solve(exc_poisson* ps, const T* src, bool vec, cudaStream_t st, const SlotBatch& sb, int ns) {
@@ -592,11 +830,7 @@ struct RegSolve {
       rr2c_kernel<T, B1, B2, true><<<gx, XG::NT, XG::SMEM, st>>>(src, (T)(1.0 / ps->h), g, P, tw, tlh, sb);
     else
       rr2c_kernel<T, B1, B2, false><<<gx, XG::NT, XG::SMEM, st>>>(src, (T)1, g, P, tw, tlh, sb);
-    const int ntx = (nkx + CG::W - 1) / CG::W;
-    const dim3 gc((unsigned)(ntx * n), 1, ns);
-    rcols_kernel<T, A1, A2, false><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, sb);
-    rzsolve_kernel<T, A1, A2><<<gc, CG::NT, CG::SMEM_Z, st>>>(g, n, nkx, ntx, P, tln, ps->invlap, sb);
-    rcols_kernel<T, A1, A2, true><<<gc, CG::NT, CG::SMEM, st>>>(g, nkx, ntx, P, (long long)n * P, tln, sb);
+    columns(g, nkx, P, tln, ps->invlap, st, sb, ns);
     rc2r_kernel<T, B1, B2><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, sb);
     return cudaGetLastError();
   }

@@ -92,41 +92,64 @@ constexpr size_t plane_smem_bytes() {
   return sizeof(PlaneSmem<T, NC>) + 128;
 }
 
+// Stress values.  FP32 form (SC false): 4 sigma of the velocities in shared
+// memory, the divergence takes 1/(4h).  FP64 form (SC true): the planes in
+// shared memory hold w = s u - q (s = sqrt(kd), kd = 1/(4h), rho = rv s, q =
+// rho/2, rv = 4 visc/h) and the stresses are -kd 4 sigma up to a constant per
+// component, which the divergence's differences cancel:
+//   -kd 4 sigma_ii = -(w_i + w_i(-e_i))^2 - 4 rho w_i(-e_i) - rho^2,
+//   -kd 4 sigma_ij = -(w_i + w_i(+e_j)) (w_j + w_j(+e_i)) - 2 rho (w_i + w_j) - rho^2,
+// (expand 4 sigma_ii = (a + b)^2 - 2 rv (a - b), 4 sigma_ij = (a + b)(c + d)
+// - rv ((b - a) + (d - c)) with a = (w_a + q) / s ...): 3 and 5 FP64
+// operations instead of 4 and 7, and no scaling in the divergence -- the FP64
+// pipe, about two operations per clock per SM, bounds this sweep.
+// Diagonal: a at the cell, b its lower neighbour along i; cd = rv2 (FP32
+// form) or -4 rho (FP64 form).
+template <bool SC, typename T>
+__device__ __forceinline__ T sdiag_of(T a, T b, T cd) {
+  const T s = a + b;
+  if constexpr (SC) {
+    return fma(-s, s, cd * b);
+  } else {
+    const T d = a - b;
+    return s * s - cd * d;
+  }
+}
+// Off-diagonal: a = u_i, b = u_i(+e_j), c = u_j, d = u_j(+e_i); co = rv (FP32
+// form) or -2 rho (FP64 form).
+template <bool SC, typename T>
+__device__ __forceinline__ T soff_of(T a, T b, T c, T d, T co) {
+  if constexpr (SC) return fma(-(a + b), c + d, co * (a + c));
+  else return (a + b) * (c + d) - co * ((b - a) + (d - c));
+}
 // sigma_ii at box (bx, by) of plane buffer b (uses u_i at the cell and at -e_i)
-template <typename T, int I, typename U>
-__device__ __forceinline__ T sdiag(const U& u, int bx, int by, T rv2) {
+template <bool SC, typename T, int I, typename U>
+__device__ __forceinline__ T sdiag(const U& u, int bx, int by, T cd) {
   bx += SH<T>;
-  const T a = u[I][by][bx];
-  const T b = I == 0 ? u[0][by][bx - 1] : u[1][by - 1][bx];
-  const T s = a + b, d = a - b;
-  return s * s - rv2 * d;
+  return sdiag_of<SC>(u[I][by][bx], I == 0 ? u[0][by][bx - 1] : u[1][by - 1][bx], cd);
 }
 // sigma_12 at box (bx, by): u1, u1(+y), u2, u2(+x)
-template <typename T, typename U>
-__device__ __forceinline__ T s12(const U& u, int bx, int by, T rv) {
+template <bool SC, typename T, typename U>
+__device__ __forceinline__ T s12(const U& u, int bx, int by, T co) {
   bx += SH<T>;
-  const T a = u[0][by][bx], b = u[0][by + 1][bx], c = u[1][by][bx], d = u[1][by][bx + 1];
-  return (a + b) * (c + d) - rv * ((b - a) + (d - c));
+  return soff_of<SC>(u[0][by][bx], u[0][by + 1][bx], u[1][by][bx], u[1][by][bx + 1], co);
 }
 // sigma_13 at box (bx, by): u1, u1(+z) [next plane], u3, u3(+x)
-template <typename T, typename U>
-__device__ __forceinline__ T s13(const U& uc, const U& un, int bx, int by, T rv) {
+template <bool SC, typename T, typename U>
+__device__ __forceinline__ T s13(const U& uc, const U& un, int bx, int by, T co) {
   bx += SH<T>;
-  const T a = uc[0][by][bx], b = un[0][by][bx], c = uc[2][by][bx], d = uc[2][by][bx + 1];
-  return (a + b) * (c + d) - rv * ((b - a) + (d - c));
+  return soff_of<SC>(uc[0][by][bx], un[0][by][bx], uc[2][by][bx], uc[2][by][bx + 1], co);
 }
 // sigma_23 at box (bx, by): u2, u2(+z) [next plane], u3, u3(+y)
-template <typename T, typename U>
-__device__ __forceinline__ T s23(const U& uc, const U& un, int bx, int by, T rv) {
+template <bool SC, typename T, typename U>
+__device__ __forceinline__ T s23(const U& uc, const U& un, int bx, int by, T co) {
   bx += SH<T>;
-  const T a = uc[1][by][bx], b = un[1][by][bx], c = uc[2][by][bx], d = uc[2][by + 1][bx];
-  return (a + b) * (c + d) - rv * ((b - a) + (d - c));
+  return soff_of<SC>(uc[1][by][bx], un[1][by][bx], uc[2][by][bx], uc[2][by + 1][bx], co);
 }
 // sigma_33 between planes: u3 of the upper plane and of the lower plane
-template <typename T>
-__device__ __forceinline__ T s33(T up, T lo, T rv2) {
-  const T s = up + lo, d = up - lo;
-  return s * s - rv2 * d;
+template <bool SC, typename T>
+__device__ __forceinline__ T s33(T up, T lo, T cd) {
+  return sdiag_of<SC>(up, lo, cd);
 }
 
 template <typename T, int NC, bool DOADD>
@@ -149,10 +172,17 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int lane = tx, warp = ty;
   const int x0 = blockIdx.x * PTX, y0 = blockIdx.y * PTY, z0 = zb * ptz;
-  // stresses are kept as 4 sigma (rv = 4 visc / h), the divergence takes 1/(4h)
+  // FP32: stresses kept as 4 sigma (rv = 4 visc / h), the divergence takes
+  // 1/(4h).  FP64 (SC): shared memory holds w = s u - q, stresses are -kd 4
+  // sigma up to constants (see sdiag_of / soff_of)
+  constexpr bool SC = sizeof(T) == 8;
   const T kd = (T)0.25 * inv_h;
   const T rv = (T)4 * visc * inv_h;
-  const T rv2 = (T)2 * rv;
+  const T sq = SC ? (T)sqrt((double)kd) : (T)1;
+  const T rho = rv * sq;
+  const T qs = (T)0.5 * rho;
+  const T cd = SC ? (T)-4 * rho : (T)2 * rv;
+  const T co = SC ? (T)-2 * rho : rv;
   auto wrap = [n](int g) { return g < 0 ? g + n : (g >= n ? g - n : g); };
   auto wrapm = [n](int g) { return ((g % n) + n) % n; };
   const bool big = n >= PBX;
@@ -256,20 +286,62 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     }
     parity ^= 1u << buf;
   };
+  // FP64 form: w = s u - q in place over what this thread may touch of
+  // buffer buf after its wait -- the whole plane for TMA tiles (the mbarrier
+  // wait makes every copy visible to every waiting thread), else its own
+  // 16-byte pieces or words; the barrier after the wait publishes the result
+  auto shift_plane = [&](int buf) {
+    if constexpr (SC) {
+      if (tma) {
+        constexpr int HALF = PBY * UROW<T> / 2;  // 16-byte pairs per component plane
+        static_assert(PBY * UROW<T> % 2 == 0, "component plane of whole pairs");
+        for (int i = tid; i < 3 * HALF; i += PTX * NWARP) {
+          const int c = i / HALF;
+          double2* const p2 = reinterpret_cast<double2*>(&sm.u[buf][c].r[0][0]) + (i - c * HALF);
+          double2 v = *p2;
+          v.x = fma(sq, v.x, -qs);
+          v.y = fma(sq, v.y, -qs);
+          *p2 = v;
+        }
+      } else if (vec) {
+        T* const sb0 = &sm.u[buf][0].r[0][0];
+#pragma unroll
+        for (int i = 0; i < NSLOT; ++i)
+          if (goff[i] >= 0) {
+            double2* const p2 = reinterpret_cast<double2*>(sb0 + soff[i]);
+            double2 v = *p2;
+            v.x = fma(sq, v.x, -qs);
+            v.y = fma(sq, v.y, -qs);
+            *p2 = v;
+          }
+      } else {
+        for (int rr = ty; rr < PBY; rr += NWARP)
+          for (int bxx = tx; bxx < PBX; bxx += PTX)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              T& w = sm.u[buf][c][rr][bxx + SH<T>];
+              w = fma(sq, w, -qs);
+            }
+      }
+    }
+  };
   load_plane(0, zwrap(z0 - 1));
   load_plane(1, zwrap(z0));
   load_plane(2, zwrap(z0 + 1));
   wait_plane(0);
   wait_plane(1);
   wait_plane(2);
+  shift_plane(0);
+  shift_plane(1);
+  shift_plane(2);
   __syncthreads();
   T s13_prev[NC], s23_prev[NC], s33_cur[NC];
 #pragma unroll
   for (int i = 0; i < NC; ++i) {
     const int by = NC * ty + 1 + i;
-    s13_prev[i] = s13<T>(sm.u[0], sm.u[1], bx, by, rv);
-    s23_prev[i] = s23<T>(sm.u[0], sm.u[1], bx, by, rv);
-    s33_cur[i] = s33<T>(sm.u[1][2][by][bx + SH<T>], sm.u[0][2][by][bx + SH<T>], rv2);
+    s13_prev[i] = s13<SC, T>(sm.u[0], sm.u[1], bx, by, co);
+    s23_prev[i] = s23<SC, T>(sm.u[0], sm.u[1], bx, by, co);
+    s33_cur[i] = s33<SC, T>(sm.u[1][2][by][bx + SH<T>], sm.u[0][2][by][bx + SH<T>], cd);
   }
   __syncthreads();  // buffer 0 is refilled by the first prefetch
   // buffers: cur = plane z, nxt = plane z + 1, pre = the free one
@@ -291,12 +363,12 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
 #pragma unroll
     for (int i = 0; i < NC; ++i) {
       const int by = NC * ty + 1 + i;
-      v11[i] = sdiag<T, 0>(uc, bx, by, rv2);
-      v22[i] = sdiag<T, 1>(uc, bx, by, rv2);
-      v12[i] = s12<T>(uc, bx, by, rv);
-      v13[i] = s13<T>(uc, un, bx, by, rv);
-      v23[i] = s23<T>(uc, un, bx, by, rv);
-      v33n[i] = s33<T>(un[2][by][bx + SH<T>], uc[2][by][bx + SH<T>], rv2);
+      v11[i] = sdiag<SC, T, 0>(uc, bx, by, cd);
+      v22[i] = sdiag<SC, T, 1>(uc, bx, by, cd);
+      v12[i] = s12<SC, T>(uc, bx, by, co);
+      v13[i] = s13<SC, T>(uc, un, bx, by, co);
+      v23[i] = s23<SC, T>(uc, un, bx, by, co);
+      v33n[i] = s33<SC, T>(un[2][by][bx + SH<T>], uc[2][by][bx + SH<T>], cd);
       // s22 is read from the row above and s23 from the row below: inside a
       // thread's rows they stay in registers
       sm.s[0][by][bx] = v11[i];
@@ -309,17 +381,17 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
     // on the upper halo row, s12 and s13 on the left halo column, s11 on the
     // right halo column
     if (warp == 0) {
-      sm.s[2][0][lane + 1] = s12<T>(uc, lane + 1, 0, rv);
+      sm.s[2][0][lane + 1] = s12<SC, T>(uc, lane + 1, 0, co);
     } else if (warp == 1) {
-      sm.s[4][0][lane + 1] = s23<T>(uc, un, lane + 1, 0, rv);
+      sm.s[4][0][lane + 1] = s23<SC, T>(uc, un, lane + 1, 0, co);
     } else if (warp == 2) {
-      sm.s[1][PTY + 1][lane + 1] = sdiag<T, 1>(uc, lane + 1, PTY + 1, rv2);
+      sm.s[1][PTY + 1][lane + 1] = sdiag<SC, T, 1>(uc, lane + 1, PTY + 1, cd);
     } else if (warp == 3) {
-      for (int r = lane; r <= PTY; r += 32) sm.s[2][r][0] = s12<T>(uc, 0, r, rv);
+      for (int r = lane; r <= PTY; r += 32) sm.s[2][r][0] = s12<SC, T>(uc, 0, r, co);
     } else if (warp == 4) {
-      for (int r = lane + 1; r <= PTY; r += 32) sm.s[3][r][0] = s13<T>(uc, un, 0, r, rv);
+      for (int r = lane + 1; r <= PTY; r += 32) sm.s[3][r][0] = s13<SC, T>(uc, un, 0, r, co);
     } else if (warp == 5) {
-      for (int r = lane + 1; r <= PTY; r += 32) sm.s[0][r][PTX + 1] = sdiag<T, 0>(uc, PTX + 1, r, rv2);
+      for (int r = lane + 1; r <= PTY; r += 32) sm.s[0][r][PTX + 1] = sdiag<SC, T, 0>(uc, PTX + 1, r, cd);
     }
     __syncthreads();
     if (gx < n) {
@@ -338,7 +410,17 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
           const T d2 = (v12[i] - S[2][by][bx - 1]) + (s22_above - v22[i]) + (v23[i] - s23_prev[i]);
           const T d3 = (v13[i] - S[3][by][bx - 1]) + (v23[i] - s23_below) + (v33n[i] - s33_cur[i]);
           const long long g = ((long long)z * n + gy) * n + gx;
-          if (DOADD) {
+          if constexpr (SC) {  // the stresses carry -kd
+            if (DOADD) {
+              du1[g] += d1;
+              du2[g] += d2;
+              du3[g] += d3;
+            } else {
+              du1[g] = d1;
+              du2[g] = d2;
+              du3[g] = d3;
+            }
+          } else if (DOADD) {
             du1[g] -= kd * d1;
             du2[g] -= kd * d2;
             du3[g] -= kd * d3;
@@ -353,7 +435,10 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
         s33_cur[i] = v33n[i];
       }
     }
-    if (kz + 1 < ptz && z + 1 < n) wait_plane(pre);
+    if (kz + 1 < ptz && z + 1 < n) {
+      wait_plane(pre);
+      shift_plane(pre);
+    }
     __syncthreads();
     const int freed = cur;
     cur = nxt;

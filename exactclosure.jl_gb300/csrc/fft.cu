@@ -600,6 +600,7 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
     invlap_kernel<<<blocks, 256>>>(n, ps->mix->sin2, coef_mix, ps->mix->invlap);
     invlap_split_kernel<<<blocks, 256>>>(tot, ps->mix->invlap);
     if (cudaMalloc(&ps->mix_d, (size_t)n * n * n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&ps->mix_q, (size_t)n * n * n * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&ps->mix_part, (size_t)fftmix_part_words(n) * sizeof(double)) != cudaSuccess) {
       set_last_error("out of device memory (mixed-precision poisson buffers)");
       poisson_free(ps);
@@ -630,8 +631,10 @@ void poisson_free(exc_poisson* ps) {
     ps->mix = nullptr;
   }
   if (ps->mix_d) cudaFree(ps->mix_d);
+  if (ps->mix_q) cudaFree(ps->mix_q);
   if (ps->mix_part) cudaFree(ps->mix_part);
   ps->mix_d = ps->mix_part = nullptr;
+  ps->mix_q = nullptr;
   if (ps->tw) cudaFree(ps->tw);
   if (ps->sin2) cudaFree(ps->sin2);
   if (ps->invlap) cudaFree(ps->invlap);

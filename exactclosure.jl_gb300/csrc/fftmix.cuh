@@ -7,8 +7,9 @@
 // of fftreg.cuh, bound by HBM) and recovers FP64 accuracy by refinement with
 // residuals formed in FP64:
 //
-//   p  = S32(d)
-//   p += S32(d - L_h p)          (twice)
+//   q1 = S32(d),       p  = q1,   r1 = d  - L_h q1
+//   q2 = S32(r1),      p += q2,   r2 = r1 - L_h q2
+//   q3 = S32(r2),      p += q3
 //
 // where S32 is the FP32 spectral solve (relative error about 1e-7) and L_h
 // the 7-point staggered Laplacian, (sum of the 6 neighbours - 6 p) / h^2,
@@ -16,8 +17,13 @@
 // correction shrinks the error by about the FP32 solve's relative error, so
 // after two corrections p agrees with the FP64 FFT solve to FP64 rounding
 // (about 1e-15 relative for smooth and for white-noise right-hand sides).
-// The divergence is formed once in FP64 and kept (unscaled by 1/h: the FP32
-// solves carry the factor 1/h in their 1/(lambda N) table); the pressure's
+// The corrections q_k are FP32 fields, so the stencil sums of L_h q_k are
+// formed from FP32 values by error-free extraction (stencil7_f32) on the
+// FP32 pipe and rounded once to FP64, more accurate than the six FP64
+// additions they replace; each residual then costs three FP64 operations
+// per cell instead of seven.  The divergence is formed once in FP64
+// (unscaled by 1/h: the FP32 solves carry the factor 1/h in their
+// 1/(lambda N) table) and the first residual replaces it; the pressure's
 // mean (the solution's free constant, which the FP32 solves leave at their
 // rounding level) is measured during the last residual pass and removed in
 // the last accumulation, so p has zero mean like the reference's -- unless
@@ -65,6 +71,54 @@ __device__ __forceinline__ double f32_to_f64(float v) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// The FP32 value the conversion above puts into p: float subnormals become a
+// signed zero, so the correction kept for the next residual is the one added.
+__device__ __forceinline__ float f32_flush(float v) {
+  const unsigned b = __float_as_uint(v);
+  return (b & 0x7F800000u) ? v : __uint_as_float(b & 0x80000000u);
+}
+
+// One level of error-free extraction (ExtractScalar of Rump, Ogita and Oishi,
+// "Accurate floating-point summation part I: faithful rounding", SIAM J. Sci.
+// Comput. 31(1), 2008): for a power of two sigma and |t| <= sigma / 2, hi =
+// fl(fl(sigma + t) - sigma) is exact (Sterbenz) and a multiple of u sigma (u =
+// 2^-24), and t - hi is exact with |t - hi| <= u sigma; t becomes t - hi.
+__device__ __forceinline__ float extract_hi(float sigma, float& t) {
+  const float hi = __fsub_rn(__fadd_rn(sigma, t), sigma);
+  t = __fsub_rn(t, hi);
+  return hi;
+}
+
+// (n0 + ... + n5) - 6 c of FP32 values, rounded once to FP64.  The eight
+// terms (the neighbours, -4c, -2c) have |t| <= M < 2^(E+1); with sigma1 =
+// 2^(E+5) every partial sum of the extracted parts is a multiple of u sigma1
+// below sigma1 (sum |t| <= 8M < sigma1 / 2), so their FP32 sum h1 is exact;
+// the remainders (|t| <= u sigma1) go through a second level at sigma2 =
+// 2^-19 sigma1 (exact h2, a multiple of 2^(E-38)), and the last remainders
+// (|t| <= 2^(E-38)) are summed in FP32, an error below 2^(E-58).  h1 + h2
+// spans 43 bits and is exact in FP64; adding the last sum rounds once.  The
+// six FP64 additions this replaces err by up to about 2^(E-48).
+__device__ __forceinline__ double stencil7_f32(float n0, float n1, float n2, float n3, float n4, float n5,
+                                               float c) {
+  float t[8] = {n0, n1, n2, n3, n4, n5, -4.0f * c, -2.0f * c};
+  unsigned mb = 0u;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) mb = max(mb, __float_as_uint(t[i]) & 0x7FFFFFFFu);
+  // biased exponent of the largest term (0: zero or subnormal), capped so
+  // sigma1 stays finite; sigma2 at least the smallest normal float
+  const unsigned e1 = min((mb >> 23) + 5u, 254u);
+  const float s1 = __uint_as_float(e1 << 23);
+  const float s2 = __uint_as_float((e1 > 20u ? e1 - 19u : 1u) << 23);
+  float h1 = 0.0f, h2 = 0.0f, l2 = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) h1 = __fadd_rn(h1, extract_hi(s1, t[i]));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) h2 = __fadd_rn(h2, extract_hi(s2, t[i]));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) l2 = __fadd_rn(l2, t[i]);
+  return (f32_to_f64(h1) + f32_to_f64(h2)) + f32_to_f64(l2);
+}
+
 template <typename C>
 __device__ __forceinline__ C to_f32c(double a, double b) {
   C r;
@@ -78,14 +132,18 @@ __device__ __forceinline__ C to_f32c(double a, double b) {
 //   MIX_SCAL: d' = h (d - mean d) from a scalar FP64 right-hand side (its
 //             mean, the part no pressure can balance, is removed first so the
 //             FP32 residual solves do not carry it), stored, transformed;
-//   MIX_RES:  r' = d' - (sum of neighbours of p - 6 p) / h, transformed
-//             (p: FP64 real view of the FP64 work array, row pitch 2P);
-//   MIX_RES_MEAN: as MIX_RES, and the CTA's sum of p goes to part[blockIdx.x].
+//   MIX_RES:  r' = r'_prev - (sum of neighbours of q - 6 q) / h with the
+//             previous residual r'_prev in d (the divergence at first) and
+//             the last FP32 correction q (n^3 floats), transformed; stored
+//             back to d when `store` is set;
+//   MIX_RES_MEAN: as MIX_RES, and the CTA's sum of p (FP64 real view of the
+//             FP64 work array, row pitch 2P) goes to part[blockIdx.x].
 template <int N1, int N2, int MODE>
 __global__ void __launch_bounds__(XGeom<float, N1, N2>::NT)
 mr2c_kernel(const double* __restrict__ src, double h, double* __restrict__ d, const double* __restrict__ p, int P,
             double inv_h, cplx<float>* __restrict__ out, const cplx<float>* __restrict__ tw,
-            const cplx<float>* __restrict__ tl, double* __restrict__ part) {
+            const cplx<float>* __restrict__ tl, double* __restrict__ part, const float* __restrict__ q,
+            int store) {
   using C = cplx<float>;
   using G = XGeom<float, N1, N2>;
   constexpr int L = N1 * N2, n = 2 * L, RW = G::RW, XS = G::XS;
@@ -138,29 +196,31 @@ mr2c_kernel(const double* __restrict__ src, double h, double* __restrict__ d, co
           v[m1] = to_f32c<C>(dv.x, dv.y);
         }
       } else {
-        const long long pp = 2LL * P;
-        const double* pr = p + row * pp;
-        const double2* pc2 = reinterpret_cast<const double2*>(pr);
-        const double2* pym = reinterpret_cast<const double2*>(p + ((long long)z * n + wrap_dn(y, n)) * pp);
-        const double2* pyp = reinterpret_cast<const double2*>(p + ((long long)z * n + wrap_up(y, n)) * pp);
-        const double2* pzm = reinterpret_cast<const double2*>(p + ((long long)wrap_dn(z, n) * n + y) * pp);
-        const double2* pzp = reinterpret_cast<const double2*>(p + ((long long)wrap_up(z, n) * n + y) * pp);
-        const double2* d2 = reinterpret_cast<const double2*>(d + base);
+        const float* qr = q + base;
+        const float2* qc2 = reinterpret_cast<const float2*>(qr);
+        const float2* qym = reinterpret_cast<const float2*>(q + ((long long)z * n + wrap_dn(y, n)) * n);
+        const float2* qyp = reinterpret_cast<const float2*>(q + ((long long)z * n + wrap_up(y, n)) * n);
+        const float2* qzm = reinterpret_cast<const float2*>(q + ((long long)wrap_dn(z, n) * n + y) * n);
+        const float2* qzp = reinterpret_cast<const float2*>(q + ((long long)wrap_up(z, n) * n + y) * n);
+        double2* d2 = reinterpret_cast<double2*>(d + base);
+        const double2* pc2 = reinterpret_cast<const double2*>(p + row * 2LL * P);
 #pragma unroll
         for (int m1 = 0; m1 < N1; ++m1) {
           const int m = m2 + N2 * m1;
-          const double2 pc = pc2[m];
-          const double pxm = pr[m == 0 ? n - 1 : 2 * m - 1];
-          const double pxp = pr[m == L - 1 ? 0 : 2 * m + 2];
-          const double2 a = pym[m], b = pyp[m], c = pzm[m], e = pzp[m];
-          const double2 dv = d2[m];
-          // neighbours of x = 2m: pxm and 2m + 1; of x = 2m + 1: 2m and pxp
-          const double sx = ((pxm + pc.y) + (a.x + b.x)) + (c.x + e.x);
-          const double sy = ((pc.x + pxp) + (a.y + b.y)) + (c.y + e.y);
-          const double rx = fma(-inv_h, fma(-6.0, pc.x, sx), dv.x);
-          const double ry = fma(-inv_h, fma(-6.0, pc.y, sy), dv.y);
-          if constexpr (MODE == MIX_RES_MEAN) psum += pc.x + pc.y;
-          v[m1] = to_f32c<C>(rx, ry);
+          const float2 qc = qc2[m];
+          const float qxm = qr[m == 0 ? n - 1 : 2 * m - 1];
+          const float qxp = qr[m == L - 1 ? 0 : 2 * m + 2];
+          const float2 a = qym[m], b = qyp[m], c = qzm[m], e = qzp[m];
+          double2 rv = d2[m];
+          // neighbours of x = 2m: qxm and 2m + 1; of x = 2m + 1: 2m and qxp
+          rv.x = fma(-inv_h, stencil7_f32(qxm, qc.y, a.x, b.x, c.x, e.x, qc.x), rv.x);
+          rv.y = fma(-inv_h, stencil7_f32(qc.x, qxp, a.y, b.y, c.y, e.y, qc.y), rv.y);
+          if (store) d2[m] = rv;
+          if constexpr (MODE == MIX_RES_MEAN) {
+            const double2 pc = pc2[m];
+            psum += pc.x + pc.y;
+          }
+          v[m1] = to_f32c<C>(rv.x, rv.y);
         }
       }
     } else {
@@ -230,13 +290,14 @@ mr2c_kernel(const double* __restrict__ src, double h, double* __restrict__ d, co
   }
 }
 
-// x pass, FP32 half spectrum -> reals (the rc2r_kernel transform), written
+// x pass, FP32 half spectrum -> reals c (the rc2r_kernel transform), written
 // to the FP64 pressure p (row pitch 2P): MIX_SET p = c; MIX_ADD p += c;
-// MIX_ADD_MEAN p += c - mean.
+// MIX_ADD_MEAN p += c - mean; and c itself to q (n^3 floats) unless q is null.
 template <int N1, int N2, int MODE>
 __global__ void __launch_bounds__(XGeom<float, N1, N2>::NT)
 mc2r_kernel(const cplx<float>* __restrict__ g, int P, const cplx<float>* __restrict__ tw,
-            const cplx<float>* __restrict__ tl, double* __restrict__ p, const double* __restrict__ mean) {
+            const cplx<float>* __restrict__ tl, double* __restrict__ p, const double* __restrict__ mean,
+            float* __restrict__ q) {
   using C = cplx<float>;
   using G = XGeom<float, N1, N2>;
   constexpr int L = N1 * N2, n = 2 * L, RW = G::RW, XS = G::XS;
@@ -279,6 +340,7 @@ mc2r_kernel(const cplx<float>* __restrict__ g, int P, const cplx<float>* __restr
     for (int q = 0; q < N2; ++q) zz[q] = xs[lb * XS + k1 * (N2 + 1) + q];
     dft_reg<N2, true>(zz);
     double2* r = reinterpret_cast<double2*>(p + row * 2LL * P);
+    float2* qo = q ? reinterpret_cast<float2*>(q + row * n) : nullptr;
     double mu = 0.0;
     if constexpr (MODE == MIX_ADD_MEAN) mu = *mean;
 #pragma unroll
@@ -286,6 +348,7 @@ mc2r_kernel(const cplx<float>* __restrict__ g, int P, const cplx<float>* __restr
       const int m = k1 + N1 * k2;
       double2 o;
       const double cx = f32_to_f64(zz[k2].x), cy = f32_to_f64(zz[k2].y);
+      if (qo) qo[m] = make_float2(f32_flush(zz[k2].x), f32_flush(zz[k2].y));
       if constexpr (MODE == MIX_SET) {
         o.x = cx;
         o.y = cy;
@@ -378,28 +441,30 @@ struct MixSolve {
     const unsigned gx = (unsigned)NPARTS;
     const SlotBatch one;
     auto columns = [&]() { RS::columns(g, nkx, P, tln, sp->invlap, st, one, 1); };
+    float* q = ps->mix_q;
     if (vec) {
-      mr2c_kernel<B1, B2, MIX_DIV><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+      mr2c_kernel<B1, B2, MIX_DIV><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q, 0);
     } else {
       // mean of d into part[0] (partials in part[1 .. SUM_CTAS])
       mix_sum_kernel<<<SUM_CTAS, 256, 0, st>>>(src, (long long)n * n * n, part + 1);
       mix_mean_kernel<<<1, 256, 0, st>>>(part + 1, SUM_CTAS, 1.0 / ((double)n * n * n), part);
-      mr2c_kernel<B1, B2, MIX_SCAL><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+      mr2c_kernel<B1, B2, MIX_SCAL><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q, 0);
     }
     columns();
-    mc2r_kernel<B1, B2, MIX_SET><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
-    mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+    mc2r_kernel<B1, B2, MIX_SET><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, q);
+    mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q, 1);
     columns();
-    mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+    mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, q);
     if (ps->mix_zero_mean) {
-      mr2c_kernel<B1, B2, MIX_RES_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+      mr2c_kernel<B1, B2, MIX_RES_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q,
+                                                                      0);
       mix_mean_kernel<<<1, 256, 0, st>>>(part, (int)NPARTS, 1.0 / ((double)n * n * n), mean);
       columns();
-      mc2r_kernel<B1, B2, MIX_ADD_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+      mc2r_kernel<B1, B2, MIX_ADD_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, nullptr);
     } else {
-      mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part);
+      mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q, 0);
       columns();
-      mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean);
+      mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, nullptr);
     }
     return cudaGetLastError();
   }

@@ -28,11 +28,13 @@ struct exc_poisson {
   // 1: the FP64 shared-memory Stockham passes; 2: the FP64 register passes
   // where planned, else Stockham (no mixed precision)
   int engine = 0;
-  // mixed-precision FP64 solve (fftmix.cu): the FP32 inner solver (its own
+  // mixed-precision FP64 solve (fftmix.cuh): the FP32 inner solver (its own
   // work array and tables, 1/(lambda N h) divide table), the FP64 divergence
-  // (n^3, unscaled by 1/h) and per-CTA partial sums of p with the mean last
+  // (n^3, unscaled by 1/h; the first residual replaces it), the last FP32
+  // correction (n^3 floats) and per-CTA partial sums of p with the mean last
   exc_poisson* mix = nullptr;
   double* mix_d = nullptr;
+  float* mix_q = nullptr;
   double* mix_part = nullptr;
   // remove the pressure's mean (its free constant) in the mixed solve; false
   // where p is only used through its gradient

@@ -37,6 +37,9 @@ struct LesState {
   int tb_from = -1;
   bool tb_same = false;
   T* tb2 = nullptr;  // root LES of a fused stepper: sums of the stage state
+  // FP64 stepper: sums of the step's initial state; the stage states u0 + cs
+  // k_(s-1) take theirs by linearity from these and the sums of k_(s-1)
+  T* tbu0 = nullptr;
   T *ub, *fk, *mcl, *mlast, *rtmp;
   T *ve[2], *ves, *ke;  // exact LES: state (ping-pong), stage, k
   T *vn[2], *vns, *kn;  // no-model LES
@@ -67,6 +70,7 @@ namespace exc {
 template <typename T>
 struct CaseImpl {
   int fuse_root = -1;  // LES whose ratio the fused RK stage sums (-1: separate passes)
+  bool tb_lin = false;  // stage-state sums by linearity (LesState::tbu0)
   int n = 0;
   long long N = 0;
   double h = 0;
@@ -153,6 +157,48 @@ static int les_tb_fill(CaseImpl<T>* ci, const T* src, cudaStream_t st) {
 template <typename T>
 static const T* les_tb(const CaseImpl<T>* ci, const LesState<T>& L) {
   return L.tb_same ? ci->les[L.tb_from].tb : L.tb;
+}
+
+// y = a + cs y with the RK stage coefficient of stage sprev (cs = dt/2, dt/2,
+// dt: the stage state u0 + cs k of rk_stage2_kernel), dt read on the device.
+template <typename T>
+__global__ void tb_lin_kernel(long long count, const T* __restrict__ a, T* __restrict__ y,
+                              const double* __restrict__ dtp, int sprev) {
+  const double dt = dtp[0];
+  const T cs = (T)(sprev == 2 ? dt : 0.5 * dt);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    y[i] = fma(cs, y[i], a[i]);
+}
+
+// Keep the sums of the step's initial state (stage 0) for the linearity form.
+template <typename T>
+static int les_tb_keep(CaseImpl<T>* ci, cudaStream_t st) {
+  for (int li = 0; li < ci->nles; ++li) {
+    LesState<T>& L = ci->les[li];
+    if (L.tb_same) continue;
+    const cudaError_t e =
+        cudaMemcpyAsync(L.tbu0, L.tb, 3 * (size_t)ci->n * L.m * L.m * sizeof(T), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  }
+  return EXC_OK;
+}
+
+// Sums of the stage state of stage sprev + 1 from the sums of the initial state
+// and those of k_sprev (in tb since the end of stage sprev): the box sums are
+// linear, so this replaces a pass over the fine field by one over the sums
+// (n^3 / c^2 words per component); the results differ from summing the stage
+// state only by rounding.
+template <typename T>
+static int les_tb_lin(CaseImpl<T>* ci, int sprev, const double* dt, cudaStream_t st) {
+  for (int li = 0; li < ci->nles; ++li) {
+    LesState<T>& L = ci->les[li];
+    if (L.tb_same) continue;
+    const long long cnt = 3LL * ci->n * L.m * L.m;
+    tb_lin_kernel<T><<<grid_for_count(cnt), 256, 0, st>>>(cnt, L.tbu0, L.tb, dt, sprev);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  }
+  return EXC_OK;
 }
 
 // Fused stepper (one root ratio for every LES): the root's sums come from
@@ -250,9 +296,12 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
       if (fused && s > 0) {
         troot = root_s;
         rc = les_tb_coarsen<T>(ci, troot, st);
+      } else if (ci->tb_lin && s > 0) {
+        rc = les_tb_lin<T>(ci, s - 1, dt, st);
       } else {
         rc = les_tb_fill<T>(ci, src, st);
         if (fused) troot = root_k;
+        if (!rc && ci->tb_lin) rc = les_tb_keep<T>(ci, st);
       }
       if (rc) return rc;
     }
@@ -417,6 +466,7 @@ static void case_destroy(exc_case* cs) {
     if (ci->les[li].buf) cudaFree(ci->les[li].buf);
     if (ci->les[li].tb) cudaFree(ci->les[li].tb);
     if (ci->les[li].tb2) cudaFree(ci->les[li].tb2);
+    if (ci->les[li].tbu0) cudaFree(ci->les[li].tbu0);
     if (ci->les[li].fb) cudaFree(ci->les[li].fb);
   }
   delete ci;
@@ -516,6 +566,17 @@ static int case_create(exc_case* cs) {
         ci->fuse_root = root;
       }
     }
+  }
+  // FP64 with separate sum passes: stage-state sums by linearity
+  ci->tb_lin = false;
+  if (sizeof(T) == 8 && ci->fuse_root < 0 && d.nles > 0) {
+    for (int li = 0; li < d.nles; ++li) {
+      LesState<T>& L = ci->les[li];
+      if (L.tb_same) continue;
+      const size_t tbb = 3 * (size_t)d.n * L.m * L.m * sizeof(T);
+      if (cudaMalloc(&L.tbu0, tbb) != cudaSuccess) { set_last_error("out of device memory (LES filter scratch)"); return EXC_ERR_OOM; }
+    }
+    ci->tb_lin = true;
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }

@@ -19,9 +19,9 @@ cudaError_t launch_rk_stage_sums(int n, int c0, T h, const T* k, const T* p, int
                                  int stage, const double* dtp, T* tbk, T* tbs, cudaStream_t st);
 // Chunk width (cells per row) of rk_stage_sums_kernel for ratio c0; 0 when
 // the fused stage is not used: FP64 (measured slower than the separate
-// passes: 512^3 with LES ratios 8 and 4, 197.6 against 196.2 ms per RK4
-// step), ratios without a kernel, or rows under 128 bytes wide (poorly
-// coalesced).
+// passes: 512^3 with LES ratios 8 and 4, 103.5 against 101.9 ms per RK4
+// step with k's sums only and the stage-state sums by linearity), ratios
+// without a kernel, or rows under 128 bytes wide (poorly coalesced).
 template <typename T>
 inline int rk_sums_chunk(int c0) {
   const int V = 16 / (int)sizeof(T);

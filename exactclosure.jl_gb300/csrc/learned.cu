@@ -36,6 +36,12 @@ __device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erf
 __device__ __forceinline__ float gelu_grad_f(float x) {
   return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
+// GELU(x) and GELU'(x) with one erf: the same values as gelu_f and gelu_grad_f
+__device__ __forceinline__ void gelu_and_grad(float x, float& g, float& d) {
+  const float e = erff(x * 0.70710678118654752f);
+  g = 0.5f * x * (1.0f + e);
+  d = 0.5f * (1.0f + e) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
 
 __device__ __forceinline__ unsigned ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const unsigned*>(p); }
 
@@ -74,14 +80,15 @@ __device__ __forceinline__ long long neighbour(long long v, int n, int dz, int d
 // Implicit-GEMM convolution on the tensor cores:
 //   out[v][co] = bias[co] + sum_{tap, ci} in[v + tap][ci] * Wt[tap][co][ci]
 // KP: input channels (multiple of 16), NP: output channels (multiple of 8).
-// EPI 0: store pre (FP32) and GELU(pre) (BF16);  EPI 1: store out (FP32);
-// EPI 2: input gradient: multiply by GELU'(pre_prev[v][co]), store BF16.
+// EPI 0: store GELU(pre) (BF16) and, unless dg is null (inference), GELU'(pre)
+// (BF16) into dg for the backward pass;  EPI 1: store out (FP32);
+// EPI 2: input gradient: multiply by GELU'(pre) read from dg, store BF16.
 // ---------------------------------------------------------------------------
 template <int KP, int NP, int EPI>
 __global__ void __launch_bounds__(CONV_THREADS)
 conv_mma_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
                 const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
-                const float* __restrict__ pre_prev, int nout_valid) {
+                __nv_bfloat16* __restrict__ dg, int nout_valid) {
   constexpr int AS = KP + 8;  // padded row stride (bf16) against bank conflicts
   __shared__ __align__(16) __nv_bfloat16 sA[CONV_M * AS];
   __shared__ __align__(16) __nv_bfloat16 sW[NP * AS];
@@ -138,13 +145,19 @@ conv_mma_kernel(long long V, int n, const __nv_bfloat16* __restrict__ in, const 
         float x = acc[j][h * 2 + e];
         if (EPI == 0) {
           x += bias[co];
-          pre_out[v * NP + co] = x;
-          act_out[v * NP + co] = __float2bfloat16(gelu_f(x));
+          if (dg) {
+            float gx, dx;
+            gelu_and_grad(x, gx, dx);
+            act_out[v * NP + co] = __float2bfloat16(gx);
+            dg[v * NP + co] = __float2bfloat16(dx);
+          } else {
+            act_out[v * NP + co] = __float2bfloat16(gelu_f(x));
+          }
         } else if (EPI == 1) {
           x += bias[co];
           pre_out[v * NP + co] = co < nout_valid ? x : 0.f;
         } else {
-          act_out[v * NP + co] = __float2bfloat16(x * gelu_grad_f(pre_prev[v * NP + co]));
+          act_out[v * NP + co] = __float2bfloat16(x * __bfloat162float(dg[v * NP + co]));
         }
       }
     }
@@ -165,7 +178,7 @@ template <int KP, int NP, int EPI>
 __global__ void __launch_bounds__(CONV_THREADS)
 conv_tile_kernel(int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
                  const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
-                 const float* __restrict__ pre_prev, int nout_valid) {
+                 __nv_bfloat16* __restrict__ dg, int nout_valid) {
   constexpr int AS = KP + 8;  // padded row stride (bf16) against bank conflicts
   constexpr int CH = KP / 8;  // 16-byte chunks per voxel row
   __shared__ __align__(16) __nv_bfloat16 sT[TVOX * AS];
@@ -239,13 +252,19 @@ conv_tile_kernel(int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat1
         float x = acc[j][h * 2 + e];
         if (EPI == 0) {
           x += bias[co];
-          pre_out[v * NP + co] = x;
-          act_out[v * NP + co] = __float2bfloat16(gelu_f(x));
+          if (dg) {
+            float gx, dx;
+            gelu_and_grad(x, gx, dx);
+            act_out[v * NP + co] = __float2bfloat16(gx);
+            dg[v * NP + co] = __float2bfloat16(dx);
+          } else {
+            act_out[v * NP + co] = __float2bfloat16(gelu_f(x));
+          }
         } else if (EPI == 1) {
           x += bias[co];
           pre_out[v * NP + co] = co < nout_valid ? x : 0.f;
         } else {
-          act_out[v * NP + co] = __float2bfloat16(x * gelu_grad_f(pre_prev[v * NP + co]));
+          act_out[v * NP + co] = __float2bfloat16(x * __bfloat162float(dg[v * NP + co]));
         }
       }
     }
@@ -288,7 +307,7 @@ template <int KP, int NP, int EPI>
 __global__ void __launch_bounds__(CR_THREADS)
 conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ Wt,
                 const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
-                const float* __restrict__ pre_prev, int nout_valid) {
+                __nv_bfloat16* __restrict__ dg, int nout_valid) {
   constexpr int AS = KP + 8, NTL = NP / 8;
   static_assert(NTL % 2 == 0, "B fragments load two n-tiles at a time");
   extern __shared__ __align__(16) unsigned char cr_smem[];
@@ -390,18 +409,27 @@ conv_res_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const __
         if (EPI == 0) {
           x0v += bias[co];
           x1v += bias[co + 1];
-          *reinterpret_cast<float2*>(pre_out + v * NP + co) = make_float2(x0v, x1v);
-          *reinterpret_cast<__nv_bfloat162*>(act_out + v * NP + co) =
-              __halves2bfloat162(__float2bfloat16(gelu_f(x0v)), __float2bfloat16(gelu_f(x1v)));
+          if (dg) {
+            float g0, d0, g1, d1;
+            gelu_and_grad(x0v, g0, d0);
+            gelu_and_grad(x1v, g1, d1);
+            *reinterpret_cast<__nv_bfloat162*>(act_out + v * NP + co) =
+                __halves2bfloat162(__float2bfloat16(g0), __float2bfloat16(g1));
+            *reinterpret_cast<__nv_bfloat162*>(dg + v * NP + co) =
+                __halves2bfloat162(__float2bfloat16(d0), __float2bfloat16(d1));
+          } else {
+            *reinterpret_cast<__nv_bfloat162*>(act_out + v * NP + co) =
+                __halves2bfloat162(__float2bfloat16(gelu_f(x0v)), __float2bfloat16(gelu_f(x1v)));
+          }
         } else if (EPI == 1) {
           x0v += bias[co];
           x1v += bias[co + 1];
           *reinterpret_cast<float2*>(pre_out + v * NP + co) =
               make_float2(co < nout_valid ? x0v : 0.f, co + 1 < nout_valid ? x1v : 0.f);
         } else {
-          const float2 pp = *reinterpret_cast<const float2*>(pre_prev + v * NP + co);
+          const float2 dd = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(dg + v * NP + co));
           *reinterpret_cast<__nv_bfloat162*>(act_out + v * NP + co) =
-              __halves2bfloat162(__float2bfloat16(x0v * gelu_grad_f(pp.x)), __float2bfloat16(x1v * gelu_grad_f(pp.y)));
+              __halves2bfloat162(__float2bfloat16(x0v * dd.x), __float2bfloat16(x1v * dd.y));
         }
       }
     }
@@ -556,7 +584,7 @@ template <int NP, int EPI>
 __global__ void __launch_bounds__(CU_THREADS, 1)
 conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bfloat16* __restrict__ Wt,
                  const float* __restrict__ bias, float* __restrict__ pre_out, __nv_bfloat16* __restrict__ act_out,
-                 const float* __restrict__ pre_prev, int nout_valid) {
+                 __nv_bfloat16* __restrict__ dg, int nout_valid) {
   constexpr int n = CU_N, KP = CU_KP, KC = CU_KC, NT = 3 * NP, NH = NP / 2;
   constexpr int HB = cu_halo_bytes, WB = cu_w_bytes<NP>();
   constexpr unsigned TCOLS = cu_tmem_cols<NP>();
@@ -768,8 +796,26 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
             v.z = co + 2 < nout_valid ? v.z : 0.f;
             v.w = co + 3 < nout_valid ? v.w : 0.f;
           }
-          *reinterpret_cast<float4*>(pre_out + g * NP + cb + j) = v;
-          if (EPI == 0) {
+          if (EPI == 1) {
+            *reinterpret_cast<float4*>(pre_out + g * NP + cb + j) = v;
+          } else if (dg) {
+            float ga, da, gb, db, gc, dc, gd, dd;
+            gelu_and_grad(v.x, ga, da);
+            gelu_and_grad(v.y, gb, db);
+            gelu_and_grad(v.z, gc, dc);
+            gelu_and_grad(v.w, gd, dd);
+            __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(ga), __float2bfloat16(gb));
+            __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(gc), __float2bfloat16(gd));
+            uint2 pk;
+            pk.x = *reinterpret_cast<unsigned*>(&h0);
+            pk.y = *reinterpret_cast<unsigned*>(&h1);
+            *reinterpret_cast<uint2*>(act_out + g * NP + cb + j) = pk;
+            h0 = __halves2bfloat162(__float2bfloat16(da), __float2bfloat16(db));
+            h1 = __halves2bfloat162(__float2bfloat16(dc), __float2bfloat16(dd));
+            pk.x = *reinterpret_cast<unsigned*>(&h0);
+            pk.y = *reinterpret_cast<unsigned*>(&h1);
+            *reinterpret_cast<uint2*>(dg + g * NP + cb + j) = pk;
+          } else {
             __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(gelu_f(v.x)), __float2bfloat16(gelu_f(v.y)));
             __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(gelu_f(v.z)), __float2bfloat16(gelu_f(v.w)));
             uint2 pk;
@@ -781,11 +827,11 @@ conv_umma_kernel(int batch, const __grid_constant__ HaloMaps maps, const __nv_bf
       } else {
 #pragma unroll
         for (int j = 0; j < NH; j += 4) {
-          const float4 pp = *reinterpret_cast<const float4*>(pre_prev + g * NP + cb + j);
-          __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(f[j] * gelu_grad_f(pp.x)),
-                                                 __float2bfloat16(f[j + 1] * gelu_grad_f(pp.y)));
-          __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(f[j + 2] * gelu_grad_f(pp.z)),
-                                                 __float2bfloat16(f[j + 3] * gelu_grad_f(pp.w)));
+          const uint2 dq = *reinterpret_cast<const uint2*>(dg + g * NP + cb + j);
+          const float2 pa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&dq.x));
+          const float2 pb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&dq.y));
+          __nv_bfloat162 h0 = __halves2bfloat162(__float2bfloat16(f[j] * pa.x), __float2bfloat16(f[j + 1] * pa.y));
+          __nv_bfloat162 h1 = __halves2bfloat162(__float2bfloat16(f[j + 2] * pb.x), __float2bfloat16(f[j + 3] * pb.y));
           uint2 pk;
           pk.x = *reinterpret_cast<unsigned*>(&h0);
           pk.y = *reinterpret_cast<unsigned*>(&h1);
@@ -826,7 +872,7 @@ static bool halo_maps(const __nv_bfloat16* in, int batch, HaloMaps* m) {
 // forms only.
 template <int KP, int NP, int EPI>
 static void conv_launch(int engine, long long V, int n, const __nv_bfloat16* in, const __nv_bfloat16* W,
-                        const float* bias, float* pre_out, __nv_bfloat16* act_out, const float* pre_prev,
+                        const float* bias, float* pre_out, __nv_bfloat16* act_out, __nv_bfloat16* dg,
                         int nout_valid, cudaStream_t st) {
   if constexpr (KP == CU_KP) {
     if (engine == 0 && n == CU_N) {
@@ -838,7 +884,7 @@ static void conv_launch(int engine, long long V, int n, const __nv_bfloat16* in,
         const long long nblk = (long long)batch * n * (n / CU_ROWS);
         const long long ctas = std::min<long long>(nblk, 152);
         conv_umma_kernel<NP, EPI><<<(unsigned)ctas, CU_THREADS, conv_umma_smem<NP>(), st>>>(
-            batch, maps, W, bias, pre_out, act_out, pre_prev, nout_valid);
+            batch, maps, W, bias, pre_out, act_out, dg, nout_valid);
         return;
       }
     }
@@ -848,15 +894,15 @@ static void conv_launch(int engine, long long V, int n, const __nv_bfloat16* in,
     const long long nblk = V / CR_BV;
     const long long ctas = std::min<long long>(nblk, (long long)conv_res_per_sm<KP, NP>() * 152);
     conv_res_kernel<KP, NP, EPI><<<(unsigned)ctas, CR_THREADS, conv_res_smem<KP, NP>(), st>>>(
-        (int)(V / N), n, in, W, bias, pre_out, act_out, pre_prev, nout_valid);
+        (int)(V / N), n, in, W, bias, pre_out, act_out, dg, nout_valid);
   } else if (n % TB == 0) {
     const long long N = (long long)n * n * n;
     const long long blocks = (V / N) * (N / (TB * TB * TB));
     conv_tile_kernel<KP, NP, EPI><<<(unsigned)blocks, CONV_THREADS, 0, st>>>(n, in, W, bias, pre_out, act_out,
-                                                                          pre_prev, nout_valid);
+                                                                          dg, nout_valid);
   } else {
     conv_mma_kernel<KP, NP, EPI><<<(unsigned)((V + CONV_M - 1) / CONV_M), CONV_THREADS, 0, st>>>(
-        V, n, in, W, bias, pre_out, act_out, pre_prev, nout_valid);
+        V, n, in, W, bias, pre_out, act_out, dg, nout_valid);
   }
 }
 
@@ -1111,6 +1157,250 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient on the tcgen05 tensor cores (64^3 grids, conv engine 0):
+//   dW[tap][ci][co] = sum_v in[v + tap][ci] g[v][co]
+// reduced one output row at a time (64 voxels along x at fixed y, z, sample).
+// For the row, the A operand holds the nine input rows (y + dy, z + dz) (TMA
+// boxes of 8 channels x 64 voxels, 1 KB each) and the B operand the row of g
+// rotated by -dx for dx = -1, 0, 1: the unrotated copy arrives by TMA, the two
+// rotations (periodic along x, which a TMA box cannot wrap) are copied in
+// shared memory by the helper warps.  Both operands are MN-major (channels
+// contiguous per voxel, as stored), and
+//   D[(s, ci)][(dx, co)] += sum_x in[x, input row s][ci] g[x - dx][co]
+// is the row's contribution to dW[tap (dx, dy_s, dz_s)].  M = 128 holds 128 /
+// KP row shifts s, so the nine shifts take ceil(9 KP / 128) products per
+// 16-voxel step (the last partly unused); N = 3 NP.  The CTA's whole dW stays
+// in tensor memory over its rows and is written once as the CTA's partial
+// (folded by wgrad_fold_kernel in a fixed order).  Roles: warp 0 issues the
+// products, warp 1 the copies, warps 2-5 rotate g, sum it for the bias
+// gradient (FP32 per row segment, FP64 over rows, one partial per CTA) and, at
+// the end, read the accumulators.  Three or four stages of buffers keep
+// copies of later rows in flight; every wait is bounded as in
+// conv_umma_kernel (a wait that gives up records the fault, every role stops,
+// copies and products in flight are waited for, the tensor memory is freed).
+// ---------------------------------------------------------------------------
+constexpr int WU_THREADS = 192;
+struct WgMaps {
+  CUtensorMap a[4];  // input rows, per 8-channel chunk
+  CUtensorMap b[4];  // g rows, per 8-channel chunk
+};
+template <int KP> __host__ __device__ constexpr int wu_spg() { return 128 / KP; }
+template <int KP> __host__ __device__ constexpr int wu_groups() { return (9 + 128 / KP - 1) / (128 / KP); }
+template <int KP> __host__ __device__ constexpr int wu_a_bytes() { return wu_groups<KP>() * wu_spg<KP>() * (KP / 8) * 1024; }
+template <int NP> __host__ __device__ constexpr int wu_b_bytes() { return 3 * (NP / 8) * 1024; }
+template <int KP, int NP> __host__ __device__ constexpr int wu_stage_bytes() { return wu_a_bytes<KP>() + wu_b_bytes<NP>(); }
+// stages of buffers that fit in 216 KB (at most four)
+template <int KP, int NP> __host__ __device__ constexpr int wu_stages() {
+  return 216 * 1024 / wu_stage_bytes<KP, NP>() >= 4 ? 4 : (216 * 1024 / wu_stage_bytes<KP, NP>() >= 3 ? 3 : 2);
+}
+template <int KP, int NP> __host__ __device__ constexpr size_t wgrad_umma_smem() {
+  return 1024 + (size_t)wu_stages<KP, NP>() * wu_stage_bytes<KP, NP>() + 16 * 8;  // 1024: alignment slack
+}
+template <int KP, int NP> __host__ __device__ constexpr unsigned wu_tmem_cols() {
+  return wu_groups<KP>() * 3 * NP <= 256 ? 256u : 512u;
+}
+
+template <int KP, int NP>
+__global__ void __launch_bounds__(WU_THREADS, 1)
+wgrad_umma_kernel(int batch, const __grid_constant__ WgMaps maps, float* __restrict__ part,
+                  double* __restrict__ bpart) {
+  constexpr int n = CU_N, KC = KP / 8, NC = NP / 8, SPG = wu_spg<KP>(), NG = wu_groups<KP>(), NT = 3 * NP;
+  constexpr int AB = wu_a_bytes<KP>(), SB = wu_stage_bytes<KP, NP>(), NS = wu_stages<KP, NP>();
+  constexpr int SEGS = 128 / NP, SL = CU_N / SEGS;  // bias sums: row segments per channel
+  constexpr unsigned TCOLS = wu_tmem_cols<KP, NP>();
+  // kind::f16, FP32 accumulator, BF16 A and B, both MN-major (bits 15, 16)
+  constexpr unsigned IDESC = umma_idesc_bf16(128, NT) | (1u << 15) | (1u << 16);
+  constexpr unsigned TX = (unsigned)(9 * KC + NC) * 1024u;  // copy bytes per row
+  static_assert(NP % 16 == 0 && NT <= 256 && KC <= 4 && NC <= 4, "shape");
+  static_assert(wgrad_umma_smem<KP, NP>() <= 232448, "shared memory");
+  extern __shared__ unsigned char wu_raw[];
+  unsigned char* const sm = wu_raw + ((1024u - (cu_smem_u32(wu_raw) & 1023u)) & 1023u);
+  unsigned long long* const bars = reinterpret_cast<unsigned long long*>(sm + NS * SB);
+  unsigned long long* const full = bars;            // [NS] copies landed (TMA bytes)
+  unsigned long long* const rot = bars + NS;        // [NS] rotated copies written (4 helper warps)
+  unsigned long long* const empty = bars + 2 * NS;  // [NS] products done with the stage (commit)
+  unsigned long long* const done = bars + 3 * NS;   // every product done (commit)
+  unsigned* const s_tmem = reinterpret_cast<unsigned*>(bars + 3 * NS + 1);
+  volatile int* const s_abort = reinterpret_cast<volatile int*>(s_tmem + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long nrows = (long long)batch * n * n;
+  const int nb = blockIdx.x < nrows ? (int)((nrows - 1 - blockIdx.x) / gridDim.x) + 1 : 0;
+  auto fault = [&]() {
+    atomicExch(&g_learned_fault, 1);
+    *s_abort = 1;
+  };
+  const bool drill = g_learned_drill != 0;
+  const int polls = drill ? CU_DRILL_POLLS : CU_POLLS;
+  double bsum = 0.0;  // helper threads: bias sum of their channel and row segment
+  if (tid == 0) {
+    for (int k = 0; k < 3 * NS + 1; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(cu_smem_u32(&bars[k])),
+                   "r"(k >= NS && k < 2 * NS ? 4 : 1)
+                   : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    *s_abort = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(cu_smem_u32(s_tmem)),
+                 "r"(TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = *s_tmem;
+
+  if (warp == 1) {
+    // ---- copies ----
+    int i = 0;
+    for (; i < nb && !drill; ++i) {
+      const int buf = i % NS;
+      if (i >= NS && !__all_sync(0xffffffffu, cu_wait(&empty[buf], (unsigned)((i / NS - 1) & 1), polls))) {
+        if (lane == 0) fault();
+        break;
+      }
+      if (*s_abort) break;
+      const long long row = blockIdx.x + (long long)i * gridDim.x;
+      const int smp = (int)(row / (n * n)), r = (int)(row - (long long)smp * n * n), z = r / n, y = r - z * n;
+      unsigned char* const A = sm + buf * SB;
+      unsigned char* const B = A + AB;
+      if (lane == 0) cu_expect_tx(&full[buf], TX);
+      __syncwarp();
+      for (int j = lane; j < 9 * KC + NC; j += 32) {
+        if (j < 9 * KC) {
+          // input row s = (dz + 1) 3 + (dy + 1), chunk c
+          const int sh = j / KC, c = j - sh * KC;
+          int yy = y + sh % 3 - 1, zz = z + sh / 3 - 1;
+          yy = yy < 0 ? yy + n : (yy >= n ? yy - n : yy);
+          zz = zz < 0 ? zz + n : (zz >= n ? zz - n : zz);
+          cu_tma_3d(A + j * 1024, &maps.a[c], 0, 0, (smp * n + zz) * n + yy, &full[buf]);
+        } else {
+          const int c = j - 9 * KC;  // the unrotated copy (dx = 0) of g
+          cu_tma_3d(B + (NC + c) * 1024, &maps.b[c], 0, 0, (int)row, &full[buf]);
+        }
+      }
+    }
+    // copies in flight: the last NS issued stages land (bounded)
+    for (int j = i - NS; j < i; ++j)
+      if (j >= 0 && !__all_sync(0xffffffffu, cu_wait(&full[j % NS], (unsigned)((j / NS) & 1), polls)) && lane == 0)
+        fault();
+  } else if (warp == 0) {
+    // ---- products ----
+    if (lane == 0) {
+      int i = 0;
+      for (; i < nb; ++i) {
+        const int buf = i % NS;
+        if (!cu_wait(&rot[buf], (unsigned)((i / NS) & 1), polls)) {
+          fault();
+          break;
+        }
+        if (*s_abort) break;
+        tc_fence_after();
+        // MN-major, no swizzle: 8-channel chunks 1 KB apart (stride byte
+        // offset), 8-voxel groups 128 bytes apart (leading byte offset)
+        const unsigned a0 = cu_smem_u32(sm + buf * SB), b0 = a0 + AB;
+#pragma unroll
+        for (int gr = 0; gr < NG; ++gr)
+#pragma unroll
+          for (int kk = 0; kk < CU_N / 16; ++kk)
+            umma_bf16(tmem + (unsigned)(gr * NT), umma_sdesc(a0 + gr * SPG * KC * 1024 + kk * 256, 128, 1024),
+                      umma_sdesc(b0 + kk * 256, 128, 1024), IDESC, (i | kk) != 0);
+        umma_commit(&empty[buf]);
+      }
+      if (i > 0) {
+        umma_commit(done);
+        if (!cu_wait(done, 0u, polls)) fault();
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---- rotations of g: dx = -1 (copy 0, g[x + 1]) and dx = +1 (copy 2, g[x - 1]) ----
+    const int ht = tid - 64;
+    const int bco = ht % NP, bseg = ht / NP;
+    for (int i = 0; i < nb; ++i) {
+      const int buf = i % NS;
+      if (!__all_sync(0xffffffffu, cu_wait(&full[buf], (unsigned)((i / NS) & 1), polls))) {
+        if (lane == 0) fault();
+        break;
+      }
+      if (*s_abort) break;
+      unsigned char* const B = sm + buf * SB + AB;
+      const uint4* const src = reinterpret_cast<const uint4*>(B + NC * 1024);
+      {
+        // bias gradient: channel bco over the row segment bseg
+        const __nv_bfloat16* const gb = reinterpret_cast<const __nv_bfloat16*>(src) + (bco / 8) * CU_N * 8 + bco % 8;
+        float fs = 0.f;
+#pragma unroll 4
+        for (int x = bseg * SL; x < (bseg + 1) * SL; ++x) fs += __bfloat162float(gb[x * 8]);
+        bsum += (double)fs;
+      }
+      for (int p = ht; p < 2 * NC * CU_N; p += 128) {
+        const int h = p / (NC * CU_N), rem = p - h * (NC * CU_N), c = rem / CU_N, x = rem % CU_N;
+        const int xs = h == 0 ? (x + 1) % CU_N : (x + CU_N - 1) % CU_N;
+        reinterpret_cast<uint4*>(B + ((2 * h) * NC + c) * 1024)[x] = src[c * CU_N + xs];
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // generic writes -> tensor-core reads
+      __syncwarp();
+      if (lane == 0) cu_arrive(&rot[buf]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  // ---- bias partial of this CTA: the segments of each channel in order (the
+  // first stage's A buffer is free: no copy or product is in flight) ----
+  double* const red = reinterpret_cast<double*>(sm);
+  if (warp >= 2) red[(tid - 64) / NP * NP + (tid - 64) % NP] = bsum;
+  __syncthreads();
+  if (warp >= 2 && tid - 64 < NP && !*s_abort) {
+    double b = 0.0;
+    for (int sg = 0; sg < SEGS; ++sg) b += red[sg * NP + tid - 64];
+    bpart[(long long)blockIdx.x * NP + tid - 64] = b;
+  }
+  // ---- partial of this CTA: accumulator row m = (s, ci), column (dx, co) ----
+  if (warp >= 2 && !*s_abort && nb > 0) {
+    const int q = warp & 3, m = 32 * q + lane;
+#pragma unroll 1
+    for (int gr = 0; gr < NG; ++gr) {
+      const int sh = gr * SPG + m / KP, ci = m % KP;
+#pragma unroll 1
+      for (int c0 = 0; c0 < NT; c0 += 16) {
+        unsigned r[16];
+        tmem_ld_nowait<16>(tmem + ((unsigned)(32 * q) << 16) + (unsigned)(gr * NT + c0), r);
+        tmem_wait_ld();
+        if (sh < 9) {
+          const int t = c0 / NP, co0 = c0 - t * NP;
+          float* const o = part + ((long long)blockIdx.x * NET_TAPS + sh * 3 + t) * (KP * NP) + ci * NP + co0;
+#pragma unroll
+          for (int j = 0; j < 16; j += 4)
+            *reinterpret_cast<float4*>(o + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
+                                                            __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]));
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
+  }
+}
+
+// Row maps of a [batch][64^3][ch] BF16 tensor per 8-channel chunk (boxes of 8
+// channels x 64 voxels); false when they cannot be made.
+static bool wgrad_row_maps(const __nv_bfloat16* t, int ch, int batch, CUtensorMap* m) {
+  if ((reinterpret_cast<uintptr_t>(t) & 15) != 0) return false;
+  const cuuint64_t dims[3] = {8, (cuuint64_t)CU_N, (cuuint64_t)batch * CU_N * CU_N};
+  const cuuint64_t strides[2] = {(cuuint64_t)ch * 2, (cuuint64_t)CU_N * ch * 2};
+  const cuuint32_t box[3] = {8, (cuuint32_t)CU_N, 1};
+  for (int c = 0; c < ch / 8; ++c)
+    if (!encode_tiled_map(&m[c], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, t + c * 8, dims, strides, box)) return false;
+  return true;
+}
+
 // fold partials over chunks; bias gradient from the g sums of tap 13 (centre)
 template <int KP, int NP>
 __global__ void wgrad_fold_kernel(int nchunk, const float* __restrict__ part, float* __restrict__ dW) {
@@ -1303,7 +1593,10 @@ struct exc_net {
   long long vcap = 0;  // voxel capacity of the workspace
   int ws_gen = 0;       // bumped whenever the workspace moves (captured graphs must re-capture)
   __nv_bfloat16 *x0 = nullptr, *a1 = nullptr, *a2 = nullptr, *g3 = nullptr, *gp2 = nullptr, *gp1 = nullptr;
-  float *pre1 = nullptr, *pre2 = nullptr, *out = nullptr, *wpart = nullptr;
+  // GELU'(pre-activation) of the hidden layers (BF16), written by a training
+  // forward pass for the backward pass
+  __nv_bfloat16 *dg1 = nullptr, *dg2 = nullptr;
+  float *out = nullptr, *wpart = nullptr;
   double* lpart = nullptr;  // loss partials + result
   float* W(int l) { return params + (l == 0 ? 0 : l == 1 ? W1 + N1 : W1 + N1 + W2 + N2); }
   float* B(int l) { return W(l) + (l == 0 ? W1 : l == 1 ? W2 : W3); }
@@ -1316,12 +1609,13 @@ struct exc_net {
 namespace exc {
 
 static void free_workspace(exc_net* net) {
-  void* ps[] = {net->x0, net->a1, net->a2, net->g3, net->gp2, net->gp1, net->pre1, net->pre2, net->out, net->wpart,
+  void* ps[] = {net->x0, net->a1, net->a2, net->g3, net->gp2, net->gp1, net->dg1, net->dg2, net->out, net->wpart,
                 net->lpart};
   for (void* p : ps)
     if (p) cudaFree(p);
   net->x0 = net->a1 = net->a2 = net->g3 = net->gp2 = net->gp1 = nullptr;
-  net->pre1 = net->pre2 = net->out = net->wpart = nullptr;
+  net->dg1 = net->dg2 = nullptr;
+  net->out = net->wpart = nullptr;
   net->lpart = nullptr;
   net->vcap = 0;
 }
@@ -1337,8 +1631,8 @@ static int ensure_workspace(exc_net* net, long long V) {
             cudaMalloc(&net->g3, V * exc_net::N3 * 2) == cudaSuccess &&
             cudaMalloc(&net->gp2, V * exc_net::N2 * 2) == cudaSuccess &&
             cudaMalloc(&net->gp1, V * exc_net::N1 * 2) == cudaSuccess &&
-            cudaMalloc(&net->pre1, V * exc_net::N1 * 4) == cudaSuccess &&
-            cudaMalloc(&net->pre2, V * exc_net::N2 * 4) == cudaSuccess &&
+            cudaMalloc(&net->dg1, V * exc_net::N1 * 2) == cudaSuccess &&
+            cudaMalloc(&net->dg2, V * exc_net::N2 * 2) == cudaSuccess &&
             cudaMalloc(&net->out, V * exc_net::N3 * 4) == cudaSuccess &&
             cudaMalloc(&net->wpart, nchunk * 27 * 32 * 32 * 4 + (long long)WT_CTAS * 2 * 32 * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&net->lpart, (1024 + 8) * sizeof(double)) == cudaSuccess;
@@ -1365,10 +1659,13 @@ static cudaError_t refresh(exc_net* net, cudaStream_t st) {
 }
 
 
-// forward from the packed input x0; leaves pre1, a1, pre2, a2, out
-static cudaError_t forward_packed(exc_net* net, long long V, int n, cudaStream_t st) {
-  conv_launch<16, 32, 0>(net->conv_engine, V, n, net->x0, net->Wt(0), net->B(0), net->pre1, net->a1, nullptr, 32, st);
-  conv_launch<32, 32, 0>(net->conv_engine, V, n, net->a1, net->Wt(1), net->B(1), net->pre2, net->a2, nullptr, 32, st);
+// forward from the packed input x0; leaves a1, a2, out and, for training,
+// the GELU derivatives dg1, dg2
+static cudaError_t forward_packed(exc_net* net, long long V, int n, bool train, cudaStream_t st) {
+  conv_launch<16, 32, 0>(net->conv_engine, V, n, net->x0, net->Wt(0), net->B(0), nullptr, net->a1,
+                         train ? net->dg1 : nullptr, 32, st);
+  conv_launch<32, 32, 0>(net->conv_engine, V, n, net->a1, net->Wt(1), net->B(1), nullptr, net->a2,
+                         train ? net->dg2 : nullptr, 32, st);
   conv_launch<32, 16, 1>(net->conv_engine, V, n, net->a2, net->Wt(2), net->B(2), net->out, nullptr, nullptr, 3, st);
   return cudaGetLastError();
 }
@@ -1378,6 +1675,20 @@ static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfl
                          cudaStream_t st) {
   int nchunk;
   const long long N = (long long)n * n * n;
+  if (net->conv_engine == 0 && n == CU_N) {
+    const int batch = (int)(V / N);
+    WgMaps maps;
+    if (batch > 0 && wgrad_row_maps(in, KP, batch, maps.a) && wgrad_row_maps(g, NP, batch, maps.b)) {
+      nchunk = (int)std::min<long long>((long long)batch * n * n, 152);
+      // bias partials (one per CTA) after the weight partials
+      double* bpart = reinterpret_cast<double*>(net->wpart + (size_t)WT_CTAS * NET_TAPS * 32 * 32);
+      wgrad_umma_kernel<KP, NP><<<nchunk, WU_THREADS, wgrad_umma_smem<KP, NP>(), st>>>(batch, maps, net->wpart,
+                                                                                       bpart);
+      wgrad_fold_kernel<KP, NP><<<(4 * 27 * KP * NP + 255) / 256, 256, 0, st>>>(nchunk, net->wpart, net->dW(l));
+      bgrad_fold_kernel<NP><<<1, 32 * NP, 0, st>>>(nchunk, bpart, net->dB(l));
+      return cudaGetLastError();
+    }
+  }
   if (n % 8 == 0) {
     // all taps per CTA over 8 x 2 x 4 voxel blocks, one persistent CTA per
     // SM; the bias partials follow the weight partials in the buffer
@@ -1410,9 +1721,9 @@ static cudaError_t backward(exc_net* net, long long V, int n, long long N, const
   sum_kernel<<<1, 256, 0, st>>>(lb, net->lpart, 1.0 / (3.0 * (double)V), net->lpart + 1024);
   cudaError_t e = wgrad<32, 16>(net, 2, V, n, net->a2, net->g3, st);
   // input gradient of layer 3 times GELU'(pre2)
-  conv_launch<16, 32, 2>(net->conv_engine, V, n, net->g3, net->Wb(2), nullptr, nullptr, net->gp2, net->pre2, 32, st);
+  conv_launch<16, 32, 2>(net->conv_engine, V, n, net->g3, net->Wb(2), nullptr, nullptr, net->gp2, net->dg2, 32, st);
   if (e == cudaSuccess) e = wgrad<32, 32>(net, 1, V, n, net->a1, net->gp2, st);
-  conv_launch<32, 32, 2>(net->conv_engine, V, n, net->gp2, net->Wb(1), nullptr, nullptr, net->gp1, net->pre1, 32, st);
+  conv_launch<32, 32, 2>(net->conv_engine, V, n, net->gp2, net->Wb(1), nullptr, nullptr, net->gp1, net->dg1, 32, st);
   if (e == cudaSuccess) e = wgrad<16, 32>(net, 0, V, n, net->x0, net->gp1, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e;
@@ -1425,7 +1736,7 @@ static int net_forward_t(exc_net* net, int batch, int n, const T* u, T* m, cudaS
   if (rc) return rc;
   const int gb = (int)std::min<long long>((V + 255) / 256, 152LL * 32);
   pack_input_kernel<T><<<gb, 256, 0, st>>>(V, N, u, 1.0 / net->in_scale, net->x0, exc_net::K1);
-  cudaError_t e = forward_packed(net, V, n, st);
+  cudaError_t e = forward_packed(net, V, n, false, st);
   if (e == cudaSuccess) {
     unpack_output_kernel<T><<<gb, 256, 0, st>>>(V, N, net->out, net->out_scale, m);
     e = cudaGetLastError();
@@ -1441,7 +1752,7 @@ static int net_grad_t(exc_net* net, int batch, int n, const T* u, const T* m, cu
   if (rc) return rc;
   const int gb = (int)std::min<long long>((V + 255) / 256, 152LL * 32);
   pack_input_kernel<T><<<gb, 256, 0, st>>>(V, N, u, 1.0 / net->in_scale, net->x0, exc_net::K1);
-  cudaError_t e = forward_packed(net, V, n, st);
+  cudaError_t e = forward_packed(net, V, n, true, st);
   if (e == cudaSuccess) e = backward<T>(net, V, n, N, m, st);
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   return EXC_OK;
@@ -1479,6 +1790,11 @@ static cudaError_t conv_umma_attr() {
                               (int)conv_umma_smem<NP>());
 }
 template <int KP, int NP>
+static cudaError_t wgrad_umma_attr() {
+  return cudaFuncSetAttribute(wgrad_umma_kernel<KP, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)wgrad_umma_smem<KP, NP>());
+}
+template <int KP, int NP>
 static cudaError_t wgrad_tile_attr() {
   return cudaFuncSetAttribute(wgrad_tile_kernel<KP, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)wgrad_tile_smem<KP, NP>());
@@ -1504,6 +1820,9 @@ static int configure_learned() {
   if (e == cudaSuccess) e = conv_umma_attr<32, 0>();
   if (e == cudaSuccess) e = conv_umma_attr<16, 1>();
   if (e == cudaSuccess) e = conv_umma_attr<32, 2>();
+  if (e == cudaSuccess) e = wgrad_umma_attr<16, 32>();
+  if (e == cudaSuccess) e = wgrad_umma_attr<32, 32>();
+  if (e == cudaSuccess) e = wgrad_umma_attr<32, 16>();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   done[dev] = true;
   return EXC_OK;

@@ -42,9 +42,10 @@ def emulated(params, u, m, in_scale, out_scale):
     g3 = bf16(2.0 * diff / diff.size)
     _, dW3, db3 = onet.conv_backward(a2, Ws[2][0], g3)
     dx3, _, _ = onet.conv_backward(a2, Ws[2][0], g3)
-    gp2 = bf16(dx3 * onet.gelu_grad(pre2))
+    # the forward pass keeps GELU'(pre) in BF16 for the backward pass
+    gp2 = bf16(dx3 * bf16(onet.gelu_grad(pre2)))
     dx2, dW2, db2 = onet.conv_backward(a1, Ws[1][0], gp2)
-    gp1 = bf16(dx2 * onet.gelu_grad(pre1))
+    gp1 = bf16(dx2 * bf16(onet.gelu_grad(pre1)))
     _, dW1, db1 = onet.conv_backward(x0, Ws[0][0], gp1)
     return out, loss, [(dW1, db1), (dW2, db2), (dW3, db3)]
 

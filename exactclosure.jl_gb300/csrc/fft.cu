@@ -601,6 +601,7 @@ int poisson_init(exc_poisson* ps, int precision, int n, double l, void* work) {
     invlap_split_kernel<<<blocks, 256>>>(tot, ps->mix->invlap);
     if (cudaMalloc(&ps->mix_d, (size_t)n * n * n * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&ps->mix_q, (size_t)n * n * n * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&ps->mix_q2, (size_t)n * n * n * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&ps->mix_part, (size_t)fftmix_part_words(n) * sizeof(double)) != cudaSuccess) {
       set_last_error("out of device memory (mixed-precision poisson buffers)");
       poisson_free(ps);
@@ -632,9 +633,10 @@ void poisson_free(exc_poisson* ps) {
   }
   if (ps->mix_d) cudaFree(ps->mix_d);
   if (ps->mix_q) cudaFree(ps->mix_q);
+  if (ps->mix_q2) cudaFree(ps->mix_q2);
   if (ps->mix_part) cudaFree(ps->mix_part);
   ps->mix_d = ps->mix_part = nullptr;
-  ps->mix_q = nullptr;
+  ps->mix_q = ps->mix_q2 = nullptr;
   if (ps->tw) cudaFree(ps->tw);
   if (ps->sin2) cudaFree(ps->sin2);
   if (ps->invlap) cudaFree(ps->invlap);

@@ -7,9 +7,9 @@
 // of fftreg.cuh, bound by HBM) and recovers FP64 accuracy by refinement with
 // residuals formed in FP64:
 //
-//   q1 = S32(d),       p  = q1,   r1 = d  - L_h q1
-//   q2 = S32(r1),      p += q2,   r2 = r1 - L_h q2
-//   q3 = S32(r2),      p += q3
+//   q1 = S32(d),       r1 = d  - L_h q1
+//   q2 = S32(r1),      r2 = r1 - L_h q2
+//   q3 = S32(r2),      p  = (q1 + q2) + q3
 //
 // where S32 is the FP32 spectral solve (relative error about 1e-7) and L_h
 // the 7-point staggered Laplacian, (sum of the 6 neighbours - 6 p) / h^2,
@@ -17,7 +17,8 @@
 // correction shrinks the error by about the FP32 solve's relative error, so
 // after two corrections p agrees with the FP64 FFT solve to FP64 rounding
 // (about 1e-15 relative for smooth and for white-noise right-hand sides).
-// The corrections q_k are FP32 fields, so the stencil sums of L_h q_k are
+// The corrections q1, q2 are kept as FP32 fields and p is written once, by
+// the last pass; the stencil sums of L_h q_k are
 // formed from FP32 values by error-free extraction (stencil7_f32) on the
 // FP32 pipe and rounded once to FP64, more accurate than the six FP64
 // additions they replace; each residual then costs three FP64 operations
@@ -39,7 +40,7 @@
 namespace exc {
 
 enum { MIX_DIV = 0, MIX_SCAL = 1, MIX_RES = 2, MIX_RES_MEAN = 3 };
-enum { MIX_SET = 0, MIX_ADD = 1, MIX_ADD_MEAN = 2 };
+enum { MIX_Q = 0, MIX_FIN = 1, MIX_FIN_MEAN = 2 };
 
 // Conversions between the FP64 fields and the FP32 transforms on the integer
 // pipe (the FP64 pipe, about two operations per clock per SM on GB300, is the
@@ -136,14 +137,14 @@ __device__ __forceinline__ C to_f32c(double a, double b) {
 //             previous residual r'_prev in d (the divergence at first) and
 //             the last FP32 correction q (n^3 floats), transformed; stored
 //             back to d when `store` is set;
-//   MIX_RES_MEAN: as MIX_RES, and the CTA's sum of p (FP64 real view of the
-//             FP64 work array, row pitch 2P) goes to part[blockIdx.x].
+//   MIX_RES_MEAN: as MIX_RES, and the CTA's sum of the pressure so far,
+//             q1 + q2 (qp = q1, q = q2), goes to part[blockIdx.x].
 template <int N1, int N2, int MODE>
 __global__ void __launch_bounds__(XGeom<float, N1, N2>::NT)
 mr2c_kernel(const double* __restrict__ src, double h, double* __restrict__ d, const double* __restrict__ p, int P,
             double inv_h, cplx<float>* __restrict__ out, const cplx<float>* __restrict__ tw,
             const cplx<float>* __restrict__ tl, double* __restrict__ part, const float* __restrict__ q,
-            int store) {
+            const float* __restrict__ qp, int store) {
   using C = cplx<float>;
   using G = XGeom<float, N1, N2>;
   constexpr int L = N1 * N2, n = 2 * L, RW = G::RW, XS = G::XS;
@@ -203,7 +204,7 @@ mr2c_kernel(const double* __restrict__ src, double h, double* __restrict__ d, co
         const float2* qzm = reinterpret_cast<const float2*>(q + ((long long)wrap_dn(z, n) * n + y) * n);
         const float2* qzp = reinterpret_cast<const float2*>(q + ((long long)wrap_up(z, n) * n + y) * n);
         double2* d2 = reinterpret_cast<double2*>(d + base);
-        const double2* pc2 = reinterpret_cast<const double2*>(p + row * 2LL * P);
+        const float2* const qp2 = reinterpret_cast<const float2*>(qp + base);
 #pragma unroll
         for (int m1 = 0; m1 < N1; ++m1) {
           const int m = m2 + N2 * m1;
@@ -217,8 +218,8 @@ mr2c_kernel(const double* __restrict__ src, double h, double* __restrict__ d, co
           rv.y = fma(-inv_h, stencil7_f32(qc.x, qxp, a.y, b.y, c.y, e.y, qc.y), rv.y);
           if (store) d2[m] = rv;
           if constexpr (MODE == MIX_RES_MEAN) {
-            const double2 pc = pc2[m];
-            psum += pc.x + pc.y;
+            const float2 pa = qp2[m];
+            psum += (f32_to_f64(pa.x) + f32_to_f64(qc.x)) + (f32_to_f64(pa.y) + f32_to_f64(qc.y));
           }
           v[m1] = to_f32c<C>(rv.x, rv.y);
         }
@@ -290,14 +291,18 @@ mr2c_kernel(const double* __restrict__ src, double h, double* __restrict__ d, co
   }
 }
 
-// x pass, FP32 half spectrum -> reals c (the rc2r_kernel transform), written
-// to the FP64 pressure p (row pitch 2P): MIX_SET p = c; MIX_ADD p += c;
-// MIX_ADD_MEAN p += c - mean; and c itself to q (n^3 floats) unless q is null.
+// x pass, FP32 half spectrum -> reals c (the rc2r_kernel transform):
+//   MIX_Q:        c to q (n^3 floats; a correction kept for the residual and
+//                 the final sum);
+//   MIX_FIN:      the FP64 pressure p (row pitch 2P) = (q1 + q2) + c;
+//   MIX_FIN_MEAN: p = ((q1 + q2) - mean) + c.
+// Summed in this order, p has the bits of accumulating each correction into
+// an FP64 p as it arrives, without the FP64 field's reads and writes between.
 template <int N1, int N2, int MODE>
 __global__ void __launch_bounds__(XGeom<float, N1, N2>::NT)
 mc2r_kernel(const cplx<float>* __restrict__ g, int P, const cplx<float>* __restrict__ tw,
             const cplx<float>* __restrict__ tl, double* __restrict__ p, const double* __restrict__ mean,
-            float* __restrict__ q) {
+            float* __restrict__ q, const float* __restrict__ q1, const float* __restrict__ q2) {
   using C = cplx<float>;
   using G = XGeom<float, N1, N2>;
   constexpr int L = N1 * N2, n = 2 * L, RW = G::RW, XS = G::XS;
@@ -339,30 +344,32 @@ mc2r_kernel(const cplx<float>* __restrict__ g, int P, const cplx<float>* __restr
 #pragma unroll
     for (int q = 0; q < N2; ++q) zz[q] = xs[lb * XS + k1 * (N2 + 1) + q];
     dft_reg<N2, true>(zz);
-    double2* r = reinterpret_cast<double2*>(p + row * 2LL * P);
-    float2* qo = q ? reinterpret_cast<float2*>(q + row * n) : nullptr;
-    double mu = 0.0;
-    if constexpr (MODE == MIX_ADD_MEAN) mu = *mean;
+    if constexpr (MODE == MIX_Q) {
+      float2* const qo = reinterpret_cast<float2*>(q + row * n);
 #pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2) {
-      const int m = k1 + N1 * k2;
-      double2 o;
-      const double cx = f32_to_f64(zz[k2].x), cy = f32_to_f64(zz[k2].y);
-      if (qo) qo[m] = make_float2(f32_flush(zz[k2].x), f32_flush(zz[k2].y));
-      if constexpr (MODE == MIX_SET) {
-        o.x = cx;
-        o.y = cy;
-      } else {
-        const double2 a = r[m];
-        if constexpr (MODE == MIX_ADD) {
-          o.x = a.x + cx;
-          o.y = a.y + cy;
+      for (int k2 = 0; k2 < N2; ++k2)
+        qo[k1 + N1 * k2] = make_float2(f32_flush(zz[k2].x), f32_flush(zz[k2].y));
+    } else {
+      double2* const r = reinterpret_cast<double2*>(p + row * 2LL * P);
+      const float2* const a1 = reinterpret_cast<const float2*>(q1 + row * n);
+      const float2* const a2 = reinterpret_cast<const float2*>(q2 + row * n);
+      double mu = 0.0;
+      if constexpr (MODE == MIX_FIN_MEAN) mu = *mean;
+#pragma unroll
+      for (int k2 = 0; k2 < N2; ++k2) {
+        const int m = k1 + N1 * k2;
+        const float2 b1 = a1[m], b2 = a2[m];
+        const double sx = f32_to_f64(b1.x) + f32_to_f64(b2.x), sy = f32_to_f64(b1.y) + f32_to_f64(b2.y);
+        double2 o;
+        if constexpr (MODE == MIX_FIN) {
+          o.x = sx + f32_to_f64(zz[k2].x);
+          o.y = sy + f32_to_f64(zz[k2].y);
         } else {
-          o.x = (a.x - mu) + cx;
-          o.y = (a.y - mu) + cy;
+          o.x = (sx - mu) + f32_to_f64(zz[k2].x);
+          o.y = (sy - mu) + f32_to_f64(zz[k2].y);
         }
+        r[m] = o;
       }
-      r[m] = o;
     }
   }
 }
@@ -418,9 +425,9 @@ struct MixSolve {
     set((const void*)mr2c_kernel<B1, B2, MIX_SCAL>, XG::SMEM);
     set((const void*)mr2c_kernel<B1, B2, MIX_RES>, XG::SMEM);
     set((const void*)mr2c_kernel<B1, B2, MIX_RES_MEAN>, XG::SMEM);
-    set((const void*)mc2r_kernel<B1, B2, MIX_SET>, XG::SMEM);
-    set((const void*)mc2r_kernel<B1, B2, MIX_ADD>, XG::SMEM);
-    set((const void*)mc2r_kernel<B1, B2, MIX_ADD_MEAN>, XG::SMEM);
+    set((const void*)mc2r_kernel<B1, B2, MIX_Q>, XG::SMEM);
+    set((const void*)mc2r_kernel<B1, B2, MIX_FIN>, XG::SMEM);
+    set((const void*)mc2r_kernel<B1, B2, MIX_FIN_MEAN>, XG::SMEM);
     return e;
   }
 
@@ -441,30 +448,33 @@ struct MixSolve {
     const unsigned gx = (unsigned)NPARTS;
     const SlotBatch one;
     auto columns = [&]() { RS::columns(g, nkx, P, tln, sp->invlap, st, one, 1); };
-    float* q = ps->mix_q;
+    float* const q1 = ps->mix_q;
+    float* const q2 = ps->mix_q2;
     if (vec) {
-      mr2c_kernel<B1, B2, MIX_DIV><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q, 0);
+      mr2c_kernel<B1, B2, MIX_DIV><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q1, q1, 0);
     } else {
       // mean of d into part[0] (partials in part[1 .. SUM_CTAS])
       mix_sum_kernel<<<SUM_CTAS, 256, 0, st>>>(src, (long long)n * n * n, part + 1);
       mix_mean_kernel<<<1, 256, 0, st>>>(part + 1, SUM_CTAS, 1.0 / ((double)n * n * n), part);
-      mr2c_kernel<B1, B2, MIX_SCAL><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q, 0);
+      mr2c_kernel<B1, B2, MIX_SCAL><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q1, q1,
+                                                                  0);
     }
     columns();
-    mc2r_kernel<B1, B2, MIX_SET><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, q);
-    mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q, 1);
+    mc2r_kernel<B1, B2, MIX_Q><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, q1, nullptr, nullptr);
+    mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q1, q1, 1);
     columns();
-    mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, q);
+    mc2r_kernel<B1, B2, MIX_Q><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, q2, nullptr, nullptr);
     if (ps->mix_zero_mean) {
-      mr2c_kernel<B1, B2, MIX_RES_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q,
-                                                                      0);
+      mr2c_kernel<B1, B2, MIX_RES_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q2,
+                                                                      q1, 0);
       mix_mean_kernel<<<1, 256, 0, st>>>(part, (int)NPARTS, 1.0 / ((double)n * n * n), mean);
       columns();
-      mc2r_kernel<B1, B2, MIX_ADD_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, nullptr);
+      mc2r_kernel<B1, B2, MIX_FIN_MEAN><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, nullptr, q1, q2);
     } else {
-      mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q, 0);
+      mr2c_kernel<B1, B2, MIX_RES><<<gx, XG::NT, XG::SMEM, st>>>(src, h, d, p, P, inv_h, g, tw, tlh, part, q2, q1,
+                                                                 0);
       columns();
-      mc2r_kernel<B1, B2, MIX_ADD><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, nullptr);
+      mc2r_kernel<B1, B2, MIX_FIN><<<gx, XG::NT, XG::SMEM, st>>>(g, P, tw, tlh, p, mean, nullptr, q1, q2);
     }
     return cudaGetLastError();
   }

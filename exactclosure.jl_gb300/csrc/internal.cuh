@@ -30,11 +30,13 @@ struct exc_poisson {
   int engine = 0;
   // mixed-precision FP64 solve (fftmix.cuh): the FP32 inner solver (its own
   // work array and tables, 1/(lambda N h) divide table), the FP64 divergence
-  // (n^3, unscaled by 1/h; the first residual replaces it), the last FP32
-  // correction (n^3 floats) and per-CTA partial sums of p with the mean last
+  // (n^3, unscaled by 1/h; the first residual replaces it), the first two
+  // FP32 corrections (n^3 floats each) and per-CTA partial sums of p with
+  // the mean last
   exc_poisson* mix = nullptr;
   double* mix_d = nullptr;
   float* mix_q = nullptr;
+  float* mix_q2 = nullptr;
   double* mix_part = nullptr;
   // remove the pressure's mean (its free constant) in the mixed solve; false
   // where p is only used through its gradient

@@ -333,30 +333,33 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
       LesState<T>& L = ci->les[li];
       const int m = L.m;
       const T H = (T)(cs->desc.l / m);
-      // m_s = P_H(filter(k_s) - RHS_H(ubar_s))
+      // m_s = P_H(filter(k_s) - RHS_H(ubar_s)); mcl keeps the unprojected
+      // difference (the projection is linear: the exact LES projects it
+      // together with its own RHS, one solve instead of two)
       e = box_oa<T>(n, L.c, L.kind, fused ? les_tb_from_root(ci, L, root_k) : les_tb(ci, L), L.mcl, st);
       if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
       int rc;
       e = launch_rhs<T>(m, H, visc, L.ub, L.rtmp, false, st);
       if (e == cudaSuccess) e = launch_axpy<T>(3 * L.M, L.mcl, L.rtmp, (T)-1, st);
       if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-      rc = project_vec<T>(&L.ps, L.mcl, st);
-      if (rc) return rc;
       if (s == 0) {
+        // the closure of stage 0 (snapshot pairs, diagnostics): m_0 itself
         e = cudaMemcpyAsync(L.mlast, L.mcl, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess)
           e = cudaMemcpyAsync(L.ublast, L.ub, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+        rc = project_vec<T>(&L.ps, L.mlast, st);
+        if (rc) return rc;
       }
-      // exact-closure LES
+      // exact-closure LES: k = P_H(RHS_H(v_s) + filter(k_s) - RHS_H(ubar_s))
       T* ve0 = L.ve[cur];
       T* vefin = L.ve[cur ^ 1];
       e = launch_rhs<T>(m, H, visc, s == 0 ? ve0 : L.ves, L.ke, false, st);
+      if (e == cudaSuccess) e = launch_axpy<T>(3 * L.M, L.ke, L.mcl, (T)1, st);
       if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
       rc = project_vec<T>(&L.ps, L.ke, st);
       if (rc) return rc;
-      e = launch_axpy<T>(3 * L.M, L.ke, L.mcl, (T)1, st);
-      if (e == cudaSuccess) e = launch_rk_stage<T>(m, H, L.ke, nullptr, 0, ve0, L.ves, vefin, s, dt, st);
+      e = launch_rk_stage<T>(m, H, L.ke, nullptr, 0, ve0, L.ves, vefin, s, dt, st);
       // no-model LES
       T* vn0 = L.vn[cur];
       T* vnfin = L.vn[cur ^ 1];

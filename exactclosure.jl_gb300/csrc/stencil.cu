@@ -1,5 +1,7 @@
 // Staggered-grid stencils: the convection-diffusion RHS, divergence,
 // pressure gradient and explicit tensor divergences (src/N.jl:94-254).
+#include <type_traits>
+
 #include "internal.cuh"
 
 namespace exc {
@@ -107,6 +109,43 @@ __global__ void gradient_kernel(int n, T inv_h, T* __restrict__ u, const T* __re
   }
 }
 
+// The same update for even n, two cells of a row per thread (vector loads
+// and stores, one 32-bit division per thread): the expressions of
+// gradient_kernel, so the results are bit-identical.
+template <typename T>
+__global__ void gradient2_kernel(int n, T inv_h, T* __restrict__ u, const T* __restrict__ p, int ppitch) {
+  using V2 = typename std::conditional<sizeof(T) == 8, double2, float2>::type;
+  const long long N = (long long)n * n * n;
+  const int hx = n >> 1;
+  const long long total = N >> 1;
+  // total < 2^31 (launch condition): 32-bit index arithmetic
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const unsigned r32 = (unsigned)t / (unsigned)hx;
+    const long long row = r32;
+    const int x = 2 * (int)((unsigned)t - r32 * (unsigned)hx);
+    const int z = (int)(r32 / (unsigned)n), y = (int)(r32 - (unsigned)z * (unsigned)n);
+    const T* const pr = p + row * ppitch;
+    const V2 pc = *reinterpret_cast<const V2*>(pr + x);
+    const T pn = pr[x + 2 == n ? 0 : x + 2];
+    const V2 py = *reinterpret_cast<const V2*>(p + ((long long)z * n + wrap_up(y, n)) * ppitch + x);
+    const V2 pz = *reinterpret_cast<const V2*>(p + ((long long)wrap_up(z, n) * n + y) * ppitch + x);
+    const long long g = row * n + x;
+    V2* const u0 = reinterpret_cast<V2*>(u + g);
+    V2* const u1 = reinterpret_cast<V2*>(u + N + g);
+    V2* const u2 = reinterpret_cast<V2*>(u + 2 * N + g);
+    V2 a = *u0, b = *u1, c = *u2;
+    a.x -= (pc.y - pc.x) * inv_h;
+    a.y -= (pn - pc.y) * inv_h;
+    b.x -= (py.x - pc.x) * inv_h;
+    b.y -= (py.y - pc.y) * inv_h;
+    c.x -= (pz.x - pc.x) * inv_h;
+    c.y -= (pz.y - pc.y) * inv_h;
+    *u0 = a;
+    *u1 = b;
+    *u2 = c;
+  }
+}
+
 static inline int grid_for(long long N, int threads) {
   long long b = (N + threads - 1) / threads;
   return (int)(b < 152LL * 32 ? b : 152LL * 32);
@@ -133,7 +172,12 @@ cudaError_t launch_divergence(int n, T h, const T* u, T* d, cudaStream_t st) {
 template <typename T>
 cudaError_t launch_gradient(int n, T h, T* u, const T* p, int ppitch, cudaStream_t st) {
   long long N = (long long)n * n * n;
-  gradient_kernel<T><<<grid_for(N, 256), 256, 0, st>>>(n, (T)(1.0 / (double)h), u, p, ppitch);
+  const bool vec = n % 2 == 0 && ppitch % 2 == 0 && N / 2 < (1LL << 31) && (reinterpret_cast<uintptr_t>(u) % (2 * sizeof(T))) == 0 &&
+                   (reinterpret_cast<uintptr_t>(p) % (2 * sizeof(T))) == 0;
+  if (vec)
+    gradient2_kernel<T><<<grid_for(N / 2, 256), 256, 0, st>>>(n, (T)(1.0 / (double)h), u, p, ppitch);
+  else
+    gradient_kernel<T><<<grid_for(N, 256), 256, 0, st>>>(n, (T)(1.0 / (double)h), u, p, ppitch);
   return cudaGetLastError();
 }
 

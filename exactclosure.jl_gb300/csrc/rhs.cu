@@ -2,7 +2,7 @@
 // src/N.jl:94-160), marching along z.
 //
 // A CTA of 32 x 8 threads owns a PTX x PTY column of cells (PTY = 8 NC, NC
-// consecutive rows per thread) and walks ptz planes (8 to 32).  Three plane buffers of u
+// consecutive rows per thread) and walks ptz planes (4 to 32).  Three plane buffers of u
 // with a one-cell x/y halo sit in shared memory: planes z and z+1 are read
 // while plane z+2 streams in with cp.async; each thread evaluates the six
 // stress components at its own cells (the edge stresses s13, s23 and the
@@ -798,15 +798,22 @@ template <typename T>
 cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st, const SlotBatch& sb,
                        int nslots) {
   constexpr int NC = CYT<T>;
-  // planes per CTA: 32, halved (down to 8) while the launch would give fewer
-  // than two waves of resident CTAs (`per_sm` per SM), so small grids and
-  // single solves still fill the GPU (each CTA re-reads three planes to start)
+  // planes per CTA (4 to 32): the fewest waves of resident CTAs (`per_sm`
+  // per SM) times the planes each CTA walks plus one for its start (three
+  // planes loaded, the previous plane's stresses), ties to more planes -- so
+  // small grids and single solves still fill the GPU without a nearly empty
+  // last wave.  The split changes no cell's arithmetic.
   auto zsplit = [&](long long columns, int per_sm, int& ptz, int& zblocks) {
-    ptz = 32;
-    zblocks = (n + ptz - 1) / ptz;
-    while (ptz > 8 && columns * zblocks * nslots < 2LL * per_sm * 152) {
-      ptz /= 2;
-      zblocks = (n + ptz - 1) / ptz;
+    const long long slots = (long long)per_sm * 152;
+    long long best = -1;
+    for (int c = 32; c >= 4; --c) {
+      const int zb = (n + c - 1) / c;
+      const long long waves = (columns * zb * nslots + slots - 1) / slots;
+      if (best < 0 || waves * (c + 1) < best) {
+        best = waves * (c + 1);
+        ptz = c;
+        zblocks = zb;
+      }
     }
     return columns * zblocks * nslots;
   };

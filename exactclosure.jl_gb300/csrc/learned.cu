@@ -1160,35 +1160,40 @@ wgrad_tile_kernel(int batch, int n, const __nv_bfloat16* __restrict__ in, const 
 // ---------------------------------------------------------------------------
 // Weight gradient on the tcgen05 tensor cores (64^3 grids, conv engine 0):
 //   dW[tap][ci][co] = sum_v in[v + tap][ci] g[v][co]
-// reduced one output row at a time (64 voxels along x at fixed y, z, sample).
-// For the row, the A operand holds the nine input rows (y + dy, z + dz) (TMA
-// boxes of 8 channels x 64 voxels, 1 KB each) and the B operand the row of g
-// rotated by -dx for dx = -1, 0, 1: the unrotated copy arrives by TMA, the two
-// rotations (periodic along x, which a TMA box cannot wrap) are copied in
-// shared memory by the helper warps.  Both operands are MN-major (channels
-// contiguous per voxel, as stored), and
-//   D[(s, ci)][(dx, co)] += sum_x in[x, input row s][ci] g[x - dx][co]
-// is the row's contribution to dW[tap (dx, dy_s, dz_s)].  M = 128 holds 128 /
-// KP row shifts s, so the nine shifts take ceil(9 KP / 128) products per
-// 16-voxel step (the last partly unused); N = 3 NP.  The CTA's whole dW stays
-// in tensor memory over its rows and is written once as the CTA's partial
+// reduced over blocks of WU_RB = 2 output rows (64 voxels along x, rows y0,
+// y0 + 1 at fixed z and sample).  For a block the A operand holds, for each
+// dz, the window of four input rows y0 - 1 .. y0 + 2 at z + dz (TMA boxes of
+// 8 channels x 64 voxels, 1 KB each; rows shared by the block's two output
+// rows, so 12 rows per two output rows cross L2 instead of 18), laid out
+// [dz][window row][channel chunk][x], and the B operand each output row of g
+// with its two copies rotated by -dx for dx = -1, +1 (periodic along x, which
+// a TMA box cannot wrap: the helper warps copy them in shared memory).  Both
+// operands are MN-major (channels contiguous per voxel, as stored): for
+// output row r the M = 128 rows of a product are (window rows r .. r + 3 of
+// 128 / (4 KP) consecutive dz, input channel) at a uniform 1 KB chunk stride,
+// and
+//   D[(dz, w, ci)][(dx, co)] += sum_x in[x, y0 - 1 + r + w, z + dz][ci] g[x - dx, y0 + r][co]
+// is the contribution to dW[tap (dx, dy = w - 1, dz)] (w = 3 lands on the
+// next window or buffer and is not used).  N = 3 NP.  The CTA's whole dW stays
+// in tensor memory over its blocks and is written once as the CTA's partial
 // (folded by wgrad_fold_kernel in a fixed order).  Roles: warp 0 issues the
 // products, warp 1 the copies, warps 2-5 rotate g, sum it for the bias
 // gradient (FP32 per row segment, FP64 over rows, one partial per CTA) and, at
 // the end, read the accumulators.  Three or four stages of buffers keep
-// copies of later rows in flight; every wait is bounded as in
+// copies of later blocks in flight; every wait is bounded as in
 // conv_umma_kernel (a wait that gives up records the fault, every role stops,
 // copies and products in flight are waited for, the tensor memory is freed).
 // ---------------------------------------------------------------------------
 constexpr int WU_THREADS = 192;
+constexpr int WU_RB = 2;  // output rows per block
 struct WgMaps {
   CUtensorMap a[4];  // input rows, per 8-channel chunk
   CUtensorMap b[4];  // g rows, per 8-channel chunk
 };
-template <int KP> __host__ __device__ constexpr int wu_spg() { return 128 / KP; }
-template <int KP> __host__ __device__ constexpr int wu_groups() { return (9 + 128 / KP - 1) / (128 / KP); }
-template <int KP> __host__ __device__ constexpr int wu_a_bytes() { return wu_groups<KP>() * wu_spg<KP>() * (KP / 8) * 1024; }
-template <int NP> __host__ __device__ constexpr int wu_b_bytes() { return 3 * (NP / 8) * 1024; }
+template <int KP> __host__ __device__ constexpr int wu_spg() { return 128 / KP; }  // window rows per product
+template <int KP> __host__ __device__ constexpr int wu_groups() { return (3 * 4 * KP + 127) / 128; }
+template <int KP> __host__ __device__ constexpr int wu_a_bytes() { return 3 * (WU_RB + 2) * (KP / 8) * 1024; }
+template <int NP> __host__ __device__ constexpr int wu_b_bytes() { return WU_RB * 3 * (NP / 8) * 1024; }
 template <int KP, int NP> __host__ __device__ constexpr int wu_stage_bytes() { return wu_a_bytes<KP>() + wu_b_bytes<NP>(); }
 // stages of buffers that fit in 216 KB (at most four)
 template <int KP, int NP> __host__ __device__ constexpr int wu_stages() {
@@ -1207,13 +1212,17 @@ wgrad_umma_kernel(int batch, const __grid_constant__ WgMaps maps, float* __restr
                   double* __restrict__ bpart) {
   constexpr int n = CU_N, KC = KP / 8, NC = NP / 8, SPG = wu_spg<KP>(), NG = wu_groups<KP>(), NT = 3 * NP;
   constexpr int AB = wu_a_bytes<KP>(), SB = wu_stage_bytes<KP, NP>(), NS = wu_stages<KP, NP>();
+  constexpr int WR = WU_RB + 2;                     // window rows per dz
+  constexpr int NA = 3 * WR * KC, NB = WU_RB * NC;  // copies per block
   constexpr int SEGS = 128 / NP, SL = CU_N / SEGS;  // bias sums: row segments per channel
   constexpr unsigned TCOLS = wu_tmem_cols<KP, NP>();
   // kind::f16, FP32 accumulator, BF16 A and B, both MN-major (bits 15, 16)
   constexpr unsigned IDESC = umma_idesc_bf16(128, NT) | (1u << 15) | (1u << 16);
-  constexpr unsigned TX = (unsigned)(9 * KC + NC) * 1024u;  // copy bytes per row
-  static_assert(NP % 16 == 0 && NT <= 256 && KC <= 4 && NC <= 4, "shape");
+  constexpr unsigned TX = (unsigned)(NA + NB) * 1024u;  // copy bytes per block
+  static_assert(NP % 16 == 0 && NT <= 256 && KC <= 4 && NC <= 4 && SPG % WR == 0, "shape");
   static_assert(wgrad_umma_smem<KP, NP>() <= 232448, "shared memory");
+  // the last product group reads 16 KB from its start: inside the stage
+  static_assert((NG - 1) * SPG * KC * 1024 + (WU_RB - 1) * KC * 1024 + 16 * 1024 <= SB, "operand span");
   extern __shared__ unsigned char wu_raw[];
   unsigned char* const sm = wu_raw + ((1024u - (cu_smem_u32(wu_raw) & 1023u)) & 1023u);
   unsigned long long* const bars = reinterpret_cast<unsigned long long*>(sm + NS * SB);
@@ -1224,8 +1233,8 @@ wgrad_umma_kernel(int batch, const __grid_constant__ WgMaps maps, float* __restr
   unsigned* const s_tmem = reinterpret_cast<unsigned*>(bars + 3 * NS + 1);
   volatile int* const s_abort = reinterpret_cast<volatile int*>(s_tmem + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long nrows = (long long)batch * n * n;
-  const int nb = blockIdx.x < nrows ? (int)((nrows - 1 - blockIdx.x) / gridDim.x) + 1 : 0;
+  const long long nblk = (long long)batch * n * (n / WU_RB);
+  const int nb = blockIdx.x < nblk ? (int)((nblk - 1 - blockIdx.x) / gridDim.x) + 1 : 0;
   auto fault = [&]() {
     atomicExch(&g_learned_fault, 1);
     *s_abort = 1;
@@ -1262,23 +1271,25 @@ wgrad_umma_kernel(int batch, const __grid_constant__ WgMaps maps, float* __restr
         break;
       }
       if (*s_abort) break;
-      const long long row = blockIdx.x + (long long)i * gridDim.x;
-      const int smp = (int)(row / (n * n)), r = (int)(row - (long long)smp * n * n), z = r / n, y = r - z * n;
+      const long long blk = blockIdx.x + (long long)i * gridDim.x;
+      const int smp = (int)(blk / (n * (n / WU_RB))), r = (int)(blk - (long long)smp * n * (n / WU_RB));
+      const int z = r / (n / WU_RB), y0 = WU_RB * (r - z * (n / WU_RB));
       unsigned char* const A = sm + buf * SB;
       unsigned char* const B = A + AB;
       if (lane == 0) cu_expect_tx(&full[buf], TX);
       __syncwarp();
-      for (int j = lane; j < 9 * KC + NC; j += 32) {
-        if (j < 9 * KC) {
-          // input row s = (dz + 1) 3 + (dy + 1), chunk c
-          const int sh = j / KC, c = j - sh * KC;
-          int yy = y + sh % 3 - 1, zz = z + sh / 3 - 1;
+      for (int j = lane; j < NA + NB; j += 32) {
+        if (j < NA) {
+          // window row w of dz (layout [dz][w][chunk])
+          const int dz = j / (WR * KC), w = (j / KC) % WR, c = j % KC;
+          int yy = y0 - 1 + w, zz = z + dz - 1;
           yy = yy < 0 ? yy + n : (yy >= n ? yy - n : yy);
           zz = zz < 0 ? zz + n : (zz >= n ? zz - n : zz);
           cu_tma_3d(A + j * 1024, &maps.a[c], 0, 0, (smp * n + zz) * n + yy, &full[buf]);
         } else {
-          const int c = j - 9 * KC;  // the unrotated copy (dx = 0) of g
-          cu_tma_3d(B + (NC + c) * 1024, &maps.b[c], 0, 0, (int)row, &full[buf]);
+          // the unrotated copy (dx = 0) of output row rr of g
+          const int rr = (j - NA) / NC, c = (j - NA) % NC;
+          cu_tma_3d(B + (rr * 3 * NC + NC + c) * 1024, &maps.b[c], 0, 0, (smp * n + z) * n + y0 + rr, &full[buf]);
         }
       }
     }
@@ -1302,11 +1313,14 @@ wgrad_umma_kernel(int batch, const __grid_constant__ WgMaps maps, float* __restr
         // offset), 8-voxel groups 128 bytes apart (leading byte offset)
         const unsigned a0 = cu_smem_u32(sm + buf * SB), b0 = a0 + AB;
 #pragma unroll
-        for (int gr = 0; gr < NG; ++gr)
+        for (int rr = 0; rr < WU_RB; ++rr)
 #pragma unroll
-          for (int kk = 0; kk < CU_N / 16; ++kk)
-            umma_bf16(tmem + (unsigned)(gr * NT), umma_sdesc(a0 + gr * SPG * KC * 1024 + kk * 256, 128, 1024),
-                      umma_sdesc(b0 + kk * 256, 128, 1024), IDESC, (i | kk) != 0);
+          for (int gr = 0; gr < NG; ++gr)
+#pragma unroll
+            for (int kk = 0; kk < CU_N / 16; ++kk)
+              umma_bf16(tmem + (unsigned)(gr * NT),
+                        umma_sdesc(a0 + gr * SPG * KC * 1024 + rr * KC * 1024 + kk * 256, 128, 1024),
+                        umma_sdesc(b0 + rr * 3 * NC * 1024 + kk * 256, 128, 1024), IDESC, (i | rr | kk) != 0);
         umma_commit(&empty[buf]);
       }
       if (i > 0) {
@@ -1327,19 +1341,24 @@ wgrad_umma_kernel(int batch, const __grid_constant__ WgMaps maps, float* __restr
       }
       if (*s_abort) break;
       unsigned char* const B = sm + buf * SB + AB;
-      const uint4* const src = reinterpret_cast<const uint4*>(B + NC * 1024);
-      {
-        // bias gradient: channel bco over the row segment bseg
-        const __nv_bfloat16* const gb = reinterpret_cast<const __nv_bfloat16*>(src) + (bco / 8) * CU_N * 8 + bco % 8;
-        float fs = 0.f;
+#pragma unroll
+      for (int rr = 0; rr < WU_RB; ++rr) {
+        unsigned char* const Br = B + rr * 3 * NC * 1024;
+        const uint4* const src = reinterpret_cast<const uint4*>(Br + NC * 1024);
+        {
+          // bias gradient: channel bco over the row segment bseg
+          const __nv_bfloat16* const gb =
+              reinterpret_cast<const __nv_bfloat16*>(src) + (bco / 8) * CU_N * 8 + bco % 8;
+          float fs = 0.f;
 #pragma unroll 4
-        for (int x = bseg * SL; x < (bseg + 1) * SL; ++x) fs += __bfloat162float(gb[x * 8]);
-        bsum += (double)fs;
-      }
-      for (int p = ht; p < 2 * NC * CU_N; p += 128) {
-        const int h = p / (NC * CU_N), rem = p - h * (NC * CU_N), c = rem / CU_N, x = rem % CU_N;
-        const int xs = h == 0 ? (x + 1) % CU_N : (x + CU_N - 1) % CU_N;
-        reinterpret_cast<uint4*>(B + ((2 * h) * NC + c) * 1024)[x] = src[c * CU_N + xs];
+          for (int x = bseg * SL; x < (bseg + 1) * SL; ++x) fs += __bfloat162float(gb[x * 8]);
+          bsum += (double)fs;
+        }
+        for (int p = ht; p < 2 * NC * CU_N; p += 128) {
+          const int h = p / (NC * CU_N), rem = p - h * (NC * CU_N), c = rem / CU_N, x = rem % CU_N;
+          const int xs = h == 0 ? (x + 1) % CU_N : (x + CU_N - 1) % CU_N;
+          reinterpret_cast<uint4*>(Br + ((2 * h) * NC + c) * 1024)[x] = src[c * CU_N + xs];
+        }
       }
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // generic writes -> tensor-core reads
       __syncwarp();
@@ -1359,20 +1378,22 @@ wgrad_umma_kernel(int batch, const __grid_constant__ WgMaps maps, float* __restr
     for (int sg = 0; sg < SEGS; ++sg) b += red[sg * NP + tid - 64];
     bpart[(long long)blockIdx.x * NP + tid - 64] = b;
   }
-  // ---- partial of this CTA: accumulator row m = (s, ci), column (dx, co) ----
+  // ---- partial of this CTA: accumulator row m = (dz, window row w, ci), column (dx, co) ----
   if (warp >= 2 && !*s_abort && nb > 0) {
     const int q = warp & 3, m = 32 * q + lane;
 #pragma unroll 1
     for (int gr = 0; gr < NG; ++gr) {
-      const int sh = gr * SPG + m / KP, ci = m % KP;
+      const int slot = m / KP, ci = m % KP;
+      const int dzp = gr * (SPG / WR) + slot / WR, w = slot % WR;  // dz + 1, dy + 1 = w
 #pragma unroll 1
       for (int c0 = 0; c0 < NT; c0 += 16) {
         unsigned r[16];
         tmem_ld_nowait<16>(tmem + ((unsigned)(32 * q) << 16) + (unsigned)(gr * NT + c0), r);
         tmem_wait_ld();
-        if (sh < 9) {
+        if (dzp < 3 && w < 3) {
           const int t = c0 / NP, co0 = c0 - t * NP;
-          float* const o = part + ((long long)blockIdx.x * NET_TAPS + sh * 3 + t) * (KP * NP) + ci * NP + co0;
+          float* const o =
+              part + ((long long)blockIdx.x * NET_TAPS + dzp * 9 + w * 3 + t) * (KP * NP) + ci * NP + co0;
 #pragma unroll
           for (int j = 0; j < 16; j += 4)
             *reinterpret_cast<float4*>(o + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
@@ -1679,7 +1700,7 @@ static cudaError_t wgrad(exc_net* net, int l, long long V, int n, const __nv_bfl
     const int batch = (int)(V / N);
     WgMaps maps;
     if (batch > 0 && wgrad_row_maps(in, KP, batch, maps.a) && wgrad_row_maps(g, NP, batch, maps.b)) {
-      nchunk = (int)std::min<long long>((long long)batch * n * n, 152);
+      nchunk = (int)std::min<long long>((long long)batch * n * (n / WU_RB), 152);
       // bias partials (one per CTA) after the weight partials
       double* bpart = reinterpret_cast<double*>(net->wpart + (size_t)WT_CTAS * NET_TAPS * 32 * 32);
       wgrad_umma_kernel<KP, NP><<<nchunk, WU_THREADS, wgrad_umma_smem<KP, NP>(), st>>>(batch, maps, net->wpart,

@@ -350,7 +350,16 @@ struct PipeGeom {
   static constexpr int RS1 = N2 * W + PADC;  // y pass exchange: row k1 of [m2][line]
   static constexpr int XSC = N1 * RS1;       // y pass exchange size, complex words
   static constexpr size_t SMEM_COLS = ((size_t)XSC + (size_t)W * L) * 2 * sizeof(T);
-  static constexpr size_t SMEM_Z = 2 * (size_t)W * L * 2 * sizeof(T) + (size_t)W * L * 8;
+  // z pass exchange rows: level B reads rows k1 (stride RZ1), the last level
+  // reads rows j1 (stride RZ2); PZ1, PZ2 pad them (complex words).  Unpadded,
+  // a warp's four row groups share banks (4-way conflicts), yet 64-byte pads
+  // measured slower at 512^3 FP32 (step 16.98 ms unpadded; 17.04, 17.18 and
+  // 17.17 ms padding the first, the second and both): the pass is bound by
+  // its instruction stream, not by these conflicts.
+  static constexpr int PZ1 = 0, PZ2 = 0;
+  static constexpr int RZ1 = N2 * W + PZ1, RZ2 = N1 * W + PZ2;
+  static constexpr int XZ = (N1 * RZ1 > N2 * RZ2 ? N1 * RZ1 : N2 * RZ2);  // exchange size, complex words
+  static constexpr size_t SMEM_Z = ((size_t)XZ + (size_t)W * L) * 2 * sizeof(T) + (size_t)W * L * 8;
   static constexpr bool OK = sizeof(T) == 4 && CG::TABS && SMEM_Z <= 110 * 1024;
 };
 
@@ -433,11 +442,11 @@ rzsolve_pipe_kernel(cplx<T>* __restrict__ g, int n, int nkx, int ntx, int ntiles
   using C = cplx<T>;
   using G = ColGeom<T, N1, N2>;
   using Gp = PipeGeom<T, N1, N2>;
-  constexpr int W = G::W, L = N1 * N2, RS1 = N2 * W, RS2 = N1 * W;
+  constexpr int W = G::W, L = N1 * N2, RS1 = Gp::RZ1, RS2 = Gp::RZ2;
   static_assert(G::TABS, "the pipelined z pass stages the divide table");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* xs = reinterpret_cast<C*>(smem_raw);
-  C* stg = xs + W * L;
+  C* stg = xs + Gp::XZ;
   double* tab = reinterpret_cast<double*>(stg + W * L);  // [kz][line]
   if (sb.active && !sb.active[blockIdx.z]) return;
   g += blockIdx.z * sb.wstride;

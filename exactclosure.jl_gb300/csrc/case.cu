@@ -40,6 +40,9 @@ struct LesState {
   // FP64 stepper: sums of the step's initial state; the stage states u0 + cs
   // k_(s-1) take theirs by linearity from these and the sums of k_(s-1)
   T* tbu0 = nullptr;
+  // overlapped FP64 stepper: the stage-state sums (targets of the next stage),
+  // apart from tb, which holds k's sums while the LES streams read them
+  T* tbs = nullptr;
   T *ub, *fk, *mcl, *mlast, *rtmp;
   T *ve[2], *ves, *ke;  // exact LES: state (ping-pong), stage, k
   T *vn[2], *vns, *kn;  // no-model LES
@@ -71,6 +74,11 @@ template <typename T>
 struct CaseImpl {
   int fuse_root = -1;  // LES whose ratio the fused RK stage sums (-1: separate passes)
   bool tb_lin = false;  // stage-state sums by linearity (LesState::tbu0)
+  // LES work on a stream of its own (FP64 with linear sums): the LES of stage
+  // s runs beside the DNS of stage s + 1 (events order the shared sums)
+  bool overlap = false;
+  cudaStream_t lst = nullptr;  // the LES stream
+  cudaEvent_t ev_s = nullptr, ev_k[4] = {}, ev_rd[4] = {};
   int n = 0;
   long long N = 0;
   double h = 0;
@@ -159,15 +167,16 @@ static const T* les_tb(const CaseImpl<T>* ci, const LesState<T>& L) {
   return L.tb_same ? ci->les[L.tb_from].tb : L.tb;
 }
 
-// y = a + cs y with the RK stage coefficient of stage sprev (cs = dt/2, dt/2,
-// dt: the stage state u0 + cs k of rk_stage2_kernel), dt read on the device.
+// y = a + cs x (y may be x) with the RK stage coefficient of stage sprev (cs =
+// dt/2, dt/2, dt: the stage state u0 + cs k of the RK stage kernels), dt read
+// on the device.
 template <typename T>
-__global__ void tb_lin_kernel(long long count, const T* __restrict__ a, T* __restrict__ y,
+__global__ void tb_lin_kernel(long long count, const T* __restrict__ a, const T* x, T* y,
                               const double* __restrict__ dtp, int sprev) {
   const double dt = dtp[0];
   const T cs = (T)(sprev == 2 ? dt : 0.5 * dt);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
-    y[i] = fma(cs, y[i], a[i]);
+    y[i] = fma(cs, x[i], a[i]);
 }
 
 // Keep the sums of the step's initial state (stage 0) for the linearity form.
@@ -178,24 +187,6 @@ static int les_tb_keep(CaseImpl<T>* ci, cudaStream_t st) {
     if (L.tb_same) continue;
     const cudaError_t e =
         cudaMemcpyAsync(L.tbu0, L.tb, 3 * (size_t)ci->n * L.m * L.m * sizeof(T), cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-  }
-  return EXC_OK;
-}
-
-// Sums of the stage state of stage sprev + 1 from the sums of the initial state
-// and those of k_sprev (in tb since the end of stage sprev): the box sums are
-// linear, so this replaces a pass over the fine field by one over the sums
-// (n^3 / c^2 words per component); the results differ from summing the stage
-// state only by rounding.
-template <typename T>
-static int les_tb_lin(CaseImpl<T>* ci, int sprev, const double* dt, cudaStream_t st) {
-  for (int li = 0; li < ci->nles; ++li) {
-    LesState<T>& L = ci->les[li];
-    if (L.tb_same) continue;
-    const long long cnt = 3LL * ci->n * L.m * L.m;
-    tb_lin_kernel<T><<<grid_for_count(cnt), 256, 0, st>>>(cnt, L.tbu0, L.tb, dt, sprev);
-    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   }
   return EXC_OK;
@@ -253,6 +244,147 @@ static int les_target(CaseImpl<T>* ci, LesState<T>& L, const T* src, T* out, cud
   return les_target_tb<T>(ci, L, out, st);
 }
 
+// One LES grid's work of RK stage s once the box sums of k_s (ksums) are
+// ready, on stream sl: the closure m_s, then the exact, no-model and learned
+// LES stages.
+template <typename T>
+static int les_stage(exc_case* cs, CaseImpl<T>* ci, LesState<T>& L, int s, int cur, const double* dt,
+                     const T* ksums, cudaStream_t sl) {
+  const T visc = (T)cs->desc.visc;
+  cudaError_t e;
+  const int m = L.m;
+  const T H = (T)(cs->desc.l / m);
+  // m_s = P_H(filter(k_s) - RHS_H(ubar_s)); mcl keeps the unprojected
+  // difference (the projection is linear: the exact LES projects it
+  // together with its own RHS, one solve instead of two)
+  e = box_oa<T>(ci->n, L.c, L.kind, ksums, L.mcl, sl);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  int rc;
+  e = launch_rhs<T>(m, H, visc, L.ub, L.rtmp, false, sl);
+  if (e == cudaSuccess) e = launch_axpy<T>(3 * L.M, L.mcl, L.rtmp, (T)-1, sl);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  if (s == 0) {
+    // the closure of stage 0 (snapshot pairs, diagnostics): m_0 itself
+    e = cudaMemcpyAsync(L.mlast, L.mcl, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, sl);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(L.ublast, L.ub, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, sl);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    rc = project_vec<T>(&L.ps, L.mlast, sl);
+    if (rc) return rc;
+  }
+  // exact-closure LES: k = P_H(RHS_H(v_s) + filter(k_s) - RHS_H(ubar_s))
+  T* ve0 = L.ve[cur];
+  T* vefin = L.ve[cur ^ 1];
+  e = launch_rhs<T>(m, H, visc, s == 0 ? ve0 : L.ves, L.ke, false, sl);
+  if (e == cudaSuccess) e = launch_axpy<T>(3 * L.M, L.ke, L.mcl, (T)1, sl);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  rc = project_vec<T>(&L.ps, L.ke, sl);
+  if (rc) return rc;
+  e = launch_rk_stage<T>(m, H, L.ke, nullptr, 0, ve0, L.ves, vefin, s, dt, sl);
+  // no-model LES
+  T* vn0 = L.vn[cur];
+  T* vnfin = L.vn[cur ^ 1];
+  if (e == cudaSuccess) e = launch_rhs<T>(m, H, visc, s == 0 ? vn0 : L.vns, L.kn, false, sl);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  rc = project_vec<T>(&L.ps, L.kn, sl);
+  if (rc) return rc;
+  e = launch_rk_stage<T>(m, H, L.kn, nullptr, 0, vn0, L.vns, vnfin, s, dt, sl);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  if (L.net) {
+    // learned-closure LES: k = P_H(RHS_H(v_s) + net(v_s))
+    T* vl0 = L.vl[cur];
+    T* vlfin = L.vl[cur ^ 1];
+    const T* vsrc = s == 0 ? vl0 : L.vls;
+    e = launch_rhs<T>(m, H, visc, vsrc, L.kl, false, sl);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    rc = exc_net_forward(L.net, cs->precision, 1, m, vsrc, L.nn, sl);
+    if (rc) return rc;
+    add_unless_kernel<T><<<grid_for_count(3 * L.M), 256, 0, sl>>>(3 * L.M, L.kl, L.nn, L.fb);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+    rc = project_vec<T>(&L.ps, L.kl, sl);
+    if (rc) return rc;
+    e = launch_rk_stage<T>(m, H, L.kl, nullptr, 0, vl0, L.vls, vlfin, s, dt, sl);
+    if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  }
+  return EXC_OK;
+}
+
+// ubar_s of one LES from the box sums of the stage state (own-axis taps, then
+// the projection for the volume filter), on stream sl.
+template <typename T>
+static int les_target_from(CaseImpl<T>* ci, LesState<T>& L, const T* ssums, cudaStream_t sl) {
+  cudaError_t e = box_oa<T>(ci->n, L.c, L.kind, ssums, L.ub, sl);
+  if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
+  return L.kind == EXC_FILTER_VOLUME ? project_vec<T>(&L.ps, L.ub, sl) : EXC_OK;
+}
+
+// Stage sums of LES L (shared by LES of the same ratio).
+template <typename T>
+static const T* les_tbs(const CaseImpl<T>* ci, const LesState<T>& L) {
+  return L.tb_same ? ci->les[L.tb_from].tbs : L.tbs;
+}
+
+// The four RK stages with the LES work on the LES stream: the LES of stage s
+// (closure, LES stages, the targets of stage s + 1) runs beside the DNS of
+// stage s + 1.  The DNS stream writes k's box sums (tb) and the next stage
+// state's sums (tbs, by linearity) only after the LES stream has finished the
+// previous stage (events), and joins the LES stream at the end; the kernels
+// and their inputs are those of the sequential stepper, so the results are
+// the same bits.
+template <typename T>
+static int enqueue_stages_overlap(exc_case* cs, CaseImpl<T>* ci, int cur, T* u0, T* ufin, const double* dt,
+                                  cudaStream_t st) {
+  const int n = ci->n;
+  const T h = (T)ci->h, visc = (T)cs->desc.visc;
+  cudaStream_t sl = ci->lst;
+  auto cuda_rc = [](cudaError_t err) {
+    if (err == cudaSuccess) return (int)EXC_OK;
+    set_last_error(cudaGetErrorString(err));
+    return (int)EXC_ERR_CUDA;
+  };
+  // box sums of u0: kept for the linearity form and as the stage-0 targets' sums
+  int rc = les_tb_fill<T>(ci, u0, st);
+  if (!rc) rc = les_tb_keep<T>(ci, st);
+  for (int li = 0; li < ci->nles && !rc; ++li) {
+    LesState<T>& L = ci->les[li];
+    if (L.tb_same) continue;
+    rc = cuda_rc(cudaMemcpyAsync(L.tbs, L.tb, 3 * (size_t)n * L.m * L.m * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  }
+  if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_s, st));
+  if (!rc) rc = cuda_rc(cudaStreamWaitEvent(sl, ci->ev_s, 0));
+  for (int li = 0; li < ci->nles && !rc; ++li) rc = les_target_from<T>(ci, ci->les[li], les_tbs(ci, ci->les[li]), sl);
+  for (int s = 0; s < 4 && !rc; ++s) {
+    const T* src = s == 0 ? u0 : ci->us;
+    rc = cuda_rc(launch_rhs<T>(n, h, visc, src, ci->rhs, false, st));
+    if (!rc) rc = cuda_rc(poisson_solve_inplace<T>(&ci->ps, ci->rhs, true, st));
+    if (!rc)
+      rc = cuda_rc(launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0,
+                                      ci->us, ufin, s, dt, st, SlotBatch(), 1, true));
+    // the LES stream is done with the sums of the previous stage
+    if (!rc && s > 0) rc = cuda_rc(cudaStreamWaitEvent(st, ci->ev_rd[s - 1], 0));
+    if (!rc) rc = les_tb_fill<T>(ci, ci->rhs, st);
+    if (s < 3) {
+      for (int li = 0; li < ci->nles && !rc; ++li) {
+        LesState<T>& L = ci->les[li];
+        if (L.tb_same) continue;
+        const long long cnt = 3LL * n * L.m * L.m;
+        tb_lin_kernel<T><<<grid_for_count(cnt), 256, 0, st>>>(cnt, L.tbu0, L.tb, L.tbs, dt, s);
+        rc = cuda_rc(cudaGetLastError());
+      }
+    }
+    if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_k[s], st));
+    if (!rc) rc = cuda_rc(cudaStreamWaitEvent(sl, ci->ev_k[s], 0));
+    for (int li = 0; li < ci->nles && !rc; ++li) rc = les_stage<T>(cs, ci, ci->les[li], s, cur, dt, les_tb(ci, ci->les[li]), sl);
+    if (s < 3)
+      for (int li = 0; li < ci->nles && !rc; ++li)
+        rc = les_target_from<T>(ci, ci->les[li], les_tbs(ci, ci->les[li]), sl);
+    if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_rd[s], sl));
+  }
+  if (!rc) rc = cuda_rc(cudaStreamWaitEvent(st, ci->ev_rd[3], 0));
+  return rc;
+}
+
 // Enqueue one RK4 step (no host synchronisation).
 template <typename T>
 static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed) {
@@ -280,6 +412,7 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
     }
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   }
+  if (ci->overlap) return enqueue_stages_overlap<T>(cs, ci, cur, u0, ufin, dt, st);
   const bool fused = ci->fuse_root >= 0;
   T* const root_k = fused ? ci->les[ci->fuse_root].tb : nullptr;   // sums of k_s
   T* const root_s = fused ? ci->les[ci->fuse_root].tb2 : nullptr;  // sums of the stage state
@@ -296,25 +429,15 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
       if (fused && s > 0) {
         troot = root_s;
         rc = les_tb_coarsen<T>(ci, troot, st);
-      } else if (ci->tb_lin && s > 0) {
-        rc = les_tb_lin<T>(ci, s - 1, dt, st);
       } else {
         rc = les_tb_fill<T>(ci, src, st);
         if (fused) troot = root_k;
-        if (!rc && ci->tb_lin) rc = les_tb_keep<T>(ci, st);
       }
       if (rc) return rc;
     }
     for (int li = 0; li < ci->nles; ++li) {
       LesState<T>& L = ci->les[li];
-      int rc;
-      if (fused) {
-        e = box_oa<T>(n, L.c, L.kind, les_tb_from_root(ci, L, troot), L.ub, st);
-        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-        rc = L.kind == EXC_FILTER_VOLUME ? project_vec<T>(&L.ps, L.ub, st) : EXC_OK;
-      } else {
-        rc = les_target_tb<T>(ci, L, L.ub, st);
-      }
+      const int rc = les_target_from<T>(ci, L, fused ? les_tb_from_root(ci, L, troot) : les_tb(ci, L), st);
       if (rc) return rc;
     }
     if (fused) {
@@ -331,61 +454,8 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
     }
     for (int li = 0; li < ci->nles; ++li) {
       LesState<T>& L = ci->les[li];
-      const int m = L.m;
-      const T H = (T)(cs->desc.l / m);
-      // m_s = P_H(filter(k_s) - RHS_H(ubar_s)); mcl keeps the unprojected
-      // difference (the projection is linear: the exact LES projects it
-      // together with its own RHS, one solve instead of two)
-      e = box_oa<T>(n, L.c, L.kind, fused ? les_tb_from_root(ci, L, root_k) : les_tb(ci, L), L.mcl, st);
-      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-      int rc;
-      e = launch_rhs<T>(m, H, visc, L.ub, L.rtmp, false, st);
-      if (e == cudaSuccess) e = launch_axpy<T>(3 * L.M, L.mcl, L.rtmp, (T)-1, st);
-      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-      if (s == 0) {
-        // the closure of stage 0 (snapshot pairs, diagnostics): m_0 itself
-        e = cudaMemcpyAsync(L.mlast, L.mcl, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, st);
-        if (e == cudaSuccess)
-          e = cudaMemcpyAsync(L.ublast, L.ub, 3 * L.M * sizeof(T), cudaMemcpyDeviceToDevice, st);
-        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-        rc = project_vec<T>(&L.ps, L.mlast, st);
-        if (rc) return rc;
-      }
-      // exact-closure LES: k = P_H(RHS_H(v_s) + filter(k_s) - RHS_H(ubar_s))
-      T* ve0 = L.ve[cur];
-      T* vefin = L.ve[cur ^ 1];
-      e = launch_rhs<T>(m, H, visc, s == 0 ? ve0 : L.ves, L.ke, false, st);
-      if (e == cudaSuccess) e = launch_axpy<T>(3 * L.M, L.ke, L.mcl, (T)1, st);
-      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-      rc = project_vec<T>(&L.ps, L.ke, st);
+      const int rc = les_stage<T>(cs, ci, L, s, cur, dt, fused ? les_tb_from_root(ci, L, root_k) : les_tb(ci, L), st);
       if (rc) return rc;
-      e = launch_rk_stage<T>(m, H, L.ke, nullptr, 0, ve0, L.ves, vefin, s, dt, st);
-      // no-model LES
-      T* vn0 = L.vn[cur];
-      T* vnfin = L.vn[cur ^ 1];
-      if (e == cudaSuccess) e = launch_rhs<T>(m, H, visc, s == 0 ? vn0 : L.vns, L.kn, false, st);
-      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-      rc = project_vec<T>(&L.ps, L.kn, st);
-      if (rc) return rc;
-      e = launch_rk_stage<T>(m, H, L.kn, nullptr, 0, vn0, L.vns, vnfin, s, dt, st);
-      if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-      if (L.net) {
-        // learned-closure LES: k = P_H(RHS_H(v_s) + net(v_s))
-        T* vl0 = L.vl[cur];
-        T* vlfin = L.vl[cur ^ 1];
-        const T* vsrc = s == 0 ? vl0 : L.vls;
-        e = launch_rhs<T>(m, H, visc, vsrc, L.kl, false, st);
-        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-        rc = exc_net_forward(L.net, cs->precision, 1, m, vsrc, L.nn, st);
-        if (rc) return rc;
-        add_unless_kernel<T><<<grid_for_count(3 * L.M), 256, 0, st>>>(3 * L.M, L.kl, L.nn, L.fb);
-        e = cudaGetLastError();
-        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-        rc = project_vec<T>(&L.ps, L.kl, st);
-        if (rc) return rc;
-        e = launch_rk_stage<T>(m, H, L.kl, nullptr, 0, vl0, L.vls, vlfin, s, dt, st);
-        if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
-      }
     }
   }
   return EXC_OK;
@@ -459,6 +529,12 @@ static void case_destroy(exc_case* cs) {
   CaseImpl<T>* ci = reinterpret_cast<CaseImpl<T>*>(cs->impl);
   if (!ci) return;
   for (int k = 0; k < 2; ++k) if (ci->graph[k]) cudaGraphExecDestroy(ci->graph[k]);
+  if (ci->ev_s) cudaEventDestroy(ci->ev_s);
+  for (int k = 0; k < 4; ++k) {
+    if (ci->ev_k[k]) cudaEventDestroy(ci->ev_k[k]);
+    if (ci->ev_rd[k]) cudaEventDestroy(ci->ev_rd[k]);
+  }
+  if (ci->lst) cudaStreamDestroy(ci->lst);
   poisson_free(&ci->ps);
   if (ci->u[0]) cudaFree(ci->u[0]);
   if (ci->dscal) cudaFree(ci->dscal);
@@ -470,6 +546,7 @@ static void case_destroy(exc_case* cs) {
     if (ci->les[li].tb) cudaFree(ci->les[li].tb);
     if (ci->les[li].tb2) cudaFree(ci->les[li].tb2);
     if (ci->les[li].tbu0) cudaFree(ci->les[li].tbu0);
+    if (ci->les[li].tbs) cudaFree(ci->les[li].tbs);
     if (ci->les[li].fb) cudaFree(ci->les[li].fb);
   }
   delete ci;
@@ -580,6 +657,19 @@ static int case_create(exc_case* cs) {
       if (cudaMalloc(&L.tbu0, tbb) != cudaSuccess) { set_last_error("out of device memory (LES filter scratch)"); return EXC_ERR_OOM; }
     }
     ci->tb_lin = true;
+    for (int li = 0; li < d.nles; ++li) {
+      LesState<T>& L = ci->les[li];
+      if (L.tb_same) continue;
+      const size_t tbb = 3 * (size_t)d.n * L.m * L.m * sizeof(T);
+      if (cudaMalloc(&L.tbs, tbb) != cudaSuccess) { set_last_error("out of device memory (LES filter scratch)"); return EXC_ERR_OOM; }
+    }
+    bool ok = cudaEventCreateWithFlags(&ci->ev_s, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; k < 4 && ok; ++k)
+      ok = cudaEventCreateWithFlags(&ci->ev_k[k], cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&ci->ev_rd[k], cudaEventDisableTiming) == cudaSuccess;
+    if (ok) ok = cudaStreamCreateWithFlags(&ci->lst, cudaStreamNonBlocking) == cudaSuccess;
+    if (!ok) { set_last_error("cannot create the LES stream"); return EXC_ERR_CUDA; }
+    ci->overlap = true;
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }

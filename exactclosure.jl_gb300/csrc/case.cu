@@ -78,7 +78,7 @@ struct CaseImpl {
   // s runs beside the DNS of stage s + 1 (events order the shared sums)
   bool overlap = false;
   cudaStream_t lst = nullptr;  // the LES stream
-  cudaEvent_t ev_s = nullptr, ev_k[4] = {}, ev_rd[4] = {};
+  cudaEvent_t ev_s = nullptr, ev_t0 = nullptr, ev_k[4] = {}, ev_rd[4] = {};
   int n = 0;
   long long N = 0;
   double h = 0;
@@ -194,9 +194,9 @@ static int les_tb_keep(CaseImpl<T>* ci, cudaStream_t st) {
 
 // Fused stepper (one root ratio for every LES): the root's sums come from
 // rk_stage_sums_kernel in `root`; the other LES coarsen from them (in
-// increasing ratio) into their own buffers.
+// increasing ratio) into their own buffers (tb, or tbs with `stage`).
 template <typename T>
-static int les_tb_coarsen(CaseImpl<T>* ci, const T* root, cudaStream_t st) {
+static int les_tb_coarsen(CaseImpl<T>* ci, const T* root, cudaStream_t st, bool stage = false) {
   int order[EXC_MAX_LES];
   for (int i = 0; i < ci->nles; ++i) order[i] = i;
   for (int i = 1; i < ci->nles; ++i)
@@ -209,8 +209,9 @@ static int les_tb_coarsen(CaseImpl<T>* ci, const T* root, cudaStream_t st) {
   for (int k = 0; k < ci->nles && e == cudaSuccess; ++k) {
     LesState<T>& L = ci->les[order[k]];
     if (L.tb_same || L.tb_from < 0) continue;
-    const T* src = ci->les[L.tb_from].tb_from < 0 && !ci->les[L.tb_from].tb_same ? root : ci->les[L.tb_from].tb;
-    e = box_tb_coarsen<T>(ci->n, ci->les[L.tb_from].c, L.c, src, L.tb, st);
+    const LesState<T>& F = ci->les[L.tb_from];
+    const T* src = F.tb_from < 0 && !F.tb_same ? root : (stage ? F.tbs : F.tb);
+    e = box_tb_coarsen<T>(ci->n, F.c, L.c, src, stage ? L.tbs : L.tb, st);
   }
   if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   return EXC_OK;
@@ -354,6 +355,7 @@ static int enqueue_stages_overlap(exc_case* cs, CaseImpl<T>* ci, int cur, T* u0,
   if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_s, st));
   if (!rc) rc = cuda_rc(cudaStreamWaitEvent(sl, ci->ev_s, 0));
   for (int li = 0; li < ci->nles && !rc; ++li) rc = les_target_from<T>(ci, ci->les[li], les_tbs(ci, ci->les[li]), sl);
+  if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_t0, sl));
   for (int s = 0; s < 4 && !rc; ++s) {
     const T* src = s == 0 ? u0 : ci->us;
     rc = cuda_rc(launch_rhs<T>(n, h, visc, src, ci->rhs, false, st));
@@ -361,8 +363,9 @@ static int enqueue_stages_overlap(exc_case* cs, CaseImpl<T>* ci, int cur, T* u0,
     if (!rc)
       rc = cuda_rc(launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0,
                                       ci->us, ufin, s, dt, st, SlotBatch(), 1, true));
-    // the LES stream is done with the sums of the previous stage
-    if (!rc && s > 0) rc = cuda_rc(cudaStreamWaitEvent(st, ci->ev_rd[s - 1], 0));
+    // the LES stream is done with the sums of the previous stage (stage 0:
+    // with the targets' sums)
+    if (!rc) rc = cuda_rc(cudaStreamWaitEvent(st, s > 0 ? ci->ev_rd[s - 1] : ci->ev_t0, 0));
     if (!rc) rc = les_tb_fill<T>(ci, ci->rhs, st);
     if (s < 3) {
       for (int li = 0; li < ci->nles && !rc; ++li) {
@@ -379,6 +382,70 @@ static int enqueue_stages_overlap(exc_case* cs, CaseImpl<T>* ci, int cur, T* u0,
     if (s < 3)
       for (int li = 0; li < ci->nles && !rc; ++li)
         rc = les_target_from<T>(ci, ci->les[li], les_tbs(ci, ci->les[li]), sl);
+    if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_rd[s], sl));
+  }
+  if (!rc) rc = cuda_rc(cudaStreamWaitEvent(st, ci->ev_rd[3], 0));
+  return rc;
+}
+
+// Stage-state sums of LES L in the fused stepper: the root's (tb2, written by
+// the RK stage kernel) or the coarsened ones of L's owner.
+template <typename T>
+static const T* les_tbs_fused(const CaseImpl<T>* ci, const LesState<T>& L) {
+  const LesState<T>& O = L.tb_same ? ci->les[L.tb_from] : L;
+  return O.tb_from < 0 ? ci->les[ci->fuse_root].tb2 : O.tbs;
+}
+
+// The fused stepper's four RK stages with the LES work on the LES stream, as
+// in enqueue_stages_overlap: the RK stage kernel writes k's sums and the next
+// stage state's sums itself, so the DNS stream waits for the LES stream's
+// previous stage just before it.
+template <typename T>
+static int enqueue_stages_overlap_fused(exc_case* cs, CaseImpl<T>* ci, int cur, T* u0, T* ufin, const double* dt,
+                                        cudaStream_t st) {
+  const int n = ci->n;
+  const T h = (T)ci->h, visc = (T)cs->desc.visc;
+  cudaStream_t sl = ci->lst;
+  LesState<T>& R = ci->les[ci->fuse_root];
+  T* const root_k = R.tb;
+  T* const root_s = R.tb2;
+  auto cuda_rc = [](cudaError_t err) {
+    if (err == cudaSuccess) return (int)EXC_OK;
+    set_last_error(cudaGetErrorString(err));
+    return (int)EXC_ERR_CUDA;
+  };
+  // box sums of u0 as the stage-0 targets' sums
+  int rc = les_tb_fill<T>(ci, u0, st);
+  const size_t rb = 3 * (size_t)n * R.m * R.m * sizeof(T);
+  if (!rc) rc = cuda_rc(cudaMemcpyAsync(root_s, root_k, rb, cudaMemcpyDeviceToDevice, st));
+  for (int li = 0; li < ci->nles && !rc; ++li) {
+    LesState<T>& L = ci->les[li];
+    if (L.tb_same || L.tb_from < 0) continue;
+    rc = cuda_rc(cudaMemcpyAsync(L.tbs, L.tb, 3 * (size_t)n * L.m * L.m * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  }
+  if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_s, st));
+  if (!rc) rc = cuda_rc(cudaStreamWaitEvent(sl, ci->ev_s, 0));
+  for (int li = 0; li < ci->nles && !rc; ++li)
+    rc = les_target_from<T>(ci, ci->les[li], les_tbs_fused(ci, ci->les[li]), sl);
+  if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_t0, sl));
+  for (int s = 0; s < 4 && !rc; ++s) {
+    const T* src = s == 0 ? u0 : ci->us;
+    rc = cuda_rc(launch_rhs<T>(n, h, visc, src, ci->rhs, false, st));
+    if (!rc) rc = cuda_rc(poisson_solve_inplace<T>(&ci->ps, ci->rhs, true, st));
+    // the LES stream is done with the sums the RK stage kernel rewrites
+    if (!rc) rc = cuda_rc(cudaStreamWaitEvent(st, s > 0 ? ci->ev_rd[s - 1] : ci->ev_t0, 0));
+    if (!rc)
+      rc = cuda_rc(launch_rk_stage_sums<T>(n, R.c, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P,
+                                           u0, ci->us, ufin, s, dt, root_k, s < 3 ? root_s : nullptr, st));
+    if (!rc) rc = les_tb_coarsen<T>(ci, root_k, st);
+    if (!rc && s < 3) rc = les_tb_coarsen<T>(ci, root_s, st, true);
+    if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_k[s], st));
+    if (!rc) rc = cuda_rc(cudaStreamWaitEvent(sl, ci->ev_k[s], 0));
+    for (int li = 0; li < ci->nles && !rc; ++li)
+      rc = les_stage<T>(cs, ci, ci->les[li], s, cur, dt, les_tb_from_root(ci, ci->les[li], root_k), sl);
+    if (s < 3)
+      for (int li = 0; li < ci->nles && !rc; ++li)
+        rc = les_target_from<T>(ci, ci->les[li], les_tbs_fused(ci, ci->les[li]), sl);
     if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_rd[s], sl));
   }
   if (!rc) rc = cuda_rc(cudaStreamWaitEvent(st, ci->ev_rd[3], 0));
@@ -412,7 +479,9 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
     }
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
   }
-  if (ci->overlap) return enqueue_stages_overlap<T>(cs, ci, cur, u0, ufin, dt, st);
+  if (ci->overlap)
+    return ci->fuse_root >= 0 ? enqueue_stages_overlap_fused<T>(cs, ci, cur, u0, ufin, dt, st)
+                              : enqueue_stages_overlap<T>(cs, ci, cur, u0, ufin, dt, st);
   const bool fused = ci->fuse_root >= 0;
   T* const root_k = fused ? ci->les[ci->fuse_root].tb : nullptr;   // sums of k_s
   T* const root_s = fused ? ci->les[ci->fuse_root].tb2 : nullptr;  // sums of the stage state
@@ -530,6 +599,7 @@ static void case_destroy(exc_case* cs) {
   if (!ci) return;
   for (int k = 0; k < 2; ++k) if (ci->graph[k]) cudaGraphExecDestroy(ci->graph[k]);
   if (ci->ev_s) cudaEventDestroy(ci->ev_s);
+  if (ci->ev_t0) cudaEventDestroy(ci->ev_t0);
   for (int k = 0; k < 4; ++k) {
     if (ci->ev_k[k]) cudaEventDestroy(ci->ev_k[k]);
     if (ci->ev_rd[k]) cudaEventDestroy(ci->ev_rd[k]);
@@ -551,6 +621,19 @@ static void case_destroy(exc_case* cs) {
   }
   delete ci;
   cs->impl = nullptr;
+}
+
+// The LES stream of the overlapped steppers and the events that order it.
+template <typename T>
+static int create_les_stream(CaseImpl<T>* ci) {
+  bool ok = cudaEventCreateWithFlags(&ci->ev_s, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&ci->ev_t0, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; k < 4 && ok; ++k)
+    ok = cudaEventCreateWithFlags(&ci->ev_k[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&ci->ev_rd[k], cudaEventDisableTiming) == cudaSuccess;
+  if (ok) ok = cudaStreamCreateWithFlags(&ci->lst, cudaStreamNonBlocking) == cudaSuccess;
+  if (!ok) { set_last_error("cannot create the LES stream"); return EXC_ERR_CUDA; }
+  return EXC_OK;
 }
 
 template <typename T>
@@ -647,6 +730,19 @@ static int case_create(exc_case* cs) {
       }
     }
   }
+  // fused stepper: LES work on the LES stream beside the DNS (stage sums of
+  // the coarser LES in tbs)
+  if (ci->fuse_root >= 0) {
+    for (int li = 0; li < d.nles; ++li) {
+      LesState<T>& L = ci->les[li];
+      if (L.tb_same || L.tb_from < 0) continue;
+      const size_t tbb = 3 * (size_t)d.n * L.m * L.m * sizeof(T);
+      if (cudaMalloc(&L.tbs, tbb) != cudaSuccess) { set_last_error("out of device memory (LES filter scratch)"); return EXC_ERR_OOM; }
+    }
+    int rc2 = create_les_stream<T>(ci);
+    if (rc2) return rc2;
+    ci->overlap = true;
+  }
   // FP64 with separate sum passes: stage-state sums by linearity
   ci->tb_lin = false;
   if (sizeof(T) == 8 && ci->fuse_root < 0 && d.nles > 0) {
@@ -663,12 +759,8 @@ static int case_create(exc_case* cs) {
       const size_t tbb = 3 * (size_t)d.n * L.m * L.m * sizeof(T);
       if (cudaMalloc(&L.tbs, tbb) != cudaSuccess) { set_last_error("out of device memory (LES filter scratch)"); return EXC_ERR_OOM; }
     }
-    bool ok = cudaEventCreateWithFlags(&ci->ev_s, cudaEventDisableTiming) == cudaSuccess;
-    for (int k = 0; k < 4 && ok; ++k)
-      ok = cudaEventCreateWithFlags(&ci->ev_k[k], cudaEventDisableTiming) == cudaSuccess &&
-           cudaEventCreateWithFlags(&ci->ev_rd[k], cudaEventDisableTiming) == cudaSuccess;
-    if (ok) ok = cudaStreamCreateWithFlags(&ci->lst, cudaStreamNonBlocking) == cudaSuccess;
-    if (!ok) { set_last_error("cannot create the LES stream"); return EXC_ERR_CUDA; }
+    int rc2 = create_les_stream<T>(ci);
+    if (rc2) return rc2;
     ci->overlap = true;
   }
   cudaError_t e = cudaGetLastError();

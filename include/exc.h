@@ -195,7 +195,10 @@ typedef struct {
 
 typedef struct exc_case exc_case;
 
-/* `stream` (cudaStream_t, may be NULL) is bound to the case for life. */
+/* `stream` (cudaStream_t, may be NULL) is bound to the case for life.  A case
+ * with LES grids also runs the LES work of each RK stage on a stream of its own
+ * (created here), forked from and joined back into `stream` inside every step:
+ * work the caller orders on `stream` sees complete steps. */
 int exc_case_create(const exc_case_desc* desc, void* stream, exc_case** out);
 int exc_case_destroy(exc_case* cs);
 

@@ -358,11 +358,13 @@ static int enqueue_stages_overlap(exc_case* cs, CaseImpl<T>* ci, int cur, T* u0,
   if (!rc) rc = cuda_rc(cudaEventRecord(ci->ev_t0, sl));
   for (int s = 0; s < 4 && !rc; ++s) {
     const T* src = s == 0 ? u0 : ci->us;
-    rc = cuda_rc(launch_rhs<T>(n, h, visc, src, ci->rhs, false, st));
+    // the stage states 1-3 are stored in the sweep's shifted form
+    const bool wsh = rk_writes_shifted<T>(n);
+    rc = cuda_rc(launch_rhs<T>(n, h, visc, src, ci->rhs, false, st, SlotBatch(), 1, s > 0 && wsh));
     if (!rc) rc = cuda_rc(poisson_solve_inplace<T>(&ci->ps, ci->rhs, true, st));
     if (!rc)
       rc = cuda_rc(launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0,
-                                      ci->us, ufin, s, dt, st, SlotBatch(), 1, true));
+                                      ci->us, ufin, s, dt, st, SlotBatch(), 1, true, wsh, cs->desc.visc));
     // the LES stream is done with the sums of the previous stage (stage 0:
     // with the targets' sums)
     if (!rc) rc = cuda_rc(cudaStreamWaitEvent(st, s > 0 ? ci->ev_rd[s - 1] : ci->ev_t0, 0));
@@ -485,9 +487,12 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
   const bool fused = ci->fuse_root >= 0;
   T* const root_k = fused ? ci->les[ci->fuse_root].tb : nullptr;   // sums of k_s
   T* const root_s = fused ? ci->les[ci->fuse_root].tb2 : nullptr;  // sums of the stage state
+  // without LES nothing but the next sweep reads the stage states: FP64
+  // stores them in the sweep's shifted form
+  const bool wsh = ci->nles == 0 && rk_writes_shifted<T>(n);
   for (int s = 0; s < 4; ++s) {
     const T* src = s == 0 ? u0 : ci->us;
-    e = launch_rhs<T>(n, h, visc, src, ci->rhs, false, st);
+    e = launch_rhs<T>(n, h, visc, src, ci->rhs, false, st, SlotBatch(), 1, s > 0 && wsh);
     if (e == cudaSuccess) e = poisson_solve_inplace<T>(&ci->ps, ci->rhs, true, st);
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
     // LES targets use the stage state before it is overwritten; the fused
@@ -514,7 +519,7 @@ static int enqueue_step(exc_case* cs, CaseImpl<T>* ci, int cur, double dt_fixed)
                                   2 * ci->ps.P, u0, ci->us, ufin, s, dt, root_k, s < 3 ? root_s : nullptr, st);
     } else {
       e = launch_rk_stage<T>(n, h, ci->rhs, reinterpret_cast<const T*>(ci->ps.work), 2 * ci->ps.P, u0, ci->us, ufin,
-                             s, dt, st, SlotBatch(), 1, ci->nles > 0);
+                             s, dt, st, SlotBatch(), 1, ci->nles > 0, wsh, cs->desc.visc);
     }
     if (e != cudaSuccess) { set_last_error(cudaGetErrorString(e)); return EXC_ERR_CUDA; }
     if (ci->nles > 0) {

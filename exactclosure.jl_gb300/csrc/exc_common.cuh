@@ -52,6 +52,21 @@ __host__ __device__ __forceinline__ int spec_pitch(int n) { return pad8(n / 2 + 
 // reciprocal m = ceil(2^64 / d): x / d exactly for every x < 2^64 / d, which
 // covers every index here.  Built once per thread (one 64-bit division), it
 // replaces the per-element 64-bit divisions of grid-stride index splits.
+// Constants of the FP64 RHS sweep's shifted stress form, w = sq u - qs
+// (sq = sqrt(1/(4h)), qs = rho/2, rho = (4 visc/h) sq): one definition for
+// the sweep and for the RK stage kernel that stores the next stage state in
+// that form, so both produce the same bits.
+struct Fp64Shift {
+  double sq, rho, qs;
+};
+__device__ __forceinline__ Fp64Shift fp64_shift(double inv_h, double visc) {
+  const double kd = 0.25 * inv_h;
+  const double rv = 4.0 * visc * inv_h;
+  const double sq = sqrt(kd);
+  const double rho = rv * sq;
+  return {sq, rho, 0.5 * rho};
+}
+
 struct IdxDiv {
   unsigned long long m;
   long long d;

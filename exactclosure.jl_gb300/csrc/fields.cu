@@ -150,10 +150,13 @@ __global__ void rk_stage4_kernel(int n, float inv_h, float* __restrict__ k, cons
 __device__ __forceinline__ double2 ld2(const double* p) { return *reinterpret_cast<const double2*>(p); }
 __device__ __forceinline__ void st2(double* p, double2 v) { *reinterpret_cast<double2*>(p) = v; }
 
-template <bool STORE_K>
+// WOUT: the stage state goes out in the RHS sweep's shifted form w = sq x -
+// qs (fp64_shift of inv_h and wvisc), the only form its one reader, the next
+// RHS sweep, needs: the same bits as the sweep shifting the plain state.
+template <bool STORE_K, bool WOUT = false>
 __global__ void rk_stage2_kernel(int n, double inv_h, double* __restrict__ k, const double* __restrict__ p, int ppitch,
                                  const double* __restrict__ x0, double* __restrict__ xs, double* __restrict__ xfin,
-                                 int stage, const double* __restrict__ dtp, SlotBatch sb) {
+                                 int stage, const double* __restrict__ dtp, SlotBatch sb, double wvisc = 0.0) {
   const long long N = (long long)n * n * n;
   const int slot = blockIdx.y;
   if (sb.active && !sb.active[slot]) return;
@@ -165,6 +168,7 @@ __global__ void rk_stage2_kernel(int n, double inv_h, double* __restrict__ k, co
   const double dt = dtp[slot];
   const double cf = (stage == 0 || stage == 3) ? dt / 6.0 : dt / 3.0;
   const double cs = stage == 2 ? dt : 0.5 * dt;
+  const Fp64Shift fs = fp64_shift(inv_h, wvisc);
   const IdxDiv dn(n);
   const long long Q = N / 2;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < Q; q += (long long)gridDim.x * blockDim.x) {
@@ -201,7 +205,11 @@ __global__ void rk_stage2_kernel(int n, double inv_h, double* __restrict__ k, co
         f.y += cf * kc.y;
       }
       st2(xfin + c * N + g, f);
-      if (stage < 3) st2(xs + c * N + g, make_double2(a.x + cs * kc.x, a.y + cs * kc.y));
+      if (stage < 3) {
+        double2 v = make_double2(fma(cs, kc.x, a.x), fma(cs, kc.y, a.y));
+        if (WOUT) v = make_double2(fma(fs.sq, v.x, -fs.qs), fma(fs.sq, v.y, -fs.qs));
+        st2(xs + c * N + g, v);
+      }
     }
   }
 }
@@ -335,7 +343,9 @@ cudaError_t launch_rk_stage_sums(int n, int c0, T h, const T* k, const T* p, int
 
 template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
-                            const double* dtp, cudaStream_t st, const SlotBatch& sb, int nslots, bool store_k) {
+                            const double* dtp, cudaStream_t st, const SlotBatch& sb, int nslots, bool store_k,
+                            bool shifted_out, double visc) {
+  if (shifted_out && (!p || !rk_writes_shifted<T>(n))) return cudaErrorInvalidValue;
   long long N = (long long)n * n * n;
   dim3 grid(nslots > 1 ? std::min(grid_for(N), 152 * 8) : grid_for(N), nslots);
   if constexpr (sizeof(T) == 4) {
@@ -354,7 +364,15 @@ cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x
     if (p && n % 2 == 0) {
       dim3 g2(nslots > 1 ? std::min(grid_for(N / 2), 152 * 8) : grid_for(N / 2), nslots);
       const double ih = 1.0 / (double)h;
-      if (store_k)
+      if (shifted_out && store_k)
+        rk_stage2_kernel<true, true><<<g2, 256, 0, st>>>(n, ih, (double*)k, (const double*)p, ppitch,
+                                                         (const double*)x0, (double*)xs, (double*)xfin, stage, dtp, sb,
+                                                         visc);
+      else if (shifted_out)
+        rk_stage2_kernel<false, true><<<g2, 256, 0, st>>>(n, ih, (double*)k, (const double*)p, ppitch,
+                                                          (const double*)x0, (double*)xs, (double*)xfin, stage, dtp, sb,
+                                                          visc);
+      else if (store_k)
         rk_stage2_kernel<true><<<g2, 256, 0, st>>>(n, ih, (double*)k, (const double*)p, ppitch, (const double*)x0,
                                                    (double*)xs, (double*)xfin, stage, dtp, sb);
       else
@@ -714,7 +732,7 @@ cudaError_t launch_convert(long long count, const A* a, B* b, cudaStream_t st) {
   template cudaError_t launch_rk_stage_sums<T>(int, int, T, const T*, const T*, int, const T*, T*, T*, int,     \
                                                const double*, T*, T*, cudaStream_t);                           \
   template cudaError_t launch_rk_stage<T>(int, T, T*, const T*, int, const T*, T*, T*, int, const double*,      \
-                                          cudaStream_t, const SlotBatch&, int, bool);                                                        \
+                                          cudaStream_t, const SlotBatch&, int, bool, bool, double);                                                        \
   template cudaError_t launch_axpy<T>(long long, T*, const T*, T, cudaStream_t);                                \
   template cudaError_t launch_normals<T>(long long, unsigned long long, T*, cudaStream_t);                      \
   template cudaError_t launch_sqdiff<T>(long long, const T*, const T*, double*, double*, cudaStream_t);         \

@@ -6,10 +6,17 @@ namespace exc {
 
 constexpr int SHELL_BLOCKS = 152;
 
+// shifted_out (FP64, rk_writes_shifted, with p): the stage state xs is stored
+// in the RHS sweep's shifted form for viscosity `visc` (read with pre_shifted)
 template <typename T>
 cudaError_t launch_rk_stage(int n, T h, T* k, const T* p, int ppitch, const T* x0, T* xs, T* xfin, int stage,
                             const double* dtp, cudaStream_t st, const SlotBatch& sb = SlotBatch(), int nslots = 1,
-                            bool store_k = true);
+                            bool store_k = true, bool shifted_out = false, double visc = 0.0);
+// Whether the RK stage kernel of this grid can store the shifted form.
+template <typename T>
+inline bool rk_writes_shifted(int n) {
+  return sizeof(T) == 8 && n % 2 == 0;
+}
 // RK stage (GRAD form, k not stored) that also writes the transverse box sums
 // of ratio c0 of k into tbk and of the stage output xs (stages 0-2) into tbs
 // (may be null), bit-identical to tb_kernel's (fields.cu); for grids with

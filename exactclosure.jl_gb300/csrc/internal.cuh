@@ -120,9 +120,11 @@ template <typename T>
 cudaError_t copy_pressure(const exc_poisson* ps, T* p, cudaStream_t st);
 
 // ---- stencil kernels (stencil.cu) ----
+// pre_shifted (FP64): u holds the sweep's shifted form (fp64_shift), as the
+// RK stage kernel stores it on request
 template <typename T>
 cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st,
-                       const SlotBatch& sb = SlotBatch(), int nslots = 1);
+                       const SlotBatch& sb = SlotBatch(), int nslots = 1, bool pre_shifted = false);
 template <typename T>
 cudaError_t launch_stress(int n, T h, T visc, const T* u, T* s6, cudaStream_t st);
 template <typename T>

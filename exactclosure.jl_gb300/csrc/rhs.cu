@@ -155,7 +155,7 @@ __device__ __forceinline__ T s33(T up, T lo, T cd) {
 template <typename T, int NC, bool DOADD>
 __global__ void __launch_bounds__(PTX * NWARP, sizeof(T) == 4 ? 4 : 3)
 rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, SlotBatch sb, int zblocks, int ptz,
-           const __grid_constant__ CUtensorMap umap, int have_map) {
+           const __grid_constant__ CUtensorMap umap, int have_map, int pre_shifted) {
   constexpr int PTY = PTYT<NC>, PBY = PBYT<NC>;
   constexpr int CSTRIDE = (int)(sizeof(CompPlane<T, NC>) / sizeof(T));
   extern __shared__ __align__(128) unsigned char rhs_smem[];
@@ -178,9 +178,10 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   constexpr bool SC = sizeof(T) == 8;
   const T kd = (T)0.25 * inv_h;
   const T rv = (T)4 * visc * inv_h;
-  const T sq = SC ? (T)sqrt((double)kd) : (T)1;
-  const T rho = rv * sq;
-  const T qs = (T)0.5 * rho;
+  const Fp64Shift fs = fp64_shift((double)inv_h, (double)visc);
+  const T sq = SC ? (T)fs.sq : (T)1;
+  const T rho = (T)fs.rho;
+  const T qs = (T)fs.qs;
   const T cd = SC ? (T)-4 * rho : (T)2 * rv;
   const T co = SC ? (T)-2 * rho : rv;
   auto wrap = [n](int g) { return g < 0 ? g + n : (g >= n ? g - n : g); };
@@ -292,6 +293,7 @@ rhs_kernel(int n, T inv_h, T visc, const T* __restrict__ u, T* __restrict__ du, 
   // 16-byte pieces or words; the barrier after the wait publishes the result
   auto shift_plane = [&](int buf) {
     if constexpr (SC) {
+      if (pre_shifted) return;  // the field is stored in the shifted form already
       if (tma) {
         constexpr int HALF = PBY * UROW<T> / 2;  // 16-byte pairs per component plane
         static_assert(PBY * UROW<T> % 2 == 0, "component plane of whole pairs");
@@ -796,7 +798,7 @@ static bool field_tensor_map(const T* u, int n, int nslots, const SlotBatch& sb,
 
 template <typename T>
 cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaStream_t st, const SlotBatch& sb,
-                       int nslots) {
+                       int nslots, bool pre_shifted) {
   constexpr int NC = CYT<T>;
   // planes per CTA (4 to 32): the fewest waves of resident CTAs (`per_sm`
   // per SM) times the planes each CTA walks plus one for its start (three
@@ -844,10 +846,10 @@ cudaError_t launch_rhs(int n, T h, T visc, const T* u, T* du, bool doadd, cudaSt
   const int have = field_tensor_map<T>(u, n, nslots, sb, UROW<T>, PBYT<NC>, &map) ? 1 : 0;
   if (doadd)
     rhs_kernel<T, NC, true><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks, ptz,
-                                                                map, have);
+                                                                map, have, pre_shifted ? 1 : 0);
   else
     rhs_kernel<T, NC, false><<<grid, dim3(PTX, NWARP), sh, st>>>(n, (T)(1.0 / (double)h), visc, u, du, sb, zblocks,
-                                                                 ptz, map, have);
+                                                                 ptz, map, have, pre_shifted ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -872,9 +874,9 @@ cudaError_t configure_stencil() {
 }
 
 template cudaError_t launch_rhs<double>(int, double, double, const double*, double*, bool, cudaStream_t,
-                                        const SlotBatch&, int);
+                                        const SlotBatch&, int, bool);
 template cudaError_t launch_rhs<float>(int, float, float, const float*, float*, bool, cudaStream_t, const SlotBatch&,
-                                       int);
+                                       int, bool);
 
 }  // namespace exc
 

@@ -7,8 +7,8 @@ discrete filters and its exact-closure commutator.  Every function cites the
 reference file:line it follows.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
-``bench.py`` may import this package, and only as the checker (or as the
-timed CPU baseline).  The product path (``libexc.so`` behind the C ABI) never
+``bench.py`` may import this package, and only as the reference the CUDA
+results are compared with (or as the timed CPU baseline).  The product path (``libexc.so`` behind the C ABI) never
 calls it and has no CPU fallback.
 
 Parity pinning.  The reference is Julia and Julia is absent on every machine

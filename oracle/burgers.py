@@ -1,7 +1,7 @@
 """Float64 NumPy restatement of the reference's 1-D ``Burgers`` module.
 
-TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): the checker for the
-CUDA Burgers path and the timed CPU baseline; never part of the product.
+TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): what the CUDA Burgers
+path is compared with, and the timed CPU baseline; never part of the product.
 
 Layout: a batch of samples is a ``(nsample, n)`` array, x fastest -- the
 byte layout of the reference's ``zeros(nh, nsample)`` column-major matrices

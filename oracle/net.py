@@ -1,7 +1,7 @@
 """CPU restatement of the learned closure network -- TEST INFRASTRUCTURE ONLY.
 
-The checker of the CUDA training and inference kernels (gradients, forward
-outputs) for the learned-closure form: a 3-D convolutional net on the LES grid
+What the CUDA training and inference kernels (gradients, forward outputs) of
+the learned-closure form are compared with: a 3-D convolutional net on the LES grid
 with periodic 3x3x3 kernels, channels 3 -> 32 -> 32 -> 3 and GELU after the
 first two layers (no counterpart in the reference; its closures are the
 exact and classic ones of ``src/N.jl:1137-1226``).

@@ -1,7 +1,7 @@
 """Float64 NumPy restatement of the reference's 3-D ``NavierStokes`` operators.
 
-TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): the checker for the
-CUDA path and the timed CPU baseline; never part of the product.
+TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): what the CUDA path is
+compared with, and the timed CPU baseline; never part of the product.
 
 Layout: a scalar field is an ``(n, n, n)`` array indexed ``[z, y, x]`` (C
 order, x fastest), which is byte-identical to the reference's column-major
